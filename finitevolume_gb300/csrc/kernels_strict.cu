@@ -1,0 +1,5 @@
+// The same kernels compiled with --fmad=false: IEEE op-for-op identical to
+// the reference built without -ffast-math (bit-identical fields for the
+// Rusanov and HLLC fluxes).
+#define FV_KNS strict
+#include "euler_o1.cuh"

@@ -1,0 +1,334 @@
+// Host-side mesh construction for the device layout.
+//
+// Topology derivation follows the reference reader's rule
+// (src/MeshReader.cpp:317-456): faces are created while walking each
+// cell's polygon edges in order; the first cell to visit an edge owns the
+// face (cell_left) and fixes its node order, the second becomes cell_right.
+// Reproducing that rule exactly is what makes face numbering, face
+// orientation and every cell's face order identical to the reference, and
+// with them the summation order of each cell residual.
+#include "mesh_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <queue>
+#include <unordered_map>
+
+namespace fvgb {
+
+namespace {
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw MeshError{code, msg}; }
+
+constexpr int kBadArg = 1;
+constexpr int kBadMesh = 5;
+
+inline uint64_t edge_key(int32_t a, int32_t b) {
+    uint32_t lo = (uint32_t)std::min(a, b), hi = (uint32_t)std::max(a, b);
+    return ((uint64_t)lo << 32) | hi;
+}
+
+bool segments_cross(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy) {
+    auto side = [](double ox, double oy, double px, double py, double qx, double qy) {
+        return (px - ox) * (qy - oy) - (py - oy) * (qx - ox);
+    };
+    double d1 = side(cx, cy, dx, dy, ax, ay), d2 = side(cx, cy, dx, dy, bx, by);
+    double d3 = side(ax, ay, bx, by, cx, cy), d4 = side(ax, ay, bx, by, dx, dy);
+    return ((d1 > 0 && d2 < 0) || (d1 < 0 && d2 > 0)) && ((d3 > 0 && d4 < 0) || (d3 < 0 && d4 > 0));
+}
+
+}  // namespace
+
+// Face midpoint, length and unit normal (edge rotated -90 degrees):
+// UnstructuredMesh::compute_geometry, include/UnstructuredMesh.h:89-105.
+void HostMesh::compute_face_geometry() {
+    fnx.resize(n_faces); fny.resize(n_faces); farea.resize(n_faces); fxm.resize(n_faces); fym.resize(n_faces);
+    for (int32_t f = 0; f < n_faces; ++f) {
+        double x1 = nx_[fn1[f]], y1 = ny_[fn1[f]], x2 = nx_[fn2[f]], y2 = ny_[fn2[f]];
+        fxm[f] = 0.5 * (x1 + x2);
+        fym[f] = 0.5 * (y1 + y2);
+        double dx = x2 - x1, dy = y2 - y1;
+        double a = std::sqrt(dx * dx + dy * dy);
+        farea[f] = a;
+        fnx[f] = dy / a;
+        fny[f] = -dx / a;
+    }
+}
+
+void build_from_polygons(HostMesh& m, int32_t n_nodes, const double* xy, int32_t n_cells, const int64_t* cell_off,
+                         const int32_t* cell_nodes, int32_t n_bedges, const int32_t* bedge_nodes,
+                         const int32_t* bedge_patch, int32_t n_patches) {
+    if (n_nodes <= 0 || n_cells <= 0 || !xy || !cell_off || !cell_nodes || n_bedges < 0 || n_patches < 0)
+        fail(kBadArg, "mesh: empty or null input");
+    if (n_bedges > 0 && (!bedge_nodes || !bedge_patch)) fail(kBadArg, "mesh: null boundary arrays");
+    m.n_nodes = n_nodes; m.n_cells = n_cells; m.n_patches = n_patches;
+    m.nx_.resize(n_nodes); m.ny_.resize(n_nodes);
+    for (int32_t i = 0; i < n_nodes; ++i) {
+        m.nx_[i] = xy[2 * i]; m.ny_[i] = xy[2 * i + 1];
+        if (!std::isfinite(m.nx_[i]) || !std::isfinite(m.ny_[i]))
+            fail(kBadMesh, "mesh: node " + std::to_string(i) + " has a non-finite coordinate");
+    }
+    if (cell_off[0] != 0) fail(kBadArg, "mesh: cell_off[0] != 0");
+    std::unordered_map<uint64_t, int32_t> edge_to_face;
+    edge_to_face.reserve((size_t)(cell_off[n_cells] * 0.6) + 16);
+    m.cf_off.assign(n_cells + 1, 0);
+    m.cf.reserve((size_t)cell_off[n_cells]);
+    m.vol.resize(n_cells); m.cx.resize(n_cells); m.cy.resize(n_cells);
+    for (int32_t c = 0; c < n_cells; ++c) {
+        int64_t lo = cell_off[c], hi = cell_off[c + 1];
+        int32_t k = (int32_t)(hi - lo);
+        if (k < 3) fail(kBadMesh, "mesh: cell " + std::to_string(c) + " has fewer than 3 vertices");
+        const int32_t* ids = cell_nodes + lo;
+        for (int32_t e = 0; e < k; ++e) {
+            int32_t a = ids[e], b = ids[(e + 1) % k];
+            if (a < 0 || a >= n_nodes || b < 0 || b >= n_nodes)
+                fail(kBadMesh, "mesh: cell " + std::to_string(c) + " references an out-of-range node");
+            auto it = edge_to_face.find(edge_key(a, b));
+            if (it == edge_to_face.end()) {
+                int32_t f = (int32_t)m.fn1.size();
+                m.fn1.push_back(a); m.fn2.push_back(b); m.fl.push_back(c); m.fr.push_back(-1);
+                m.fpatch.push_back(-1);
+                edge_to_face.emplace(edge_key(a, b), f);
+                m.cf.push_back(f);
+            } else {
+                int32_t f = it->second;
+                if (m.fr[f] != -1) fail(kBadMesh, "mesh: edge shared by more than two cells");
+                m.fr[f] = c;
+                m.cf.push_back(f);
+            }
+        }
+        m.cf_off[c + 1] = (int32_t)m.cf.size();
+        // Shoelace area and centroid with the signed area
+        // (src/MeshReader.cpp:32-41, :56-76).
+        double area = 0.0;
+        for (int32_t i = 0; i < k; ++i) {
+            int32_t p0 = ids[i], p1 = ids[(i + 1) % k];
+            area += m.nx_[p0] * m.ny_[p1] - m.nx_[p1] * m.ny_[p0];
+        }
+        area = 0.5 * area;
+        double sx = 0.0, sy = 0.0;
+        for (int32_t i = 0; i < k; ++i) {
+            int32_t p0 = ids[i], p1 = ids[(i + 1) % k];
+            double cross = m.nx_[p0] * m.ny_[p1] - m.nx_[p1] * m.ny_[p0];
+            sx += (m.nx_[p0] + m.nx_[p1]) * cross;
+            sy += (m.ny_[p0] + m.ny_[p1]) * cross;
+        }
+        sx /= (6.0 * area);
+        sy /= (6.0 * area);
+        if (!std::isfinite(area) || area <= 0.0)
+            fail(kBadMesh, "mesh: cell " + std::to_string(c) + " has non-positive signed area (clockwise or degenerate)");
+        for (int32_t i = 0; i < k; ++i)
+            for (int32_t j = i + 2; j < k; ++j) {
+                if (i == 0 && j == k - 1) continue;
+                int32_t a0 = ids[i], a1 = ids[(i + 1) % k], b0 = ids[j], b1 = ids[(j + 1) % k];
+                if (segments_cross(m.nx_[a0], m.ny_[a0], m.nx_[a1], m.ny_[a1], m.nx_[b0], m.ny_[b0], m.nx_[b1],
+                                   m.ny_[b1]))
+                    fail(kBadMesh, "mesh: cell " + std::to_string(c) + " is self-intersecting");
+            }
+        m.vol[c] = std::fabs(area);
+        m.cx[c] = sx;
+        m.cy[c] = sy;
+    }
+    m.n_faces = (int32_t)m.fn1.size();
+    for (int32_t i = 0; i < n_bedges; ++i) {
+        int32_t a = bedge_nodes[2 * i], b = bedge_nodes[2 * i + 1], p = bedge_patch[i];
+        if (p < 0 || p >= n_patches) fail(kBadArg, "mesh: boundary edge patch index out of range");
+        auto it = edge_to_face.find(edge_key(a, b));
+        if (it == edge_to_face.end()) continue;  // matches no cell edge: ignored, as in the reference
+        m.fpatch[it->second] = p;
+    }
+    int64_t untagged = 0;
+    for (int32_t f = 0; f < m.n_faces; ++f)
+        if (m.fr[f] == -1 && m.fpatch[f] == -1) ++untagged;
+    if (untagged) fail(kBadMesh, "mesh: " + std::to_string(untagged) + " boundary faces have no patch");
+    m.compute_face_geometry();
+    for (int32_t f = 0; f < m.n_faces; ++f)
+        if (!(m.farea[f] > 0.0) || !std::isfinite(m.farea[f]))
+            fail(kBadMesh, "mesh: face " + std::to_string(f) + " has zero or non-finite length");
+}
+
+void build_from_faces(HostMesh& m, int32_t n_nodes, const double* xy, int32_t n_faces, const int32_t* face_nodes,
+                      const int32_t* face_cells, const int32_t* face_patch, int32_t n_cells,
+                      const int32_t* cell_face_off, const int32_t* cell_faces, const double* cell_geom,
+                      int32_t n_patches) {
+    if (n_nodes <= 0 || n_cells <= 0 || n_faces <= 0 || !xy || !face_nodes || !face_cells || !face_patch ||
+        !cell_face_off || !cell_faces || !cell_geom)
+        fail(kBadArg, "mesh: empty or null input");
+    m.n_nodes = n_nodes; m.n_cells = n_cells; m.n_faces = n_faces; m.n_patches = n_patches;
+    m.nx_.resize(n_nodes); m.ny_.resize(n_nodes);
+    for (int32_t i = 0; i < n_nodes; ++i) { m.nx_[i] = xy[2 * i]; m.ny_[i] = xy[2 * i + 1]; }
+    m.fn1.resize(n_faces); m.fn2.resize(n_faces); m.fl.resize(n_faces); m.fr.resize(n_faces);
+    m.fpatch.resize(n_faces);
+    for (int32_t f = 0; f < n_faces; ++f) {
+        m.fn1[f] = face_nodes[2 * f]; m.fn2[f] = face_nodes[2 * f + 1];
+        m.fl[f] = face_cells[2 * f]; m.fr[f] = face_cells[2 * f + 1];
+        m.fpatch[f] = face_patch[f];
+        if (m.fn1[f] < 0 || m.fn1[f] >= n_nodes || m.fn2[f] < 0 || m.fn2[f] >= n_nodes)
+            fail(kBadMesh, "mesh: face node index out of range");
+        if (m.fl[f] < 0 || m.fl[f] >= n_cells || m.fr[f] < -1 || m.fr[f] >= n_cells)
+            fail(kBadMesh, "mesh: face cell index out of range");
+        if (m.fr[f] == -1 && (m.fpatch[f] < 0 || m.fpatch[f] >= n_patches))
+            fail(kBadMesh, "mesh: boundary face " + std::to_string(f) + " has no valid patch");
+    }
+    m.cf_off.assign(cell_face_off, cell_face_off + n_cells + 1);
+    if (m.cf_off[0] != 0) fail(kBadArg, "mesh: cell_face_off[0] != 0");
+    m.cf.assign(cell_faces, cell_faces + m.cf_off[n_cells]);
+    for (int32_t c = 0; c < n_cells; ++c)
+        for (int32_t e = m.cf_off[c]; e < m.cf_off[c + 1]; ++e) {
+            int32_t f = m.cf[e];
+            if (f < 0 || f >= n_faces || (m.fl[f] != c && m.fr[f] != c))
+                fail(kBadMesh, "mesh: cell " + std::to_string(c) + " lists a face it does not bound");
+        }
+    m.vol.resize(n_cells); m.cx.resize(n_cells); m.cy.resize(n_cells);
+    for (int32_t c = 0; c < n_cells; ++c) {
+        m.vol[c] = cell_geom[3 * c]; m.cx[c] = cell_geom[3 * c + 1]; m.cy[c] = cell_geom[3 * c + 2];
+        if (!(m.vol[c] > 0.0) || !std::isfinite(m.vol[c])) fail(kBadMesh, "mesh: non-positive cell volume");
+    }
+    m.compute_face_geometry();
+    for (int32_t f = 0; f < n_faces; ++f)
+        if (!(m.farea[f] > 0.0) || !std::isfinite(m.farea[f])) fail(kBadMesh, "mesh: zero-length face");
+}
+
+namespace {
+
+uint64_t interleave32(uint32_t x, uint32_t y) {
+    auto spread = [](uint64_t v) {
+        v &= 0xffffffffull;
+        v = (v | (v << 16)) & 0x0000ffff0000ffffull;
+        v = (v | (v << 8)) & 0x00ff00ff00ff00ffull;
+        v = (v | (v << 4)) & 0x0f0f0f0f0f0f0f0full;
+        v = (v | (v << 2)) & 0x3333333333333333ull;
+        v = (v | (v << 1)) & 0x5555555555555555ull;
+        return v;
+    };
+    return spread(x) | (spread(y) << 1);
+}
+
+std::vector<int32_t> morton_order(const HostMesh& m) {
+    double xmin = *std::min_element(m.cx.begin(), m.cx.end()), xmax = *std::max_element(m.cx.begin(), m.cx.end());
+    double ymin = *std::min_element(m.cy.begin(), m.cy.end()), ymax = *std::max_element(m.cy.begin(), m.cy.end());
+    double span = std::max(xmax - xmin, ymax - ymin);
+    if (!(span > 0.0)) span = 1.0;
+    double s = 4294967295.0 / span;
+    std::vector<std::pair<uint64_t, int32_t>> key(m.n_cells);
+    for (int32_t c = 0; c < m.n_cells; ++c) {
+        uint32_t qx = (uint32_t)std::min(4294967295.0, (m.cx[c] - xmin) * s);
+        uint32_t qy = (uint32_t)std::min(4294967295.0, (m.cy[c] - ymin) * s);
+        key[c] = {interleave32(qx, qy), c};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int32_t> perm(m.n_cells);
+    for (int32_t i = 0; i < m.n_cells; ++i) perm[i] = key[i].second;
+    return perm;
+}
+
+// Reverse Cuthill-McKee over the cell adjacency graph (internal faces).
+std::vector<int32_t> rcm_order(const HostMesh& m) {
+    int32_t n = m.n_cells;
+    std::vector<int32_t> deg(n, 0);
+    for (int32_t c = 0; c < n; ++c)
+        for (int32_t e = m.cf_off[c]; e < m.cf_off[c + 1]; ++e)
+            if (m.fr[m.cf[e]] >= 0) ++deg[c];
+    auto neighbors = [&](int32_t c, std::vector<int32_t>& out) {
+        out.clear();
+        for (int32_t e = m.cf_off[c]; e < m.cf_off[c + 1]; ++e) {
+            int32_t f = m.cf[e];
+            if (m.fr[f] < 0) continue;
+            out.push_back(m.fl[f] == c ? m.fr[f] : m.fl[f]);
+        }
+        std::sort(out.begin(), out.end(), [&](int32_t a, int32_t b) { return deg[a] < deg[b] || (deg[a] == deg[b] && a < b); });
+    };
+    std::vector<int32_t> order;
+    order.reserve(n);
+    std::vector<char> seen(n, 0);
+    std::vector<int32_t> nb;
+    auto bfs = [&](int32_t start, std::vector<int32_t>* out) {
+        // Returns the last node reached; appends visit order to *out if given.
+        std::vector<int32_t> local;
+        std::queue<int32_t> q;
+        std::vector<char> s2;
+        std::vector<char>& mark = out ? seen : (s2 = seen, s2);
+        q.push(start); mark[start] = 1;
+        int32_t last = start;
+        while (!q.empty()) {
+            int32_t c = q.front(); q.pop();
+            last = c;
+            if (out) out->push_back(c);
+            neighbors(c, nb);
+            for (int32_t o : nb) if (!mark[o]) { mark[o] = 1; q.push(o); }
+        }
+        return last;
+    };
+    for (int32_t c0 = 0; c0 < n; ++c0) {
+        if (seen[c0]) continue;
+        int32_t far1 = bfs(c0, nullptr);
+        int32_t far2 = bfs(far1, nullptr);
+        bfs(far2, &order);
+    }
+    std::reverse(order.begin(), order.end());
+    return order;
+}
+
+}  // namespace
+
+void HostMesh::build_device_layout(int reorder) {
+    if (reorder == 1) perm = morton_order(*this);
+    else if (reorder == 2) perm = rcm_order(*this);
+    else { perm.resize(n_cells); std::iota(perm.begin(), perm.end(), 0); }
+    iperm.assign(n_cells, 0);
+    for (int32_t i = 0; i < n_cells; ++i) iperm[perm[i]] = i;
+
+    // Faces: internal first sorted by (owner, neighbour) in device order,
+    // then boundary faces sorted by (patch, owner).
+    fperm.resize(n_faces);
+    std::iota(fperm.begin(), fperm.end(), 0);
+    std::sort(fperm.begin(), fperm.end(), [&](int32_t a, int32_t b) {
+        bool ba = fr[a] < 0, bb = fr[b] < 0;
+        if (ba != bb) return !ba;
+        if (ba) {
+            if (fpatch[a] != fpatch[b]) return fpatch[a] < fpatch[b];
+            return iperm[fl[a]] < iperm[fl[b]];
+        }
+        if (iperm[fl[a]] != iperm[fl[b]]) return iperm[fl[a]] < iperm[fl[b]];
+        return iperm[fr[a]] < iperm[fr[b]];
+    });
+    ifperm.assign(n_faces, 0);
+    n_int_faces = 0;
+    for (int32_t i = 0; i < n_faces; ++i) {
+        ifperm[fperm[i]] = i;
+        if (fr[fperm[i]] >= 0) ++n_int_faces;
+    }
+    d_fl.resize(n_faces); d_fr.resize(n_faces); d_fpatch.resize(n_faces);
+    d_fgeom.resize(4 * (size_t)n_faces); d_fmid.resize(2 * (size_t)n_faces);
+    for (int32_t i = 0; i < n_faces; ++i) {
+        int32_t f = fperm[i];
+        d_fl[i] = iperm[fl[f]];
+        d_fr[i] = fr[f] >= 0 ? iperm[fr[f]] : -1;
+        d_fpatch[i] = fpatch[f];
+        d_fgeom[4 * i + 0] = fnx[f];
+        d_fgeom[4 * i + 1] = fny[f];
+        d_fgeom[4 * i + 2] = farea[f];
+        // Characteristic length of the CFL estimate (src/EulerFVMSolver.cpp:151-156).
+        d_fgeom[4 * i + 3] = fr[f] >= 0 ? std::min(vol[fl[f]], vol[fr[f]]) / farea[f] : vol[fl[f]] / farea[f];
+        d_fmid[2 * i] = fxm[f];
+        d_fmid[2 * i + 1] = fym[f];
+    }
+    d_cf_off.assign(n_cells + 1, 0);
+    d_cf.resize(cf.size());
+    d_vol.resize(n_cells); d_cxy.resize(2 * (size_t)n_cells);
+    int32_t pos = 0;
+    for (int32_t i = 0; i < n_cells; ++i) {
+        int32_t c = perm[i];
+        d_vol[i] = vol[c];
+        d_cxy[2 * i] = cx[c];
+        d_cxy[2 * i + 1] = cy[c];
+        for (int32_t e = cf_off[c]; e < cf_off[c + 1]; ++e) {
+            int32_t f = cf[e];
+            d_cf[pos++] = (ifperm[f] << 1) | (fl[f] == c ? 1 : 0);
+        }
+        d_cf_off[i + 1] = pos;
+    }
+}
+
+}  // namespace fvgb

@@ -1,0 +1,52 @@
+// Host-side mesh: topology derivation, geometry, validation and the
+// reordered structure-of-arrays layout that the device kernels read.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace fvgb {
+
+struct MeshError {
+    int code;
+    std::string msg;
+};
+
+// Mesh in reference numbering (the fields of include/UnstructuredMesh.h:20-106
+// as plain arrays), plus the device-order layout derived from it.
+struct HostMesh {
+    // --- reference numbering ---------------------------------------------
+    int32_t n_nodes = 0, n_cells = 0, n_faces = 0, n_patches = 0;
+    std::vector<double> nx_, ny_;                // node coordinates
+    std::vector<int32_t> fn1, fn2, fl, fr, fpatch;
+    std::vector<double> fnx, fny, farea, fxm, fym;
+    std::vector<int32_t> cf_off, cf;              // cell -> faces, reference order
+    std::vector<double> vol, cx, cy;
+
+    // --- device order (perm[new] = reference cell, fperm[new] = ref face) --
+    std::vector<int32_t> perm, iperm, fperm, ifperm;
+    int32_t n_int_faces = 0;                     // faces [0, n_int) are internal
+    // SoA arrays in device order
+    std::vector<int32_t> d_fl, d_fr, d_fpatch;   // right = -1 on boundary faces
+    std::vector<double> d_fgeom;                 // [4F] nx, ny, area, dt-length
+    std::vector<double> d_fmid;                  // [2F] x_mid, y_mid
+    std::vector<int32_t> d_cf_off, d_cf;         // entries: face<<1 | (cell is owner)
+    std::vector<double> d_vol, d_cxy;            // [N], [2N]
+
+    void compute_face_geometry();                // UnstructuredMesh::compute_geometry
+    void build_device_layout(int reorder);
+};
+
+// src/MeshReader.cpp:317-456 (+ validate_mesh_geometry :125-288).
+// Throws MeshError on invalid input.
+void build_from_polygons(HostMesh& m, int32_t n_nodes, const double* xy, int32_t n_cells, const int64_t* cell_off,
+                         const int32_t* cell_nodes, int32_t n_bedges, const int32_t* bedge_nodes,
+                         const int32_t* bedge_patch, int32_t n_patches);
+
+void build_from_faces(HostMesh& m, int32_t n_nodes, const double* xy, int32_t n_faces, const int32_t* face_nodes,
+                      const int32_t* face_cells, const int32_t* face_patch, int32_t n_cells,
+                      const int32_t* cell_face_off, const int32_t* cell_faces, const double* cell_geom,
+                      int32_t n_patches);
+
+}  // namespace fvgb

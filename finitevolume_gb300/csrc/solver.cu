@@ -1,0 +1,543 @@
+// Solver object and the C ABI (include/fv_gb300.h).
+//
+// One solver = one mesh uploaded in device order + the conserved state and
+// its work arrays, all resident in HBM for the solver's lifetime.  Steps are
+// replayed from captured CUDA graphs (one graph per chunk length), so a
+// 3000-step run is ~100 graph launches; everything a graph reads that the
+// host may change (CFL number, step counter) lives in device memory.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "../../include/fv_gb300.h"
+#include "errors.h"
+#include "mesh_host.h"
+#include "solver.h"
+#include "types.h"
+
+using fvgb::HostMesh;
+
+struct fv_mesh_s {
+    HostMesh h;
+};
+
+namespace fvgb {
+
+template <typename T>
+static T* dalloc(size_t n, std::vector<void*>& owned) {
+    void* p = nullptr;
+    FV_CUDA(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+    owned.push_back(p);
+    return static_cast<T*>(p);
+}
+
+template <typename T>
+static T* dupload(const std::vector<T>& v, std::vector<void*>& owned) {
+    T* p = dalloc<T>(v.size(), owned);
+    if (!v.empty()) FV_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+}
+
+Solver::~Solver() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (void* p : owned) cudaFree(p);
+    if (hist) cudaFree(hist);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, double cfl0, const fv_ic_t& ic,
+                  const fv_options_t& o) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) raise(FV_ERR_CUDA, "no CUDA device available");
+    if (n_bcs < hm.n_patches) raise(FV_ERR_BAD_ARG, "fewer boundary conditions than mesh patches");
+    if (hm.n_patches > kMaxPatches) raise(FV_ERR_UNSUPPORTED, "more than 32 boundary patches");
+    if (!(g > 1.0)) raise(FV_ERR_BAD_ARG, "gamma must be > 1");
+    opt = o;
+    if (opt.order != 1 || opt.rk_stages != 1 || opt.viscous || opt.precision != FV_PREC_FP64)
+        raise(FV_ERR_UNSUPPORTED, "this build supports order 1, forward Euler, inviscid FP64");
+    if (opt.flux < 0 || opt.flux > 2) raise(FV_ERR_BAD_ARG, "unknown flux scheme");
+    gamma = g;
+    N = hm.n_cells;
+    F = hm.n_faces;
+    perm = hm.perm;
+    wall_faces.clear();
+    std::memset(&bc, 0, sizeof(bc));
+    bc.n = hm.n_patches;
+    for (int p = 0; p < hm.n_patches; ++p) {
+        const fv_bc_t& b = bcs[p];
+        if (b.type < FV_BC_WALL || b.type > FV_BC_NOSLIP) raise(FV_ERR_BAD_ARG, "unknown boundary type");
+        bc.type[p] = b.type;
+        for (int k = 0; k < 4; ++k) bc.st[p][k] = b.state[k];
+        bc.wall_u[p] = b.wall_u;
+        bc.wall_v[p] = b.wall_v;
+        bc.isothermal[p] = b.isothermal;
+        bc.wall_T[p] = b.wall_T;
+    }
+    // Host copies needed after construction (wall forces in reference numbering).
+    for (int i = hm.n_int_faces; i < F; ++i) {
+        int p = hm.d_fpatch[i];
+        if (bc.type[p] == FV_BC_WALL || bc.type[p] == FV_BC_NOSLIP) {
+            int f = hm.fperm[i];
+            wall_faces.push_back({hm.fl[f], hm.fnx[f], hm.fny[f], hm.farea[f], hm.fxm[f], hm.fym[f]});
+        }
+    }
+
+    FV_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    own_stream = true;
+
+    DevMesh& m = dm;
+    m.n_cells = N;
+    m.n_faces = F;
+    m.n_int_faces = hm.n_int_faces;
+    m.fl = dupload(hm.d_fl, owned);
+    m.fr = dupload(hm.d_fr, owned);
+    m.fpatch = dupload(hm.d_fpatch, owned);
+    m.fgeom = reinterpret_cast<const double4_32a*>(dupload(hm.d_fgeom, owned));
+    m.fmid = reinterpret_cast<const double2*>(dupload(hm.d_fmid, owned));
+    m.cf_off = dupload(hm.d_cf_off, owned);
+    m.cf = dupload(hm.d_cf, owned);
+    m.vol = dupload(hm.d_vol, owned);
+    m.cxy = reinterpret_cast<const double2*>(dupload(hm.d_cxy, owned));
+
+    U = dalloc<St>(N, owned);
+    ff = dalloc<St>(F, owned);
+    dtf = dalloc<double>(F, owned);
+    n_cell_blocks = (N + kCellBlock - 1) / kCellBlock;
+    partials = dalloc<double>(4 * (size_t)n_cell_blocks, owned);
+    ctl = dalloc<StepCtl>(1, owned);
+    StepCtl c0;
+    std::memset(&c0, 0, sizeof(c0));
+    c0.cfl = cfl0;
+    double dmax = DBL_MAX;
+    std::memcpy(&c0.dt_bits, &dmax, sizeof(dmax));
+    FV_CUDA(cudaMemcpy(ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice));
+    ensure_history(64);
+
+    // Initial condition, reference numbering then device order
+    // (src/EulerFVMSolver.cpp:24-37).
+    std::vector<St> u0(N);
+    for (int c = 0; c < N; ++c) {
+        double r, u, v, p;
+        if (!ic.two_region) { r = ic.rho; u = ic.u; v = ic.v; p = ic.p; }
+        else if (hm.cx[c] < ic.x0) { r = ic.rho_l; u = ic.u_l; v = ic.v_l; p = ic.p_l; }
+        else { r = ic.rho_r; u = ic.u_r; v = ic.v_r; p = ic.p_r; }
+        St s;
+        s.r = r;
+        s.ru = r * u;
+        s.rv = r * v;
+        s.E = p / (g - 1.0) + 0.5 * r * (u * u + v * v);
+        u0[c] = s;
+    }
+    upload_field(u0.data());
+}
+
+void Solver::ensure_history(int n) {
+    if (hist && hist_cap >= n) return;
+    int cap = std::max(64, n);
+    double* h = nullptr;
+    FV_CUDA(cudaMalloc(&h, sizeof(double) * 4 * (size_t)cap));
+    FV_CUDA(cudaMemsetAsync(h, 0, sizeof(double) * 4 * (size_t)cap, stream));
+    FV_CUDA(cudaStreamSynchronize(stream));
+    if (hist) cudaFree(hist);
+    hist = h;
+    hist_cap = cap;
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+}
+
+O1Args Solver::o1_args() const {
+    O1Args a;
+    a.m = dm;
+    a.U = U;
+    a.ff = ff;
+    a.dtf = dtf;
+    a.ctl = ctl;
+    a.partials = partials;
+    a.hist = hist;
+    a.hist_cap = hist_cap;
+    a.bc = bc;
+    a.gamma = gamma;
+    a.exact_tol = opt.exact_tol;
+    a.exact_max_iter = opt.exact_max_iter;
+    a.flux = opt.flux;
+    a.local_dt = opt.dt_mode == FV_DT_LOCAL;
+    return a;
+}
+
+void Solver::launch_step() {
+    O1Args a = o1_args();
+    if (opt.strict) strict::launch_o1_step(a, stream);
+    else fast::launch_o1_step(a, stream);
+}
+
+cudaGraphExec_t Solver::graph_for(int k) {
+    auto it = graphs.find(k);
+    if (it != graphs.end()) return it->second;
+    cudaGraph_t g = nullptr;
+    FV_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < k; ++i) launch_step();
+    FV_CUDA(cudaStreamEndCapture(stream, &g));
+    cudaGraphExec_t ge = nullptr;
+    FV_CUDA(cudaGraphInstantiate(&ge, g, 0));
+    cudaGraphDestroy(g);
+    graphs[k] = ge;
+    return ge;
+}
+
+void Solver::step_async(int n) {
+    if (n < 0) raise(FV_ERR_BAD_ARG, "negative step count");
+    ensure_history(std::min(n, 1 << 20));
+    const int chunk = kGraphChunk;
+    int q = n / chunk, r = n % chunk;
+    if (q) {
+        cudaGraphExec_t ge = graph_for(chunk);
+        for (int i = 0; i < q; ++i) FV_CUDA(cudaGraphLaunch(ge, stream));
+    }
+    if (r) FV_CUDA(cudaGraphLaunch(graph_for(r), stream));
+    steps_taken += n;
+}
+
+void Solver::read_ctl(StepCtl& c) {
+    FV_CUDA(cudaMemcpyAsync(&c, ctl, sizeof(c), cudaMemcpyDeviceToHost, stream));
+    FV_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Solver::history(int n, double* out) {
+    if (n > hist_cap) raise(FV_ERR_BAD_ARG, "history longer than the recorded window");
+    StepCtl c;
+    read_ctl(c);
+    std::vector<double> all(4 * (size_t)hist_cap);
+    FV_CUDA(cudaMemcpy(all.data(), hist, all.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) {
+        int s = c.step - n + i;
+        int row = ((s % hist_cap) + hist_cap) % hist_cap;
+        std::memcpy(out + 4 * i, all.data() + 4 * row, 4 * sizeof(double));
+    }
+}
+
+void Solver::download_field(double* out) {
+    std::vector<St> d(N);
+    FV_CUDA(cudaMemcpyAsync(d.data(), U, sizeof(St) * (size_t)N, cudaMemcpyDeviceToHost, stream));
+    FV_CUDA(cudaStreamSynchronize(stream));
+    for (int i = 0; i < N; ++i) {
+        const St& s = d[i];
+        double* o = out + 4 * (size_t)perm[i];
+        o[0] = s.r; o[1] = s.ru; o[2] = s.rv; o[3] = s.E;
+    }
+}
+
+void Solver::upload_field(const void* in_ref_order) {
+    const St* in = static_cast<const St*>(in_ref_order);
+    std::vector<St> d(N);
+    for (int i = 0; i < N; ++i) d[i] = in[perm[i]];
+    FV_CUDA(cudaMemcpyAsync(U, d.data(), sizeof(St) * (size_t)N, cudaMemcpyHostToDevice, stream));
+    // residual() resets to zero (include/EulerFVMSolver.h:151-155)
+    static const double z[4] = {0, 0, 0, 0};
+    static const int zi = 0;
+    FV_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(ctl) + offsetof(StepCtl, norms), z, sizeof(z),
+                            cudaMemcpyHostToDevice, stream));
+    FV_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(ctl) + offsetof(StepCtl, nonfinite), &zi, sizeof(zi),
+                            cudaMemcpyHostToDevice, stream));
+    FV_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Solver::set_cfl(double cfl) {
+    FV_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(ctl) + offsetof(StepCtl, cfl), &cfl, sizeof(cfl),
+                            cudaMemcpyHostToDevice, stream));
+    FV_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Solver::set_stream(void* s) {
+    FV_CUDA(cudaStreamSynchronize(stream));
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    if (own_stream) cudaStreamDestroy(stream);
+    if (s) {
+        stream = static_cast<cudaStream_t>(s);
+        own_stream = false;
+    } else {
+        FV_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+    }
+}
+
+// compute_wall_forces with zero viscosity (src/WallTraction.cpp:163-217):
+// wall pressure is the owner cell's pressure (include/WallTraction.h:59-66).
+void Solver::wall_forces(const double ref[7], double out[11]) {
+    std::vector<double> f(4 * (size_t)N);
+    download_field(f.data());
+    double vmag = std::hypot(ref[1], ref[2]);
+    double dx = ref[1] / vmag, dy = ref[2] / vmag;
+    double lx = -dy, ly = dx;
+    double qL = 0.5 * ref[0] * vmag * vmag * ref[4];
+    double qL2 = qL * ref[4];
+    double fd = 0, pd = 0, td = 0, lift = 0, mom = 0;
+    for (const WallFace& w : wall_faces) {
+        const double* s = f.data() + 4 * (size_t)w.cell;
+        double u = s[1] / s[0], v = s[2] / s[0];
+        double p = (gamma - 1.0) * (s[3] - 0.5 * s[0] * (u * u + v * v));
+        double fx = 0.0, fy = 0.0;  // friction: zero for the inviscid solver
+        double px = w.area * p * w.nx, py = w.area * p * w.ny;
+        double rx = w.xm - ref[5], ry = w.ym - ref[6];
+        double dfx = fx + px, dfy = fy + py;
+        double fdi = fx * dx + fy * dy, pdi = px * dx + py * dy;
+        fd += fdi;
+        pd += pdi;
+        td += fdi + pdi;
+        lift += (fx + px) * lx + (fy + py) * ly;
+        mom += rx * dfy - ry * dfx;
+    }
+    out[0] = fd; out[1] = pd; out[2] = td; out[3] = lift; out[4] = mom;
+    out[5] = fd / qL; out[6] = pd / qL; out[7] = td / qL; out[8] = lift / qL; out[9] = mom / qL2;
+    out[10] = (double)wall_faces.size();
+}
+
+}  // namespace fvgb
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using fvgb::Solver;
+
+struct fv_solver_s {
+    Solver s;
+};
+
+template <typename Fn>
+static int guarded(Fn&& fn) {
+    try {
+        fn();
+        return FV_OK;
+    } catch (const fvgb::Error& e) {
+        fvgb::set_last_error(e.msg);
+        return e.code;
+    } catch (const fvgb::MeshError& e) {
+        fvgb::set_last_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        fvgb::set_last_error("host allocation failed");
+        return FV_ERR_BAD_ARG;
+    } catch (const std::exception& e) {
+        fvgb::set_last_error(e.what());
+        return FV_ERR_BAD_ARG;
+    }
+}
+
+extern "C" {
+
+const char* fv_last_error(void) { return fvgb::last_error(); }
+int fv_abi_version(void) { return 100; }
+int fv_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int fv_mesh_create_polygons(int32_t n_nodes, const double* xy, int32_t n_cells, const int64_t* cell_off,
+                            const int32_t* cell_nodes, int32_t n_bedges, const int32_t* bedge_nodes,
+                            const int32_t* bedge_patch, int32_t n_patches, int32_t reorder, fv_mesh_t* out) {
+    return guarded([&] {
+        if (!out) fvgb::raise(FV_ERR_BAD_ARG, "null output handle");
+        auto m = std::make_unique<fv_mesh_s>();
+        fvgb::build_from_polygons(m->h, n_nodes, xy, n_cells, cell_off, cell_nodes, n_bedges, bedge_nodes,
+                                  bedge_patch, n_patches);
+        m->h.build_device_layout(reorder);
+        *out = m.release();
+    });
+}
+
+int fv_mesh_create_faces(int32_t n_nodes, const double* xy, int32_t n_faces, const int32_t* face_nodes,
+                         const int32_t* face_cells, const int32_t* face_patch, int32_t n_cells,
+                         const int32_t* cell_face_off, const int32_t* cell_faces, const double* cell_geom,
+                         int32_t n_patches, int32_t reorder, fv_mesh_t* out) {
+    return guarded([&] {
+        if (!out) fvgb::raise(FV_ERR_BAD_ARG, "null output handle");
+        auto m = std::make_unique<fv_mesh_s>();
+        fvgb::build_from_faces(m->h, n_nodes, xy, n_faces, face_nodes, face_cells, face_patch, n_cells,
+                               cell_face_off, cell_faces, cell_geom, n_patches);
+        m->h.build_device_layout(reorder);
+        *out = m.release();
+    });
+}
+
+int fv_mesh_counts(fv_mesh_t mesh, int64_t counts[5]) {
+    return guarded([&] {
+        if (!mesh || !counts) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        const HostMesh& h = mesh->h;
+        counts[0] = h.n_cells;
+        counts[1] = h.n_faces;
+        counts[2] = h.n_faces - h.n_int_faces;
+        counts[3] = h.n_patches;
+        counts[4] = (int64_t)h.cf.size();
+    });
+}
+
+int fv_mesh_export(fv_mesh_t mesh, int32_t* face_i32, double* face_f64, double* cell_f64, int32_t* cell_face_off,
+                   int32_t* cell_faces) {
+    return guarded([&] {
+        if (!mesh) fvgb::raise(FV_ERR_BAD_ARG, "null mesh");
+        const HostMesh& h = mesh->h;
+        for (int32_t f = 0; f < h.n_faces; ++f) {
+            if (face_i32) {
+                int32_t* o = face_i32 + 5 * (size_t)f;
+                o[0] = h.fn1[f]; o[1] = h.fn2[f]; o[2] = h.fl[f]; o[3] = h.fr[f]; o[4] = h.fpatch[f];
+            }
+            if (face_f64) {
+                double* o = face_f64 + 5 * (size_t)f;
+                o[0] = h.fnx[f]; o[1] = h.fny[f]; o[2] = h.farea[f]; o[3] = h.fxm[f]; o[4] = h.fym[f];
+            }
+        }
+        for (int32_t c = 0; c < h.n_cells; ++c)
+            if (cell_f64) {
+                cell_f64[3 * (size_t)c] = h.vol[c];
+                cell_f64[3 * (size_t)c + 1] = h.cx[c];
+                cell_f64[3 * (size_t)c + 2] = h.cy[c];
+            }
+        if (cell_face_off) std::copy(h.cf_off.begin(), h.cf_off.end(), cell_face_off);
+        if (cell_faces) std::copy(h.cf.begin(), h.cf.end(), cell_faces);
+    });
+}
+
+int fv_mesh_permutation(fv_mesh_t mesh, int32_t* perm) {
+    return guarded([&] {
+        if (!mesh || !perm) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        std::copy(mesh->h.perm.begin(), mesh->h.perm.end(), perm);
+    });
+}
+
+int fv_mesh_destroy(fv_mesh_t mesh) {
+    delete mesh;
+    return FV_OK;
+}
+
+void fv_options_default(fv_options_t* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->flux = FV_FLUX_RUSANOV;
+    o->order = 1;
+    o->gradient = FV_GRAD_LSQ;
+    o->limiter = FV_LIM_VENKAT;
+    o->venkat_k = 5.0;
+    o->rk_stages = 1;
+    o->dt_mode = FV_DT_GLOBAL;
+    o->precision = FV_PREC_FP64;
+    o->strict = 0;
+    o->exact_tol = 1e-6;
+    o->exact_max_iter = 20;
+    o->viscous = 0;
+    o->gas_constant = 287.0;
+    o->mu = 0.0;
+    o->prandtl = 0.72;
+}
+
+int fv_solver_create(fv_mesh_t mesh, const fv_bc_t* bcs, int32_t n_bcs, double gamma, double cfl, const fv_ic_t* ic,
+                     const fv_options_t* opt, fv_solver_t* out) {
+    return guarded([&] {
+        if (!mesh || !out || !ic || (!bcs && mesh->h.n_patches > 0)) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        fv_options_t o;
+        if (opt) o = *opt;
+        else fv_options_default(&o);
+        auto s = std::make_unique<fv_solver_s>();
+        s->s.init(mesh->h, bcs, n_bcs, gamma, cfl, *ic, o);
+        *out = s.release();
+    });
+}
+
+int fv_solver_destroy(fv_solver_t s) {
+    delete s;
+    return FV_OK;
+}
+
+int fv_solver_set_stream(fv_solver_t s, void* stream) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        s->s.set_stream(stream);
+    });
+}
+
+int fv_step_async(fv_solver_t s, int32_t n) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        s->s.step_async(n);
+    });
+}
+
+int fv_step(fv_solver_t s, int32_t n, double* history) {
+    int rc = guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        s->s.step_async(n);
+        fvgb::StepCtl c;
+        s->s.read_ctl(c);
+        if (history && n > 0) s->s.history(n, history);
+        if (c.nonfinite) fvgb::raise(FV_ERR_NONFINITE, "non-finite residual norm");
+    });
+    return rc;
+}
+
+int fv_get_history(fv_solver_t s, int32_t n, double* history) {
+    return guarded([&] {
+        if (!s || !history || n < 0) fvgb::raise(FV_ERR_BAD_ARG, "bad argument");
+        s->s.history(n, history);
+    });
+}
+
+int fv_get_field(fv_solver_t s, double* U) {
+    return guarded([&] {
+        if (!s || !U) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        s->s.download_field(U);
+    });
+}
+
+int fv_set_field(fv_solver_t s, const double* U) {
+    return guarded([&] {
+        if (!s || !U) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        s->s.upload_field(U);
+    });
+}
+
+int fv_get_residual(fv_solver_t s, double norms[4]) {
+    return guarded([&] {
+        if (!s || !norms) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        fvgb::StepCtl c;
+        s->s.read_ctl(c);
+        for (int k = 0; k < 4; ++k) norms[k] = c.norms[k];
+    });
+}
+
+int fv_set_cfl(fv_solver_t s, double cfl) {
+    return guarded([&] {
+        if (!s || !(cfl > 0.0)) fvgb::raise(FV_ERR_BAD_ARG, "bad argument");
+        s->s.set_cfl(cfl);
+    });
+}
+
+int fv_get_gamma(fv_solver_t s, double* g) {
+    return guarded([&] {
+        if (!s || !g) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        *g = s->s.gamma;
+    });
+}
+
+int fv_device_state(fv_solver_t s, void** U_dev, void** stream) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        if (U_dev) *U_dev = s->s.U;
+        if (stream) *stream = s->s.stream;
+    });
+}
+
+int fv_wall_forces(fv_solver_t s, const double ref[7], double out[11]) {
+    return guarded([&] {
+        if (!s || !ref || !out) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        s->s.wall_forces(ref, out);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,60 @@
+// Solver state held behind an fv_solver_t handle.
+#pragma once
+
+#include <map>
+#include <vector>
+
+#include "../../include/fv_gb300.h"
+#include "mesh_host.h"
+#include "types.h"
+
+namespace fvgb {
+
+struct WallFace {
+    int cell;  // owner cell, reference numbering
+    double nx, ny, area, xm, ym;
+};
+
+struct Solver {
+    static constexpr int kGraphChunk = 32;
+
+    fv_options_t opt{};
+    double gamma = 1.4;
+    int N = 0, F = 0, n_cell_blocks = 0;
+    std::vector<int32_t> perm;  // device cell -> reference cell
+    std::vector<WallFace> wall_faces;
+    BCTable bc{};
+    DevMesh dm{};
+
+    St* U = nullptr;
+    St* ff = nullptr;
+    double* dtf = nullptr;
+    double* partials = nullptr;
+    double* hist = nullptr;
+    int hist_cap = 0;
+    StepCtl* ctl = nullptr;
+    long long steps_taken = 0;
+
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::map<int, cudaGraphExec_t> graphs;
+    std::vector<void*> owned;
+
+    ~Solver();
+    void init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, double cfl, const fv_ic_t& ic,
+              const fv_options_t& o);
+    void ensure_history(int n);
+    O1Args o1_args() const;
+    void launch_step();
+    cudaGraphExec_t graph_for(int k);
+    void step_async(int n);
+    void read_ctl(StepCtl& c);
+    void history(int n, double* out);
+    void download_field(double* out);
+    void upload_field(const void* in_ref_order);
+    void set_cfl(double cfl);
+    void set_stream(void* s);
+    void wall_forces(const double ref[7], double out[11]);
+};
+
+}  // namespace fvgb

@@ -1,0 +1,411 @@
+"""Seeded synthetic mesh generators for the benchmark and parity cases.
+
+All generators return a :class:`~finitevolume_gb300.fvmesh.PolyMesh` with
+counter-clockwise cells and tagged boundary edges, ready for
+``write_fvmesh`` (reference side) and ``Mesh.from_polymesh`` (GPU side).
+
+* :func:`naca_ogrid`     NACA 4-digit O-grid (closed trailing edge, geometric
+                         wall-normal stretching, circular farfield)
+* :func:`naca_mixed`     O-grid core + a Lloyd-relaxed polygonal outer region
+                         (dual of a Delaunay triangulation, 3-9 sided cells)
+* :func:`sod_strip`      randomly perturbed triangle strip (shock tube)
+* :func:`wavy_quads`     non-affine ("wavy") structured quads, for gradient
+                         exactness checks
+* :func:`cartesian`      plain structured quads
+
+NACA sections come from the public 4-digit formula (thickness polynomial with
+the -0.1036 x^4 coefficient that closes the trailing edge).
+"""
+from __future__ import annotations
+
+import math
+from typing import Tuple
+
+import numpy as np
+
+from .fvmesh import PolyMesh, from_cells, signed_areas
+
+
+# --------------------------------------------------------------------------
+# NACA 4-digit geometry
+# --------------------------------------------------------------------------
+def naca4(code: str, x: np.ndarray) -> Tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+    """Upper and lower surface coordinates at chord stations ``x`` in [0, 1]."""
+    m = int(code[0]) / 100.0
+    p = int(code[1]) / 10.0
+    t = int(code[2:]) / 100.0
+    return naca4_params(m, p, t, x)
+
+
+def naca4_params(m: float, p: float, t: float, x: np.ndarray):
+    yt = 5.0 * t * (0.2969 * np.sqrt(x) - 0.1260 * x - 0.3516 * x**2 + 0.2843 * x**3 - 0.1036 * x**4)
+    if m > 0.0 and p > 0.0:
+        yc = np.where(x < p, m / p**2 * (2 * p * x - x**2), m / (1 - p)**2 * ((1 - 2 * p) + 2 * p * x - x**2))
+        dyc = np.where(x < p, 2 * m / p**2 * (p - x), 2 * m / (1 - p)**2 * (p - x))
+    else:
+        yc = np.zeros_like(x)
+        dyc = np.zeros_like(x)
+    th = np.arctan(dyc)
+    xu, yu = x - yt * np.sin(th), yc + yt * np.cos(th)
+    xl, yl = x + yt * np.sin(th), yc - yt * np.cos(th)
+    return xu, yu, xl, yl
+
+
+def airfoil_loop(ni: int, m: float = 0.0, p: float = 0.0, t: float = 0.12) -> np.ndarray:
+    """``ni`` surface points, TE -> upper -> LE -> lower, counter-clockwise.
+
+    Cosine clustering in chord; point 0 is the (closed) trailing edge.
+    """
+    if ni % 2:
+        raise ValueError("ni must be even")
+    h = ni // 2
+    s_up = np.linspace(1.0, 0.0, h + 1)          # TE .. LE inclusive
+    s_lo = np.linspace(0.0, 1.0, h + 1)[1:-1]    # LE .. TE exclusive
+    xu_c = 0.5 * (1.0 - np.cos(np.pi * s_up))
+    xl_c = 0.5 * (1.0 - np.cos(np.pi * s_lo))
+    xu, yu, _, _ = naca4_params(m, p, t, xu_c)
+    _, _, xl, yl = naca4_params(m, p, t, xl_c)
+    pts = np.concatenate([np.stack([xu, yu], 1), np.stack([xl, yl], 1)], 0)
+    pts[0] = (1.0, 0.0)
+    pts[h] = (0.0, 0.0)
+    return pts
+
+
+def _stretch(n: int, first: float, total: float) -> np.ndarray:
+    """Cumulative distances 0..total over n geometric intervals, first = ``first``."""
+    if first * n >= total:
+        return np.linspace(0.0, total, n + 1)
+    lo, hi = 1.0 + 1e-12, 2.0
+    for _ in range(200):
+        g = 0.5 * (lo + hi)
+        s = first * (g**n - 1.0) / (g - 1.0)
+        lo, hi = (g, hi) if s < total else (lo, g)
+    g = 0.5 * (lo + hi)
+    d = first * (g ** np.arange(n + 1) - 1.0) / (g - 1.0)
+    return d * (total / d[-1])
+
+
+def _ogrid_nodes(ni: int, nj: int, first: float, r_out: float, center=(0.5, 0.0), m=0.0, p=0.0, t=0.12):
+    """O-grid node array [nj+1, ni, 2]; ring nj lies on the circle r_out."""
+    s = airfoil_loop(ni, m, p, t)
+    c = np.asarray(center)
+    # Outward unit normals (right of the CCW traversal), central differences.
+    tang = np.roll(s, -1, axis=0) - np.roll(s, 1, axis=0)
+    nrm = np.stack([tang[:, 1], -tang[:, 0]], 1)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    theta = 2.0 * np.pi * np.arange(ni) / ni
+    circ = c + r_out * np.stack([np.cos(theta), np.sin(theta)], 1)
+    dist = np.linalg.norm(circ - s, axis=1)
+    d = _stretch(nj, first, float(dist.mean()))
+    f = d / d[-1]
+    w = f ** 0.5
+    nodes = np.empty((nj + 1, ni, 2))
+    for j in range(nj + 1):
+        pn = s + (d[j] * dist / d[-1])[:, None] * nrm
+        ps = s + f[j] * (circ - s)
+        nodes[j] = (1.0 - w[j]) * pn + w[j] * ps
+    nodes[nj] = circ
+    return nodes
+
+
+def naca_ogrid(ni: int = 256, nj: int = 128, first: float = 1e-3, r_far: float = 20.0,
+               code: str = "0012") -> PolyMesh:
+    """NACA 4-digit O-grid: ``ni`` cells around, ``nj`` radially.
+
+    Patches: ``airfoil`` (the wall) and ``farfield`` (circle of radius
+    ``r_far`` chords about mid-chord).
+    """
+    m, p, t = int(code[0]) / 100.0, int(code[1]) / 10.0, int(code[2:]) / 100.0
+    nodes3 = _ogrid_nodes(ni, nj, first, r_far, m=m, p=p, t=t)
+    nodes = nodes3.reshape(-1, 2)
+    jj, ii = np.meshgrid(np.arange(nj), np.arange(ni), indexing="ij")
+    a = jj * ni + ii
+    b = jj * ni + (ii + 1) % ni
+    cells = np.stack([a, b, b + ni, a + ni], -1).reshape(-1, 4)
+    wall = np.stack([np.arange(ni), (np.arange(ni) + 1) % ni], 1)
+    far = nj * ni + wall
+    mesh = from_cells(nodes, cells, np.concatenate([wall, far]),
+                      np.r_[np.zeros(ni, np.int32), np.ones(ni, np.int32)], ["airfoil", "farfield"])
+    _orient(mesh)
+    return mesh
+
+
+def _orient(mesh: PolyMesh) -> None:
+    """Reverse the vertex order of any clockwise cell in place."""
+    a = signed_areas(mesh)
+    bad = np.nonzero(a < 0.0)[0]
+    for c in bad:
+        lo, hi = mesh.cell_off[c], mesh.cell_off[c + 1]
+        mesh.cell_nodes[lo:hi] = mesh.cell_nodes[lo:hi][::-1]
+
+
+# --------------------------------------------------------------------------
+# Mixed mesh: O-grid core + Lloyd-relaxed polygonal outer region
+# --------------------------------------------------------------------------
+def _circumcenters(p: np.ndarray, tri: np.ndarray) -> np.ndarray:
+    a, b, c = p[tri[:, 0]], p[tri[:, 1]], p[tri[:, 2]]
+    ax, ay = a[:, 0], a[:, 1]
+    bx, by = b[:, 0] - ax, b[:, 1] - ay
+    cx, cy = c[:, 0] - ax, c[:, 1] - ay
+    d = 2.0 * (bx * cy - by * cx)
+    b2, c2 = bx * bx + by * by, cx * cx + cy * cy
+    ux = (cy * b2 - by * c2) / d
+    uy = (bx * c2 - cx * b2) / d
+    return np.stack([ax + ux, ay + uy], 1)
+
+
+def _fans(tri: np.ndarray, pts: np.ndarray, vert_xy: np.ndarray, n_vert: int):
+    """Group (vertex, triangle) incidences by vertex, sorted by angle.
+
+    Returns (order, starts): ``order`` lists triangle ids, grouped per vertex
+    0..n_vert-1 and sorted counter-clockwise by the angle of ``pts[t]`` about
+    ``vert_xy[v]``; ``starts[v]:starts[v+1]`` is vertex v's group.
+    """
+    v = tri.reshape(-1)
+    t = np.repeat(np.arange(tri.shape[0]), 3)
+    keep = v < n_vert
+    v, t = v[keep], t[keep]
+    d = pts[t] - vert_xy[v]
+    ang = np.arctan2(d[:, 1], d[:, 0])
+    o = np.lexsort((ang, v))
+    counts = np.bincount(v, minlength=n_vert)
+    starts = np.zeros(n_vert + 1, dtype=np.int64)
+    np.cumsum(counts, out=starts[1:])
+    return t[o], starts, v[o]
+
+
+def _poly_centroids(poly_xy: np.ndarray, starts: np.ndarray) -> np.ndarray:
+    """Centroids of closed polygons given as grouped vertex lists."""
+    n = starts.size - 1
+    sizes = np.diff(starts)
+    idx = np.arange(poly_xy.shape[0])
+    nxt = idx + 1
+    nxt[starts[1:] - 1] = starts[:-1]
+    p0, p1 = poly_xy, poly_xy[nxt]
+    cr = p0[:, 0] * p1[:, 1] - p1[:, 0] * p0[:, 1]
+    g = np.repeat(np.arange(n), sizes)
+    a = np.bincount(g, cr, n) * 0.5
+    cx = np.bincount(g, (p0[:, 0] + p1[:, 0]) * cr, n) / (6.0 * a)
+    cy = np.bincount(g, (p0[:, 1] + p1[:, 1]) * cr, n) / (6.0 * a)
+    return np.stack([cx, cy], 1)
+
+
+def _periodic_delaunay(fixed: np.ndarray, free: np.ndarray, period: float, band: float):
+    """Delaunay of points periodic in y; returns (triangles over base ids, n_base).
+
+    Base ids: free points first, then fixed points.  Triangles are kept once
+    (centroid y in [0, period)).
+    """
+    from scipy.spatial import Delaunay
+
+    base = np.concatenate([free, fixed], 0)
+    nb = base.shape[0]
+    lo = base[:, 1] < band
+    hi = base[:, 1] >= period - band
+    ext = np.concatenate([base, base[lo] + [0.0, period], base[hi] - [0.0, period]], 0)
+    ids = np.concatenate([np.arange(nb), np.nonzero(lo)[0], np.nonzero(hi)[0]])
+    tri = Delaunay(ext).simplices
+    cy = ext[tri, 1].mean(1)
+    tri = tri[(cy >= 0.0) & (cy < period)]
+    return tri, ids, ext
+
+
+def naca_mixed(ni: int = 1024, nj: int = 512, first: float = 1e-3, r_core: float = 2.0,
+               r_far: float = 20.0, code: str = "0012", lloyd_iters: int = 4, seed: int = 0) -> PolyMesh:
+    """NACA O-grid core of ni x nj quads, surrounded by a polygonal region.
+
+    The outer region (r_core < r < r_far about mid-chord) is built in
+    log-polar coordinates (xi = ln r, eta = angle), where uniform point
+    density gives cells whose size grows in proportion to r.  Seeded uniform
+    random points are relaxed by ``lloyd_iters`` Lloyd iterations
+    (Voronoi-centroid moves, periodic in eta), then triangulated; each point
+    becomes one polygonal cell whose vertices are the centroids of its
+    Delaunay triangles (the centroid dual: always a simple, star-shaped
+    polygon, 3-9 sided after relaxation).  The core's outer ring nodes are
+    the dual's inner boundary vertices: their cells close on the ring edge
+    midpoints, which also become the fifth vertex of the core's outermost
+    quads, so the two regions share faces exactly.
+
+    Patches: ``airfoil`` (wall), ``farfield``.
+    """
+    rng = np.random.default_rng(seed)
+    m, p, t = int(code[0]) / 100.0, int(code[1]) / 10.0, int(code[2:]) / 100.0
+    center = np.array([0.5, 0.0])
+    core = _ogrid_nodes(ni, nj, first, r_core, center=center, m=m, p=p, t=t)
+
+    two_pi = 2.0 * np.pi
+    dlt = two_pi / ni
+    xi0, xi1 = math.log(r_core), math.log(r_far)
+    n_far = ni
+    eta_in = two_pi * np.arange(ni) / ni
+    eta_out = two_pi * (np.arange(n_far) + 0.5) / n_far
+    row = dlt * math.sqrt(3.0) / 2.0
+    ring_in = np.stack([np.full(ni, xi0), eta_in], 1)
+    ring_out = np.stack([np.full(n_far, xi1), eta_out], 1)
+    ghost_in = np.stack([np.full(ni, xi0 - row), eta_in + 0.5 * dlt], 1) % [np.inf, two_pi]
+    ghost_out = np.stack([np.full(n_far, xi1 + row), eta_out + 0.5 * dlt], 1) % [np.inf, two_pi]
+    fixed = np.concatenate([ring_in, ring_out, ghost_in, ghost_out], 0)
+
+    area = (xi1 - xi0 - 2 * 0.5 * dlt) * two_pi
+    n_free = int(round(area / (dlt * dlt * math.sqrt(3.0) / 2.0)))
+    free = np.stack([rng.uniform(xi0 + 0.5 * dlt, xi1 - 0.5 * dlt, n_free),
+                     rng.uniform(0.0, two_pi, n_free)], 1)
+    band = 12.0 * dlt
+    for _ in range(lloyd_iters):
+        tri, ids, ext = _periodic_delaunay(fixed, free, two_pi, band)
+        cc = _circumcenters(ext, tri)
+        vid = ids[tri]
+        order, starts, _ = _fans(vid, cc, np.concatenate([free, fixed]), n_free)
+        cen = _poly_centroids(cc[order], starts)
+        # Clamp so the free points stay strictly inside the band.
+        cen[:, 0] = np.clip(cen[:, 0], xi0 + 0.3 * dlt, xi1 - 0.3 * dlt)
+        free = np.stack([cen[:, 0], cen[:, 1] % two_pi], 1)
+
+    tri, ids, ext = _periodic_delaunay(fixed, free, two_pi, band)
+    vid = ids[tri]
+    n_keep = n_free + ni + n_far          # free, inner ring, outer ring (no ghosts)
+    tri_ok = (vid < n_keep).all(1)
+    vid = vid[tri_ok]
+    base = np.concatenate([free, fixed[:ni + n_far]], 0)
+    phys = center + np.exp(base[:, :1]) * np.stack([np.cos(base[:, 1]), np.sin(base[:, 1])], 1)
+    # The inner ring must coincide with the core's outer ring nodes exactly.
+    phys[n_free:n_free + ni] = core[nj]
+    # Orient every triangle CCW in physical space.
+    a, b, c = phys[vid[:, 0]], phys[vid[:, 1]], phys[vid[:, 2]]
+    cr = (b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0])
+    vid[cr < 0] = vid[cr < 0][:, ::-1]
+    tcen = phys[vid].mean(1)
+    n_tri = vid.shape[0]
+
+    # ---- node numbering of the final mesh --------------------------------
+    n_core = (nj + 1) * ni
+    k_in = np.arange(ni)
+    off_mid_in = n_core
+    off_tri = off_mid_in + ni
+    off_out = off_tri + n_tri
+    off_mid_out = off_out + n_far
+    mid_in = 0.5 * (core[nj][k_in] + core[nj][(k_in + 1) % ni])
+    out_xy = phys[n_free + ni:n_keep]
+    mid_out = 0.5 * (out_xy + np.roll(out_xy, -1, axis=0))
+    nodes = np.concatenate([core.reshape(-1, 2), mid_in, tcen, out_xy, mid_out], 0)
+
+    def node_of_base(v):
+        v = np.asarray(v)
+        return np.where(v < n_free, -1, np.where(v < n_free + ni, nj * ni + (v - n_free), off_out + (v - n_free - ni)))
+
+    cells = []
+    # Core quads j < nj-1 and pentagons at j = nj-1 (outer edge split at the midpoint).
+    for j in range(nj):
+        i = np.arange(ni)
+        a0 = j * ni + i
+        b0 = j * ni + (i + 1) % ni
+        if j < nj - 1:
+            cells.extend(np.stack([a0, b0, b0 + ni, a0 + ni], 1).tolist())
+        else:
+            cells.extend(np.stack([a0, b0, b0 + ni, off_mid_in + i, a0 + ni], 1).tolist())
+    core_cells = len(cells)
+
+    order, starts, _ = _fans(vid, tcen, phys, n_keep)
+    tri_node = off_tri + order
+    # Interior points: closed fans.
+    for v in range(n_free):
+        cells.append(tri_node[starts[v]:starts[v + 1]].tolist())
+    # Ring points: open fans closed by the ring vertex and two edge midpoints.
+    for k in range(ni):
+        v = n_free + k
+        w = phys[v]
+        fan_t = order[starts[v]:starts[v + 1]]
+        outward = w - center
+        outward /= np.linalg.norm(outward)
+        tang = np.array([-outward[1], outward[0]])        # CCW tangent (toward ring k+1)
+        d = tcen[fan_t] - w
+        ang = np.arctan2(d @ outward, d @ tang)           # 0 at +tangent, pi at -tangent
+        fan = off_tri + fan_t[np.argsort(ang)]
+        cells.append([nj * ni + k, off_mid_in + k] + fan.tolist() + [off_mid_in + (k - 1) % ni])
+    for k in range(n_far):
+        v = n_free + ni + k
+        w = phys[v]
+        fan_t = order[starts[v]:starts[v + 1]]
+        inward = center - w
+        inward /= np.linalg.norm(inward)
+        tang = np.array([-inward[1], inward[0]])          # CW along the ring (toward k-1)
+        d = tcen[fan_t] - w
+        ang = np.arctan2(d @ inward, d @ tang)
+        fan = off_tri + fan_t[np.argsort(ang)]
+        cells.append([off_out + k, off_mid_out + (k - 1) % n_far] + fan.tolist() + [off_mid_out + k])
+
+    wall = np.stack([np.arange(ni), (np.arange(ni) + 1) % ni], 1)
+    kk = np.arange(n_far)
+    far = np.concatenate([np.stack([off_out + kk, off_mid_out + kk], 1),
+                          np.stack([off_mid_out + kk, off_out + (kk + 1) % n_far], 1)])
+    mesh = from_cells(nodes, cells, np.concatenate([wall, far]),
+                      np.r_[np.zeros(ni, np.int32), np.ones(far.shape[0], np.int32)], ["airfoil", "farfield"])
+    _orient(mesh)
+    mesh.validate_ccw()
+    return mesh
+
+
+# --------------------------------------------------------------------------
+# Simple test meshes
+# --------------------------------------------------------------------------
+def cartesian(nx: int, ny: int, lx: float = 1.0, ly: float = 1.0) -> PolyMesh:
+    """Structured quads on [0,lx]x[0,ly]; patches bottom,right,top,left."""
+    x = np.linspace(0.0, lx, nx + 1)
+    y = np.linspace(0.0, ly, ny + 1)
+    X, Y = np.meshgrid(x, y)
+    return _structured(np.stack([X.ravel(), Y.ravel()], 1), nx, ny)
+
+
+def wavy_quads(n: int = 8, amp: float = 0.04) -> PolyMesh:
+    """Unit-square quads with a smooth non-affine interior perturbation."""
+    x = np.linspace(0.0, 1.0, n + 1)
+    X, Y = np.meshgrid(x, x)
+    dx = amp * np.sin(2 * np.pi * Y) * np.sin(np.pi * X)
+    dy = amp * np.sin(2 * np.pi * X) * np.sin(np.pi * Y)
+    return _structured(np.stack([(X + dx).ravel(), (Y + dy).ravel()], 1), n, n)
+
+
+def _structured(nodes: np.ndarray, nx: int, ny: int) -> PolyMesh:
+    jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    a = jj * (nx + 1) + ii
+    cells = np.stack([a, a + 1, a + nx + 2, a + nx + 1], -1).reshape(-1, 4)
+    i = np.arange(nx)
+    j = np.arange(ny)
+    bottom = np.stack([i, i + 1], 1)
+    top = np.stack([ny * (nx + 1) + i + 1, ny * (nx + 1) + i], 1)
+    left = np.stack([(j + 1) * (nx + 1), j * (nx + 1)], 1)
+    right = np.stack([j * (nx + 1) + nx, (j + 1) * (nx + 1) + nx], 1)
+    be = np.concatenate([bottom, right, top, left])
+    bp = np.repeat(np.arange(4, dtype=np.int32), [nx, ny, nx, ny])
+    return from_cells(nodes, cells, be, bp, ["bottom", "right", "top", "left"])
+
+
+def sod_strip(nx: int, ny: int, length: float = 1.0, height: float = None, jitter: float = 0.2,
+              seed: int = 0) -> PolyMesh:
+    """Randomly perturbed triangle strip on [0,length] x [0,height].
+
+    ``nx * ny`` rectangles, each split along a randomly chosen diagonal;
+    interior nodes moved by up to ``jitter`` of the local spacing.  Patches:
+    bottom, right, top, left.  2*nx*ny triangles.
+    """
+    rng = np.random.default_rng(seed)
+    if height is None:
+        height = length * ny / nx
+    x = np.linspace(0.0, length, nx + 1)
+    y = np.linspace(0.0, height, ny + 1)
+    X, Y = np.meshgrid(x, y)
+    hx, hy = length / nx, height / ny
+    inner = np.zeros_like(X, dtype=bool)
+    inner[1:-1, 1:-1] = True
+    X = X + np.where(inner, rng.uniform(-jitter, jitter, X.shape) * hx, 0.0)
+    Y = Y + np.where(inner, rng.uniform(-jitter, jitter, Y.shape) * hy, 0.0)
+    nodes = np.stack([X.ravel(), Y.ravel()], 1)
+    jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    a = (jj * (nx + 1) + ii).ravel()
+    b, c, d = a + 1, a + nx + 2, a + nx + 1
+    flip = rng.random(a.size) < 0.5
+    t1 = np.where(flip[:, None], np.stack([a, b, d], 1), np.stack([a, b, c], 1))
+    t2 = np.where(flip[:, None], np.stack([b, c, d], 1), np.stack([a, c, d], 1))
+    cells = np.stack([t1, t2], 1).reshape(-1, 3)
+    quads = _structured(nodes, nx, ny)
+    return from_cells(nodes, cells, quads.bedges, quads.bpatch, quads.patch_names)

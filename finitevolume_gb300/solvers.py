@@ -1,0 +1,279 @@
+"""Python mirror of the reference's solver interface over the C ABI.
+
+Names, argument order and meaning follow the reference classes so that code
+written against them reads the same:
+
+* ``EulerFVMSolver(mesh, boundary_conditions, gamma, cfl, initial_condition,
+  flux_scheme, exact_riemann_tol, exact_riemann_max_iter)`` with ``step``,
+  ``run``, ``field``, ``residual``, ``set_field``, ``set_cfl``, ``gas_gamma``
+  (include/EulerFVMSolver.h:107-160).
+* ``EulerBoundaryType`` / ``EulerBoundaryCondition`` / ``EulerICMode`` /
+  ``EulerInitialCondition`` / ``NumericalFluxScheme`` /
+  ``EulerResidualNorms`` (include/EulerFVMSolver.h:17-67).
+
+All arithmetic runs in the CUDA library; these classes only marshal arrays.
+Extensions beyond the reference (second order, SSP-RK3, local time
+stepping, characteristic farfield, FP32 flux, strict IEEE mode) are keyword
+arguments with reference-mode defaults.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import enum
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import capi
+from .fvmesh import PolyMesh
+
+
+class EulerBoundaryType(enum.IntEnum):
+    Wall = 0
+    Farfield = 1
+    Outflow = 2
+    CharacteristicFarfield = 3  # extension: Riemann-invariant farfield
+
+
+class NumericalFluxScheme(enum.IntEnum):
+    Rusanov = 0
+    HLLC = 1
+    Exact = 2
+
+
+class EulerICMode(enum.IntEnum):
+    Freestream = 0
+    TwoRegion = 1
+
+
+class GradientScheme(enum.IntEnum):
+    LeastSquares = 0
+    GreenGauss = 1
+
+
+class Limiter(enum.IntEnum):
+    NoLimiter = 0
+    BarthJespersen = 1
+    Venkatakrishnan = 2
+
+
+def from_primitive(rho: float, u: float, v: float, p: float, gamma: float) -> np.ndarray:
+    """Conserved state from primitives, E = p/(g-1) + rho (u^2+v^2)/2 (EulerState.h:45-52)."""
+    return np.array([rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)])
+
+
+@dataclasses.dataclass
+class EulerBoundaryCondition:
+    type: EulerBoundaryType = EulerBoundaryType.Wall
+    farfield_state: Sequence[float] = (0.0, 0.0, 0.0, 0.0)  # conserved
+
+
+@dataclasses.dataclass
+class EulerInitialCondition:
+    mode: EulerICMode = EulerICMode.Freestream
+    rho: float = 1.0
+    u: float = 0.0
+    v: float = 0.0
+    p: float = 1.0
+    rho_l: float = 1.0
+    u_l: float = 0.0
+    v_l: float = 0.0
+    p_l: float = 1.0
+    rho_r: float = 0.125
+    u_r: float = 0.0
+    v_r: float = 0.0
+    p_r: float = 0.1
+    x0: float = 0.0
+
+
+@dataclasses.dataclass
+class EulerResidualNorms:
+    rho: float = 0.0
+    rho_u: float = 0.0
+    rho_v: float = 0.0
+    E: float = 0.0
+
+    def as_array(self) -> np.ndarray:
+        return np.array([self.rho, self.rho_u, self.rho_v, self.E])
+
+
+class Mesh:
+    """Device-ready mesh built by the library from a :class:`PolyMesh`.
+
+    Topology follows the reference reader (first visitor owns each face);
+    ``reorder`` chooses the device cell order ("morton", "rcm" or "none").
+    """
+
+    def __init__(self, poly: PolyMesh, reorder: str = "morton"):
+        L = capi.lib()
+        h = C.c_void_p()
+        nodes = np.ascontiguousarray(poly.nodes, dtype=np.float64)
+        off = np.ascontiguousarray(poly.cell_off, dtype=np.int64)
+        cn = np.ascontiguousarray(poly.cell_nodes, dtype=np.int32)
+        be = np.ascontiguousarray(poly.bedges, dtype=np.int32)
+        bp = np.ascontiguousarray(poly.bpatch, dtype=np.int32)
+        capi.check(L.fv_mesh_create_polygons(nodes.shape[0], capi.dptr(nodes), poly.n_cells, capi.i64ptr(off),
+                                             capi.i32ptr(cn), be.shape[0], capi.i32ptr(be), capi.i32ptr(bp),
+                                             len(poly.patch_names), capi.REORDER[reorder], C.byref(h)))
+        self._h = h
+        self.poly = poly
+        self.patch_names = list(poly.patch_names)
+        cnt = np.zeros(5, dtype=np.int64)
+        capi.check(L.fv_mesh_counts(h, capi.i64ptr(cnt)))
+        self.n_cells, self.n_faces, self.n_bfaces, self.n_patches, self.n_entries = (int(x) for x in cnt)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def export(self):
+        """Reference-numbered topology: dict of numpy arrays."""
+        F, N = self.n_faces, self.n_cells
+        fi = np.zeros((F, 5), np.int32)
+        fd = np.zeros((F, 5), np.float64)
+        cd = np.zeros((N, 3), np.float64)
+        off = np.zeros(N + 1, np.int32)
+        cf = np.zeros(self.n_entries, np.int32)
+        capi.check(capi.lib().fv_mesh_export(self._h, capi.i32ptr(fi), capi.dptr(fd), capi.dptr(cd),
+                                             capi.i32ptr(off), capi.i32ptr(cf)))
+        return {"faces_i32": fi, "faces_f64": fd, "cells_f64": cd, "cell_face_off": off, "cell_faces": cf}
+
+    def permutation(self) -> np.ndarray:
+        p = np.zeros(self.n_cells, np.int32)
+        capi.check(capi.lib().fv_mesh_permutation(self._h, capi.i32ptr(p)))
+        return p
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                capi.lib().fv_mesh_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+def _bc_array(bcs: Sequence[EulerBoundaryCondition]):
+    arr = (capi.BC * max(1, len(bcs)))()
+    for i, b in enumerate(bcs):
+        arr[i].type = int(b.type)
+        for k in range(4):
+            arr[i].state[k] = float(b.farfield_state[k])
+    return arr
+
+
+def _ic_struct(ic: EulerInitialCondition) -> capi.IC:
+    s = capi.IC()
+    s.two_region = 1 if ic.mode == EulerICMode.TwoRegion else 0
+    for f in ("rho", "u", "v", "p", "rho_l", "u_l", "v_l", "p_l", "rho_r", "u_r", "v_r", "p_r", "x0"):
+        setattr(s, f, float(getattr(ic, f)))
+    return s
+
+
+class EulerFVMSolver:
+    """GPU explicit Euler solver with the reference's constructor and methods."""
+
+    def __init__(self, input_mesh: Mesh, boundary_conditions: Sequence[EulerBoundaryCondition], gamma: float,
+                 cfl: float, initial_condition: EulerInitialCondition,
+                 flux_scheme: NumericalFluxScheme = NumericalFluxScheme.Rusanov, exact_riemann_tol: float = 1e-6,
+                 exact_riemann_max_iter: int = 20, *, order: int = 1, rk_stages: int = 1, local_dt: bool = False,
+                 gradient: GradientScheme = GradientScheme.LeastSquares, limiter: Limiter = Limiter.Venkatakrishnan,
+                 venkat_k: float = 5.0, fp32_flux: bool = False, strict: bool = False):
+        if not isinstance(input_mesh, Mesh):
+            input_mesh = Mesh(input_mesh)
+        self.mesh = input_mesh
+        L = capi.lib()
+        o = capi.default_options()
+        o.flux = int(flux_scheme)
+        o.exact_tol = float(exact_riemann_tol)
+        o.exact_max_iter = int(exact_riemann_max_iter)
+        o.order = int(order)
+        o.rk_stages = int(rk_stages)
+        o.dt_mode = 1 if local_dt else 0
+        o.gradient = int(gradient)
+        o.limiter = int(limiter)
+        o.venkat_k = float(venkat_k)
+        o.precision = 1 if fp32_flux else 0
+        o.strict = 1 if strict else 0
+        self._opt = o
+        bc = _bc_array(boundary_conditions)
+        ic = _ic_struct(initial_condition)
+        h = C.c_void_p()
+        capi.check(L.fv_solver_create(input_mesh.handle, bc, len(boundary_conditions), float(gamma), float(cfl),
+                                      C.byref(ic), C.byref(o), C.byref(h)))
+        self._h = h
+        self.n_cells = input_mesh.n_cells
+
+    # -- reference API -----------------------------------------------------
+    def step(self) -> None:
+        capi.check(capi.lib().fv_step(self._h, 1, None))
+
+    def run(self, total_steps: int, history: bool = False) -> Optional[np.ndarray]:
+        """Advance ``total_steps`` steps; optionally return the n x 4 norm history."""
+        if history:
+            out = np.zeros((total_steps, 4))
+            capi.check(capi.lib().fv_step(self._h, total_steps, capi.dptr(out)))
+            return out
+        capi.check(capi.lib().fv_step(self._h, total_steps, None))
+        return None
+
+    def field(self) -> np.ndarray:
+        out = np.zeros((self.n_cells, 4))
+        capi.check(capi.lib().fv_get_field(self._h, capi.dptr(out)))
+        return out
+
+    def set_field(self, new_U: np.ndarray) -> None:
+        u = np.ascontiguousarray(new_U, dtype=np.float64)
+        if u.shape != (self.n_cells, 4):
+            raise ValueError(f"set_field expects shape {(self.n_cells, 4)}, got {u.shape}")
+        capi.check(capi.lib().fv_set_field(self._h, capi.dptr(u)))
+
+    def residual(self) -> EulerResidualNorms:
+        out = np.zeros(4)
+        capi.check(capi.lib().fv_get_residual(self._h, capi.dptr(out)))
+        return EulerResidualNorms(*out.tolist())
+
+    def set_cfl(self, new_cfl: float) -> None:
+        capi.check(capi.lib().fv_set_cfl(self._h, float(new_cfl)))
+
+    def gas_gamma(self) -> float:
+        g = C.c_double()
+        capi.check(capi.lib().fv_get_gamma(self._h, C.byref(g)))
+        return g.value
+
+    # -- extensions ----------------------------------------------------------
+    def step_async(self, n: int) -> None:
+        capi.check(capi.lib().fv_step_async(self._h, int(n)))
+
+    def history(self, n: int) -> np.ndarray:
+        out = np.zeros((n, 4))
+        capi.check(capi.lib().fv_get_history(self._h, int(n), capi.dptr(out)))
+        return out
+
+    def set_stream(self, stream_handle: int) -> None:
+        capi.check(capi.lib().fv_solver_set_stream(self._h, C.c_void_p(stream_handle)))
+
+    def device_state(self):
+        u = C.c_void_p()
+        s = C.c_void_p()
+        capi.check(capi.lib().fv_device_state(self._h, C.byref(u), C.byref(s)))
+        return u.value, s.value
+
+    def wall_forces(self, rho_ref=1.0, u_ref=1.0, v_ref=0.0, p_ref=0.0, length_ref=1.0, moment_x=0.25,
+                    moment_y=0.0) -> dict:
+        ref = np.array([rho_ref, u_ref, v_ref, p_ref, length_ref, moment_x, moment_y], dtype=np.float64)
+        out = np.zeros(11)
+        capi.check(capi.lib().fv_wall_forces(self._h, capi.dptr(ref), capi.dptr(out)))
+        keys = ["friction_drag", "pressure_drag", "total_drag", "lift", "moment", "cd_friction", "cd_pressure",
+                "cd_total", "cl", "cm", "n_wall_faces"]
+        return dict(zip(keys, out.tolist()))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                capi.lib().fv_solver_destroy(h)
+            except Exception:
+                pass
+            self._h = None

@@ -1,0 +1,213 @@
+/*
+ * fv_gb300.h -- C ABI of the GB300-native (sm_103a) explicit
+ * residual-and-update loop of FiniteVolume.
+ *
+ * The reference has no FFI or plugin layer: its solvers are C++ classes
+ * linked into one executable.  Each entry point below replaces one method of
+ * those classes (cited per function); include/fvgb300/*.hpp re-creates the
+ * classes themselves on top of this ABI so a reference-style driver compiles
+ * unchanged.  Every function returns an fv_status; fv_last_error() gives the
+ * message of the calling thread's last failure.  There is no CPU fallback:
+ * without a usable CUDA device every solver entry point fails with
+ * FV_ERR_CUDA.
+ *
+ * Conventions
+ *  - Fields cross the ABI as AoS double[4] per cell {rho, rho_u, rho_v, E}
+ *    in the caller's (reference) cell order; the device layout is reordered
+ *    internally and mapped back on every get/set.
+ *  - Indices are 0-based int32; cell counts up to 2^31-1.
+ *  - A solver is not re-entrant (same contract as the reference classes).
+ */
+#ifndef FV_GB300_H
+#define FV_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FV_OK = 0,
+    FV_ERR_BAD_ARG = 1,     /* invalid argument / size mismatch              */
+    FV_ERR_CUDA = 2,        /* CUDA runtime error or no usable device        */
+    FV_ERR_NONFINITE = 3,   /* NaN/Inf detected in the residual norms        */
+    FV_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up            */
+    FV_ERR_BAD_MESH = 5,    /* untagged boundary face, degenerate geometry.. */
+    FV_ERR_UNSUPPORTED = 6  /* option combination not implemented            */
+} fv_status;
+
+typedef struct fv_mesh_s* fv_mesh_t;
+typedef struct fv_solver_s* fv_solver_t;
+
+/* Thread-local text of the last error returned on this thread. */
+const char* fv_last_error(void);
+/* ABI version (major*100 + minor). */
+int fv_abi_version(void);
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int fv_device_count(void);
+
+/* ------------------------------------------------------------------------
+ * Mesh
+ * ------------------------------------------------------------------------ */
+enum { FV_REORDER_NONE = 0, FV_REORDER_MORTON = 1, FV_REORDER_RCM = 2 };
+
+/*
+ * Build a mesh from CCW polygon cells + tagged boundary edges.
+ * Replaces MeshReader::read_fvmesh + build_cells_faces_patches
+ * (src/MeshReader.cpp:317-456, :825-958): faces are derived by walking each
+ * cell's edges in order, the first cell to visit an edge owns it
+ * (cell_left) and fixes its node order, so face numbering, orientation and
+ * each cell's face order match the reference reader exactly.  Boundary edges
+ * that match no cell edge are ignored; an untagged boundary face, a
+ * non-positive or non-finite cell area, a zero-length face or a
+ * self-intersecting cell fails with FV_ERR_BAD_MESH (validate_mesh_geometry,
+ * src/MeshReader.cpp:125-288).
+ *   xy          [2*n_nodes]   node coordinates
+ *   cell_off    [n_cells+1]   CSR offsets into cell_nodes
+ *   cell_nodes  [cell_off[n_cells]]
+ *   bedge_nodes [2*n_bedges], bedge_patch [n_bedges] (0..n_patches-1)
+ */
+int fv_mesh_create_polygons(int32_t n_nodes, const double* xy, int32_t n_cells, const int64_t* cell_off,
+                            const int32_t* cell_nodes, int32_t n_bedges, const int32_t* bedge_nodes,
+                            const int32_t* bedge_patch, int32_t n_patches, int32_t reorder, fv_mesh_t* out);
+
+/*
+ * Build a mesh from an already-derived face topology: the fields of the
+ * reference's UnstructuredMesh (include/UnstructuredMesh.h:20-106).
+ * Face geometry (midpoint, length, unit normal) is recomputed from the
+ * nodes as UnstructuredMesh::compute_geometry does (:89-105); cell volume
+ * and centroid are taken as given (the reference reader fills them).
+ *   face_nodes [2*n_faces] node1,node2   face_cells [2*n_faces] left,right(-1)
+ *   face_patch [n_faces] (-1 = internal)  cell_face_off [n_cells+1], cell_faces
+ *   cell_geom  [3*n_cells] volume, x_centroid, y_centroid
+ */
+int fv_mesh_create_faces(int32_t n_nodes, const double* xy, int32_t n_faces, const int32_t* face_nodes,
+                         const int32_t* face_cells, const int32_t* face_patch, int32_t n_cells,
+                         const int32_t* cell_face_off, const int32_t* cell_faces, const double* cell_geom,
+                         int32_t n_patches, int32_t reorder, fv_mesh_t* out);
+
+/* counts[0..4] = cells, faces, boundary faces, patches, cell-face entries */
+int fv_mesh_counts(fv_mesh_t mesh, int64_t counts[5]);
+
+/*
+ * Topology and geometry in reference numbering (test/inspection helper).
+ * Any pointer may be NULL.  face_i32 [5*F] node1,node2,left,right,patch;
+ * face_f64 [5*F] nx,ny,area,x_mid,y_mid; cell_f64 [3*N] volume,cx,cy;
+ * cell_face_off [N+1]; cell_faces [entries].
+ */
+int fv_mesh_export(fv_mesh_t mesh, int32_t* face_i32, double* face_f64, double* cell_f64,
+                   int32_t* cell_face_off, int32_t* cell_faces);
+/* Device-order permutation: perm[new] = reference cell index. */
+int fv_mesh_permutation(fv_mesh_t mesh, int32_t* perm);
+int fv_mesh_destroy(fv_mesh_t mesh);
+
+/* ------------------------------------------------------------------------
+ * Euler / Navier-Stokes solver
+ * ------------------------------------------------------------------------ */
+enum {
+    FV_BC_WALL = 0,          /* slip wall (Euler) -- EulerBoundaryType::Wall      */
+    FV_BC_FARFIELD = 1,      /* fixed state -- EulerBoundaryType::Farfield        */
+    FV_BC_OUTFLOW = 2,       /* zero gradient -- EulerBoundaryType::Outflow       */
+    FV_BC_CHAR_FARFIELD = 3, /* characteristic (Riemann-invariant) farfield; new  */
+    FV_BC_NOSLIP = 4         /* no-slip wall (NS) -- NSBoundaryType::NoSlipWall   */
+};
+enum { FV_FLUX_RUSANOV = 0, FV_FLUX_HLLC = 1, FV_FLUX_EXACT = 2 };
+enum { FV_GRAD_LSQ = 0, FV_GRAD_GG = 1 };
+enum { FV_LIM_NONE = 0, FV_LIM_BARTH = 1, FV_LIM_VENKAT = 2 };
+enum { FV_DT_GLOBAL = 0, FV_DT_LOCAL = 1 };
+enum { FV_PREC_FP64 = 0, FV_PREC_FP32_FLUX = 1 };
+
+/* One boundary condition per mesh patch (EulerBoundaryCondition,
+ * include/EulerFVMSolver.h:25-29; NSBoundaryCondition,
+ * include/NavierStokesFVMSolver.h:25-32). */
+typedef struct {
+    int32_t type;        /* FV_BC_*                                              */
+    int32_t isothermal;  /* NOSLIP: 1 = isothermal at wall_T, 0 = adiabatic     */
+    double state[4];     /* FARFIELD / CHAR_FARFIELD: conserved freestream state */
+    double wall_u, wall_v, wall_T;
+} fv_bc_t;
+
+/* EulerInitialCondition (include/EulerFVMSolver.h:59-67), primitive form. */
+typedef struct {
+    int32_t two_region;  /* 0 freestream, 1 left/right split at x0 */
+    int32_t pad;
+    double rho, u, v, p;
+    double rho_l, u_l, v_l, p_l;
+    double rho_r, u_r, v_r, p_r;
+    double x0;
+} fv_ic_t;
+
+typedef struct {
+    int32_t flux;          /* FV_FLUX_*                                        */
+    int32_t order;         /* 1 = piecewise constant (reference), 2 = MUSCL    */
+    int32_t gradient;      /* FV_GRAD_* (order 2 reconstruction, NS viscous)   */
+    int32_t limiter;       /* FV_LIM_* (order 2)                               */
+    double venkat_k;       /* Venkatakrishnan K                                */
+    int32_t rk_stages;     /* 1 forward Euler (reference), 3 SSP-RK3           */
+    int32_t dt_mode;       /* FV_DT_GLOBAL (reference) or FV_DT_LOCAL          */
+    int32_t precision;     /* FV_PREC_*                                        */
+    int32_t strict;        /* 1: IEEE op-for-op with the reference (no FMA)    */
+    double exact_tol;      /* exact Riemann Newton relative tolerance          */
+    int32_t exact_max_iter;
+    int32_t viscous;       /* 1: Navier-Stokes viscous + heat flux             */
+    double gas_constant, mu, prandtl;
+} fv_options_t;
+
+/* Fill *opt with the reference's defaults: Rusanov, order 1, forward Euler,
+ * global dt, FP64, exact tol 1e-6 / 20 iterations, LSQ, Venkatakrishnan K=5. */
+void fv_options_default(fv_options_t* opt);
+
+/*
+ * Construct a solver (EulerFVMSolver ctor, include/EulerFVMSolver.h:107-113,
+ * src/EulerFVMSolver.cpp:12-38; NavierStokesFVMSolver ctor when
+ * opt->viscous, include/NavierStokesFVMSolver.h:118-121).  bcs[] is indexed
+ * by patch.  The initial condition is applied from cell centroids exactly as
+ * the reference constructors do.  The mesh may be destroyed afterwards.
+ */
+int fv_solver_create(fv_mesh_t mesh, const fv_bc_t* bcs, int32_t n_bcs, double gamma, double cfl,
+                     const fv_ic_t* ic, const fv_options_t* opt, fv_solver_t* out);
+int fv_solver_destroy(fv_solver_t s);
+
+/* Use this CUDA stream (cudaStream_t) for all work; NULL = solver-owned. */
+int fv_solver_set_stream(fv_solver_t s, void* stream);
+
+/*
+ * Advance n steps (EulerFVMSolver::step / run, src/EulerFVMSolver.cpp:58-121).
+ * Replayed from a captured CUDA graph.  If history != NULL it receives the
+ * n x 4 residual norms (EulerResidualNorms of each step, same definition as
+ * the reference: L2 of the un-normalised flux residual, taken before the
+ * dt/volume scaling).  Synchronises the stream before returning; returns
+ * FV_ERR_NONFINITE if the last step's norms are not finite.
+ */
+int fv_step(fv_solver_t s, int32_t n, double* history);
+/* Enqueue n steps without synchronising (history stays on the device). */
+int fv_step_async(fv_solver_t s, int32_t n);
+/* Copy the last n residual-norm rows recorded on the device (n x 4). */
+int fv_get_history(fv_solver_t s, int32_t n, double* history);
+
+/* EulerFVMSolver::field / set_field / residual / set_cfl / gas_gamma
+ * (include/EulerFVMSolver.h:121-160). */
+int fv_get_field(fv_solver_t s, double* U);
+int fv_set_field(fv_solver_t s, const double* U);
+int fv_get_residual(fv_solver_t s, double norms[4]);
+int fv_set_cfl(fv_solver_t s, double cfl);
+int fv_get_gamma(fv_solver_t s, double* gamma);
+/* Device pointer to the AoS state in device cell order, and the solver's
+ * stream (for callers that time or chain work on it). */
+int fv_device_state(fv_solver_t s, void** U_dev, void** stream);
+
+/* Wall force integration over every boundary face whose patch is a wall
+ * (FV_BC_WALL or FV_BC_NOSLIP): compute_wall_traction + compute_wall_forces
+ * (src/WallTraction.cpp:95-217).  Wall pressure is the owner cell's
+ * pressure; friction is added for viscous solvers.  ref[7] = rho_ref,
+ * u_ref, v_ref, p_ref, length_ref, moment_x, moment_y.  out[11] =
+ * friction_drag, pressure_drag, total_drag, lift, moment, cd_friction,
+ * cd_pressure, cd_total, cl, cm, n_wall_faces (domain total). */
+int fv_wall_forces(fv_solver_t s, const double ref[7], double out[11]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FV_GB300_H */

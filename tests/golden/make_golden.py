@@ -1,0 +1,123 @@
+"""Generate the golden fixtures of the reference's own outputs.
+
+Runs the reference solver classes (compiled in place by ``oracle/Makefile``
+into ``oracle/_ref/fvref``) on small seeded meshes and stores inputs and
+outputs as compressed ``.npz`` files in this directory.  The reference
+checkout is only needed to regenerate the fixtures; the tests read the
+committed ``.npz`` files.
+
+    python tests/golden/make_golden.py [--ref /path/to/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from finitevolume_gb300 import fvmesh, meshgen  # noqa: E402
+
+GAMMA = 1.4
+
+
+def fvref(mode, mesh_path, outdir, **kw):
+    args = [os.path.join(ROOT, "oracle", "_ref", "fvref"), mode, f"mesh={mesh_path}", f"out={outdir}"]
+    for k, v in kw.items():
+        vals = v if isinstance(v, list) else [v]
+        args += [f"{k}={x}" for x in vals]
+    r = subprocess.run(args, capture_output=True, text=True, check=True)
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def mesh_arrays(m):
+    return dict(nodes=m.nodes, cell_off=m.cell_off, cell_nodes=m.cell_nodes, bedges=m.bedges, bpatch=m.bpatch,
+                patch_names=np.array(m.patch_names))
+
+
+def prim_str(rho, u, v, p):
+    return ":".join(repr(float(x)) for x in (rho, u, v, p))
+
+
+def euler_case(name, mesh, case, tmp, steps):
+    path = os.path.join(tmp, name + ".fvmesh")
+    fvmesh.write_fvmesh(mesh, path)
+    out = os.path.join(tmp, name)
+    os.makedirs(out, exist_ok=True)
+    res = {}
+    for flux in case["fluxes"]:
+        fvref("euler", path, out, flux=flux, cfl=case["cfl"], ic=case["ic"], bc=case["bc"], steps=steps,
+              gamma=GAMMA)
+        res[f"field_{flux}"] = np.fromfile(os.path.join(out, "field.f64")).reshape(-1, 4)
+        res[f"hist_{flux}"] = np.fromfile(os.path.join(out, "resid.f64")).reshape(-1, 4)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **mesh_arrays(mesh), **res,
+                        case=np.array(json.dumps({**case, "steps": steps})))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        # NACA0012 O-grid, M=0.5, AoA=2 deg, slip wall + fixed farfield.
+        M, aoa = 0.5, np.radians(2.0)
+        u, v, p = M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA
+        og = meshgen.naca_ogrid(64, 32)
+        euler_case("naca_og64", og, {
+            "fluxes": ["rusanov", "hllc", "exact"], "cfl": 0.5, "ic": "free:" + prim_str(1.0, u, v, p),
+            "bc": ["airfoil:wall", "farfield:farfield:" + prim_str(1.0, u, v, p)],
+            "mach": M, "aoa_deg": 2.0}, tmp, 200)
+        # Sod shock tube on a perturbed triangle strip, walls all round.
+        sod = meshgen.sod_strip(100, 4, seed=1)
+        euler_case("sod_tri", sod, {
+            "fluxes": ["rusanov", "hllc", "exact"], "cfl": 0.5, "ic": "two:1:0:0:1:0.125:0:0:0.1:0.5",
+            "bc": ["bottom:wall", "right:outflow", "top:wall", "left:outflow"]}, tmp, 120)
+        # Gradients on the wavy (non-affine) quad mesh: linear + quadratic field.
+        wavy = meshgen.wavy_quads(8)
+        path = os.path.join(tmp, "wavy.fvmesh")
+        fvmesh.write_fvmesh(wavy, path)
+        res = {}
+        for scheme in ("lsq", "gg"):
+            for tag, coef in (("lin", "1.5:2:-3:0:0:0"), ("quad", "0.5:1:2:0.7:-1.1:0.4")):
+                out = os.path.join(tmp, f"g_{scheme}_{tag}")
+                os.makedirs(out)
+                fvref("grad", path, out, grad=scheme, phi=coef)
+                res[f"grad_{scheme}_{tag}"] = np.fromfile(os.path.join(out, "grad.f64")).reshape(-1, 2)
+                res[f"facegrad_{scheme}_{tag}"] = np.fromfile(os.path.join(out, "facegrad.f64")).reshape(-1, 4)
+                res[f"coef_{tag}"] = np.array([float(x) for x in coef.split(":")])
+        out = os.path.join(tmp, "wavy_mesh")
+        os.makedirs(out)
+        fvref("mesh", path, out)
+        for f in ("faces_i32", "faces_f64", "cells_f64", "cell_face_off", "cell_faces"):
+            dt = np.int32 if ("i32" in f or "cell_face" in f) else np.float64
+            res["mesh_" + f] = np.fromfile(os.path.join(out, f + ".bin"), dtype=dt)
+        np.savez_compressed(os.path.join(HERE, "wavy_grad.npz"), **mesh_arrays(wavy), **res)
+        # Scalar diffusion on a Cartesian patch: Dirichlet + Neumann sides.
+        cart = meshgen.cartesian(12, 10, 2.0, 1.5)
+        cart.nodes -= np.array([1.0, 0.75])
+        path = os.path.join(tmp, "cart.fvmesh")
+        fvmesh.write_fvmesh(cart, path)
+        out = os.path.join(tmp, "diff")
+        os.makedirs(out)
+        case = {"alpha": 0.3, "dt": 2e-3, "v0": 2.0, "r0": 0.5, "steps": 80,
+                "bc": ["bottom:dirichlet:0.25", "right:neumann:-0.5", "top:dirichlet:1.0", "left:neumann:0.0"]}
+        fvref("diff", path, out, alpha=case["alpha"], dt=case["dt"], v0=case["v0"], r0=case["r0"],
+              steps=case["steps"], bc=case["bc"])
+        np.savez_compressed(os.path.join(HERE, "diffusion_cart.npz"), **mesh_arrays(cart),
+                            field=np.fromfile(os.path.join(out, "field.f64")),
+                            hist=np.fromfile(os.path.join(out, "resid.f64")), case=np.array(json.dumps(case)))
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()
