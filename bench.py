@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Benchmark of the explicit residual-and-update loop on one GB300.
+
+Workload (the headline configuration): 2nd-order Euler on a ~1M-cell
+mixed-polygon mesh -- a NACA0012 O-grid core of 1024 x 512 quads plus a
+seeded, Lloyd-relaxed polygonal outer region to 20 chords -- with
+least-squares gradients, the Venkatakrishnan limiter (K = 5), the HLLC
+flux, SSP-RK3 at CFL 1.2 with local time stepping, slip wall and
+characteristic farfield, M = 0.8, AoA = 1.25 deg, FP64.  One step = one
+full iteration (three RK stages).  Synthetic, seeded inputs; nothing is
+read from disk except the mesh cache this script itself writes.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
+restatement of the reference's loop (oracle/, extended to this scheme) on
+the host cores instead; the reference itself has no 2nd-order path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GAMMA = 1.4
+MACH, AOA_DEG, CFL, VENKAT_K = 0.8, 1.25, 1.2, 5.0
+MESH_KW = dict(ni=1024, nj=512, first=1e-3, r_core=2.0, r_far=20.0, code="0012", lloyd_iters=4, seed=0)
+METRIC = "Mcell-iters/s, 2nd-order HLLC Euler at 1M cells; batched/FP32/adjoint vs plain"
+
+
+def freestream():
+    a = np.radians(AOA_DEG)
+    return 1.0, MACH * np.cos(a), MACH * np.sin(a), 1.0 / GAMMA
+
+
+def load_mesh():
+    from finitevolume_gb300 import meshgen
+    return meshgen.cached("naca_mixed", **MESH_KW)
+
+
+def make_solver(poly, fp32=False):
+    from finitevolume_gb300 import solvers as S
+    r, u, v, p = freestream()
+    mesh = S.Mesh(poly, reorder="morton")
+    bcs = [S.EulerBoundaryCondition(S.EulerBoundaryType.Wall),
+           S.EulerBoundaryCondition(S.EulerBoundaryType.CharacteristicFarfield, S.from_primitive(r, u, v, p, GAMMA))]
+    ic = S.EulerInitialCondition(S.EulerICMode.Freestream, rho=r, u=u, v=v, p=p)
+    s = S.EulerFVMSolver(mesh, bcs, GAMMA, CFL, ic, S.NumericalFluxScheme.HLLC, order=2, rk_stages=3,
+                         local_dt=True, gradient=S.GradientScheme.LeastSquares, limiter=S.Limiter.Venkatakrishnan,
+                         venkat_k=VENKAT_K, fp32_flux=fp32)
+    return s, mesh
+
+
+def force_ref():
+    r, u, v, p = freestream()
+    return (r, u, v, p, 1.0, 0.25, 0.0)
+
+
+# --------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------
+def cpu_port_rate(poly, max_seconds: float, threads: int = 0):
+    """Time the oracle port (CPU restatement, OpenMP) on the same workload."""
+    from oracle import port
+    if threads:
+        port.set_threads(threads)
+    r, u, v, p = freestream()
+    om = port.OracleMesh(poly)
+    st = [r, r * u, r * v, p / (GAMMA - 1.0) + 0.5 * r * (u * u + v * v)]
+    e = port.OracleEuler(om, [(0, [0.0] * 4), (3, st)], gamma=GAMMA, cfl=CFL,
+                         ic={"mode": "free", "rho": r, "u": u, "v": v, "p": p}, flux=1, order=2, rk=3, local_dt=True,
+                         gradient=0, limiter=2, venkat_k=VENKAT_K)
+    t0 = time.perf_counter()
+    e.run(1)  # warm-up iteration (page faults, thread start-up)
+    first = time.perf_counter() - t0
+    n = max(1, min(200, int(max_seconds / max(first, 1e-3))))
+    t0 = time.perf_counter()
+    e.run(n)
+    dt = time.perf_counter() - t0
+    return om.n_cells * n / dt / 1e6, n, dt, port.num_threads()
+
+
+def run_reference(args, rank):
+    """--impl reference: the CPU restatement of the reference's loop."""
+    if rank != 0:
+        return
+    poly = load_mesh()
+    budget = float(os.environ.get("FV_REF_SECONDS", "60"))
+    from oracle import port
+    r, u, v, p = freestream()
+    om = port.OracleMesh(poly)
+    st = [r, r * u, r * v, p / (GAMMA - 1.0) + 0.5 * r * (u * u + v * v)]
+    e = port.OracleEuler(om, [(0, [0.0] * 4), (3, st)], gamma=GAMMA, cfl=CFL,
+                         ic={"mode": "free", "rho": r, "u": u, "v": v, "p": p}, flux=1, order=2, rk=3, local_dt=True,
+                         gradient=0, limiter=2, venkat_k=VENKAT_K)
+    t0 = time.perf_counter()
+    e.run(min(args.warmup, 1))
+    per = (time.perf_counter() - t0) / max(min(args.warmup, 1), 1)
+    k = max(1, min(args.steps, int(budget / max(per, 1e-3))))
+    t0 = time.perf_counter()
+    e.run(k)
+    dt = time.perf_counter() - t0
+    value = om.n_cells * k / dt / 1e6
+    sample = f"{k} of the requested {args.steps} iterations on the full {om.n_cells}-cell mesh"
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": args.gpus,
+            "steps": k, "warmup": min(args.warmup, 1), "ms_per_step": round(dt / k * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "naca0012_mixed_1M_o2_hllc_lsq_venkat_rk3", "cells": om.n_cells,
+                       "faces": om.n_faces},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mcell-iters/s", "cores": port.num_threads(),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": "Mcell-iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    from finitevolume_gb300 import capi, roofline, __version__  # noqa: F401
+
+    # CPU baseline first (before the first GPU call in this process: OpenMP
+    # threads only, no fork).
+    poly = load_mesh()
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, n, dt, cores = cpu_port_rate(poly, float(os.environ.get("FV_CPU_SECONDS", "15")))
+        cpu = {"value": round(v, 3), "unit": "Mcell-iters/s", "cores": cores, "kind": "port",
+               "sample": f"{n} SSP-RK3 iterations of the same 2nd-order HLLC scheme on the full mesh, "
+                         f"OpenMP over {cores} threads ({dt:.1f} s)"}
+
+    solver, mesh = make_solver(poly)
+    n_cells, n_faces, n_bf = mesh.n_cells, mesh.n_faces, mesh.n_bfaces
+    u_ptr, s_ptr = solver.device_state()
+    stream = torch.cuda.ExternalStream(s_ptr)
+
+    solver.run(max(args.warmup, 3))  # warm-up through the graph path
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        ev0.record(stream)
+        ms, launches = solver.step_timed(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+        dist.barrier()
+    clocks = clk.summary()
+    value = world * n_cells * args.steps / (elapsed_ms / 1e3) / 1e6
+
+    # Roofline of the dominant kernel class (largest summed device time).
+    hbm, peak_src = measured_peaks()
+    k_dom = int(np.argmax(ms))
+    kname = roofline.KERNEL_NAMES[k_dom]
+    per_launch_ms = ms[k_dom] / max(launches[k_dom], 1)
+    alg = roofline.kernel_bytes(kname, n_cells, n_faces, n_bf)
+    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    stage_ms = float(np.sum(ms)) / (3 * args.steps)
+    stage_alg = roofline.survey_stage_bytes(n_cells, n_faces)
+    roof = {"bound": "hbm", "kernel": f"k_{'grad' if kname == 'gradients' else 'face' if kname == 'faces' else 'update'}",
+            "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+            "peak_source": peak_src, "traffic": roofline.measured_traffic(kname, n_cells),
+            "algorithmic_bytes_per_launch": alg, "launch_ms": round(per_launch_ms, 4),
+            "kernel_ms_per_step": {k: round(m / args.steps, 4) for k, m in zip(roofline.KERNEL_NAMES, ms)},
+            "stage": {"survey_bytes_B2": stage_alg, "ms": round(stage_ms, 4),
+                      "achieved_GBs": round(stage_alg / (stage_ms / 1e3) / 1e9, 1)}}
+
+    # End to end through the public API with host buffers: every step
+    # uploads the state from pinned host memory (set_field), advances one
+    # iteration, reads the residual norms and downloads the state (field).
+    e2e_steps = min(args.steps, 10)
+    host = torch.empty((n_cells, 4), dtype=torch.float64, pin_memory=True).numpy()
+    out = torch.empty((n_cells, 4), dtype=torch.float64, pin_memory=True).numpy()
+    from finitevolume_gb300 import capi as _c
+    L = _c.lib()
+    capi.check(L.fv_get_field(solver._h, _c.dptr(host)))
+    norms = np.zeros(4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        capi.check(L.fv_set_field(solver._h, _c.dptr(host)))
+        capi.check(L.fv_step(solver._h, 1, None))
+        capi.check(L.fv_get_residual(solver._h, _c.dptr(norms)))
+        capi.check(L.fv_get_field(solver._h, _c.dptr(out)))
+        host, out = out, host
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": round(world * n_cells * e2e_steps / e2e_s / 1e6, 3), "unit": "Mcell-iters/s",
+           "h2d_bytes_per_step": 32 * n_cells, "d2h_bytes_per_step": 32 * n_cells + 32,
+           "steps": e2e_steps, "api": "fv_set_field + fv_step(1) + fv_get_residual + fv_get_field"}
+
+    variants = {}
+    if not args.no_variants:
+        # FP32 flux/gradient arithmetic, FP64 accumulation/update/norms.
+        a, _ = make_solver(poly)
+        b, _ = make_solver(poly, fp32=True)
+        a.run(args.warmup)
+        b.run(args.warmup)
+        ms32, l32 = b.step_timed(args.steps)
+        a.run(args.steps)
+        fa, fb = a.wall_forces(*force_ref()), b.wall_forces(*force_ref())
+        Ua, Ub = a.field(), b.field()
+        v32 = n_cells * args.steps / (float(np.sum(ms32)) / 1e3) / 1e6
+        variants["fp32_flux"] = {
+            "value": round(v32, 3), "unit": "Mcell-iters/s", "speedup_vs_fp64": round(v32 / value * world, 3),
+            "kernel_ms_per_step": {k: round(m / args.steps, 4) for k, m in zip(roofline.KERNEL_NAMES, ms32)},
+            "dCL": abs(fa["cl"] - fb["cl"]), "dCD": abs(fa["cd_total"] - fb["cd_total"]),
+            "state_l2_rel": float(np.linalg.norm(Ua - Ub) / np.linalg.norm(Ua)),
+            "iterations_compared": args.warmup + args.steps}
+        del a, b
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": world,
+                "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(elapsed_ms / args.steps, 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded NACA0012 mixed mesh, uniform freestream start)",
+                "config": {"workload": "naca0012_mixed_1M_o2_hllc_lsq_venkat_rk3", "cells": n_cells,
+                           "faces": n_faces, "mach": MACH, "aoa_deg": AOA_DEG, "cfl": CFL,
+                           "l2": "inputs larger than L2 (working set > 400 MB), no flush",
+                           "parallelism": f"replicas{world}" if world > 1 else "single"},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "gpu_launches": int(np.sum(launches)), "variants": variants}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -77,6 +77,7 @@ SIGNATURES = {
     "fv_step": (C.c_int, [_P, C.c_int32, _D]),
     "fv_step_async": (C.c_int, [_P, C.c_int32]),
     "fv_get_history": (C.c_int, [_P, C.c_int32, _D]),
+    "fv_step_timed": (C.c_int, [_P, C.c_int32, _D, _I32]),
     "fv_get_field": (C.c_int, [_P, _D]),
     "fv_set_field": (C.c_int, [_P, _D]),
     "fv_get_residual": (C.c_int, [_P, _D]),

@@ -36,9 +36,10 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Per-face CFL time step, EulerFVMSolver::compute_dt (src/EulerFVMSolver.cpp:133-162).
-__device__ __forceinline__ double face_dt(const St& UL, const St& UR, bool interior, double nx, double ny,
-                                          double length, double cfl, double g) {
+// Per-face wave-speed estimate max(|Vn|+c) of EulerFVMSolver::compute_dt
+// (src/EulerFVMSolver.cpp:140-150).
+__device__ __forceinline__ double face_smax(const St& UL, const St& UR, bool interior, double nx, double ny,
+                                            double g) {
     double uL = UL.ru / UL.r;
     double vL = UL.rv / UL.r;
     double VnL = uL * nx + vL * ny;
@@ -49,7 +50,7 @@ __device__ __forceinline__ double face_dt(const St& UL, const St& UR, bool inter
         double VnR = uR * nx + vR * ny;
         Smax = rmax(Smax, fabs(VnR) + sound_speed(UR, g));
     }
-    return cfl * length / Smax;
+    return Smax;
 }
 
 template <int FLUX, bool LOCAL>
@@ -64,8 +65,11 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_face_o1(const O1Args a) {
         const St UR = (R >= 0) ? ld_state(a.U, R) : ghost_state(a.bc, a.m.fpatch[f], UL, geo.x, geo.y, g);
         const St F = num_flux<FLUX>(UL, UR, geo.x, geo.y, g, a.exact_tol, a.exact_max_iter);
         st_state(a.ff, f, geo.z * F);
-        cand = face_dt(UL, UR, R >= 0, geo.x, geo.y, geo.w, a.ctl->cfl, g);
-        if (LOCAL) a.dtf[f] = cand;
+        const double Smax = face_smax(UL, UR, R >= 0, geo.x, geo.y, g);
+        // Global: the face's CFL step cfl * length / Smax (compute_dt).
+        // Local: the face's lambda * A for dt_i = cfl V_i / sum_f lambda_f A_f.
+        if (LOCAL) a.dtf[f] = Smax * geo.z;
+        else cand = a.ctl->cfl * geo.w / Smax;
     }
     if (!LOCAL) {
         __shared__ double smin[fvgb::kFaceBlock / 32];
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_cell_o1(const O1Args a) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
     if (c < a.m.n_cells) {
-        double dt = LOCAL ? DBL_MAX : __longlong_as_double((long long)a.ctl->dt_bits);
+        double dt = LOCAL ? 0.0 : __longlong_as_double((long long)a.ctl->dt_bits);
         St R = st_make(0.0, 0.0, 0.0, 0.0);
         const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
         for (int e = e0; e < e1; ++e) {
@@ -145,8 +149,9 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_cell_o1(const O1Args a) {
             const St F = ld_state(a.ff, f);
             if (ent & 1) R = R - F;
             else R += F;
-            if (LOCAL) dt = rmin(dt, a.dtf[f]);
+            if (LOCAL) dt += a.dtf[f];
         }
+        if (LOCAL) dt = a.ctl->cfl * a.m.vol[c] / dt;
         s0 = R.r * R.r; s1 = R.ru * R.ru; s2 = R.rv * R.rv; s3 = R.E * R.E;
         const St u = ld_state(a.U, c);
         st_state(a.U, c, u + (dt / a.m.vol[c]) * R);
@@ -155,28 +160,30 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_cell_o1(const O1Args a) {
 }
 
 template <int FLUX>
-static void launch_flux(const O1Args& a, cudaStream_t s) {
+static void launch_flux(const O1Args& a, int part, cudaStream_t s) {
     const int fb = (a.m.n_faces + fvgb::kFaceBlock - 1) / fvgb::kFaceBlock;
     const int cb = (a.m.n_cells + fvgb::kCellBlock - 1) / fvgb::kCellBlock;
-    if (a.local_dt) {
-        k_face_o1<FLUX, true><<<fb, fvgb::kFaceBlock, 0, s>>>(a);
-        k_cell_o1<true><<<cb, fvgb::kCellBlock, 0, s>>>(a);
+    if (part == 0) {
+        if (a.local_dt) k_face_o1<FLUX, true><<<fb, fvgb::kFaceBlock, 0, s>>>(a);
+        else k_face_o1<FLUX, false><<<fb, fvgb::kFaceBlock, 0, s>>>(a);
     } else {
-        k_face_o1<FLUX, false><<<fb, fvgb::kFaceBlock, 0, s>>>(a);
-        k_cell_o1<false><<<cb, fvgb::kCellBlock, 0, s>>>(a);
+        if (a.local_dt) k_cell_o1<true><<<cb, fvgb::kCellBlock, 0, s>>>(a);
+        else k_cell_o1<false><<<cb, fvgb::kCellBlock, 0, s>>>(a);
     }
 }
 
 }  // namespace FV_KNS
 
+#ifdef FV_DEFINE_O1_LAUNCH
 namespace fvgb {
 namespace FV_KNS {
-void launch_o1_step(const O1Args& a, cudaStream_t s) {
+void launch_o1_part(const O1Args& a, int part, cudaStream_t s) {
     switch (a.flux) {
-        case 1: ::FV_KNS::launch_flux<1>(a, s); break;
-        case 2: ::FV_KNS::launch_flux<2>(a, s); break;
-        default: ::FV_KNS::launch_flux<0>(a, s); break;
+        case 1: ::FV_KNS::launch_flux<1>(a, part, s); break;
+        case 2: ::FV_KNS::launch_flux<2>(a, part, s); break;
+        default: ::FV_KNS::launch_flux<0>(a, part, s); break;
     }
 }
 }  // namespace FV_KNS
 }  // namespace fvgb
+#endif  // FV_DEFINE_O1_LAUNCH

@@ -1,0 +1,429 @@
+// Second-order (MUSCL) residual with SSP-RK3 / forward-Euler stages.
+//
+// No reference counterpart: the reference is first-order in space and time
+// (docs/dns-higher-order-scheme-plan.md:52-95 sketches this form).  The CPU
+// FP64 definition these kernels are checked against is
+// oracle/fv_oracle.cpp (Euler::gradients / recon / residual / step).
+//
+// Per RK stage, three passes over HBM-resident arrays:
+//   k_grad   one thread per cell: gradients of the primitive variables
+//            (rho, u, v, p) by weighted least squares (weights pre-folded
+//            with the inverse normal matrix, one pair per CSR entry) or
+//            Green-Gauss, then Barth-Jespersen or Venkatakrishnan limiting.
+//            The per-face limiter values are min-reduced by
+//            cross-multiplication, so each variable costs one division.
+//   k_face   one thread per face: linear reconstruction to the face
+//            midpoint (positivity fallback to the cell value), ghost state
+//            from the reconstructed owner state, numerical flux on
+//            primitive inputs; at stage 0 also the face's CFL time step.
+//   k_update one thread per cell: FP64 signed gather of the face fluxes in
+//            the reference's per-cell face order, stage-0 time step and
+//            residual norms, the Shu-Osher stage combination, and the
+//            primitive copy W (flux precision) + sound speed for the next
+//            stage.
+//
+// T is the flux/gradient arithmetic type: double (FP64 mode) or float
+// (FP32-flux mode).  Residual accumulation, the state update, dt and the
+// norms are always FP64.
+#pragma once
+
+#include <type_traits>
+
+#include "euler_o1.cuh"
+
+namespace FV_KNS {
+
+template <typename T> struct V4 { T r, u, v, p; };
+template <typename T> struct G8 { T gx[4], gy[4]; };
+
+template <typename T> __device__ __forceinline__ T tsqrt(T x);
+template <> __device__ __forceinline__ double tsqrt<double>(double x) { return sqrt(x); }
+template <> __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
+template <typename T> __device__ __forceinline__ T tpow(T a, T b);
+template <> __device__ __forceinline__ double tpow<double>(double a, double b) { return pow(a, b); }
+template <> __device__ __forceinline__ float tpow<float>(float a, float b) { return powf(a, b); }
+
+// W storage: double -> 32-byte {r,u,v,p}; float -> float4.
+template <typename T> struct WStore;
+template <> struct WStore<double> {
+    using type = St;
+    __device__ static V4<double> ld(const St* W, int i) {
+        St s = ld_state(W, i);
+        return {s.r, s.ru, s.rv, s.E};
+    }
+    __device__ static void st(St* W, int i, const V4<double>& w) { st_state(W, i, st_make(w.r, w.u, w.v, w.p)); }
+};
+template <> struct WStore<float> {
+    using type = float4;
+    __device__ static V4<float> ld(const float4* W, int i) {
+        float4 a = __ldg(W + i);
+        return {a.x, a.y, a.z, a.w};
+    }
+    __device__ static void st(float4* W, int i, const V4<float>& w) { W[i] = make_float4(w.r, w.u, w.v, w.p); }
+};
+
+template <typename T> struct GStore;
+template <> struct GStore<double> {
+    using type = double2;  // 4 x double2 per cell: (gx,gy) of r,u,v,p
+    __device__ static G8<double> ld(const double2* G, int i) {
+        G8<double> g;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            double2 a = __ldg(G + 4 * i + k);
+            g.gx[k] = a.x; g.gy[k] = a.y;
+        }
+        return g;
+    }
+    __device__ static void st(double2* G, int i, const G8<double>& g) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) G[4 * i + k] = make_double2(g.gx[k], g.gy[k]);
+    }
+};
+template <> struct GStore<float> {
+    using type = float4;  // 2 x float4 per cell
+    __device__ static G8<float> ld(const float4* G, int i) {
+        float4 a = __ldg(G + 2 * i), b = __ldg(G + 2 * i + 1);
+        G8<float> g;
+        g.gx[0] = a.x; g.gy[0] = a.y; g.gx[1] = a.z; g.gy[1] = a.w;
+        g.gx[2] = b.x; g.gy[2] = b.y; g.gx[3] = b.z; g.gy[3] = b.w;
+        return g;
+    }
+    __device__ static void st(float4* G, int i, const G8<float>& g) {
+        G[2 * i] = make_float4(g.gx[0], g.gy[0], g.gx[1], g.gy[1]);
+        G[2 * i + 1] = make_float4(g.gx[2], g.gy[2], g.gx[3], g.gy[3]);
+    }
+};
+
+// Face flux storage: double -> St; float -> float4.  Loaded as FP64 in the gather.
+__device__ __forceinline__ void st_flux(St* ff, int f, const V4<double>& F) { st_state(ff, f, st_make(F.r, F.u, F.v, F.p)); }
+__device__ __forceinline__ void st_flux(float4* ff, int f, const V4<float>& F) { ff[f] = make_float4(F.r, F.u, F.v, F.p); }
+__device__ __forceinline__ St ld_flux(const St* ff, int f) { return ld_state(ff, f); }
+__device__ __forceinline__ St ld_flux(const float4* ff, int f) {
+    float4 a = __ldg(ff + f);
+    return st_make((double)a.x, (double)a.y, (double)a.z, (double)a.w);
+}
+
+// ---------------------------------------------------------------------------
+// Primitive-input physics
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ V4<T> phys_flux_p(const V4<T>& w, T E, T Vn, T nx, T ny) {
+    return {w.r * Vn, w.r * w.u * Vn + w.p * nx, w.r * w.v * Vn + w.p * ny, (E + w.p) * Vn};
+}
+
+// Rusanov on primitive inputs (RusanovFlux.h:33-43 with cached primitives).
+template <typename T>
+__device__ __forceinline__ V4<T> rusanov_p(const V4<T>& L, const V4<T>& R, T nx, T ny, T g, T igm1) {
+    T cL = tsqrt<T>(g * L.p / L.r), cR = tsqrt<T>(g * R.p / R.r);
+    T VnL = L.u * nx + L.v * ny, VnR = R.u * nx + R.v * ny;
+    T EL = L.p * igm1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
+    T ER = R.p * igm1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
+    T Smax = fmax(fabs(VnL) + cL, fabs(VnR) + cR);
+    V4<T> FL = phys_flux_p(L, EL, VnL, nx, ny), FR = phys_flux_p(R, ER, VnR, nx, ny);
+    T h = T(0.5) * Smax;
+    return {T(0.5) * (FL.r + FR.r) - h * (R.r - L.r),
+            T(0.5) * (FL.u + FR.u) - h * (R.r * R.u - L.r * L.u),
+            T(0.5) * (FL.v + FR.v) - h * (R.r * R.v - L.r * L.v),
+            T(0.5) * (FL.p + FR.p) - h * (ER - EL)};
+}
+
+// HLLC on primitive inputs (HllcFlux.h:35-76), rearranged to four divisions:
+// with q = 1/(S_K - S*), the star factor is rho_K (S_K - Vn_K) q and the
+// pressure term of E* reduces to (S* - Vn_K) p_K q.
+template <typename T>
+__device__ __forceinline__ V4<T> hllc_p(const V4<T>& L, const V4<T>& R, T nx, T ny, T g, T igm1) {
+    T irL = T(1) / L.r, irR = T(1) / R.r;
+    T cL = tsqrt<T>(g * L.p * irL), cR = tsqrt<T>(g * R.p * irR);
+    T VnL = L.u * nx + L.v * ny, VnR = R.u * nx + R.v * ny;
+    T EL = L.p * igm1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
+    T ER = R.p * igm1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
+    T SL = fmin(VnL - cL, VnR - cR), SR = fmax(VnL + cL, VnR + cR);
+    if (SL >= T(0)) return phys_flux_p(L, EL, VnL, nx, ny);
+    if (SR <= T(0)) return phys_flux_p(R, ER, VnR, nx, ny);
+    T mL = L.r * (SL - VnL), mR = R.r * (SR - VnR);
+    T Ss = (R.p - L.p + mL * VnL - mR * VnR) / (mL - mR);
+    bool left = Ss >= T(0);
+    T SK = left ? SL : SR, VnK = left ? VnL : VnR, EK = left ? EL : ER, irK = left ? irL : irR;
+    T mK = left ? mL : mR;
+    V4<T> K = left ? L : R;
+    T q = T(1) / (SK - Ss);
+    T fac = mK * q;
+    T VtK = -K.u * ny + K.v * nx;
+    T mn = fac * Ss, mt = fac * VtK;
+    T Es = fac * (EK * irK + (Ss - VnK) * Ss) + (Ss - VnK) * K.p * q;
+    V4<T> FK = phys_flux_p(K, EK, VnK, nx, ny);
+    return {FK.r + SK * (fac - K.r),
+            FK.u + SK * ((mn * nx - mt * ny) - K.r * K.u),
+            FK.v + SK * ((mn * ny + mt * nx) - K.r * K.v),
+            FK.p + SK * (Es - EK)};
+}
+
+template <typename T>
+__device__ __forceinline__ V4<T> prim_of(const St& s, T g) {
+    T r = (T)s.r;
+    T u = (T)(s.ru / s.r), v = (T)(s.rv / s.r);
+    T p = (T)((g - 1.0) * (s.E - 0.5 * s.r * ((s.ru / s.r) * (s.ru / s.r) + (s.rv / s.r) * (s.rv / s.r))));
+    return {r, u, v, p};
+}
+
+// Ghost state in primitive form (EulerFVMSolver::ghost_state,
+// src/EulerFVMSolver.cpp:174-193, plus the characteristic farfield).
+template <typename T>
+__device__ __forceinline__ V4<T> ghost_prim(const BCTable& bc, int patch, const V4<T>& w, T nx, T ny, T g) {
+    int t = bc.type[patch];
+    if (t == BC_OUTFLOW) return w;
+    if (t == BC_FARFIELD || t == BC_CHAR) {
+        T rf = (T)bc.st[patch][0];
+        T uf = (T)(bc.st[patch][1] / bc.st[patch][0]), vf = (T)(bc.st[patch][2] / bc.st[patch][0]);
+        T pf = (T)((g - 1.0) * (bc.st[patch][3] - 0.5 * bc.st[patch][0] * ((bc.st[patch][1] / bc.st[patch][0]) *
+                                                                                 (bc.st[patch][1] / bc.st[patch][0]) +
+                                                                             (bc.st[patch][2] / bc.st[patch][0]) *
+                                                                                 (bc.st[patch][2] / bc.st[patch][0]))));
+        if (t == BC_FARFIELD) return {rf, uf, vf, pf};
+        T ci = tsqrt<T>(g * w.p / w.r), cf = tsqrt<T>(g * pf / rf);
+        T vni = w.u * nx + w.v * ny, vnf = uf * nx + vf * ny;
+        if (vnf <= -cf) return {rf, uf, vf, pf};
+        if (vni >= ci) return w;
+        T k = T(2) / (g - T(1));
+        T Rp = vni + k * ci, Rm = vnf - k * cf;
+        T vnb = T(0.5) * (Rp + Rm);
+        T cb = T(0.25) * (g - T(1)) * (Rp - Rm);
+        T s, ut, vt;
+        if (vnb > T(0)) { s = w.p / tpow<T>(w.r, g); ut = w.u - vni * nx; vt = w.v - vni * ny; }
+        else { s = pf / tpow<T>(rf, g); ut = uf - vnf * nx; vt = vf - vnf * ny; }
+        T rb = tpow<T>(cb * cb / (g * s), T(1) / (g - T(1)));
+        T pb = rb * cb * cb / g;
+        return {rb, ut + vnb * nx, vt + vnb * ny, pb};
+    }
+    if (t == BC_NOSLIP) return {w.r, T(2) * (T)bc.wall_u[patch] - w.u, T(2) * (T)bc.wall_v[patch] - w.v, w.p};
+    T Vn = w.u * nx + w.v * ny;
+    return {w.r, w.u - T(2) * Vn * nx, w.v - T(2) * Vn * ny, w.p};
+}
+
+using fvgb::O2Args;
+
+// ---------------------------------------------------------------------------
+template <typename T, int GRAD, int LIM>
+__global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
+    using WS = WStore<T>;
+    using WT = typename WS::type;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.m.n_cells) return;
+    const WT* W = static_cast<const WT*>(a.W);
+    const T g = (T)a.gamma;
+    const V4<T> wc = WS::ld(W, c);
+    const T* wcv = &wc.r;
+    T gx[4] = {0, 0, 0, 0}, gy[4] = {0, 0, 0, 0}, dmax[4] = {0, 0, 0, 0}, dmin[4] = {0, 0, 0, 0};
+    const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
+    for (int e = e0; e < e1; ++e) {
+        const int nb = a.cnb[e];
+        V4<T> wn;
+        if (nb >= 0) {
+            wn = WS::ld(W, nb);
+        } else {
+            const int f = -1 - nb;
+            const double4_32a geo = a.m.fgeom[f];
+            V4<T> gh = ghost_prim<T>(a.bc, a.m.fpatch[f], wc, (T)geo.x, (T)geo.y, g);
+            wn = {T(0.5) * (wc.r + gh.r), T(0.5) * (wc.u + gh.u), T(0.5) * (wc.v + gh.v), T(0.5) * (wc.p + gh.p)};
+        }
+        const T* wnv = &wn.r;
+        if (GRAD == 0) {
+            const double2 ab = __ldg(a.lsq + e);
+            const T ax = (T)ab.x, ay = (T)ab.y;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                T d = wnv[k] - wcv[k];
+                dmax[k] = fmax(dmax[k], d);
+                dmin[k] = fmin(dmin[k], d);
+                gx[k] += ax * d;
+                gy[k] += ay * d;
+            }
+        } else {
+            const double4_32a q = a.gg[e];
+            const T ax = (T)q.x, ay = (T)q.y, wgt = (T)q.z;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                T d = wnv[k] - wcv[k];
+                dmax[k] = fmax(dmax[k], d);
+                dmin[k] = fmin(dmin[k], d);
+                T phif = wgt * wcv[k] + (T(1) - wgt) * wnv[k];
+                gx[k] += ax * phif;
+                gy[k] += ay * phif;
+            }
+        }
+    }
+    if (LIM != 0) {
+        T eps2 = T(0);
+        if (LIM == 2) {
+            T kh = (T)(a.venkat_k * a.h[c]);
+            eps2 = kh * kh * kh;
+        }
+        T nmin[4] = {1, 1, 1, 1}, dmn[4] = {1, 1, 1, 1};
+        for (int e = e0; e < e1; ++e) {
+            const double2 r = __ldg(a.erf + e);
+            const T rx = (T)r.x, ry = (T)r.y;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                T d2 = gx[k] * rx + gy[k] * ry;
+                if (d2 == T(0)) continue;
+                T d1 = d2 > T(0) ? dmax[k] : dmin[k];
+                T num, den;
+                if (LIM == 1) { num = d1; den = d2; if (den < T(0)) { num = -num; den = -den; } }
+                else {
+                    num = d1 * d1 + eps2 + T(2) * d2 * d1;
+                    den = d1 * d1 + T(2) * d2 * d2 + d1 * d2 + eps2;
+                }
+                if (num * dmn[k] < nmin[k] * den) { nmin[k] = num; dmn[k] = den; }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            T psi = nmin[k] / dmn[k];
+            gx[k] *= psi;
+            gy[k] *= psi;
+        }
+    }
+    G8<T> out;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { out.gx[k] = gx[k]; out.gy[k] = gy[k]; }
+    GStore<T>::st(static_cast<typename GStore<T>::type*>(a.G), c, out);
+}
+
+template <typename T>
+__device__ __forceinline__ V4<T> recon(const V4<T>& w, const G8<T>& g, T rx, T ry) {
+    V4<T> o = {w.r + (g.gx[0] * rx + g.gy[0] * ry), w.u + (g.gx[1] * rx + g.gy[1] * ry),
+               w.v + (g.gx[2] * rx + g.gy[2] * ry), w.p + (g.gx[3] * rx + g.gy[3] * ry)};
+    if (!(o.r > T(0)) || !(o.p > T(0))) return w;
+    return o;
+}
+
+template <typename T, int FLUX>
+__device__ __forceinline__ V4<T> num_flux_p(const V4<T>& L, const V4<T>& R, T nx, T ny, T g, T igm1, double tol,
+                                            int maxit) {
+    if constexpr (FLUX == FLUX_HLLC) return hllc_p<T>(L, R, nx, ny, g, igm1);
+    else if constexpr (FLUX == FLUX_EXACT) {
+        St UL = from_primitive((double)L.r, (double)L.u, (double)L.v, (double)L.p, (double)g);
+        St UR = from_primitive((double)R.r, (double)R.u, (double)R.v, (double)R.p, (double)g);
+        St F = exact_riemann(UL, UR, (double)nx, (double)ny, (double)g, tol, maxit);
+        return {(T)F.r, (T)F.ru, (T)F.rv, (T)F.E};
+    } else return rusanov_p<T>(L, R, nx, ny, g, igm1);
+}
+
+// DT: 0 = no time step this stage, 1 = global (atomicMin), 2 = local (per face).
+template <typename T, int FLUX, int ORDER, int DT>
+__global__ void __launch_bounds__(fvgb::kFaceBlock) k_face(const O2Args a) {
+    using WS = WStore<T>;
+    using WT = typename WS::type;
+    using FT = typename std::conditional<std::is_same<T, double>::value, St, float4>::type;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    double cand = DBL_MAX;
+    if (f < a.m.n_faces) {
+        const WT* W = static_cast<const WT*>(a.W);
+        const T g = (T)a.gamma, igm1 = (T)(1.0 / (a.gamma - 1.0));
+        const int L = a.m.fl[f], R = a.m.fr[f];
+        const double4_32a geo = a.m.fgeom[f];
+        const T nx = (T)geo.x, ny = (T)geo.y;
+        V4<T> wl = WS::ld(W, L), wr;
+        const V4<T> wlc = wl;
+        if (ORDER == 2) {
+            const double4_32a rr = a.frf[f];
+            const G8<T> gl = GStore<T>::ld(static_cast<const typename GStore<T>::type*>(a.G), L);
+            wl = recon<T>(wl, gl, (T)rr.x, (T)rr.y);
+            if (R >= 0) {
+                const G8<T> gr = GStore<T>::ld(static_cast<const typename GStore<T>::type*>(a.G), R);
+                wr = recon<T>(WS::ld(W, R), gr, (T)rr.z, (T)rr.w);
+            }
+        } else if (R >= 0) {
+            wr = WS::ld(W, R);
+        }
+        if (R < 0) wr = ghost_prim<T>(a.bc, a.m.fpatch[f], wl, nx, ny, g);
+        const V4<T> F = num_flux_p<T, FLUX>(wl, wr, nx, ny, g, igm1, a.exact_tol, a.exact_max_iter);
+        const T ar = (T)geo.z;
+        st_flux(static_cast<FT*>(a.ff), f, V4<T>{ar * F.r, ar * F.u, ar * F.v, ar * F.p});
+        if (DT != 0) {
+            // compute_dt's per-face candidate from cell-centred states
+            // (src/EulerFVMSolver.cpp:140-160).
+            double Smax = fabs((double)wlc.u * geo.x + (double)wlc.v * geo.y) + a.cs[L];
+            if (R >= 0) {
+                const V4<T> wrc = WS::ld(W, R);
+                Smax = rmax(Smax, fabs((double)wrc.u * geo.x + (double)wrc.v * geo.y) + a.cs[R]);
+            }
+            if (DT == 2) a.dtf[f] = Smax * geo.z;
+            else cand = a.ctl->cfl * geo.w / Smax;
+        }
+    }
+    if (DT == 1) {
+        __shared__ double smin[fvgb::kFaceBlock / 32];
+        cand = warp_min(cand);
+        if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = cand;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double v = smin[0];
+            for (int w = 1; w < fvgb::kFaceBlock / 32; ++w) v = fmin(v, smin[w]);
+            atomicMin(&a.ctl->dt_bits, (unsigned long long)__double_as_longlong(v));
+        }
+    }
+}
+
+// STAGE: 0..NST-1; NST: 1 (forward Euler) or 3 (SSP-RK3); DT: 1 global, 2 local.
+template <typename T, int STAGE, int NST, int DT>
+__global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
+    using FT = typename std::conditional<std::is_same<T, double>::value, St, float4>::type;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    if (c < a.m.n_cells) {
+        const FT* ff = static_cast<const FT*>(a.ff);
+        St R = st_make(0.0, 0.0, 0.0, 0.0);
+        double lam = 0.0;
+        const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
+        for (int e = e0; e < e1; ++e) {
+            const int ent = a.m.cf[e];
+            const int f = ent >> 1;
+            const St F = ld_flux(ff, f);
+            if (ent & 1) R = R - F;
+            else R += F;
+            if (STAGE == 0 && DT == 2) lam += a.dtf[f];
+        }
+        double dtv;
+        if (STAGE == 0) {
+            // Local: dt_i = cfl V_i / sum_f lambda_f A_f; global: the min over faces.
+            double dt = (DT == 2) ? a.ctl->cfl * a.m.vol[c] / lam : __longlong_as_double((long long)a.ctl->dt_bits);
+            dtv = dt / a.m.vol[c];
+            if (NST > 1) a.dtv[c] = dtv;
+            s0 = R.r * R.r; s1 = R.ru * R.ru; s2 = R.rv * R.rv; s3 = R.E * R.E;
+        } else {
+            dtv = a.dtv[c];
+        }
+        const St u = ld_state(a.U, c);
+        const St e = u + dtv * R;
+        St un;
+        if (NST == 1) un = e;
+        else if (STAGE == 0) { st_state(a.U0, c, u); un = e; }
+        else if (STAGE == 1) un = 0.75 * ld_state(a.U0, c) + 0.25 * e;
+        else un = (1.0 / 3.0) * ld_state(a.U0, c) + (2.0 / 3.0) * e;
+        st_state(a.U, c, un);
+        const double g = a.gamma;
+        const double ir = 1.0 / un.r;
+        const double uu = un.ru * ir, vv = un.rv * ir;
+        const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
+        WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{(T)un.r, (T)uu, (T)vv, (T)p});
+        if (STAGE == NST - 1) a.cs[c] = sqrt(g * p * ir);
+    }
+    if (STAGE == 0) finish_norms(s0, s1, s2, s3, a.ctl, a.partials, a.hist, a.hist_cap);
+}
+
+// Primitive copy + sound speed from U (after construction / set_field).
+template <typename T>
+__global__ void __launch_bounds__(fvgb::kCellBlock) k_prim(const O2Args a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.m.n_cells) return;
+    const St un = ld_state(a.U, c);
+    const double g = a.gamma;
+    const double ir = 1.0 / un.r;
+    const double uu = un.ru * ir, vv = un.rv * ir;
+    const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
+    WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{(T)un.r, (T)uu, (T)vv, (T)p});
+    a.cs[c] = sqrt(g * p * ir);
+}
+
+}  // namespace FV_KNS

@@ -331,4 +331,81 @@ void HostMesh::build_device_layout(int reorder) {
     }
 }
 
+// Per-entry and per-face geometry of the second-order scheme (device order).
+//  LSQ: the weighted least-squares gradient of GradientCalculator
+//  (src/GradientReconstruction.cpp:45-80, :124-148; weights 1/d^2 over face
+//  neighbours, boundary-face midpoints standing in for missing neighbours)
+//  is linear in the differences phi_j - phi_c, so the inverse normal matrix
+//  is folded into one weight pair per entry: grad = sum_j (a_j, b_j) dphi_j.
+//  GG: Green-Gauss with inverse-distance face values (:89-118).
+void HostMesh::build_o2_geometry() {
+    size_t E = d_cf.size();
+    d_cnb.resize(E);
+    d_lsq.resize(2 * E);
+    d_gg.resize(4 * E);
+    d_erf.resize(2 * E);
+    d_frf.assign(4 * (size_t)n_faces, 0.0);
+    d_h.resize(n_cells);
+    for (int32_t i = 0; i < n_cells; ++i) {
+        int32_t c = perm[i];
+        double xc = cx[c], yc = cy[c];
+        d_h[i] = std::sqrt(vol[c]);
+        int32_t e0 = d_cf_off[i], e1 = d_cf_off[i + 1];
+        double m00 = 0.0, m01 = 0.0, m11 = 0.0;
+        for (int32_t e = e0; e < e1; ++e) {
+            int32_t f = fperm[d_cf[e] >> 1];
+            double px, py;
+            if (fr[f] < 0) { px = fxm[f]; py = fym[f]; }
+            else {
+                int32_t nb = fl[f] == c ? fr[f] : fl[f];
+                px = cx[nb]; py = cy[nb];
+            }
+            double dx = px - xc, dy = py - yc;
+            double w = 1.0 / (dx * dx + dy * dy);
+            m00 += w * dx * dx; m01 += w * dx * dy; m11 += w * dy * dy;
+        }
+        double det = m00 * m11 - m01 * m01;
+        double i00 = m11 / det, i01 = -m01 / det, i11 = m00 / det;
+        for (int32_t e = e0; e < e1; ++e) {
+            int32_t fd = d_cf[e] >> 1;
+            int32_t f = fperm[fd];
+            bool owner = fl[f] == c;
+            double px, py;
+            if (fr[f] < 0) {
+                px = fxm[f]; py = fym[f];
+                d_cnb[e] = -1 - fd;
+            } else {
+                int32_t nb = owner ? fr[f] : fl[f];
+                px = cx[nb]; py = cy[nb];
+                d_cnb[e] = iperm[nb];
+            }
+            double dx = px - xc, dy = py - yc;
+            double w = 1.0 / (dx * dx + dy * dy);
+            d_lsq[2 * e] = i00 * (w * dx) + i01 * (w * dy);
+            d_lsq[2 * e + 1] = i01 * (w * dx) + i11 * (w * dy);
+            double sgn = owner ? 1.0 : -1.0;
+            d_gg[4 * e] = sgn * fnx[f] * farea[f] / vol[c];
+            d_gg[4 * e + 1] = sgn * fny[f] * farea[f] / vol[c];
+            if (fr[f] < 0) d_gg[4 * e + 2] = 0.0;
+            else {
+                double d_c = std::hypot(xc - fxm[f], yc - fym[f]);
+                double d_o = std::hypot(px - fxm[f], py - fym[f]);
+                d_gg[4 * e + 2] = d_o / (d_c + d_o);
+            }
+            d_gg[4 * e + 3] = 0.0;
+            d_erf[2 * e] = fxm[f] - xc;
+            d_erf[2 * e + 1] = fym[f] - yc;
+        }
+    }
+    for (int32_t i = 0; i < n_faces; ++i) {
+        int32_t f = fperm[i];
+        d_frf[4 * i] = fxm[f] - cx[fl[f]];
+        d_frf[4 * i + 1] = fym[f] - cy[fl[f]];
+        if (fr[f] >= 0) {
+            d_frf[4 * i + 2] = fxm[f] - cx[fr[f]];
+            d_frf[4 * i + 3] = fym[f] - cy[fr[f]];
+        }
+    }
+}
+
 }  // namespace fvgb

@@ -34,8 +34,17 @@ struct HostMesh {
     std::vector<int32_t> d_cf_off, d_cf;         // entries: face<<1 | (cell is owner)
     std::vector<double> d_vol, d_cxy;            // [N], [2N]
 
+    // Second-order geometry, device order (built by build_o2_geometry).
+    std::vector<int32_t> d_cnb;                  // per entry: neighbour cell, or -1-face for boundary
+    std::vector<double> d_lsq;                   // per entry [2]: LSQ weights folded with the inverse matrix
+    std::vector<double> d_gg;                    // per entry [4]: Green-Gauss s*A*nx/V, s*A*ny/V, owner weight, 0
+    std::vector<double> d_erf;                   // per entry [2]: face midpoint - cell centroid
+    std::vector<double> d_frf;                   // per face [4]: x_f - x_L, x_f - x_R (R: zero on boundary)
+    std::vector<double> d_h;                     // per cell: sqrt(volume) (limiter length scale)
+
     void compute_face_geometry();                // UnstructuredMesh::compute_geometry
     void build_device_layout(int reorder);
+    void build_o2_geometry();
 };
 
 // src/MeshReader.cpp:317-456 (+ validate_mesh_geometry :125-288).

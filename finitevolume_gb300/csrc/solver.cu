@@ -43,6 +43,7 @@ static T* dupload(const std::vector<T>& v, std::vector<void*>& owned) {
 }
 
 Solver::~Solver() {
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     for (void* p : owned) cudaFree(p);
     if (hist) cudaFree(hist);
@@ -57,9 +58,25 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     if (hm.n_patches > kMaxPatches) raise(FV_ERR_UNSUPPORTED, "more than 32 boundary patches");
     if (!(g > 1.0)) raise(FV_ERR_BAD_ARG, "gamma must be > 1");
     opt = o;
-    if (opt.order != 1 || opt.rk_stages != 1 || opt.viscous || opt.precision != FV_PREC_FP64)
-        raise(FV_ERR_UNSUPPORTED, "this build supports order 1, forward Euler, inviscid FP64");
     if (opt.flux < 0 || opt.flux > 2) raise(FV_ERR_BAD_ARG, "unknown flux scheme");
+    if (opt.order != 1 && opt.order != 2) raise(FV_ERR_BAD_ARG, "order must be 1 or 2");
+    if (opt.rk_stages != 1 && opt.rk_stages != 3) raise(FV_ERR_BAD_ARG, "rk_stages must be 1 or 3");
+    if (opt.precision != FV_PREC_FP64 && opt.precision != FV_PREC_FP32_FLUX) raise(FV_ERR_BAD_ARG, "unknown precision");
+    if (opt.gradient < 0 || opt.gradient > 1 || opt.limiter < 0 || opt.limiter > 2)
+        raise(FV_ERR_BAD_ARG, "unknown gradient scheme or limiter");
+    if (opt.dt_mode != FV_DT_GLOBAL && opt.dt_mode != FV_DT_LOCAL) raise(FV_ERR_BAD_ARG, "unknown dt mode");
+    if (opt.viscous) raise(FV_ERR_UNSUPPORTED, "viscous terms are not in this build");
+    general = !(opt.order == 1 && opt.rk_stages == 1 && opt.precision == FV_PREC_FP64);
+    if (general && opt.strict) raise(FV_ERR_UNSUPPORTED, "strict mode covers the reference's first-order scheme only");
+    if (general && opt.precision == FV_PREC_FP32_FLUX && opt.flux == FV_FLUX_EXACT)
+        raise(FV_ERR_UNSUPPORTED, "the exact Riemann flux runs in FP64 only");
+    cfg.fp32 = opt.precision == FV_PREC_FP32_FLUX;
+    cfg.flux = opt.flux;
+    cfg.order = opt.order;
+    cfg.gradient = opt.gradient;
+    cfg.limiter = opt.limiter;
+    cfg.stages = opt.rk_stages;
+    cfg.local_dt = opt.dt_mode == FV_DT_LOCAL;
     gamma = g;
     N = hm.n_cells;
     F = hm.n_faces;
@@ -104,7 +121,9 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     m.cxy = reinterpret_cast<const double2*>(dupload(hm.d_cxy, owned));
 
     U = dalloc<St>(N, owned);
-    ff = dalloc<St>(F, owned);
+    staging = dalloc<St>(N, owned);
+    d_perm = dupload(hm.perm, owned);
+    if (!(general && cfg.fp32)) ff = dalloc<St>(F, owned);
     dtf = dalloc<double>(F, owned);
     n_cell_blocks = (N + kCellBlock - 1) / kCellBlock;
     partials = dalloc<double>(4 * (size_t)n_cell_blocks, owned);
@@ -116,6 +135,24 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     std::memcpy(&c0.dt_bits, &dmax, sizeof(dmax));
     FV_CUDA(cudaMemcpy(ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice));
     ensure_history(64);
+
+    if (general) {
+        HostMesh h2 = hm;  // the per-entry geometry is derived on a copy
+        h2.build_o2_geometry();
+        const size_t wsz = cfg.fp32 ? 16 : 32;
+        U0 = dalloc<St>(N, owned);
+        W = dalloc<char>(wsz * (size_t)N, owned);
+        G = dalloc<char>(2 * wsz * (size_t)N, owned);
+        if (cfg.fp32) ff = reinterpret_cast<St*>(dalloc<char>(16 * (size_t)F, owned));
+        cs = dalloc<double>(N, owned);
+        dtv = dalloc<double>(N, owned);
+        cnb = dupload(h2.d_cnb, owned);
+        if (cfg.gradient == 0) lsq = reinterpret_cast<const double2*>(dupload(h2.d_lsq, owned));
+        else gg = reinterpret_cast<const double4_32a*>(dupload(h2.d_gg, owned));
+        erf = reinterpret_cast<const double2*>(dupload(h2.d_erf, owned));
+        frf = reinterpret_cast<const double4_32a*>(dupload(h2.d_frf, owned));
+        hcell = dupload(h2.d_h, owned);
+    }
 
     // Initial condition, reference numbering then device order
     // (src/EulerFVMSolver.cpp:24-37).
@@ -168,10 +205,94 @@ O1Args Solver::o1_args() const {
     return a;
 }
 
-void Solver::launch_step() {
-    O1Args a = o1_args();
-    if (opt.strict) strict::launch_o1_step(a, stream);
-    else fast::launch_o1_step(a, stream);
+O2Args Solver::o2_args() const {
+    O2Args a;
+    a.m = dm;
+    a.cnb = cnb;
+    a.lsq = lsq;
+    a.gg = gg;
+    a.erf = erf;
+    a.frf = frf;
+    a.h = hcell;
+    a.U = U;
+    a.U0 = U0;
+    a.W = W;
+    a.G = G;
+    a.ff = ff;
+    a.cs = cs;
+    a.dtf = dtf;
+    a.dtv = dtv;
+    a.ctl = ctl;
+    a.partials = partials;
+    a.hist = hist;
+    a.hist_cap = hist_cap;
+    a.bc = bc;
+    a.gamma = gamma;
+    a.venkat_k = opt.venkat_k;
+    a.exact_tol = opt.exact_tol;
+    a.exact_max_iter = opt.exact_max_iter;
+    return a;
+}
+
+void Solver::refresh_primitives() {
+    if (!general) return;
+    O2Args a = o2_args();
+    if (cfg.fp32) o2::launch_prim_f32(a, stream);
+    else o2::launch_prim_f64(a, stream);
+    FV_CUDA(cudaGetLastError());
+}
+
+// Launches one step's kernels in order; kernel class of each launch is
+// appended to *classes when given (0 gradients, 1 face fluxes, 2 update).
+void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos) {
+    auto mark = [&](int cls) {
+        if (classes) classes->push_back(cls);
+        if (events) FV_CUDA(cudaEventRecord((*events)[++*ev_pos], stream));
+    };
+    if (!general) {
+        O1Args a = o1_args();
+        for (int part = 0; part < 2; ++part) {
+            if (opt.strict) strict::launch_o1_part(a, part, stream);
+            else fast::launch_o1_part(a, part, stream);
+            mark(part + 1);
+        }
+        return;
+    }
+    O2Args a = o2_args();
+    for (int st = 0; st < cfg.stages; ++st) {
+        for (int part = (cfg.order == 2 ? 0 : 1); part < 3; ++part) {
+            if (cfg.fp32) o2::launch_part_f32(a, cfg, st, part, stream);
+            else o2::launch_part_f64(a, cfg, st, part, stream);
+            mark(part);
+        }
+    }
+}
+
+void Solver::step_timed(int n, double ms[3], int launches[3]) {
+    if (n <= 0) raise(FV_ERR_BAD_ARG, "step_timed needs n > 0");
+    ensure_history(n);
+    const int per_step = general ? cfg.stages * (cfg.order == 2 ? 3 : 2) : 2;
+    const size_t need = (size_t)n * per_step + 1;
+    while (events.size() < need) {
+        cudaEvent_t e;
+        FV_CUDA(cudaEventCreate(&e));
+        events.push_back(e);
+    }
+    std::vector<int> classes;
+    classes.reserve(need);
+    size_t pos = 0;
+    FV_CUDA(cudaEventRecord(events[0], stream));
+    for (int i = 0; i < n; ++i) launch_step(&classes, &events, &pos);
+    FV_CUDA(cudaGetLastError());
+    FV_CUDA(cudaEventSynchronize(events[pos]));
+    for (int k = 0; k < 3; ++k) { ms[k] = 0.0; launches[k] = 0; }
+    for (size_t i = 0; i < classes.size(); ++i) {
+        float t = 0.f;
+        FV_CUDA(cudaEventElapsedTime(&t, events[i], events[i + 1]));
+        ms[classes[i]] += t;
+        launches[classes[i]] += 1;
+    }
+    steps_taken += n;
 }
 
 cudaGraphExec_t Solver::graph_for(int k) {
@@ -179,7 +300,7 @@ cudaGraphExec_t Solver::graph_for(int k) {
     if (it != graphs.end()) return it->second;
     cudaGraph_t g = nullptr;
     FV_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < k; ++i) launch_step();
+    for (int i = 0; i < k; ++i) launch_step(nullptr, nullptr, nullptr);
     FV_CUDA(cudaStreamEndCapture(stream, &g));
     cudaGraphExec_t ge = nullptr;
     FV_CUDA(cudaGraphInstantiate(&ge, g, 0));
@@ -219,22 +340,29 @@ void Solver::history(int n, double* out) {
     }
 }
 
+// Device-order <-> reference-order permutation of the state, on the GPU so
+// that host buffers cross PCIe/C2C once and untouched by the host.
+__global__ void k_scatter_state(const St* __restrict__ U, St* __restrict__ out, const int* __restrict__ perm, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[perm[i]] = U[i];
+}
+__global__ void k_gather_state(const St* __restrict__ in, St* __restrict__ U, const int* __restrict__ perm, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) U[i] = in[perm[i]];
+}
+
 void Solver::download_field(double* out) {
-    std::vector<St> d(N);
-    FV_CUDA(cudaMemcpyAsync(d.data(), U, sizeof(St) * (size_t)N, cudaMemcpyDeviceToHost, stream));
+    k_scatter_state<<<(N + 255) / 256, 256, 0, stream>>>(U, staging, d_perm, N);
+    FV_CUDA(cudaGetLastError());
+    FV_CUDA(cudaMemcpyAsync(out, staging, sizeof(St) * (size_t)N, cudaMemcpyDeviceToHost, stream));
     FV_CUDA(cudaStreamSynchronize(stream));
-    for (int i = 0; i < N; ++i) {
-        const St& s = d[i];
-        double* o = out + 4 * (size_t)perm[i];
-        o[0] = s.r; o[1] = s.ru; o[2] = s.rv; o[3] = s.E;
-    }
 }
 
 void Solver::upload_field(const void* in_ref_order) {
-    const St* in = static_cast<const St*>(in_ref_order);
-    std::vector<St> d(N);
-    for (int i = 0; i < N; ++i) d[i] = in[perm[i]];
-    FV_CUDA(cudaMemcpyAsync(U, d.data(), sizeof(St) * (size_t)N, cudaMemcpyHostToDevice, stream));
+    FV_CUDA(cudaMemcpyAsync(staging, in_ref_order, sizeof(St) * (size_t)N, cudaMemcpyHostToDevice, stream));
+    k_gather_state<<<(N + 255) / 256, 256, 0, stream>>>(staging, U, d_perm, N);
+    FV_CUDA(cudaGetLastError());
+    refresh_primitives();
     // residual() resets to zero (include/EulerFVMSolver.h:151-155)
     static const double z[4] = {0, 0, 0, 0};
     static const int zi = 0;
@@ -479,6 +607,18 @@ int fv_step(fv_solver_t s, int32_t n, double* history) {
         if (c.nonfinite) fvgb::raise(FV_ERR_NONFINITE, "non-finite residual norm");
     });
     return rc;
+}
+
+int fv_step_timed(fv_solver_t s, int32_t n, double kernel_ms[3], int32_t launches[3]) {
+    return guarded([&] {
+        if (!s || !kernel_ms || !launches) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        int l[3];
+        s->s.step_timed(n, kernel_ms, l);
+        for (int k = 0; k < 3; ++k) launches[k] = l[k];
+        fvgb::StepCtl c;
+        s->s.read_ctl(c);
+        if (c.nonfinite) fvgb::raise(FV_ERR_NONFINITE, "non-finite residual norm");
+    });
 }
 
 int fv_get_history(fv_solver_t s, int32_t n, double* history) {

@@ -27,6 +27,8 @@ struct Solver {
     DevMesh dm{};
 
     St* U = nullptr;
+    St* staging = nullptr;     // reference-order copy for get/set field
+    int* d_perm = nullptr;     // device cell -> reference cell
     St* ff = nullptr;
     double* dtf = nullptr;
     double* partials = nullptr;
@@ -35,17 +37,36 @@ struct Solver {
     StepCtl* ctl = nullptr;
     long long steps_taken = 0;
 
+    // second-order / multi-stage path
+    bool general = false;           // false: reference-mode first-order kernels
+    O2Config cfg{};
+    St* U0 = nullptr;
+    void* W = nullptr;
+    void* G = nullptr;
+    double* cs = nullptr;
+    double* dtv = nullptr;
+    const int* cnb = nullptr;
+    const double2* lsq = nullptr;
+    const double4_32a* gg = nullptr;
+    const double2* erf = nullptr;
+    const double4_32a* frf = nullptr;
+    const double* hcell = nullptr;
+
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::map<int, cudaGraphExec_t> graphs;
     std::vector<void*> owned;
+    std::vector<cudaEvent_t> events;  // step_timed event pool
 
     ~Solver();
     void init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, double cfl, const fv_ic_t& ic,
               const fv_options_t& o);
     void ensure_history(int n);
     O1Args o1_args() const;
-    void launch_step();
+    O2Args o2_args() const;
+    void refresh_primitives();
+    void launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos);
+    void step_timed(int n, double ms[3], int launches[3]);
     cudaGraphExec_t graph_for(int k);
     void step_async(int n);
     void read_ctl(StepCtl& c);

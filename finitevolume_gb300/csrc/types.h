@@ -54,7 +54,7 @@ struct O1Args {
     DevMesh m;
     St* U;
     St* ff;            // [F] face fluxes (times face length)
-    double* dtf;       // [F] per-face CFL time step (local dt)
+    double* dtf;       // [F] per-face lambda * length (local dt)
     StepCtl* ctl;
     double* partials;  // [cell blocks * 4]
     double* hist;      // [hist_cap * 4]
@@ -66,10 +66,55 @@ struct O1Args {
     int local_dt;
 };
 
+struct O2Args {
+    DevMesh m;
+    const int* cnb;          // per entry: neighbour or -1-face
+    const double2* lsq;      // per entry LSQ weights
+    const double4_32a* gg;   // per entry Green-Gauss coefficients
+    const double2* erf;      // per entry face offset
+    const double4_32a* frf;  // per face offsets from the owner / neighbour centroid
+    const double* h;         // per cell sqrt(volume)
+    St* U;
+    St* U0;
+    void* W;                 // primitive copy: St (FP64) or float4 (FP32 flux)
+    void* G;                 // limited gradients: 4 double2 or 2 float4 per cell
+    void* ff;                // face fluxes: St or float4
+    double* cs;              // per cell sound speed (cell-centred, for dt)
+    double* dtf;             // per face lambda * length (local dt)
+    double* dtv;             // per cell dt/volume of the current iteration
+    StepCtl* ctl;
+    double* partials;
+    double* hist;
+    int hist_cap;
+    BCTable bc;
+    double gamma, venkat_k, exact_tol;
+    int exact_max_iter;
+};
+
+// Second-order path configuration (validated by the solver).
+struct O2Config {
+    int fp32;      // 1: FP32 flux/gradient arithmetic
+    int flux;      // 0 Rusanov, 1 HLLC, 2 exact
+    int order;     // 1 or 2
+    int gradient;  // 0 LSQ, 1 Green-Gauss
+    int limiter;   // 0 none, 1 Barth-Jespersen, 2 Venkatakrishnan
+    int stages;    // 1 or 3
+    int local_dt;  // 1 local, 0 global
+};
+
 constexpr int kCellBlock = 256;
 constexpr int kFaceBlock = 256;
 
-namespace fast { void launch_o1_step(const O1Args& a, cudaStream_t s); }
-namespace strict { void launch_o1_step(const O1Args& a, cudaStream_t s); }
+namespace o2 {
+void launch_prim_f64(const O2Args& a, cudaStream_t s);
+void launch_prim_f32(const O2Args& a, cudaStream_t s);
+// part 0: gradients + limiter (order 2 only), 1: face fluxes, 2: update.
+void launch_part_f64(const O2Args& a, const O2Config& c, int stage, int part, cudaStream_t s);
+void launch_part_f32(const O2Args& a, const O2Config& c, int stage, int part, cudaStream_t s);
+}  // namespace o2
+
+// part 0: face pass, 1: cell pass.
+namespace fast { void launch_o1_part(const O1Args& a, int part, cudaStream_t s); }
+namespace strict { void launch_o1_part(const O1Args& a, int part, cudaStream_t s); }
 
 }  // namespace fvgb

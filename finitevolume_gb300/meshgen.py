@@ -345,6 +345,34 @@ def naca_mixed(ni: int = 1024, nj: int = 512, first: float = 1e-3, r_core: float
     return mesh
 
 
+def cached(name: str, **kw) -> PolyMesh:
+    """Generate ``name(**kw)`` once and keep it as .npz in a cache folder.
+
+    The folder is ``$FV_MESH_CACHE`` or ``~/.cache/finitevolume_gb300``; the
+    key is the generator name and its keyword arguments.
+    """
+    import hashlib
+    import json
+    import os
+
+    from .fvmesh import PolyMesh as _PM
+
+    root = os.environ.get("FV_MESH_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "finitevolume_gb300"))
+    key = hashlib.sha256(json.dumps([name, sorted(kw.items())], default=str).encode()).hexdigest()[:16]
+    path = os.path.join(root, f"{name}_{key}.npz")
+    if os.path.exists(path):
+        z = np.load(path, allow_pickle=False)
+        return _PM(z["nodes"], z["cell_off"], z["cell_nodes"], z["bedges"], z["bpatch"],
+                   [str(x) for x in z["patch_names"]])
+    m = globals()[name](**kw)
+    os.makedirs(root, exist_ok=True)
+    tmp = path + f".{os.getpid()}.tmp.npz"
+    np.savez(tmp, nodes=m.nodes, cell_off=m.cell_off, cell_nodes=m.cell_nodes, bedges=m.bedges, bpatch=m.bpatch,
+             patch_names=np.array(m.patch_names))
+    os.replace(tmp, path)
+    return m
+
+
 # --------------------------------------------------------------------------
 # Simple test meshes
 # --------------------------------------------------------------------------

@@ -1,0 +1,61 @@
+"""Algorithmic HBM bytes of the residual-and-update loop (one place).
+
+Counts are per launch, with every array that a kernel must read or write
+crossing HBM exactly once (neighbour gathers re-read nothing).  N cells, F
+faces, Fb boundary faces, E = 2F - Fb cell-face (CSR) entries; s = 8 bytes
+(FP64) or 4 (FP32-flux mode) for the flux-precision arrays (primitive copy
+W, gradients G, face fluxes).
+
+Whole residual evaluation, per the survey's per-stage formula (one RK stage
+of 2nd-order MUSCL with materialised gradient and limiter arrays):
+    B2 = 340 N + 56 F
+and first order, forward Euler, local dt:
+    B1 = 76 N + 40 F
+
+Per kernel of this implementation (the limiter is fused into the gradient
+kernel, so no limiter array exists; face fluxes are materialised once):
+    gradients  W r (4s N) + G w (8s N) + CSR offsets 4N + entries 4E
+               + LSQ geometry (24 inverse + 16 centroid) N + face midpoints 16F
+               + h 8N
+    faces      W r (4s N) + G r (8s N) + face normal/length 24F + owner/
+               neighbour 8F + midpoints 16F + centroids 16N + fluxes w (4s F)
+    update     fluxes r (4s F) + CSR offsets 4N + entries 4E + U r/w 64N
+               + U0 32N + W w (4s N) + dt/V 8N + volume 8N
+"""
+from __future__ import annotations
+
+
+def survey_stage_bytes(n: int, f: int) -> float:
+    """B2: algorithmic bytes of one 2nd-order RK stage (survey formula)."""
+    return 340.0 * n + 56.0 * f
+
+
+def survey_o1_bytes(n: int, f: int) -> float:
+    """B1: first order, forward Euler, local dt."""
+    return 76.0 * n + 40.0 * f
+
+
+def kernel_bytes(kind: str, n: int, f: int, fb: int, fp32: bool = False) -> float:
+    s = 4.0 if fp32 else 8.0
+    e = 2 * f - fb
+    if kind == "gradients":
+        return 4 * s * n + 8 * s * n + 4 * n + 4 * e + 40 * n + 16 * f + 8 * n
+    if kind == "faces":
+        return 4 * s * n + 8 * s * n + 24 * f + 8 * f + 16 * f + 16 * n + 4 * s * f
+    if kind == "update":
+        return 4 * s * f + 4 * n + 4 * e + 64 * n + 32 * n + 4 * s * n + 8 * n + 8 * n
+    raise ValueError(kind)
+
+
+KERNEL_NAMES = ("gradients", "faces", "update")
+
+
+# DRAM bytes per cell per launch measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) on the mixed-mesh workload; filled in from the
+# captures summarised under profiles/.  None = not captured yet.
+MEASURED_TRAFFIC_PER_CELL = {"gradients": None, "faces": None, "update": None}
+
+
+def measured_traffic(kind: str, n_cells: int):
+    b = MEASURED_TRAFFIC_PER_CELL.get(kind)
+    return None if b is None else round(b * n_cells)

@@ -246,6 +246,16 @@ class EulerFVMSolver:
     def step_async(self, n: int) -> None:
         capi.check(capi.lib().fv_step_async(self._h, int(n)))
 
+    def step_timed(self, n: int):
+        """Advance n steps with per-kernel CUDA-event timing.
+
+        Returns (ms[3], launches[3]) for kernel classes gradients, face fluxes,
+        cell update."""
+        ms = np.zeros(3)
+        cnt = np.zeros(3, np.int32)
+        capi.check(capi.lib().fv_step_timed(self._h, int(n), capi.dptr(ms), capi.i32ptr(cnt)))
+        return ms, cnt
+
     def history(self, n: int) -> np.ndarray:
         out = np.zeros((n, 4))
         capi.check(capi.lib().fv_get_history(self._h, int(n), capi.dptr(out)))

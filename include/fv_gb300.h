@@ -183,6 +183,14 @@ int fv_solver_set_stream(fv_solver_t s, void* stream);
 int fv_step(fv_solver_t s, int32_t n, double* history);
 /* Enqueue n steps without synchronising (history stays on the device). */
 int fv_step_async(fv_solver_t s, int32_t n);
+/*
+ * Advance n steps with every kernel launched directly (no graph) and a CUDA
+ * event recorded on the solver's stream after each launch; synchronises.
+ * kernel_ms[k] receives the summed device time and launches[k] the number
+ * of launches of each kernel class: 0 gradients + limiter, 1 face fluxes,
+ * 2 cell update.  Same results as fv_step.
+ */
+int fv_step_timed(fv_solver_t s, int32_t n, double kernel_ms[3], int32_t launches[3]);
 /* Copy the last n residual-norm rows recorded on the device (n x 4). */
 int fv_get_history(fv_solver_t s, int32_t n, double* history);
 

@@ -385,16 +385,32 @@ struct Euler {
         return dt;
     }
 
+    // Face spectral radius times length: max(|Vn|+c) over the face's cells
+    // (the wave-speed estimate of compute_dt) times the face length.
+    double face_lambda_area(const Face& f, const std::vector<State>& V) const {
+        const State& UL = V[f.cell_left];
+        double uL = UL.rho_u / UL.rho, vL = UL.rho_v / UL.rho;
+        double Smax = std::fabs(uL * f.nx + vL * f.ny) + sound_speed(UL, gamma);
+        if (f.cell_right != -1) {
+            const State& UR = V[f.cell_right];
+            double uR = UR.rho_u / UR.rho, vR = UR.rho_v / UR.rho;
+            Smax = std::max(Smax, std::fabs(uR * f.nx + vR * f.ny) + sound_speed(UR, gamma));
+        }
+        return Smax * f.area;
+    }
+
+    // Local time stepping (new): dt_i = CFL * V_i / sum_f lambda_f A_f, the
+    // usual local-CFL definition for steady explicit solvers.
     void compute_local_dt() {
-        std::vector<double> fdt(mesh.faces.size());
+        std::vector<double> la(mesh.faces.size());
 #pragma omp parallel for
-        for (long i = 0; i < (long)mesh.faces.size(); ++i) fdt[i] = face_dt(mesh.faces[i], U);
+        for (long i = 0; i < (long)mesh.faces.size(); ++i) la[i] = face_lambda_area(mesh.faces[i], U);
         dtc.resize(mesh.cells.size());
 #pragma omp parallel for
         for (long c = 0; c < (long)mesh.cells.size(); ++c) {
-            double d = std::numeric_limits<double>::max();
-            for (int f : mesh.cells[c].faces) d = std::min(d, fdt[f]);
-            dtc[c] = d;
+            double s = 0.0;
+            for (int f : mesh.cells[c].faces) s += la[f];
+            dtc[c] = cfl * mesh.cells[c].volume / s;
         }
     }
 
@@ -747,6 +763,18 @@ void orc_euler_field(void* ep, double* out) {
 void orc_euler_set_field(void* ep, const double* in) {
     auto* e = static_cast<orc::Euler*>(ep);
     std::memcpy(e->U.data(), in, e->U.size() * sizeof(orc::State));
+}
+// Limited gradients of (rho, u, v, p) for the current state: N x 8
+// (gx[4], gy[4]); also the primitive state N x 4.
+void orc_euler_gradients(void* ep, double* grad, double* prim) {
+    auto* e = static_cast<orc::Euler*>(ep);
+    std::vector<orc::Prim> W;
+    std::vector<orc::Grad4> G;
+    e->gradients(e->U, W, G);
+    for (size_t c = 0; c < W.size(); ++c) {
+        std::memcpy(grad + 8 * c, &G[c], 8 * sizeof(double));
+        std::memcpy(prim + 4 * c, &W[c], 4 * sizeof(double));
+    }
 }
 void orc_euler_set_cfl(void* ep, double cfl) { static_cast<orc::Euler*>(ep)->cfl = cfl; }
 // Pressure-only wall forces (inviscid): same accumulation as compute_wall_forces.

@@ -40,6 +40,7 @@ def lib():
         L.orc_euler_run.argtypes = [C.c_void_p, C.c_int, _D]
         L.orc_euler_field.argtypes = [C.c_void_p, _D]
         L.orc_euler_set_field.argtypes = [C.c_void_p, _D]
+        L.orc_euler_gradients.argtypes = [C.c_void_p, _D, _D]
         L.orc_euler_set_cfl.argtypes = [C.c_void_p, C.c_double]
         L.orc_euler_wall_forces.argtypes = [C.c_void_p, _I, _D, _D]
         L.orc_diff_create.restype = C.c_void_p
@@ -119,6 +120,13 @@ class OracleEuler:
 
     def set_cfl(self, c: float) -> None:
         lib().orc_euler_set_cfl(self.h, c)
+
+    def gradients(self):
+        """(limited gradients N x 8 as gx[4], gy[4]; primitives N x 4) of the current state."""
+        g = np.zeros((self.n_cells, 8))
+        w = np.zeros((self.n_cells, 4))
+        lib().orc_euler_gradients(self.h, g.ctypes.data_as(_D), w.ctypes.data_as(_D))
+        return g, w
 
     def wall_forces(self, is_wall, ref):
         out = np.zeros(11)
