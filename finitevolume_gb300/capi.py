@@ -51,6 +51,16 @@ class Options(C.Structure):
                 ("mu", C.c_double), ("prandtl", C.c_double)]
 
 
+class NoAllocMesh(C.Structure):
+    """fv_noalloc_mesh_t: device pointers in the caller's numbering."""
+    _fields_ = [("n_cells", C.c_int32), ("n_faces", C.c_int32), ("face_left", C.c_void_p),
+                ("face_right", C.c_void_p), ("face_patch", C.c_void_p), ("face_geom", C.c_void_p),
+                ("cell_face_off", C.c_void_p), ("cell_faces", C.c_void_p), ("cell_volume", C.c_void_p)]
+
+
+NOALLOC_MAX_FACES = 131072
+NOALLOC_MAX_CELLS = 131072
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I32 = C.POINTER(C.c_int32)
@@ -85,6 +95,8 @@ SIGNATURES = {
     "fv_get_gamma": (C.c_int, [_P, _D]),
     "fv_device_state": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P)]),
     "fv_wall_forces": (C.c_int, [_P, _D, _D]),
+    "fv_step_noalloc": (C.c_int, [C.POINTER(NoAllocMesh), C.POINTER(BC), C.c_int32, C.c_double, C.c_double,
+                                  C.c_int32, _P, _D, _P]),
 }
 
 _lib = None

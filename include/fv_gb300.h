@@ -214,6 +214,52 @@ int fv_device_state(fv_solver_t s, void** U_dev, void** stream);
  * cd_pressure, cd_total, cl, cm, n_wall_faces (domain total). */
 int fv_wall_forces(fv_solver_t s, const double ref[7], double out[11]);
 
+/* ------------------------------------------------------------------------
+ * Allocation-free step
+ * ------------------------------------------------------------------------ */
+/*
+ * No counterpart in the reference.  For callers that cannot let a library
+ * allocate device memory: an application that owns the whole device budget
+ * and serves it from its own pool, code running while other threads capture
+ * CUDA graphs in relaxed mode (allocation is illegal there), or a real-time
+ * loop that forbids allocation after start-up.  The caller keeps the mesh
+ * and the state in its own device buffers; this entry point performs one
+ * first-order step of EulerFVMSolver::step (global CFL dt, the caller's
+ * flux) and calls no cudaMalloc, cudaFree or allocating library routine.
+ *
+ * Its work arrays live in one fixed, file-scope device array of about
+ * 4 MiB, held by every GPU that loads the library until the process exits;
+ * hence the limits below (larger meshes fail with FV_ERR_BAD_ARG).  The
+ * first call on each device resolves that array's device address (and may
+ * load the module): make the first call before any stream capture.  All
+ * calls share the array; calls whose GPU work overlaps race on it and must
+ * be serialised by the caller.  The call synchronises `stream`.
+ *
+ * Mesh arrays are device pointers in the caller's cell/face numbering:
+ *   face_left/face_right [F] (right = -1 on boundary faces), face_patch [F],
+ *   face_geom [4F] = nx, ny, length, CFL length (min(V_L, V_R)/length, or
+ *   V_L/length on boundary faces), 32-byte aligned,
+ *   cell_face_off [N+1], cell_faces [E] = face << 1 | (cell owns the face),
+ *   listed in the reference's per-cell face order, cell_volume [N].
+ * U: device, AoS double[4] per cell, 32-byte aligned, updated in place.
+ * norms: host, receives the step's residual norms (EulerResidualNorms).
+ */
+#define FV_NOALLOC_MAX_FACES 131072
+#define FV_NOALLOC_MAX_CELLS 131072
+typedef struct {
+    int32_t n_cells, n_faces;
+    const int32_t* face_left;
+    const int32_t* face_right;
+    const int32_t* face_patch;
+    const double* face_geom;
+    const int32_t* cell_face_off;
+    const int32_t* cell_faces;
+    const double* cell_volume;
+} fv_noalloc_mesh_t;
+
+int fv_step_noalloc(const fv_noalloc_mesh_t* mesh, const fv_bc_t* bcs, int32_t n_bcs, double gamma, double cfl,
+                    int32_t flux, double* U, double norms[4], void* stream);
+
 #ifdef __cplusplus
 }
 #endif
