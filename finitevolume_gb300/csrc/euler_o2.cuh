@@ -130,10 +130,16 @@ __device__ __forceinline__ V4<T> rusanov_p(const V4<T>& L, const V4<T>& R, T nx,
 // HLLC on primitive inputs (HllcFlux.h:35-76), rearranged to four divisions:
 // with q = 1/(S_K - S*), the star factor is rho_K (S_K - Vn_K) q and the
 // pressure term of E* reduces to (S* - Vn_K) p_K q.
+template <typename T> __device__ __forceinline__ T trsqrt(T x);
+template <> __device__ __forceinline__ double trsqrt<double>(double x) { return rsqrt(x); }
+template <> __device__ __forceinline__ float trsqrt<float>(float x) { return rsqrtf(x); }
+
 template <typename T>
 __device__ __forceinline__ V4<T> hllc_p(const V4<T>& L, const V4<T>& R, T nx, T ny, T g, T igm1) {
     T irL = T(1) / L.r, irR = T(1) / R.r;
-    T cL = tsqrt<T>(g * L.p * irL), cR = tsqrt<T>(g * R.p * irR);
+    // c = sqrt(t) computed as t * rsqrt(t): cheaper than sqrt on the FP64 pipe.
+    const T tL = g * L.p * irL, tR = g * R.p * irR;
+    T cL = tL * trsqrt<T>(tL), cR = tR * trsqrt<T>(tR);
     T VnL = L.u * nx + L.v * ny, VnR = R.u * nx + R.v * ny;
     T EL = L.p * igm1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
     T ER = R.p * igm1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
@@ -202,6 +208,24 @@ __device__ __forceinline__ V4<T> ghost_prim(const BCTable& bc, int patch, const 
 
 using fvgb::O2Args;
 
+// Order-preserving integer key of an IEEE value (negative values have their
+// magnitude bits flipped), so that integer compares -- on the integer pipe,
+// not the scarce FP64 pipe -- order values like the floating-point compare
+// (NaNs excepted).  val() inverts key().
+template <typename T> struct OKey;
+template <> struct OKey<double> {
+    using I = long long;
+    __device__ static I bits(double x) { return __double_as_longlong(x); }
+    __device__ static I key(double x) { I b = __double_as_longlong(x); return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
+    __device__ static double val(I k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL)); }
+};
+template <> struct OKey<float> {
+    using I = int;
+    __device__ static I bits(float x) { return __float_as_int(x); }
+    __device__ static I key(float x) { I b = __float_as_int(x); return b ^ ((b >> 31) & 0x7fffffff); }
+    __device__ static float val(I k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
+};
+
 // ---------------------------------------------------------------------------
 template <typename T, int GRAD, int LIM>
 __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
@@ -213,7 +237,16 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
     const T g = (T)a.gamma;
     const V4<T> wc = WS::ld(W, c);
     const T* wcv = &wc.r;
+    using OK = OKey<T>;
+    using I = typename OK::I;
     T gx[4] = {0, 0, 0, 0}, gy[4] = {0, 0, 0, 0}, dmax[4] = {0, 0, 0, 0}, dmin[4] = {0, 0, 0, 0};
+    // Neighbour max/min on the integer pipe: order-preserving integer keys of
+    // the values, starting from the cell's own value (so that
+    // max_j W_j - W_c equals the max over the differences, including 0,
+    // bit for bit).
+    I kmax[4], kmin[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) kmax[k] = kmin[k] = OK::key(wcv[k]);
     const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
     for (int e = e0; e < e1; ++e) {
         const int nb = a.cnb[e];
@@ -228,15 +261,17 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
         }
         const T* wnv = &wn.r;
         if (GRAD == 0) {
+            // sum_j a_j (W_j - W_c) = sum_j a_j W_j - (sum_j a_j) W_c; the
+            // weight sums are per-cell geometry (lsq_sum).
             const double2 ab = __ldg(a.lsq + e);
             const T ax = (T)ab.x, ay = (T)ab.y;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                T d = wnv[k] - wcv[k];
-                dmax[k] = fmax(dmax[k], d);
-                dmin[k] = fmin(dmin[k], d);
-                gx[k] += ax * d;
-                gy[k] += ay * d;
+                const I kk = OK::key(wnv[k]);
+                kmax[k] = kmax[k] < kk ? kk : kmax[k];
+                kmin[k] = kk < kmin[k] ? kk : kmin[k];
+                gx[k] += ax * wnv[k];
+                gy[k] += ay * wnv[k];
             }
         } else {
             const double4_32a q = a.gg[e];
@@ -252,6 +287,16 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
             }
         }
     }
+    if (GRAD == 0) {
+        const double2 s = __ldg(a.lsq_sum + c);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            gx[k] -= (T)s.x * wcv[k];
+            gy[k] -= (T)s.y * wcv[k];
+            dmax[k] = OK::val(kmax[k]) - wcv[k];
+            dmin[k] = OK::val(kmin[k]) - wcv[k];
+        }
+    }
     if (LIM != 0) {
         T eps2 = T(0);
         if (LIM == 2) {
@@ -264,14 +309,20 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
             const T rx = (T)r.x, ry = (T)r.y;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                T d2 = gx[k] * rx + gy[k] * ry;
-                if (d2 == T(0)) continue;
-                T d1 = d2 > T(0) ? dmax[k] : dmin[k];
+                const T d2 = gx[k] * rx + gy[k] * ry;
+                const I bits = OK::bits(d2);
+                if ((bits << 1) == 0) continue;          // d2 == 0: the face does not limit
+                const T d1 = bits < 0 ? dmin[k] : dmax[k];
                 T num, den;
-                if (LIM == 1) { num = d1; den = d2; if (den < T(0)) { num = -num; den = -den; } }
-                else {
-                    num = d1 * d1 + eps2 + T(2) * d2 * d1;
-                    den = d1 * d1 + T(2) * d2 * d2 + d1 * d2 + eps2;
+                if (LIM == 1) {
+                    num = fabs(d1);
+                    den = fabs(d2);
+                } else {
+                    // (d1^2 + eps^2 + 2 d1 d2) / (d1^2 + 2 d2^2 + d1 d2 + eps^2)
+                    const T p = d1 * d2;
+                    const T q = d1 * d1 + eps2;
+                    num = q + T(2) * p;
+                    den = (d2 + d2) * d2 + (q + p);
                 }
                 if (num * dmn[k] < nmin[k] * den) { nmin[k] = num; dmn[k] = den; }
             }
@@ -293,7 +344,9 @@ template <typename T>
 __device__ __forceinline__ V4<T> recon(const V4<T>& w, const G8<T>& g, T rx, T ry) {
     V4<T> o = {w.r + (g.gx[0] * rx + g.gy[0] * ry), w.u + (g.gx[1] * rx + g.gy[1] * ry),
                w.v + (g.gx[2] * rx + g.gy[2] * ry), w.p + (g.gx[3] * rx + g.gy[3] * ry)};
-    if (!(o.r > T(0)) || !(o.p > T(0))) return w;
+    // Positivity fallback; "x > 0" tested on the integer pipe (sign bit clear
+    // and not +0).
+    if (OKey<T>::bits(o.r) <= 0 || OKey<T>::bits(o.p) <= 0) return w;
     return o;
 }
 
@@ -386,9 +439,10 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
         }
         double dtv;
         if (STAGE == 0) {
-            // Local: dt_i = cfl V_i / sum_f lambda_f A_f; global: the min over faces.
-            double dt = (DT == 2) ? a.ctl->cfl * a.m.vol[c] / lam : __longlong_as_double((long long)a.ctl->dt_bits);
-            dtv = dt / a.m.vol[c];
+            // Local: dt_i = cfl V_i / sum_f lambda_f A_f, so dt_i / V_i = cfl / sum;
+            // global: the min over faces, divided by the volume.
+            if (DT == 2) dtv = a.ctl->cfl / lam;
+            else dtv = __longlong_as_double((long long)a.ctl->dt_bits) / a.m.vol[c];
             if (NST > 1) a.dtv[c] = dtv;
             s0 = R.r * R.r; s1 = R.ru * R.ru; s2 = R.rv * R.rv; s3 = R.E * R.E;
         } else {
@@ -403,11 +457,28 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
         else un = (1.0 / 3.0) * ld_state(a.U0, c) + (2.0 / 3.0) * e;
         st_state(a.U, c, un);
         const double g = a.gamma;
-        const double ir = 1.0 / un.r;
-        const double uu = un.ru * ir, vv = un.rv * ir;
-        const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
-        WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{(T)un.r, (T)uu, (T)vv, (T)p});
-        if (STAGE == NST - 1) a.cs[c] = sqrt(g * p * ir);
+        if constexpr (std::is_same<T, float>::value) {
+            // FP32-flux mode: the primitive copy only feeds FP32 arithmetic,
+            // so it is derived in FP32 (off the FP64 pipe); the sound speed
+            // for the next iteration's time step stays FP64.
+            const float gf = (float)g;
+            const float rf = (float)un.r, irf = 1.0f / rf;
+            const float uf = (float)un.ru * irf, vf = (float)un.rv * irf;
+            const float pf = (gf - 1.0f) * ((float)un.E - 0.5f * rf * (uf * uf + vf * vf));
+            WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{rf, uf, vf, pf});
+            if (STAGE == NST - 1) {
+                const double ir = 1.0 / un.r;
+                const double uu = un.ru * ir, vv = un.rv * ir;
+                const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
+                a.cs[c] = sqrt(g * p * ir);
+            }
+        } else {
+            const double ir = 1.0 / un.r;
+            const double uu = un.ru * ir, vv = un.rv * ir;
+            const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
+            WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{un.r, uu, vv, p});
+            if (STAGE == NST - 1) a.cs[c] = sqrt(g * p * ir);
+        }
     }
     if (STAGE == 0) finish_norms(s0, s1, s2, s3, a.ctl, a.partials, a.hist, a.hist_cap);
 }

@@ -342,6 +342,7 @@ void HostMesh::build_o2_geometry() {
     size_t E = d_cf.size();
     d_cnb.resize(E);
     d_lsq.resize(2 * E);
+    d_lsq_sum.assign(2 * (size_t)n_cells, 0.0);
     d_gg.resize(4 * E);
     d_erf.resize(2 * E);
     d_frf.assign(4 * (size_t)n_faces, 0.0);
@@ -383,6 +384,8 @@ void HostMesh::build_o2_geometry() {
             double w = 1.0 / (dx * dx + dy * dy);
             d_lsq[2 * e] = i00 * (w * dx) + i01 * (w * dy);
             d_lsq[2 * e + 1] = i01 * (w * dx) + i11 * (w * dy);
+            d_lsq_sum[2 * i] += d_lsq[2 * e];
+            d_lsq_sum[2 * i + 1] += d_lsq[2 * e + 1];
             double sgn = owner ? 1.0 : -1.0;
             d_gg[4 * e] = sgn * fnx[f] * farea[f] / vol[c];
             d_gg[4 * e + 1] = sgn * fny[f] * farea[f] / vol[c];

@@ -37,6 +37,7 @@ struct HostMesh {
     // Second-order geometry, device order (built by build_o2_geometry).
     std::vector<int32_t> d_cnb;                  // per entry: neighbour cell, or -1-face for boundary
     std::vector<double> d_lsq;                   // per entry [2]: LSQ weights folded with the inverse matrix
+    std::vector<double> d_lsq_sum;               // per cell [2]: sums of those weights
     std::vector<double> d_gg;                    // per entry [4]: Green-Gauss s*A*nx/V, s*A*ny/V, owner weight, 0
     std::vector<double> d_erf;                   // per entry [2]: face midpoint - cell centroid
     std::vector<double> d_frf;                   // per face [4]: x_f - x_L, x_f - x_R (R: zero on boundary)

@@ -147,7 +147,10 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         cs = dalloc<double>(N, owned);
         dtv = dalloc<double>(N, owned);
         cnb = dupload(h2.d_cnb, owned);
-        if (cfg.gradient == 0) lsq = reinterpret_cast<const double2*>(dupload(h2.d_lsq, owned));
+        if (cfg.gradient == 0) {
+            lsq = reinterpret_cast<const double2*>(dupload(h2.d_lsq, owned));
+            lsq_sum = reinterpret_cast<const double2*>(dupload(h2.d_lsq_sum, owned));
+        }
         else gg = reinterpret_cast<const double4_32a*>(dupload(h2.d_gg, owned));
         erf = reinterpret_cast<const double2*>(dupload(h2.d_erf, owned));
         frf = reinterpret_cast<const double4_32a*>(dupload(h2.d_frf, owned));
@@ -210,6 +213,7 @@ O2Args Solver::o2_args() const {
     a.m = dm;
     a.cnb = cnb;
     a.lsq = lsq;
+    a.lsq_sum = lsq_sum;
     a.gg = gg;
     a.erf = erf;
     a.frf = frf;

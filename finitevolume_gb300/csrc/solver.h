@@ -47,6 +47,7 @@ struct Solver {
     double* dtv = nullptr;
     const int* cnb = nullptr;
     const double2* lsq = nullptr;
+    const double2* lsq_sum = nullptr;
     const double4_32a* gg = nullptr;
     const double2* erf = nullptr;
     const double4_32a* frf = nullptr;

@@ -70,6 +70,7 @@ struct O2Args {
     DevMesh m;
     const int* cnb;          // per entry: neighbour or -1-face
     const double2* lsq;      // per entry LSQ weights
+    const double2* lsq_sum;  // per cell sums of the LSQ weights
     const double4_32a* gg;   // per entry Green-Gauss coefficients
     const double2* erf;      // per entry face offset
     const double4_32a* frf;  // per face offsets from the owner / neighbour centroid

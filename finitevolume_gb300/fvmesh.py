@@ -78,6 +78,21 @@ def signed_areas(m: PolyMesh) -> np.ndarray:
     return 0.5 * np.bincount(cell_of, weights=cross, minlength=sizes.size)
 
 
+def cell_centroids(m: PolyMesh) -> np.ndarray:
+    """Shoelace centroids of every cell (signed-area formula), [n_cells, 2]."""
+    sizes = m.cell_sizes()
+    idx = m.cell_nodes.astype(np.int64)
+    nxt = np.arange(idx.size) + 1
+    nxt[m.cell_off[1:] - 1] = m.cell_off[:-1]
+    p0, p1 = m.nodes[idx], m.nodes[idx[nxt]]
+    cross = p0[:, 0] * p1[:, 1] - p1[:, 0] * p0[:, 1]
+    cell_of = np.repeat(np.arange(sizes.size), sizes)
+    a = 0.5 * np.bincount(cell_of, weights=cross, minlength=sizes.size)
+    cx = np.bincount(cell_of, weights=(p0[:, 0] + p1[:, 0]) * cross, minlength=sizes.size) / (6.0 * a)
+    cy = np.bincount(cell_of, weights=(p0[:, 1] + p1[:, 1]) * cross, minlength=sizes.size) / (6.0 * a)
+    return np.stack([cx, cy], 1)
+
+
 def from_cells(nodes, cells, bedges, bpatch, patch_names) -> PolyMesh:
     """Build a PolyMesh from a list (or 2D array) of per-cell vertex lists."""
     if isinstance(cells, np.ndarray) and cells.ndim == 2:
