@@ -216,12 +216,16 @@ template <typename T> struct OKey;
 template <> struct OKey<double> {
     using I = long long;
     __device__ static I bits(double x) { return __double_as_longlong(x); }
+    __device__ static double from_bits(I b) { return __longlong_as_double(b); }
+    __device__ static I sign_bit() { return (I)0x8000000000000000ULL; }
     __device__ static I key(double x) { I b = __double_as_longlong(x); return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
     __device__ static double val(I k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL)); }
 };
 template <> struct OKey<float> {
     using I = int;
     __device__ static I bits(float x) { return __float_as_int(x); }
+    __device__ static float from_bits(I b) { return __int_as_float(b); }
+    __device__ static I sign_bit() { return (I)0x80000000u; }
     __device__ static I key(float x) { I b = __float_as_int(x); return b ^ ((b >> 31) & 0x7fffffff); }
     __device__ static float val(I k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
 };
@@ -303,33 +307,51 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
             T kh = (T)(a.venkat_k * a.h[c]);
             eps2 = kh * kh * kh;
         }
-        T nmin[4] = {1, 1, 1, 1}, dmn[4] = {1, 1, 1, 1};
+        // Per face f the limiter value is psi_f = phi(D1, D2_f) with D2_f the
+        // unlimited extrapolation to the face and D1 = dmax (D2_f > 0) or
+        // dmin (D2_f < 0).  With D1 fixed per sign, phi only limits
+        // (phi < 1) where |D1| < 2|D2| (Venkatakrishnan) or |D1| < |D2|
+        // (Barth-Jespersen), and there it strictly decreases in |D2|; so
+        // min(1, min_f psi_f) = min(1, phi(dmax, max D2 > 0),
+        // phi(dmin, min D2 < 0)).  Per face only D2 is formed; its extremes
+        // are tracked as integer maxima of the bit patterns (positive side:
+        // bits of D2; negative side: bits of -D2), off the FP64 pipe.
+        I pmax[4] = {0, 0, 0, 0}, nmax[4] = {0, 0, 0, 0};
+        const I sign = OK::sign_bit();
         for (int e = e0; e < e1; ++e) {
             const double2 r = __ldg(a.erf + e);
             const T rx = (T)r.x, ry = (T)r.y;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const T d2 = gx[k] * rx + gy[k] * ry;
-                const I bits = OK::bits(d2);
-                if ((bits << 1) == 0) continue;          // d2 == 0: the face does not limit
-                const T d1 = bits < 0 ? dmin[k] : dmax[k];
-                T num, den;
-                if (LIM == 1) {
-                    num = fabs(d1);
-                    den = fabs(d2);
-                } else {
-                    // (d1^2 + eps^2 + 2 d1 d2) / (d1^2 + 2 d2^2 + d1 d2 + eps^2)
-                    const T p = d1 * d2;
-                    const T q = d1 * d1 + eps2;
-                    num = q + T(2) * p;
-                    den = (d2 + d2) * d2 + (q + p);
-                }
-                if (num * dmn[k] < nmin[k] * den) { nmin[k] = num; dmn[k] = den; }
+                const I b = OK::bits(gx[k] * rx + gy[k] * ry);
+                pmax[k] = pmax[k] < b ? b : pmax[k];
+                const I bn = b ^ sign;
+                nmax[k] = nmax[k] < bn ? bn : nmax[k];
             }
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            T psi = nmin[k] / dmn[k];
+            T nmin = T(1), dmn = T(1);
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const I yb = side == 0 ? pmax[k] : nmax[k];
+                if (yb <= 0) continue;                       // no face with D2 of this sign
+                const T y = OK::from_bits(yb);               // |D2| extreme, > 0
+                const T d1 = side == 0 ? dmax[k] : -dmin[k];  // |D1| >= 0
+                T num, den;
+                if (LIM == 1) {
+                    num = d1;
+                    den = y;
+                } else {
+                    // (d1^2 + eps^2 + 2 d1 y) / (d1^2 + 2 y^2 + d1 y + eps^2)
+                    const T p = d1 * y;
+                    const T q = d1 * d1 + eps2;
+                    num = q + T(2) * p;
+                    den = (y + y) * y + (q + p);
+                }
+                if (num * dmn < nmin * den) { nmin = num; dmn = den; }
+            }
+            const T psi = nmin / dmn;
             gx[k] *= psi;
             gy[k] *= psi;
         }

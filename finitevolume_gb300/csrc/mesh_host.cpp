@@ -276,6 +276,19 @@ void HostMesh::build_device_layout(int reorder) {
     if (reorder == 1) perm = morton_order(*this);
     else if (reorder == 2) perm = rcm_order(*this);
     else { perm.resize(n_cells); std::iota(perm.begin(), perm.end(), 0); }
+    if (reorder != 0) {
+        // Within each tile of 256 consecutive cells (one thread block), order
+        // the cells by face count: each warp then runs its per-face loops
+        // with one trip count, and a warp's instructions are issued once
+        // for all its cells.  Locality is kept at tile granularity.
+        const int32_t tile = 256;
+        for (int32_t t0 = 0; t0 < n_cells; t0 += tile) {
+            const int32_t t1 = std::min(n_cells, t0 + tile);
+            std::stable_sort(perm.begin() + t0, perm.begin() + t1, [&](int32_t a, int32_t b) {
+                return cf_off[a + 1] - cf_off[a] < cf_off[b + 1] - cf_off[b];
+            });
+        }
+    }
     iperm.assign(n_cells, 0);
     for (int32_t i = 0; i < n_cells; ++i) iperm[perm[i]] = i;
 
