@@ -146,9 +146,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_cell_o1(const O1Args a) {
         for (int e = e0; e < e1; ++e) {
             const int ent = a.m.cf[e];
             const int f = ent >> 1;
-            const St F = ld_state(a.ff, f);
-            if (ent & 1) R = R - F;
-            else R += F;
+            R += flip_if(ld_state(a.ff, f), ent);
             if (LOCAL) dt += a.dtf[f];
         }
         if (LOCAL) dt = a.ctl->cfl * a.m.vol[c] / dt;

@@ -147,7 +147,9 @@ __device__ __forceinline__ V4<T> hllc_p(const V4<T>& L, const V4<T>& R, T nx, T 
     if (SL >= T(0)) return phys_flux_p(L, EL, VnL, nx, ny);
     if (SR <= T(0)) return phys_flux_p(R, ER, VnR, nx, ny);
     T mL = L.r * (SL - VnL), mR = R.r * (SR - VnR);
-    T Ss = (R.p - L.p + mL * VnL - mR * VnR) / (mL - mR);
+    // A reciprocal plus a multiply issues fewer FP64 instructions than a
+    // general division on this part.
+    T Ss = (R.p - L.p + mL * VnL - mR * VnR) * (T(1) / (mL - mR));
     bool left = Ss >= T(0);
     T SK = left ? SL : SR, VnK = left ? VnL : VnR, EK = left ? EL : ER, irK = left ? irL : irR;
     T mK = left ? mL : mR;
@@ -454,9 +456,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
         for (int e = e0; e < e1; ++e) {
             const int ent = a.m.cf[e];
             const int f = ent >> 1;
-            const St F = ld_flux(ff, f);
-            if (ent & 1) R = R - F;
-            else R += F;
+            R += flip_if(ld_flux(ff, f), ent);
             if (STAGE == 0 && DT == 2) lam += a.dtf[f];
         }
         double dtv;

@@ -44,6 +44,19 @@ __device__ __forceinline__ void st_state(St* U, int i, const St& s) {
     p[1] = make_double2(s.rv, s.E);
 }
 
+// -F when neg is set, by flipping sign bits on the integer pipe.  IEEE
+// defines a - b as a + (-b), so R += signed(F) is bit-identical to the
+// reference's "owner subtracts, neighbour adds" (src/EulerFVMSolver.cpp:92-96)
+// while issuing one FP64 add per component instead of a predicated
+// add/subtract pair.
+__device__ __forceinline__ St flip_if(const St& F, int neg) {
+    const unsigned long long m = (unsigned long long)(neg & 1) << 63;
+    return st_make(__longlong_as_double(__double_as_longlong(F.r) ^ m),
+                   __longlong_as_double(__double_as_longlong(F.ru) ^ m),
+                   __longlong_as_double(__double_as_longlong(F.rv) ^ m),
+                   __longlong_as_double(__double_as_longlong(F.E) ^ m));
+}
+
 // EulerState.h:45-52
 __device__ __forceinline__ St from_primitive(double rho, double u, double v, double p, double g) {
     St s;
