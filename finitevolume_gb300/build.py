@@ -31,7 +31,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(ROOT, "include")]
 # Per-file extra flags: the strict kernels are built without FMA contraction.
-EXTRA = {"kernels_strict.cu": ["--fmad=false"]}
+EXTRA = {"kernels_strict.cu": ["--fmad=false"], "diffusion.cu": ["--fmad=false"], "gradients.cu": ["--fmad=false"],
+         "ns.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 
 

@@ -97,6 +97,16 @@ SIGNATURES = {
     "fv_wall_forces": (C.c_int, [_P, _D, _D]),
     "fv_step_noalloc": (C.c_int, [C.POINTER(NoAllocMesh), C.POINTER(BC), C.c_int32, C.c_double, C.c_double,
                                   C.c_int32, _P, _D, _P]),
+    "fv_diffusion_create": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_double, _I32, _D,
+                                      C.POINTER(_P)]),
+    "fv_diffusion_destroy": (C.c_int, [_P]),
+    "fv_diffusion_step": (C.c_int, [_P, C.c_int32, _D]),
+    "fv_diffusion_get_field": (C.c_int, [_P, _D]),
+    "fv_diffusion_set_field": (C.c_int, [_P, _D]),
+    "fv_diffusion_residual": (C.c_int, [_P, _D]),
+    "fv_gradient_create": (C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
+    "fv_gradient_destroy": (C.c_int, [_P]),
+    "fv_gradient_compute": (C.c_int, [_P, _D, _D, _D, _D]),
 }
 
 _lib = None

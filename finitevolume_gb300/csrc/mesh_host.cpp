@@ -425,3 +425,91 @@ void HostMesh::build_o2_geometry() {
 }
 
 }  // namespace fvgb
+
+namespace fvgb {
+
+// GradientCalculator ctor (src/GradientReconstruction.cpp:45-80): per-cell
+// inverse normal matrix, and the per-entry terms compute() needs
+// (:83-150); face_normal_geometry / face_gradient (:25-40, :153-183).
+void build_grad_geom(const HostMesh& m, HostGradGeom& g) {
+    const int32_t N = m.n_cells, F = m.n_faces;
+    const size_t E = m.d_cf.size();
+    g.nb.resize(E);
+    g.lsq_w.resize(2 * E);
+    g.gg.resize(4 * E);
+    g.lsq_inv.resize(3 * (size_t)N);
+    g.fgrad.assign(8 * (size_t)F, 0.0);
+    for (int32_t i = 0; i < N; ++i) {
+        const int32_t c = m.perm[i];
+        const double xc = m.cx[c], yc = m.cy[c];
+        double m00 = 0.0, m01 = 0.0, m11 = 0.0;
+        for (int32_t e = m.d_cf_off[i]; e < m.d_cf_off[i + 1]; ++e) {
+            const int32_t fd = m.d_cf[e] >> 1;
+            const int32_t f = m.fperm[fd];
+            double nx, ny;
+            if (m.fr[f] == -1) {
+                nx = m.fxm[f];
+                ny = m.fym[f];
+                g.nb[e] = -1 - fd;
+            } else {
+                const int32_t nbr = (m.fl[f] == c) ? m.fr[f] : m.fl[f];
+                nx = m.cx[nbr];
+                ny = m.cy[nbr];
+                g.nb[e] = m.iperm[nbr];
+            }
+            const double dx = nx - xc;
+            const double dy = ny - yc;
+            const double w = 1.0 / (dx * dx + dy * dy);
+            m00 += w * dx * dx;
+            m01 += w * dx * dy;
+            m11 += w * dy * dy;
+            g.lsq_w[2 * e] = w * dx;
+            g.lsq_w[2 * e + 1] = w * dy;
+            // Green-Gauss: outward normal of this cell, face length and the
+            // inverse-distance weight of the owning side.
+            const bool owner = m.fl[f] == c;
+            g.gg[4 * e] = owner ? m.fnx[f] : -m.fnx[f];
+            g.gg[4 * e + 1] = owner ? m.fny[f] : -m.fny[f];
+            g.gg[4 * e + 2] = m.farea[f];
+            if (m.fr[f] == -1) {
+                g.gg[4 * e + 3] = 0.0;
+            } else {
+                const int32_t other = owner ? m.fr[f] : m.fl[f];
+                const double d_c = std::hypot(xc - m.fxm[f], yc - m.fym[f]);
+                const double d_o = std::hypot(m.cx[other] - m.fxm[f], m.cy[other] - m.fym[f]);
+                g.gg[4 * e + 3] = d_o / (d_c + d_o);
+            }
+        }
+        const double det = m00 * m11 - m01 * m01;
+        g.lsq_inv[3 * (size_t)i] = m11 / det;
+        g.lsq_inv[3 * (size_t)i + 1] = -m01 / det;
+        g.lsq_inv[3 * (size_t)i + 2] = m00 / det;
+    }
+    for (int32_t i = 0; i < F; ++i) {
+        const int32_t f = m.fperm[i];
+        const int32_t cl = m.fl[f];
+        const bool bnd = m.fr[f] == -1;
+        const double xR = bnd ? m.fxm[f] : m.cx[m.fr[f]];
+        const double yR = bnd ? m.fym[f] : m.cy[m.fr[f]];
+        const double dx = xR - m.cx[cl];
+        const double dy = yR - m.cy[cl];
+        const double dist = std::hypot(dx, dy);
+        const double dhx = dx / dist, dhy = dy / dist;
+        const double cos_theta = m.fnx[f] * dhx + m.fny[f] * dhy;
+        double* o = &g.fgrad[8 * (size_t)i];
+        o[0] = dist;
+        o[1] = cos_theta;
+        o[2] = m.fnx[f] - dhx / cos_theta;
+        o[3] = m.fny[f] - dhy / cos_theta;
+        if (!bnd) {
+            const double d_L = std::hypot(m.cx[cl] - m.fxm[f], m.cy[cl] - m.fym[f]);
+            const double d_R = std::hypot(xR - m.fxm[f], yR - m.fym[f]);
+            o[4] = d_R / (d_L + d_R);
+        }
+        o[5] = dist * cos_theta;
+        o[6] = m.fnx[f];
+        o[7] = m.fny[f];
+    }
+}
+
+}  // namespace fvgb

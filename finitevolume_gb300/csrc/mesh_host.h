@@ -48,6 +48,19 @@ struct HostMesh {
     void build_o2_geometry();
 };
 
+// Geometry of the reference's GradientCalculator and face_gradient
+// (src/GradientReconstruction.cpp:12-200), device order, computed on the
+// host with the reference's own expressions (so strict device code that
+// consumes it reproduces the reference's gradients bit for bit).
+struct HostGradGeom {
+    std::vector<int32_t> nb;       // per entry: neighbour cell or -1-face
+    std::vector<double> lsq_w;     // per entry [2]: w*dx, w*dy (w = 1/d^2)
+    std::vector<double> lsq_inv;   // per cell [3]: inv00, inv01, inv11
+    std::vector<double> gg;        // per entry [4]: outward nx, ny, length, owner weight w_c
+    std::vector<double> fgrad;     // per face [8]: dist, cos_theta, kx, ky, w_L, nd, nx, ny
+};
+void build_grad_geom(const HostMesh& m, HostGradGeom& g);
+
 // src/MeshReader.cpp:317-456 (+ validate_mesh_geometry :125-288).
 // Throws MeshError on invalid input.
 void build_from_polygons(HostMesh& m, int32_t n_nodes, const double* xy, int32_t n_cells, const int64_t* cell_off,

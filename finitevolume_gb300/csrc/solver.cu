@@ -26,6 +26,10 @@ struct fv_mesh_s {
 };
 
 namespace fvgb {
+const HostMesh& host_mesh_of(const fv_mesh_s* m) { return m->h; }
+}  // namespace fvgb
+
+namespace fvgb {
 
 template <typename T>
 static T* dalloc(size_t n, std::vector<void*>& owned) {
@@ -65,8 +69,14 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     if (opt.gradient < 0 || opt.gradient > 1 || opt.limiter < 0 || opt.limiter > 2)
         raise(FV_ERR_BAD_ARG, "unknown gradient scheme or limiter");
     if (opt.dt_mode != FV_DT_GLOBAL && opt.dt_mode != FV_DT_LOCAL) raise(FV_ERR_BAD_ARG, "unknown dt mode");
-    if (opt.viscous) raise(FV_ERR_UNSUPPORTED, "viscous terms are not in this build");
-    general = !(opt.order == 1 && opt.rk_stages == 1 && opt.precision == FV_PREC_FP64);
+    if (opt.viscous && (opt.order != 1 || opt.rk_stages != 1 || opt.precision != FV_PREC_FP64 ||
+                        opt.dt_mode != FV_DT_GLOBAL))
+        raise(FV_ERR_UNSUPPORTED, "the Navier-Stokes path is the reference's scheme: order 1, forward Euler, "
+                                  "global dt, FP64");
+    if (opt.viscous && !(opt.gas_constant > 0.0 && opt.prandtl > 0.0 && opt.mu >= 0.0))
+        raise(FV_ERR_BAD_ARG, "viscous solver needs gas_constant > 0, prandtl > 0, mu >= 0");
+    viscous = opt.viscous != 0;
+    general = !viscous && !(opt.order == 1 && opt.rk_stages == 1 && opt.precision == FV_PREC_FP64);
     if (general && opt.strict) raise(FV_ERR_UNSUPPORTED, "strict mode covers the reference's first-order scheme only");
     if (general && opt.precision == FV_PREC_FP32_FLUX && opt.flux == FV_FLUX_EXACT)
         raise(FV_ERR_UNSUPPORTED, "the exact Riemann flux runs in FP64 only");
@@ -94,13 +104,13 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         bc.isothermal[p] = b.isothermal;
         bc.wall_T[p] = b.wall_T;
     }
-    // Host copies needed after construction (wall forces in reference numbering).
-    for (int i = hm.n_int_faces; i < F; ++i) {
-        int p = hm.d_fpatch[i];
-        if (bc.type[p] == FV_BC_WALL || bc.type[p] == FV_BC_NOSLIP) {
-            int f = hm.fperm[i];
-            wall_faces.push_back({hm.fl[f], hm.fnx[f], hm.fny[f], hm.farea[f], hm.fxm[f], hm.fym[f]});
-        }
+    // Host copies needed after construction: wall faces in reference face
+    // order (the order compute_wall_forces accumulates them in).
+    for (int f = 0; f < F; ++f) {
+        if (hm.fr[f] >= 0) continue;
+        int p = hm.fpatch[f];
+        if (bc.type[p] == FV_BC_WALL || bc.type[p] == FV_BC_NOSLIP)
+            wall_faces.push_back({hm.fl[f], hm.fnx[f], hm.fny[f], hm.farea[f], hm.fxm[f], hm.fym[f], hm.ifperm[f]});
     }
 
     FV_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -155,6 +165,44 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         erf = reinterpret_cast<const double2*>(dupload(h2.d_erf, owned));
         frf = reinterpret_cast<const double4_32a*>(dupload(h2.d_frf, owned));
         hcell = dupload(h2.d_h, owned);
+    }
+
+    if (viscous) {
+        HostGradGeom hg;
+        build_grad_geom(hm, hg);
+        NSArgs& a = ns;
+        a.g.n_cells = N;
+        a.g.n_faces = F;
+        a.g.scheme = opt.gradient;
+        a.g.cf_off = m.cf_off;
+        a.g.nb = dupload(hg.nb, owned);
+        a.g.lsq_w = reinterpret_cast<const double2*>(dupload(hg.lsq_w, owned));
+        a.g.lsq_inv = dupload(hg.lsq_inv, owned);
+        a.g.gg = reinterpret_cast<const double4_32a*>(dupload(hg.gg, owned));
+        a.g.vol = m.vol;
+        a.g.fgrad = dupload(hg.fgrad, owned);
+        a.g.fr = m.fr;
+        a.fl = m.fl;
+        a.fpatch = m.fpatch;
+        a.fgeom = m.fgeom;
+        a.U = U;
+        a.ff = ff;
+        a.prim = dalloc<double4_32a>(N, owned);
+        a.grad = dalloc<double2>(3 * (size_t)N, owned);
+        a.ctl = ctl;
+        a.bc = bc;
+        a.gamma = gamma;
+        a.gas_constant = opt.gas_constant;
+        a.mu = opt.mu;
+        const double cp = gamma * opt.gas_constant / (gamma - 1.0);  // src/NavierStokesFVMSolver.cpp:113-114
+        a.kcond = opt.mu * cp / opt.prandtl;
+        a.exact_tol = opt.exact_tol;
+        a.exact_max_iter = opt.exact_max_iter;
+        a.flux = opt.flux;
+        std::vector<int> wf;
+        for (const WallFace& w : wall_faces) wf.push_back(w.dev_face);
+        ns_wall_faces = dupload(wf, owned);
+        ns_wall_out = dalloc<double2>(wf.size(), owned);
     }
 
     // Initial condition, reference numbering then device order
@@ -253,6 +301,12 @@ void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* ev
         if (classes) classes->push_back(cls);
         if (events) FV_CUDA(cudaEventRecord((*events)[++*ev_pos], stream));
     };
+    if (viscous) {
+        // NS step: prim + gradients + face fluxes + cell pass, timed as one.
+        ns_launch_step(ns, o1_args(), stream);
+        mark(1);
+        return;
+    }
     if (!general) {
         O1Args a = o1_args();
         for (int part = 0; part < 2; ++part) {
@@ -275,7 +329,7 @@ void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* ev
 void Solver::step_timed(int n, double ms[3], int launches[3]) {
     if (n <= 0) raise(FV_ERR_BAD_ARG, "step_timed needs n > 0");
     ensure_history(n);
-    const int per_step = general ? cfg.stages * (cfg.order == 2 ? 3 : 2) : 2;
+    const int per_step = viscous ? 1 : (general ? cfg.stages * (cfg.order == 2 ? 3 : 2) : 2);
     const size_t need = (size_t)n * per_step + 1;
     while (events.size() < need) {
         cudaEvent_t e;
@@ -397,22 +451,41 @@ void Solver::set_stream(void* s) {
     }
 }
 
-// compute_wall_forces with zero viscosity (src/WallTraction.cpp:163-217):
-// wall pressure is the owner cell's pressure (include/WallTraction.h:59-66).
+// compute_wall_traction + compute_wall_forces (src/WallTraction.cpp:95-217),
+// domain total over the wall faces in reference face order.  Wall pressure
+// is the owner cell's pressure (include/WallTraction.h:59-66); the viscous
+// solver adds the wall shear from the corrected face gradients, the
+// inviscid one has none.
 void Solver::wall_forces(const double ref[7], double out[11]) {
-    std::vector<double> f(4 * (size_t)N);
-    download_field(f.data());
+    const size_t nw = wall_faces.size();
+    std::vector<double> tau(nw, 0.0), pw(nw, 0.0);
+    if (viscous) {
+        std::vector<double2> tp(nw);
+        ns_launch_wall(ns, ns_wall_faces, (int)nw, ns_wall_out, stream);
+        FV_CUDA(cudaGetLastError());
+        if (nw) FV_CUDA(cudaMemcpyAsync(tp.data(), ns_wall_out, sizeof(double2) * nw, cudaMemcpyDeviceToHost, stream));
+        FV_CUDA(cudaStreamSynchronize(stream));
+        for (size_t i = 0; i < nw; ++i) { tau[i] = tp[i].x; pw[i] = tp[i].y; }
+    } else {
+        std::vector<double> f(4 * (size_t)N);
+        download_field(f.data());
+        for (size_t i = 0; i < nw; ++i) {
+            const double* s = f.data() + 4 * (size_t)wall_faces[i].cell;
+            double u = s[1] / s[0], v = s[2] / s[0];
+            pw[i] = (gamma - 1.0) * (s[3] - 0.5 * s[0] * (u * u + v * v));
+        }
+    }
     double vmag = std::hypot(ref[1], ref[2]);
     double dx = ref[1] / vmag, dy = ref[2] / vmag;
     double lx = -dy, ly = dx;
     double qL = 0.5 * ref[0] * vmag * vmag * ref[4];
     double qL2 = qL * ref[4];
     double fd = 0, pd = 0, td = 0, lift = 0, mom = 0;
-    for (const WallFace& w : wall_faces) {
-        const double* s = f.data() + 4 * (size_t)w.cell;
-        double u = s[1] / s[0], v = s[2] / s[0];
-        double p = (gamma - 1.0) * (s[3] - 0.5 * s[0] * (u * u + v * v));
-        double fx = 0.0, fy = 0.0;  // friction: zero for the inviscid solver
+    for (size_t i = 0; i < nw; ++i) {
+        const WallFace& w = wall_faces[i];
+        const double p = pw[i];
+        const double tx = -w.ny, ty = w.nx;  // rotate90 (src/WallTraction.cpp:11-13)
+        double fx = w.area * tau[i] * tx, fy = w.area * tau[i] * ty;
         double px = w.area * p * w.nx, py = w.area * p * w.ny;
         double rx = w.xm - ref[5], ry = w.ym - ref[6];
         double dfx = fx + px, dfy = fy + py;

@@ -6,6 +6,7 @@
 
 #include "../../include/fv_gb300.h"
 #include "mesh_host.h"
+#include "ns.h"
 #include "types.h"
 
 namespace fvgb {
@@ -13,6 +14,7 @@ namespace fvgb {
 struct WallFace {
     int cell;  // owner cell, reference numbering
     double nx, ny, area, xm, ym;
+    int dev_face;  // the face's device index
 };
 
 struct Solver {
@@ -36,6 +38,12 @@ struct Solver {
     int hist_cap = 0;
     StepCtl* ctl = nullptr;
     long long steps_taken = 0;
+
+    // Navier-Stokes path
+    bool viscous = false;
+    NSArgs ns{};
+    int* ns_wall_faces = nullptr;   // device indices of the wall faces, reference order
+    double2* ns_wall_out = nullptr; // (tau_wall, p) per wall face
 
     // second-order / multi-stage path
     bool general = false;           // false: reference-mode first-order kernels

@@ -179,12 +179,15 @@ class EulerFVMSolver:
                  flux_scheme: NumericalFluxScheme = NumericalFluxScheme.Rusanov, exact_riemann_tol: float = 1e-6,
                  exact_riemann_max_iter: int = 20, *, order: int = 1, rk_stages: int = 1, local_dt: bool = False,
                  gradient: GradientScheme = GradientScheme.LeastSquares, limiter: Limiter = Limiter.Venkatakrishnan,
-                 venkat_k: float = 5.0, fp32_flux: bool = False, strict: bool = False):
+                 venkat_k: float = 5.0, fp32_flux: bool = False, strict: bool = False, _viscous=None):
         if not isinstance(input_mesh, Mesh):
             input_mesh = Mesh(input_mesh)
         self.mesh = input_mesh
         L = capi.lib()
         o = capi.default_options()
+        if _viscous is not None:
+            o.viscous = 1
+            o.gas_constant, o.mu, o.prandtl = (float(x) for x in _viscous)
         o.flux = int(flux_scheme)
         o.exact_tol = float(exact_riemann_tol)
         o.exact_max_iter = int(exact_riemann_max_iter)
@@ -197,7 +200,7 @@ class EulerFVMSolver:
         o.precision = 1 if fp32_flux else 0
         o.strict = 1 if strict else 0
         self._opt = o
-        bc = _bc_array(boundary_conditions)
+        bc = boundary_conditions if isinstance(boundary_conditions, C.Array) else _bc_array(boundary_conditions)
         ic = _ic_struct(initial_condition)
         h = C.c_void_p()
         capi.check(L.fv_solver_create(input_mesh.handle, bc, len(boundary_conditions), float(gamma), float(cfl),
@@ -284,6 +287,154 @@ class EulerFVMSolver:
         if h:
             try:
                 capi.lib().fv_solver_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+class BoundaryType(enum.IntEnum):
+    """Diffusion boundary kinds (include/UnstructuredMesh.h:49-52)."""
+    Dirichlet = 0
+    Neumann = 1
+
+
+class UnstructuredFVMSolver:
+    """GPU scalar diffusion solver with the reference's constructor and methods
+    (include/UnstructuredFVMSolver.h:21-92).
+
+    The reference takes each patch's BoundaryType and value from
+    ``mesh.patches``; here ``patches`` maps patch name -> (BoundaryType, value)
+    (unlisted patches: Dirichlet 0).
+    """
+
+    def __init__(self, input_mesh: Mesh, alpha: float, dt: float, initial_value: float, initial_radius: float,
+                 patches: Optional[dict] = None):
+        if not isinstance(input_mesh, Mesh):
+            input_mesh = Mesh(input_mesh)
+        self.mesh = input_mesh
+        n = len(input_mesh.patch_names)
+        pt = np.zeros(max(n, 1), np.int32)
+        pv = np.zeros(max(n, 1), np.float64)
+        for name, (kind, value) in (patches or {}).items():
+            i = input_mesh.patch_names.index(name)
+            pt[i] = int(kind)
+            pv[i] = float(value)
+        h = C.c_void_p()
+        capi.check(capi.lib().fv_diffusion_create(input_mesh.handle, float(alpha), float(dt), float(initial_value),
+                                                  float(initial_radius), capi.i32ptr(pt), capi.dptr(pv), C.byref(h)))
+        self._h = h
+        self.n_cells = input_mesh.n_cells
+
+    def step(self) -> None:
+        capi.check(capi.lib().fv_diffusion_step(self._h, 1, None))
+
+    def run(self, total_steps: int, history: bool = False):
+        out = np.zeros(max(total_steps, 1))
+        done = 0
+        while done < total_steps:
+            k = min(65536, total_steps - done)
+            capi.check(capi.lib().fv_diffusion_step(self._h, k, capi.dptr(out[done:]) if history else None))
+            done += k
+        return out[:total_steps] if history else None
+
+    def field(self) -> np.ndarray:
+        out = np.zeros(self.n_cells)
+        capi.check(capi.lib().fv_diffusion_get_field(self._h, capi.dptr(out)))
+        return out
+
+    def set_field(self, new_phi) -> None:
+        p = np.ascontiguousarray(new_phi, dtype=np.float64)
+        if p.shape != (self.n_cells,):
+            raise ValueError("set_field expects one value per cell")
+        capi.check(capi.lib().fv_diffusion_set_field(self._h, capi.dptr(p)))
+
+    def residual_norm(self) -> float:
+        out = np.zeros(1)
+        capi.check(capi.lib().fv_diffusion_residual(self._h, capi.dptr(out)))
+        return float(out[0])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                capi.lib().fv_diffusion_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+class NSBoundaryType(enum.IntEnum):
+    """include/NavierStokesFVMSolver.h:19-23 (same numbering)."""
+    NoSlipWall = 0
+    Farfield = 1
+    Outflow = 2
+
+
+@dataclasses.dataclass
+class NSBoundaryCondition:
+    """include/NavierStokesFVMSolver.h:25-32."""
+    type: NSBoundaryType = NSBoundaryType.NoSlipWall
+    wall_u: float = 0.0
+    wall_v: float = 0.0
+    is_isothermal_wall: bool = False
+    wall_temperature: float = 0.0
+    farfield_state: Sequence[float] = (0.0, 0.0, 0.0, 0.0)
+
+
+_NS_TO_ABI = {NSBoundaryType.NoSlipWall: 4, NSBoundaryType.Farfield: 1, NSBoundaryType.Outflow: 2}
+
+
+class NavierStokesFVMSolver(EulerFVMSolver):
+    """GPU Navier-Stokes solver with the reference's constructor and methods
+    (include/NavierStokesFVMSolver.h:118-218): the reference's first-order
+    scheme with the Jasak-corrected viscous flux."""
+
+    def __init__(self, input_mesh: Mesh, boundary_conditions: Sequence[NSBoundaryCondition], gamma: float,
+                 gas_constant: float, mu: float, prandtl: float, cfl: float,
+                 initial_condition: EulerInitialCondition,
+                 flux_scheme: NumericalFluxScheme = NumericalFluxScheme.Rusanov,
+                 gradient_scheme: GradientScheme = GradientScheme.LeastSquares, exact_riemann_tol: float = 1e-6,
+                 exact_riemann_max_iter: int = 20):
+        arr = (capi.BC * max(1, len(boundary_conditions)))()
+        for i, b in enumerate(boundary_conditions):
+            arr[i].type = _NS_TO_ABI[NSBoundaryType(b.type)]
+            arr[i].isothermal = 1 if b.is_isothermal_wall else 0
+            arr[i].wall_u, arr[i].wall_v, arr[i].wall_T = float(b.wall_u), float(b.wall_v), float(b.wall_temperature)
+            for k in range(4):
+                arr[i].state[k] = float(b.farfield_state[k])
+        super().__init__(input_mesh, arr, gamma, cfl, initial_condition, flux_scheme, exact_riemann_tol,
+                         exact_riemann_max_iter, gradient=gradient_scheme, _viscous=(gas_constant, mu, prandtl))
+
+
+class GradientCalculator:
+    """GPU GradientCalculator (include/GradientReconstruction.h:46-83)."""
+
+    def __init__(self, mesh: Mesh, scheme: GradientScheme = GradientScheme.LeastSquares):
+        if not isinstance(mesh, Mesh):
+            mesh = Mesh(mesh)
+        self.mesh = mesh
+        h = C.c_void_p()
+        capi.check(capi.lib().fv_gradient_create(mesh.handle, int(scheme), C.byref(h)))
+        self._h = h
+
+    def compute(self, phi, boundary_phi, face_gradients: bool = False):
+        """Cell gradients [N, 2]; with face_gradients also [F, 4] =
+        (corrected dphi/dn, corrected gradient x, y, face_normal_distance)."""
+        p = np.ascontiguousarray(phi, dtype=np.float64)
+        b = np.ascontiguousarray(boundary_phi, dtype=np.float64)
+        if p.shape != (self.mesh.n_cells,) or b.shape != (self.mesh.n_faces,):
+            raise ValueError("phi must have one value per cell and boundary_phi one per face")
+        g = np.zeros((self.mesh.n_cells, 2))
+        fo = np.zeros((self.mesh.n_faces, 4)) if face_gradients else None
+        capi.check(capi.lib().fv_gradient_compute(self._h, capi.dptr(p), capi.dptr(b), capi.dptr(g),
+                                                  capi.dptr(fo) if face_gradients else None))
+        return (g, fo) if face_gradients else g
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                capi.lib().fv_gradient_destroy(h)
             except Exception:
                 pass
             self._h = None

@@ -215,6 +215,51 @@ int fv_device_state(fv_solver_t s, void** U_dev, void** stream);
 int fv_wall_forces(fv_solver_t s, const double ref[7], double out[11]);
 
 /* ------------------------------------------------------------------------
+ * Scalar diffusion solver (UnstructuredFVMSolver)
+ * ------------------------------------------------------------------------ */
+typedef struct fv_diffusion_s* fv_diffusion_t;
+
+/*
+ * UnstructuredFVMSolver(mesh, alpha, dt, initial_value, initial_radius)
+ * (include/UnstructuredFVMSolver.h:34-35, src/UnstructuredFVMSolver.cpp:6-19).
+ * The reference reads each boundary patch's BoundaryType/value from
+ * mesh.patches (include/UnstructuredMesh.h:49-60); here they are passed per
+ * patch: patch_type 0 = Dirichlet (value at the face midpoint), 1 = Neumann
+ * (prescribed flux = value * length).
+ */
+int fv_diffusion_create(fv_mesh_t mesh, double alpha, double dt, double initial_value, double initial_radius,
+                        const int32_t* patch_type, const double* patch_value, fv_diffusion_t* out);
+int fv_diffusion_destroy(fv_diffusion_t d);
+/* step() x n (src/UnstructuredFVMSolver.cpp:44-92); history[n] receives
+ * residual_norm() after each step when non-NULL.  n <= 65536 per call. */
+int fv_diffusion_step(fv_diffusion_t d, int32_t n, double* history);
+/* field() / set_field() / residual_norm() (include/UnstructuredFVMSolver.h:48-73). */
+int fv_diffusion_get_field(fv_diffusion_t d, double* phi);
+int fv_diffusion_set_field(fv_diffusion_t d, const double* phi);
+int fv_diffusion_residual(fv_diffusion_t d, double* norm);
+
+/* ------------------------------------------------------------------------
+ * Gradient reconstruction (GradientCalculator, face_gradient)
+ * ------------------------------------------------------------------------ */
+typedef struct fv_gradient_s* fv_gradient_t;
+
+/* GradientCalculator(mesh, scheme) (include/GradientReconstruction.h:60,
+ * src/GradientReconstruction.cpp:45-80): precomputes the geometry once. */
+int fv_gradient_create(fv_mesh_t mesh, int32_t scheme, fv_gradient_t* out);
+int fv_gradient_destroy(fv_gradient_t g);
+/*
+ * GradientCalculator::compute(mesh, phi, boundary_phi)
+ * (include/GradientReconstruction.h:73, src/GradientReconstruction.cpp:83-150).
+ * phi [N] and boundary_phi [F] (only boundary-face entries are read) in
+ * reference numbering; grad [2N] = dphidx, dphidy per cell.  When face_out
+ * is non-NULL it receives, per face [4F], face_gradient's corrected normal
+ * derivative, corrected_face_gradient_vector's x and y, and
+ * face_normal_distance (src/GradientReconstruction.cpp:153-199).
+ */
+int fv_gradient_compute(fv_gradient_t g, const double* phi, const double* boundary_phi, double* grad,
+                        double* face_out);
+
+/* ------------------------------------------------------------------------
  * Allocation-free step
  * ------------------------------------------------------------------------ */
 /*

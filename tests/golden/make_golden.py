@@ -61,6 +61,27 @@ def euler_case(name, mesh, case, tmp, steps):
                         case=np.array(json.dumps({**case, "steps": steps})))
 
 
+def ns_case(name, mesh, case, tmp, steps):
+    path = os.path.join(tmp, name + ".fvmesh")
+    fvmesh.write_fvmesh(mesh, path)
+    out = os.path.join(tmp, name)
+    os.makedirs(out, exist_ok=True)
+    ref = case["ref"]
+    res = {}
+    for flux in case["fluxes"]:
+        for grad in case["grads"]:
+            fvref("ns", path, out, flux=flux, grad=grad, cfl=case["cfl"], ic=case["ic"], bc=case["bc"], steps=steps,
+                  gamma=GAMMA, R=case["R"], mu=case["mu"], Pr=case["Pr"], ref_rho=ref[0], ref_u=ref[1], ref_v=ref[2],
+                  ref_p=ref[3], ref_len=ref[4], ref_mx=ref[5], ref_my=ref[6])
+            tag = f"{flux}_{grad}"
+            res[f"field_{tag}"] = np.fromfile(os.path.join(out, "field.f64")).reshape(-1, 4)
+            res[f"hist_{tag}"] = np.fromfile(os.path.join(out, "resid.f64")).reshape(-1, 4)
+            res[f"forces_{tag}"] = np.fromfile(os.path.join(out, "forces.f64")).reshape(-1, 11)
+            res[f"wall_{tag}"] = np.fromfile(os.path.join(out, "wall.f64")).reshape(-1, 3)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **mesh_arrays(mesh), **res,
+                        case=np.array(json.dumps({**case, "steps": steps})))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -100,6 +121,23 @@ def main():
             dt = np.int32 if ("i32" in f or "cell_face" in f) else np.float64
             res["mesh_" + f] = np.fromfile(os.path.join(out, f + ".bin"), dtype=dt)
         np.savez_compressed(os.path.join(HERE, "wavy_grad.npz"), **mesh_arrays(wavy), **res)
+        # Navier-Stokes: no-slip NACA0012 at Re_c = 500 (adiabatic wall), and
+        # a channel with an isothermal moving top wall (Couette-like).
+        R = 287.0
+        T_inf = (1.0 / GAMMA) / R
+        og = meshgen.naca_ogrid(64, 32)
+        ns_case("ns_naca_og64", og, {
+            "fluxes": ["rusanov", "hllc"], "grads": ["lsq", "gg"], "cfl": 0.5, "R": R, "mu": 1e-3, "Pr": 0.72,
+            "ic": "free:" + prim_str(1.0, u, v, p),
+            "bc": ["airfoil:noslip", "farfield:farfield:" + prim_str(1.0, u, v, p)],
+            "ref": [1.0, float(u), float(v), float(p), 1.0, 0.25, 0.0]}, tmp, 150)
+        ch = meshgen.sod_strip(24, 8, length=2.0, height=1.0, jitter=0.15, seed=3)
+        ns_case("ns_channel_tri", ch, {
+            "fluxes": ["rusanov"], "grads": ["lsq", "gg"], "cfl": 0.5, "R": R, "mu": 5e-3, "Pr": 0.72,
+            "ic": "free:" + prim_str(1.0, 0.05, 0.0, 1.0 / GAMMA),
+            "bc": ["bottom:noslip:0:0:" + repr(T_inf), "top:noslip:0.2:0:" + repr(1.1 * T_inf),
+                   "left:outflow", "right:outflow"],
+            "ref": [1.0, 0.2, 0.0, 1.0 / GAMMA, 2.0, 1.0, 0.5]}, tmp, 200)
         # Scalar diffusion on a Cartesian patch: Dirichlet + Neumann sides.
         cart = meshgen.cartesian(12, 10, 2.0, 1.5)
         cart.nodes -= np.array([1.0, 0.75])
