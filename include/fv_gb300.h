@@ -260,6 +260,36 @@ int fv_gradient_compute(fv_gradient_t g, const double* phi, const double* bounda
                         double* face_out);
 
 /* ------------------------------------------------------------------------
+ * Checkpoints in the reference's file layout
+ * ------------------------------------------------------------------------ */
+/* CheckpointEquation (include/Checkpoint.h:11-18). */
+enum {
+    FV_CKPT_DIFFUSION = 0,
+    FV_CKPT_EULER = 1,
+    FV_CKPT_ADVECTION_DIFFUSION = 2,
+    FV_CKPT_NAVIER_STOKES = 3,
+    FV_CKPT_RANS_SA = 4,
+    FV_CKPT_RANS_SST = 5
+};
+/*
+ * Checkpoint::write (include/Checkpoint.h:26-46, :72-86): 40-byte header
+ * (magic, version 2, equation tag, cell count, step index, build number)
+ * then the raw payload: cell_count doubles (Diffusion, AdvectionDiffusion),
+ * cell_count x 4 (Euler, NavierStokes), x 5 (RANS_SA: U then nut),
+ * x 6 (RANS_SST: U then k then omega).
+ */
+int fv_checkpoint_write(const char* path, int32_t equation, int64_t step_index, uint64_t build_number,
+                        int64_t cell_count, const double* payload);
+/*
+ * Checkpoint::read / read_flow_field (include/Checkpoint.h:102-142): checks
+ * magic, version, equation tag and cell count, fails on a truncated file.
+ * expected_equation < 0 accepts any flow equation and reads its state block
+ * (cell_count x 4).  FV_ERR_BAD_ARG with a message on any mismatch.
+ */
+int fv_checkpoint_read(const char* path, int32_t expected_equation, int64_t expected_cell_count, int64_t* step_index,
+                       uint64_t* build_number, double* payload);
+
+/* ------------------------------------------------------------------------
  * Allocation-free step
  * ------------------------------------------------------------------------ */
 /*

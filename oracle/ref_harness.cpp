@@ -26,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "Checkpoint.h"
 #include "EulerFVMSolver.h"
 #include "GradientReconstruction.h"
 #include "MeshReader.h"
@@ -294,6 +295,45 @@ int run_walldist(UnstructuredMesh m, const std::string& out) {
     return 0;
 }
 
+// Checkpoint::write / Checkpoint::read (include/Checkpoint.h:72-116):
+//   ckpt op=write path=<f> eq=<tag> step=<n> build=<b> in=<raw doubles> cells=<n>
+//   ckpt op=read  path=<f> eq=<tag> cells=<n> out=<dir>   (prints step/build)
+int run_ckpt() {
+    const std::string path = arg("path");
+    const CheckpointEquation eq = (CheckpointEquation)argi("eq", 1);
+    const size_t cells = (size_t)argi("cells", 0);
+    const bool flow = eq != CheckpointEquation::Diffusion && eq != CheckpointEquation::AdvectionDiffusion;
+    if (arg("op") == "write") {
+        std::ifstream in(arg("in"), std::ios::binary);
+        std::vector<double> raw(cells * (flow ? 4 : 1));
+        in.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * sizeof(double)));
+        bool ok;
+        if (flow) {
+            std::vector<EulerState> U(cells);
+            for (size_t i = 0; i < cells; ++i) U[i] = {raw[4 * i], raw[4 * i + 1], raw[4 * i + 2], raw[4 * i + 3]};
+            ok = Checkpoint::write(path, eq, argi("step", 0), (unsigned long long)argi("build", 0), U);
+        } else {
+            ok = Checkpoint::write(path, eq, argi("step", 0), (unsigned long long)argi("build", 0), raw);
+        }
+        return ok ? 0 : 1;
+    }
+    long long step = 0;
+    unsigned long long build = 0;
+    std::vector<double> out;
+    bool ok;
+    if (flow) {
+        std::vector<EulerState> U;
+        ok = Checkpoint::read(path, eq, cells, step, build, U);
+        for (const EulerState& s : U) out.insert(out.end(), {s.rho, s.rho_u, s.rho_v, s.E});
+    } else {
+        ok = Checkpoint::read(path, eq, cells, step, build, out);
+    }
+    if (!ok) return 1;
+    dump(arg("out", ".") + "/payload.f64", out);
+    std::printf("{\"step\": %lld, \"build\": %llu}\n", step, build);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -307,6 +347,7 @@ int main(int argc, char** argv) {
         if (!eq) continue;
         g_args[std::string(argv[i], eq - argv[i])].push_back(eq + 1);
     }
+    if (mode == "ckpt") return run_ckpt();
     UnstructuredMesh mesh;
     if (!MeshReader::read(arg("mesh"), mesh)) return 1;
     std::string out = arg("out", ".");

@@ -152,6 +152,19 @@ def main():
         np.savez_compressed(os.path.join(HERE, "diffusion_cart.npz"), **mesh_arrays(cart),
                             field=np.fromfile(os.path.join(out, "field.f64")),
                             hist=np.fromfile(os.path.join(out, "resid.f64")), case=np.array(json.dumps(case)))
+    # Checkpoints written by the reference's Checkpoint::write.
+    with tempfile.TemporaryDirectory() as tmp:
+        rng = np.random.default_rng(7)
+        U = rng.random((10, 4))
+        phi = rng.random(7)
+        U.tofile(os.path.join(tmp, "U.f64"))
+        phi.tofile(os.path.join(tmp, "phi.f64"))
+        exe = os.path.join(ROOT, "oracle", "_ref", "fvref")
+        subprocess.run([exe, "ckpt", "op=write", f"path={os.path.join(HERE, 'ckpt_euler_ref.bin')}", "eq=1",
+                        "step=1234", "build=42", f"in={os.path.join(tmp, 'U.f64')}", "cells=10"], check=True)
+        subprocess.run([exe, "ckpt", "op=write", f"path={os.path.join(HERE, 'ckpt_diffusion_ref.bin')}", "eq=0",
+                        "step=77", "build=9", f"in={os.path.join(tmp, 'phi.f64')}", "cells=7"], check=True)
+        np.savez(os.path.join(HERE, "ckpt_payloads.npz"), euler=U, diffusion=phi)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
