@@ -107,6 +107,12 @@ SIGNATURES = {
     "fv_gradient_create": (C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
     "fv_gradient_destroy": (C.c_int, [_P]),
     "fv_gradient_compute": (C.c_int, [_P, _D, _D, _D, _D]),
+    "fv_mesh_create_batch": (C.c_int, [C.c_int32, C.POINTER(_P), C.c_int32, C.POINTER(_P)]),
+    "fv_batch_create": (C.c_int, [_P, C.POINTER(BC), C.c_int32, _D, C.c_double, C.c_double, C.POINTER(Options),
+                                  C.POINTER(_P)]),
+    "fv_batch_set_tolerance": (C.c_int, [_P, C.c_double]),
+    "fv_batch_status": (C.c_int, [_P, _I32, _I32, _D]),
+    "fv_batch_wall_forces": (C.c_int, [_P, C.c_int32, _D, _D]),
     "fv_checkpoint_write": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, C.c_uint64, C.c_int64, _D]),
     "fv_checkpoint_read": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, C.POINTER(C.c_int64),
                                      C.POINTER(C.c_uint64), _D]),

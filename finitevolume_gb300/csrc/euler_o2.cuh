@@ -176,17 +176,18 @@ __device__ __forceinline__ V4<T> prim_of(const St& s, T g) {
 
 // Ghost state in primitive form (EulerFVMSolver::ghost_state,
 // src/EulerFVMSolver.cpp:174-193, plus the characteristic farfield).
+// fs, when given, replaces the patch's freestream state (batched solves:
+// one freestream per instance).
 template <typename T>
-__device__ __forceinline__ V4<T> ghost_prim(const BCTable& bc, int patch, const V4<T>& w, T nx, T ny, T g) {
+__device__ __forceinline__ V4<T> ghost_prim(const BCTable& bc, int patch, const V4<T>& w, T nx, T ny, T g,
+                                            const double* fs = nullptr) {
     int t = bc.type[patch];
     if (t == BC_OUTFLOW) return w;
     if (t == BC_FARFIELD || t == BC_CHAR) {
-        T rf = (T)bc.st[patch][0];
-        T uf = (T)(bc.st[patch][1] / bc.st[patch][0]), vf = (T)(bc.st[patch][2] / bc.st[patch][0]);
-        T pf = (T)((g - 1.0) * (bc.st[patch][3] - 0.5 * bc.st[patch][0] * ((bc.st[patch][1] / bc.st[patch][0]) *
-                                                                                 (bc.st[patch][1] / bc.st[patch][0]) +
-                                                                             (bc.st[patch][2] / bc.st[patch][0]) *
-                                                                                 (bc.st[patch][2] / bc.st[patch][0]))));
+        const double* st = fs ? fs : bc.st[patch];
+        T rf = (T)st[0];
+        T uf = (T)(st[1] / st[0]), vf = (T)(st[2] / st[0]);
+        T pf = (T)((g - 1.0) * (st[3] - 0.5 * st[0] * ((st[1] / st[0]) * (st[1] / st[0]) + (st[2] / st[0]) * (st[2] / st[0]))));
         if (t == BC_FARFIELD) return {rf, uf, vf, pf};
         T ci = tsqrt<T>(g * w.p / w.r), cf = tsqrt<T>(g * pf / rf);
         T vni = w.u * nx + w.v * ny, vnf = uf * nx + vf * ny;
@@ -239,6 +240,14 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
     using WT = typename WS::type;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.m.n_cells) return;
+    // Batched solves: converged instances are frozen; each instance has
+    // its own freestream.
+    const double* fs = nullptr;
+    if (a.active) {
+        const int inst = a.cell_inst[c];
+        if (!a.active[inst]) return;
+        fs = a.inst_fs + 4 * inst;
+    }
     const WT* W = static_cast<const WT*>(a.W);
     const T g = (T)a.gamma;
     const V4<T> wc = WS::ld(W, c);
@@ -262,7 +271,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
         } else {
             const int f = -1 - nb;
             const double4_32a geo = a.m.fgeom[f];
-            V4<T> gh = ghost_prim<T>(a.bc, a.m.fpatch[f], wc, (T)geo.x, (T)geo.y, g);
+            V4<T> gh = ghost_prim<T>(a.bc, a.m.fpatch[f], wc, (T)geo.x, (T)geo.y, g, fs);
             wn = {T(0.5) * (wc.r + gh.r), T(0.5) * (wc.u + gh.u), T(0.5) * (wc.v + gh.v), T(0.5) * (wc.p + gh.p)};
         }
         const T* wnv = &wn.r;
@@ -394,10 +403,13 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_face(const O2Args a) {
     using FT = typename std::conditional<std::is_same<T, double>::value, St, float4>::type;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     double cand = DBL_MAX;
-    if (f < a.m.n_faces) {
+    // Batched solves (local dt only): faces of converged instances are skipped.
+    const bool live = f < a.m.n_faces && (!a.active || a.active[a.cell_inst[a.m.fl[f]]]);
+    if (live) {
         const WT* W = static_cast<const WT*>(a.W);
         const T g = (T)a.gamma, igm1 = (T)(1.0 / (a.gamma - 1.0));
         const int L = a.m.fl[f], R = a.m.fr[f];
+        const double* fs = a.active ? a.inst_fs + 4 * a.cell_inst[L] : nullptr;
         const double4_32a geo = a.m.fgeom[f];
         const T nx = (T)geo.x, ny = (T)geo.y;
         V4<T> wl = WS::ld(W, L), wr;
@@ -413,7 +425,7 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_face(const O2Args a) {
         } else if (R >= 0) {
             wr = WS::ld(W, R);
         }
-        if (R < 0) wr = ghost_prim<T>(a.bc, a.m.fpatch[f], wl, nx, ny, g);
+        if (R < 0) wr = ghost_prim<T>(a.bc, a.m.fpatch[f], wl, nx, ny, g, fs);
         const V4<T> F = num_flux_p<T, FLUX>(wl, wr, nx, ny, g, igm1, a.exact_tol, a.exact_max_iter);
         const T ar = (T)geo.z;
         st_flux(static_cast<FT*>(a.ff), f, V4<T>{ar * F.r, ar * F.u, ar * F.v, ar * F.p});
@@ -448,7 +460,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
     using FT = typename std::conditional<std::is_same<T, double>::value, St, float4>::type;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    if (c < a.m.n_cells) {
+    if (c < a.m.n_cells && (!a.active || a.active[a.cell_inst[c]])) {
         const FT* ff = static_cast<const FT*>(a.ff);
         St R = st_make(0.0, 0.0, 0.0, 0.0);
         double lam = 0.0;
@@ -467,6 +479,11 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
             else dtv = __longlong_as_double((long long)a.ctl->dt_bits) / a.m.vol[c];
             if (NST > 1) a.dtv[c] = dtv;
             s0 = R.r * R.r; s1 = R.ru * R.ru; s2 = R.rv * R.rv; s3 = R.E * R.E;
+            if (a.r2) {
+                double4_32a q;
+                q.x = s0; q.y = s1; q.z = s2; q.w = s3;
+                a.r2[c] = q;
+            }
         } else {
             dtv = a.dtv[c];
         }
@@ -502,7 +519,42 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
             if (STAGE == NST - 1) a.cs[c] = sqrt(g * p * ir);
         }
     }
-    if (STAGE == 0) finish_norms(s0, s1, s2, s3, a.ctl, a.partials, a.hist, a.hist_cap);
+    // Batched solves reduce per instance instead (k_batch_norms); a.r2 is
+    // uniform over the grid, so the block-wide reduction is all-or-nothing.
+    if (STAGE == 0 && !a.r2) finish_norms(s0, s1, s2, s3, a.ctl, a.partials, a.hist, a.hist_cap);
+}
+
+// Per-instance residual norms of a batched solve: one block per instance
+// folds the instance's cells (contiguous in device order) in a fixed
+// order, records the norms and the iteration count, and freezes the
+// instance once its density norm is below the tolerance.
+static __global__ void __launch_bounds__(256) k_batch_norms(const O2Args a, const int* __restrict__ inst_off,
+                                                      double* __restrict__ inst_norms, int* __restrict__ inst_iter,
+                                                      int* __restrict__ active, double tol) {
+    const int i = blockIdx.x;
+    if (!active[i]) return;
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int c = inst_off[i] + threadIdx.x; c < inst_off[i + 1]; c += blockDim.x) {
+        const double4_32a q = a.r2[c];
+        t[0] += q.x; t[1] += q.y; t[2] += q.z; t[3] += q.w;
+    }
+    __shared__ double red[8][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) t[k] = warp_sum(t[k]);
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 4; ++k) red[threadIdx.x >> 5][k] = t[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double n[4];
+        for (int k = 0; k < 4; ++k) {
+            double v = 0.0;
+            for (int w = 0; w < 8; ++w) v += red[w][k];
+            n[k] = sqrt(v);
+            inst_norms[4 * i + k] = n[k];
+        }
+        inst_iter[i] += 1;
+        if (n[0] < tol || !isfinite(n[0])) active[i] = 0;
+    }
 }
 
 // Primitive copy + sound speed from U (after construction / set_field).

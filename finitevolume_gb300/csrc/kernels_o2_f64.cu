@@ -33,6 +33,11 @@ void update(const O2Args& a, int local, cudaStream_t s) {
 namespace fvgb {
 namespace o2 {
 
+void launch_batch_norms(const O2Args& a, int n_inst, const int* inst_off, double* inst_norms, int* inst_iter,
+                        int* active, double tol, cudaStream_t s) {
+    ::fast::k_batch_norms<<<n_inst, 256, 0, s>>>(a, inst_off, inst_norms, inst_iter, active, tol);
+}
+
 void launch_prim_f64(const O2Args& a, cudaStream_t s) {
     const int cb = (a.m.n_cells + kCellBlock - 1) / kCellBlock;
     ::fast::k_prim<R><<<cb, kCellBlock, 0, s>>>(a);

@@ -205,21 +205,24 @@ uint64_t interleave32(uint32_t x, uint32_t y) {
     return spread(x) | (spread(y) << 1);
 }
 
-std::vector<int32_t> morton_order(const HostMesh& m) {
-    double xmin = *std::min_element(m.cx.begin(), m.cx.end()), xmax = *std::max_element(m.cx.begin(), m.cx.end());
-    double ymin = *std::min_element(m.cy.begin(), m.cy.end()), ymax = *std::max_element(m.cy.begin(), m.cy.end());
+// Morton (Z-order) of the centroids of cells [c0, c1).
+std::vector<int32_t> morton_order(const HostMesh& m, int32_t c0, int32_t c1) {
+    double xmin = *std::min_element(m.cx.begin() + c0, m.cx.begin() + c1);
+    double xmax = *std::max_element(m.cx.begin() + c0, m.cx.begin() + c1);
+    double ymin = *std::min_element(m.cy.begin() + c0, m.cy.begin() + c1);
+    double ymax = *std::max_element(m.cy.begin() + c0, m.cy.begin() + c1);
     double span = std::max(xmax - xmin, ymax - ymin);
     if (!(span > 0.0)) span = 1.0;
     double s = 4294967295.0 / span;
-    std::vector<std::pair<uint64_t, int32_t>> key(m.n_cells);
-    for (int32_t c = 0; c < m.n_cells; ++c) {
+    std::vector<std::pair<uint64_t, int32_t>> key(c1 - c0);
+    for (int32_t c = c0; c < c1; ++c) {
         uint32_t qx = (uint32_t)std::min(4294967295.0, (m.cx[c] - xmin) * s);
         uint32_t qy = (uint32_t)std::min(4294967295.0, (m.cy[c] - ymin) * s);
-        key[c] = {interleave32(qx, qy), c};
+        key[c - c0] = {interleave32(qx, qy), c};
     }
     std::sort(key.begin(), key.end());
-    std::vector<int32_t> perm(m.n_cells);
-    for (int32_t i = 0; i < m.n_cells; ++i) perm[i] = key[i].second;
+    std::vector<int32_t> perm(c1 - c0);
+    for (int32_t i = 0; i < c1 - c0; ++i) perm[i] = key[i].second;
     return perm;
 }
 
@@ -273,21 +276,36 @@ std::vector<int32_t> rcm_order(const HostMesh& m) {
 }  // namespace
 
 void HostMesh::build_device_layout(int reorder) {
-    if (reorder == 1) perm = morton_order(*this);
-    else if (reorder == 2) perm = rcm_order(*this);
-    else { perm.resize(n_cells); std::iota(perm.begin(), perm.end(), 0); }
-    if (reorder != 0) {
-        // Within each tile of 256 consecutive cells (one thread block), order
-        // the cells by face count: each warp then runs its per-face loops
-        // with one trip count, and a warp's instructions are issued once
-        // for all its cells.  Locality is kept at tile granularity.
-        const int32_t tile = 256;
-        for (int32_t t0 = 0; t0 < n_cells; t0 += tile) {
-            const int32_t t1 = std::min(n_cells, t0 + tile);
-            std::stable_sort(perm.begin() + t0, perm.begin() + t1, [&](int32_t a, int32_t b) {
-                return cf_off[a + 1] - cf_off[a] < cf_off[b + 1] - cf_off[b];
-            });
+    // Groups (batched meshes: one per instance) stay contiguous and in
+    // order; the space-filling-curve order applies within each group.
+    std::vector<int32_t> groups = group_off;
+    if (groups.empty()) groups = {0, n_cells};
+    if (reorder == 2 && groups.size() == 2) perm = rcm_order(*this);
+    else {
+        perm.clear();
+        perm.reserve(n_cells);
+        for (size_t g = 0; g + 1 < groups.size(); ++g) {
+            if (reorder == 0) {
+                for (int32_t c = groups[g]; c < groups[g + 1]; ++c) perm.push_back(c);
+            } else {
+                std::vector<int32_t> p = morton_order(*this, groups[g], groups[g + 1]);
+                perm.insert(perm.end(), p.begin(), p.end());
+            }
         }
+    }
+    if (reorder != 0) {
+        // Within each tile of 256 consecutive cells (one thread block) of a
+        // group, order the cells by face count: each warp then runs its
+        // per-face loops with one trip count, and a warp's instructions are
+        // issued once for all its cells.  Locality is kept at tile granularity.
+        const int32_t tile = 256;
+        for (size_t g = 0; g + 1 < groups.size(); ++g)
+            for (int32_t t0 = groups[g]; t0 < groups[g + 1]; t0 += tile) {
+                const int32_t t1 = std::min(groups[g + 1], t0 + tile);
+                std::stable_sort(perm.begin() + t0, perm.begin() + t1, [&](int32_t a, int32_t b) {
+                    return cf_off[a + 1] - cf_off[a] < cf_off[b + 1] - cf_off[b];
+                });
+            }
     }
     iperm.assign(n_cells, 0);
     for (int32_t i = 0; i < n_cells; ++i) iperm[perm[i]] = i;
@@ -510,6 +528,46 @@ void build_grad_geom(const HostMesh& m, HostGradGeom& g) {
         o[6] = m.fnx[f];
         o[7] = m.fny[f];
     }
+}
+
+void concat_meshes(const std::vector<const HostMesh*>& parts, HostMesh& out) {
+    if (parts.empty()) throw MeshError{1, "batch: no meshes"};
+    out = HostMesh{};
+    out.n_patches = parts[0]->n_patches;
+    out.group_off.push_back(0);
+    int32_t node0 = 0, cell0 = 0, face0 = 0;
+    for (const HostMesh* p : parts) {
+        if (p->n_patches != out.n_patches) throw MeshError{1, "batch: meshes have different patch counts"};
+        out.nx_.insert(out.nx_.end(), p->nx_.begin(), p->nx_.end());
+        out.ny_.insert(out.ny_.end(), p->ny_.begin(), p->ny_.end());
+        for (int32_t f = 0; f < p->n_faces; ++f) {
+            out.fn1.push_back(p->fn1[f] + node0);
+            out.fn2.push_back(p->fn2[f] + node0);
+            out.fl.push_back(p->fl[f] + cell0);
+            out.fr.push_back(p->fr[f] >= 0 ? p->fr[f] + cell0 : -1);
+            out.fpatch.push_back(p->fpatch[f]);
+        }
+        out.fnx.insert(out.fnx.end(), p->fnx.begin(), p->fnx.end());
+        out.fny.insert(out.fny.end(), p->fny.begin(), p->fny.end());
+        out.farea.insert(out.farea.end(), p->farea.begin(), p->farea.end());
+        out.fxm.insert(out.fxm.end(), p->fxm.begin(), p->fxm.end());
+        out.fym.insert(out.fym.end(), p->fym.begin(), p->fym.end());
+        if (out.cf_off.empty()) out.cf_off.push_back(0);
+        for (int32_t c = 0; c < p->n_cells; ++c) {
+            for (int32_t e = p->cf_off[c]; e < p->cf_off[c + 1]; ++e) out.cf.push_back(p->cf[e] + face0);
+            out.cf_off.push_back((int32_t)out.cf.size());
+        }
+        out.vol.insert(out.vol.end(), p->vol.begin(), p->vol.end());
+        out.cx.insert(out.cx.end(), p->cx.begin(), p->cx.end());
+        out.cy.insert(out.cy.end(), p->cy.begin(), p->cy.end());
+        node0 += p->n_nodes;
+        cell0 += p->n_cells;
+        face0 += p->n_faces;
+        out.group_off.push_back(cell0);
+    }
+    out.n_nodes = node0;
+    out.n_cells = cell0;
+    out.n_faces = face0;
 }
 
 }  // namespace fvgb

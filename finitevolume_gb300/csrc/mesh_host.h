@@ -27,6 +27,7 @@ struct HostMesh {
     // --- device order (perm[new] = reference cell, fperm[new] = ref face) --
     std::vector<int32_t> perm, iperm, fperm, ifperm;
     int32_t n_int_faces = 0;                     // faces [0, n_int) are internal
+    std::vector<int32_t> group_off;              // batched meshes: instance cell ranges (else empty)
     // SoA arrays in device order
     std::vector<int32_t> d_fl, d_fr, d_fpatch;   // right = -1 on boundary faces
     std::vector<double> d_fgeom;                 // [4F] nx, ny, area, dt-length
@@ -60,6 +61,11 @@ struct HostGradGeom {
     std::vector<double> fgrad;     // per face [8]: dist, cos_theta, kx, ky, w_L, nd, nx, ny
 };
 void build_grad_geom(const HostMesh& m, HostGradGeom& g);
+
+// Concatenation of independent meshes (batched solves): nodes, faces and
+// cells of mesh k follow those of mesh k-1 with offset indices; patch ids
+// are shared (every part must have the same patch count).
+void concat_meshes(const std::vector<const HostMesh*>& parts, HostMesh& out);
 
 // src/MeshReader.cpp:317-456 (+ validate_mesh_geometry :125-288).
 // Throws MeshError on invalid input.

@@ -55,7 +55,15 @@ Solver::~Solver() {
 }
 
 void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, double cfl0, const fv_ic_t& ic,
-                  const fv_options_t& o) {
+                  const fv_options_t& o, const double* batch_freestream) {
+    batch = batch_freestream != nullptr;
+    if (batch) {
+        if (hm.group_off.size() < 2) raise(FV_ERR_BAD_ARG, "batched solver needs a batch mesh (fv_mesh_create_batch)");
+        if (o.viscous || o.dt_mode != FV_DT_LOCAL)
+            raise(FV_ERR_UNSUPPORTED, "batched solves are inviscid steady solves with local time stepping");
+        group_off = hm.group_off;
+        n_inst = (int)group_off.size() - 1;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) raise(FV_ERR_CUDA, "no CUDA device available");
     if (n_bcs < hm.n_patches) raise(FV_ERR_BAD_ARG, "fewer boundary conditions than mesh patches");
@@ -76,7 +84,7 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     if (opt.viscous && !(opt.gas_constant > 0.0 && opt.prandtl > 0.0 && opt.mu >= 0.0))
         raise(FV_ERR_BAD_ARG, "viscous solver needs gas_constant > 0, prandtl > 0, mu >= 0");
     viscous = opt.viscous != 0;
-    general = !viscous && !(opt.order == 1 && opt.rk_stages == 1 && opt.precision == FV_PREC_FP64);
+    general = batch || (!viscous && !(opt.order == 1 && opt.rk_stages == 1 && opt.precision == FV_PREC_FP64));
     if (general && opt.strict) raise(FV_ERR_UNSUPPORTED, "strict mode covers the reference's first-order scheme only");
     if (general && opt.precision == FV_PREC_FP32_FLUX && opt.flux == FV_FLUX_EXACT)
         raise(FV_ERR_UNSUPPORTED, "the exact Riemann flux runs in FP64 only");
@@ -109,8 +117,12 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     for (int f = 0; f < F; ++f) {
         if (hm.fr[f] >= 0) continue;
         int p = hm.fpatch[f];
-        if (bc.type[p] == FV_BC_WALL || bc.type[p] == FV_BC_NOSLIP)
+        if (bc.type[p] == FV_BC_WALL || bc.type[p] == FV_BC_NOSLIP) {
             wall_faces.push_back({hm.fl[f], hm.fnx[f], hm.fny[f], hm.farea[f], hm.fxm[f], hm.fym[f], hm.ifperm[f]});
+            if (batch)
+                wall_inst.push_back((int)(std::upper_bound(group_off.begin(), group_off.end(), hm.fl[f]) -
+                                          group_off.begin()) - 1);
+        }
     }
 
     FV_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -167,6 +179,21 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         hcell = dupload(h2.d_h, owned);
     }
 
+    if (batch) {
+        // Instances are contiguous and in order in device numbering, with
+        // the same cell ranges as in reference numbering.
+        std::vector<int> ci(N);
+        for (int i = 0; i < n_inst; ++i)
+            for (int c = group_off[i]; c < group_off[i + 1]; ++c) ci[c] = i;
+        cell_inst = dupload(ci, owned);
+        inst_off = dupload(std::vector<int>(group_off.begin(), group_off.end()), owned);
+        active = dupload(std::vector<int>(n_inst, 1), owned);
+        inst_iter = dupload(std::vector<int>(n_inst, 0), owned);
+        inst_fs = dupload(std::vector<double>(batch_freestream, batch_freestream + 4 * (size_t)n_inst), owned);
+        inst_norms = dupload(std::vector<double>(4 * (size_t)n_inst, 0.0), owned);
+        r2 = dalloc<double4_32a>(N, owned);
+    }
+
     if (viscous) {
         HostGradGeom hg;
         build_grad_geom(hm, hg);
@@ -220,6 +247,12 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         s.E = p / (g - 1.0) + 0.5 * r * (u * u + v * v);
         u0[c] = s;
     }
+    if (batch)  // each instance starts from its own freestream
+        for (int i = 0; i < n_inst; ++i)
+            for (int c = group_off[i]; c < group_off[i + 1]; ++c) {
+                const double* q = batch_freestream + 4 * (size_t)i;
+                u0[c].r = q[0]; u0[c].ru = q[1]; u0[c].rv = q[2]; u0[c].E = q[3];
+            }
     upload_field(u0.data());
 }
 
@@ -283,6 +316,10 @@ O2Args Solver::o2_args() const {
     a.venkat_k = opt.venkat_k;
     a.exact_tol = opt.exact_tol;
     a.exact_max_iter = opt.exact_max_iter;
+    a.cell_inst = cell_inst;
+    a.active = active;
+    a.inst_fs = inst_fs;
+    a.r2 = r2;
     return a;
 }
 
@@ -324,12 +361,16 @@ void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* ev
             mark(part);
         }
     }
+    if (batch) {
+        o2::launch_batch_norms(a, n_inst, inst_off, inst_norms, inst_iter, active, tol, stream);
+        mark(2);
+    }
 }
 
 void Solver::step_timed(int n, double ms[3], int launches[3]) {
     if (n <= 0) raise(FV_ERR_BAD_ARG, "step_timed needs n > 0");
     ensure_history(n);
-    const int per_step = viscous ? 1 : (general ? cfg.stages * (cfg.order == 2 ? 3 : 2) : 2);
+    const int per_step = viscous ? 1 : (general ? cfg.stages * (cfg.order == 2 ? 3 : 2) + (batch ? 1 : 0) : 2);
     const size_t need = (size_t)n * per_step + 1;
     while (events.size() < need) {
         cudaEvent_t e;
@@ -456,7 +497,7 @@ void Solver::set_stream(void* s) {
 // is the owner cell's pressure (include/WallTraction.h:59-66); the viscous
 // solver adds the wall shear from the corrected face gradients, the
 // inviscid one has none.
-void Solver::wall_forces(const double ref[7], double out[11]) {
+void Solver::wall_forces(const double ref[7], double out[11], int instance) {
     const size_t nw = wall_faces.size();
     std::vector<double> tau(nw, 0.0), pw(nw, 0.0);
     if (viscous) {
@@ -481,7 +522,10 @@ void Solver::wall_forces(const double ref[7], double out[11]) {
     double qL = 0.5 * ref[0] * vmag * vmag * ref[4];
     double qL2 = qL * ref[4];
     double fd = 0, pd = 0, td = 0, lift = 0, mom = 0;
+    size_t counted = 0;
     for (size_t i = 0; i < nw; ++i) {
+        if (instance >= 0 && wall_inst[i] != instance) continue;
+        ++counted;
         const WallFace& w = wall_faces[i];
         const double p = pw[i];
         const double tx = -w.ny, ty = w.nx;  // rotate90 (src/WallTraction.cpp:11-13)
@@ -498,7 +542,7 @@ void Solver::wall_forces(const double ref[7], double out[11]) {
     }
     out[0] = fd; out[1] = pd; out[2] = td; out[3] = lift; out[4] = mom;
     out[5] = fd / qL; out[6] = pd / qL; out[7] = td / qL; out[8] = lift / qL; out[9] = mom / qL2;
-    out[10] = (double)wall_faces.size();
+    out[10] = (double)counted;
 }
 
 }  // namespace fvgb
@@ -754,6 +798,65 @@ int fv_wall_forces(fv_solver_t s, const double ref[7], double out[11]) {
     return guarded([&] {
         if (!s || !ref || !out) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
         s->s.wall_forces(ref, out);
+    });
+}
+
+// ---------------------------------------------------------------- batch ----
+int fv_mesh_create_batch(int32_t n, const fv_mesh_t* meshes, int32_t reorder, fv_mesh_t* out) {
+    return guarded([&] {
+        if (n <= 0 || !meshes || !out) fvgb::raise(FV_ERR_BAD_ARG, "bad argument");
+        std::vector<const HostMesh*> parts;
+        for (int i = 0; i < n; ++i) {
+            if (!meshes[i]) fvgb::raise(FV_ERR_BAD_ARG, "null mesh");
+            parts.push_back(&meshes[i]->h);
+        }
+        auto m = std::make_unique<fv_mesh_s>();
+        fvgb::concat_meshes(parts, m->h);
+        m->h.build_device_layout(reorder);
+        *out = m.release();
+    });
+}
+
+int fv_batch_create(fv_mesh_t mesh, const fv_bc_t* bcs, int32_t n_bcs, const double* inst_freestream, double gamma,
+                    double cfl, const fv_options_t* opt, fv_solver_t* out) {
+    return guarded([&] {
+        if (!mesh || !out || !inst_freestream || !opt) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        fv_ic_t ic;
+        std::memset(&ic, 0, sizeof(ic));
+        ic.rho = 1.0;
+        ic.p = 1.0;
+        auto s = std::make_unique<fv_solver_s>();
+        s->s.init(mesh->h, bcs, n_bcs, gamma, cfl, ic, *opt, inst_freestream);
+        *out = s.release();
+    });
+}
+
+int fv_batch_set_tolerance(fv_solver_t s, double tol_rho) {
+    return guarded([&] {
+        if (!s || !s->s.batch) fvgb::raise(FV_ERR_BAD_ARG, "not a batched solver");
+        s->s.tol = tol_rho;
+        FV_CUDA(cudaStreamSynchronize(s->s.stream));
+        for (auto& kv : s->s.graphs) cudaGraphExecDestroy(kv.second);  // the tolerance is a launch parameter
+        s->s.graphs.clear();
+    });
+}
+
+int fv_batch_status(fv_solver_t s, int32_t* active, int32_t* iterations, double* norms) {
+    return guarded([&] {
+        if (!s || !s->s.batch) fvgb::raise(FV_ERR_BAD_ARG, "not a batched solver");
+        fvgb::Solver& v = s->s;
+        FV_CUDA(cudaStreamSynchronize(v.stream));
+        if (active) FV_CUDA(cudaMemcpy(active, v.active, sizeof(int) * v.n_inst, cudaMemcpyDeviceToHost));
+        if (iterations) FV_CUDA(cudaMemcpy(iterations, v.inst_iter, sizeof(int) * v.n_inst, cudaMemcpyDeviceToHost));
+        if (norms) FV_CUDA(cudaMemcpy(norms, v.inst_norms, sizeof(double) * 4 * v.n_inst, cudaMemcpyDeviceToHost));
+    });
+}
+
+int fv_batch_wall_forces(fv_solver_t s, int32_t instance, const double ref[7], double out[11]) {
+    return guarded([&] {
+        if (!s || !s->s.batch || !ref || !out || instance < 0 || instance >= s->s.n_inst)
+            fvgb::raise(FV_ERR_BAD_ARG, "bad argument");
+        s->s.wall_forces(ref, out, instance);
     });
 }
 

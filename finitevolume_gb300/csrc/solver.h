@@ -39,6 +39,20 @@ struct Solver {
     StepCtl* ctl = nullptr;
     long long steps_taken = 0;
 
+    // Batched steady solves (one mesh per instance, concatenated)
+    bool batch = false;
+    int n_inst = 0;
+    std::vector<int32_t> group_off;   // instance cell ranges (same in both numberings)
+    std::vector<int> wall_inst;       // instance of each entry of wall_faces
+    int* cell_inst = nullptr;
+    int* active = nullptr;
+    int* inst_off = nullptr;
+    int* inst_iter = nullptr;
+    double* inst_fs = nullptr;
+    double* inst_norms = nullptr;
+    double4_32a* r2 = nullptr;
+    double tol = -1.0;                // density-norm tolerance; < 0 never freezes
+
     // Navier-Stokes path
     bool viscous = false;
     NSArgs ns{};
@@ -69,7 +83,7 @@ struct Solver {
 
     ~Solver();
     void init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, double cfl, const fv_ic_t& ic,
-              const fv_options_t& o);
+              const fv_options_t& o, const double* batch_freestream = nullptr);
     void ensure_history(int n);
     O1Args o1_args() const;
     O2Args o2_args() const;
@@ -84,7 +98,7 @@ struct Solver {
     void upload_field(const void* in_ref_order);
     void set_cfl(double cfl);
     void set_stream(void* s);
-    void wall_forces(const double ref[7], double out[11]);
+    void wall_forces(const double ref[7], double out[11], int instance = -1);
 };
 
 }  // namespace fvgb

@@ -90,6 +90,13 @@ struct O2Args {
     BCTable bc;
     double gamma, venkat_k, exact_tol;
     int exact_max_iter;
+    // Batched solves (all null otherwise): instance of each cell, the
+    // instance-active flags, per-instance freestream (4 conserved values),
+    // per-cell squared residuals at stage 0.
+    const int* cell_inst;
+    const int* active;
+    const double* inst_fs;
+    double4_32a* r2;
 };
 
 // Second-order path configuration (validated by the solver).
@@ -112,6 +119,8 @@ void launch_prim_f32(const O2Args& a, cudaStream_t s);
 // part 0: gradients + limiter (order 2 only), 1: face fluxes, 2: update.
 void launch_part_f64(const O2Args& a, const O2Config& c, int stage, int part, cudaStream_t s);
 void launch_part_f32(const O2Args& a, const O2Config& c, int stage, int part, cudaStream_t s);
+void launch_batch_norms(const O2Args& a, int n_inst, const int* inst_off, double* inst_norms, int* inst_iter,
+                        int* active, double tol, cudaStream_t s);
 }  // namespace o2
 
 // part 0: face pass, 1: cell pass.

@@ -363,6 +363,108 @@ class UnstructuredFVMSolver:
             self._h = None
 
 
+class _BatchMesh:
+    """Device mesh of concatenated instance meshes (fv_mesh_create_batch)."""
+
+    def __init__(self, meshes: Sequence[Mesh], reorder: str = "morton"):
+        self.parts = list(meshes)
+        arr = (C.c_void_p * len(self.parts))(*[m.handle.value for m in self.parts])
+        h = C.c_void_p()
+        capi.check(capi.lib().fv_mesh_create_batch(len(self.parts), arr, capi.REORDER[reorder], C.byref(h)))
+        self._h = h
+        self.n_cells = sum(m.n_cells for m in self.parts)
+        self.offsets = np.cumsum([0] + [m.n_cells for m in self.parts])
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                capi.lib().fv_mesh_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+class BatchSolver:
+    """Many independent steady Euler solves advanced together.
+
+    ``meshes``: one Mesh per instance (same patches); ``freestreams``:
+    (rho, u, v, p) per instance, used by the farfield patches and as the
+    initial state; ``boundary_types``: EulerBoundaryType per patch.  Every
+    instance stops (is frozen on the device) once its own L2 density
+    residual falls below ``tol``.
+    """
+
+    def __init__(self, meshes: Sequence[Mesh], boundary_types: Sequence[EulerBoundaryType], freestreams,
+                 gamma: float = 1.4, cfl: float = 1.2, flux_scheme: NumericalFluxScheme = NumericalFluxScheme.HLLC,
+                 *, order: int = 2, rk_stages: int = 3, gradient: GradientScheme = GradientScheme.LeastSquares,
+                 limiter: Limiter = Limiter.Venkatakrishnan, venkat_k: float = 5.0, fp32_flux: bool = False,
+                 tol: float = -1.0):
+        self.mesh = _BatchMesh(meshes)
+        self.n = len(meshes)
+        fs = np.array([from_primitive(*q, gamma) for q in freestreams], dtype=np.float64).reshape(-1)
+        bc = (capi.BC * len(boundary_types))()
+        for i, t in enumerate(boundary_types):
+            bc[i].type = int(t)
+        o = capi.default_options()
+        o.flux, o.order, o.rk_stages, o.dt_mode = int(flux_scheme), int(order), int(rk_stages), 1
+        o.gradient, o.limiter, o.venkat_k = int(gradient), int(limiter), float(venkat_k)
+        o.precision = 1 if fp32_flux else 0
+        h = C.c_void_p()
+        capi.check(capi.lib().fv_batch_create(self.mesh.handle, bc, len(boundary_types), capi.dptr(fs), float(gamma),
+                                              float(cfl), C.byref(o), C.byref(h)))
+        self._h = h
+        self.set_tolerance(tol)
+
+    def set_tolerance(self, tol: float) -> None:
+        capi.check(capi.lib().fv_batch_set_tolerance(self._h, float(tol)))
+
+    def run(self, n: int) -> None:
+        capi.check(capi.lib().fv_step(self._h, int(n), None))
+
+    def step_timed(self, n: int):
+        ms = np.zeros(3)
+        cnt = np.zeros(3, np.int32)
+        capi.check(capi.lib().fv_step_timed(self._h, int(n), capi.dptr(ms), capi.i32ptr(cnt)))
+        return ms, cnt
+
+    def status(self):
+        """(active[n], iterations[n], norms[n, 4])."""
+        act = np.zeros(self.n, np.int32)
+        it = np.zeros(self.n, np.int32)
+        nr = np.zeros((self.n, 4))
+        capi.check(capi.lib().fv_batch_status(self._h, capi.i32ptr(act), capi.i32ptr(it), capi.dptr(nr)))
+        return act.astype(bool), it, nr
+
+    def field(self, instance: int) -> np.ndarray:
+        out = np.zeros((self.mesh.n_cells, 4))
+        capi.check(capi.lib().fv_get_field(self._h, capi.dptr(out)))
+        o = self.mesh.offsets
+        return out[o[instance]:o[instance + 1]]
+
+    def wall_forces(self, instance: int, rho_ref, u_ref, v_ref, p_ref, length_ref=1.0, moment_x=0.25,
+                    moment_y=0.0) -> dict:
+        ref = np.array([rho_ref, u_ref, v_ref, p_ref, length_ref, moment_x, moment_y], dtype=np.float64)
+        out = np.zeros(11)
+        capi.check(capi.lib().fv_batch_wall_forces(self._h, int(instance), capi.dptr(ref), capi.dptr(out)))
+        keys = ["friction_drag", "pressure_drag", "total_drag", "lift", "moment", "cd_friction", "cd_pressure",
+                "cd_total", "cl", "cm", "n_wall_faces"]
+        return dict(zip(keys, out.tolist()))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                capi.lib().fv_solver_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
 class NSBoundaryType(enum.IntEnum):
     """include/NavierStokesFVMSolver.h:19-23 (same numbering)."""
     NoSlipWall = 0

@@ -215,6 +215,33 @@ int fv_device_state(fv_solver_t s, void** U_dev, void** stream);
 int fv_wall_forces(fv_solver_t s, const double ref[7], double out[11]);
 
 /* ------------------------------------------------------------------------
+ * Batched steady solves (many independent meshes, one launch sequence)
+ * ------------------------------------------------------------------------ */
+/*
+ * No single reference counterpart: the reference solves one case per
+ * process.  Concatenates n meshes (same patch count) into one batch mesh;
+ * each instance's cells stay contiguous in device order.
+ */
+int fv_mesh_create_batch(int32_t n, const fv_mesh_t* meshes, int32_t reorder, fv_mesh_t* out);
+/*
+ * One solver over a batch mesh: the scheme of opt (local time stepping
+ * required), shared per-patch boundary types bcs[], and one freestream per
+ * instance (inst_freestream [4n], conserved) used by the farfield patches
+ * and as each instance's initial state.  fv_step advances every active
+ * instance; each instance's residual norms are reduced on its own and the
+ * instance is frozen once its density norm falls below the tolerance
+ * (per-instance early exit).  fv_get_field returns all instances in order.
+ */
+int fv_batch_create(fv_mesh_t batch_mesh, const fv_bc_t* bcs, int32_t n_bcs, const double* inst_freestream, double gamma,
+                    double cfl, const fv_options_t* opt, fv_solver_t* out);
+/* Density-residual tolerance of the early exit (< 0: never freeze). */
+int fv_batch_set_tolerance(fv_solver_t s, double tol_rho);
+/* Per instance: active flag, iterations taken, last residual norms [4n]. */
+int fv_batch_status(fv_solver_t s, int32_t* active, int32_t* iterations, double* norms);
+/* fv_wall_forces restricted to one instance's wall faces. */
+int fv_batch_wall_forces(fv_solver_t s, int32_t instance, const double ref[7], double out[11]);
+
+/* ------------------------------------------------------------------------
  * Scalar diffusion solver (UnstructuredFVMSolver)
  * ------------------------------------------------------------------------ */
 typedef struct fv_diffusion_s* fv_diffusion_t;
