@@ -44,12 +44,12 @@ def write_mesh(mesh, path, patch_specs=None):
         f.write(f"{cd.shape[0]}\n")
         for c in range(cd.shape[0]):
             fl = cf[off[c]:off[c + 1]].tolist()
-            f.write(f"{cd[c, 0]!r} {cd[c, 1]!r} {cd[c, 2]!r} {len(fl)} {' '.join(map(str, fl))}\n")
+            f.write(f"{float(cd[c, 0])!r} {float(cd[c, 1])!r} {float(cd[c, 2])!r} {len(fl)} {' '.join(map(str, fl))}\n")
         names = mesh.patch_names
         f.write(f"{len(names)}\n")
         for n in names:
             t, v = (patch_specs or {}).get(n, (0, 0.0))
-            f.write(f"{n} {t} {v!r}\n")
+            f.write(f"{n} {t} {float(v)!r}\n")
 
 
 def test_driver_compiles_against_reference_headers(tmp_path):
@@ -60,7 +60,7 @@ def test_driver_compiles_against_reference_headers(tmp_path):
 
 def _run(exe, mesh_txt, case, out):
     with open(out + ".case", "w") as f:
-        f.write("\n".join(f"{k} {v!r}" for k, v in case.items()) + "\n")
+        f.write("\n".join(f"{k} {float(v)!r}" for k, v in case.items()) + "\n")
     subprocess.run([exe, mesh_txt, out + ".case", out], check=True, capture_output=True)
     return np.fromfile(out)
 
