@@ -36,6 +36,9 @@ GAMMA = 1.4
 MACH, AOA_DEG, CFL, VENKAT_K = 0.8, 1.25, 1.2, 5.0
 MESH_KW = dict(ni=1024, nj=512, first=1e-3, r_core=2.0, r_far=20.0, code="0012", lloyd_iters=4, seed=0)
 METRIC = "Mcell-iters/s, 2nd-order HLLC Euler at 1M cells; batched/FP32/adjoint vs plain"
+# FP64-pipe thread instructions per second of one GB300 (152 SMs at 2070 MHz,
+# a dependent-chain-free DFMA loop timed with CUDA events: 1.02 TFLOP/s).
+FP64_PIPE_GINST_S = 510.0
 
 
 def freestream():
@@ -304,6 +307,14 @@ def main():
             "kernel_ms_per_step": {k: round(m / args.steps, 4) for k, m in zip(roofline.KERNEL_NAMES, ms)},
             "stage": {"survey_bytes_B2": stage_alg, "ms": round(stage_ms, 4),
                       "achieved_GBs": round(stage_alg / (stage_ms / 1e3) / 1e9, 1)}}
+    # What actually bounds it: FP64-pipe issue (ncu instruction count per
+    # cell of this kernel x cells / live launch time, against the GB300
+    # DFMA rate of 0.51e12 thread instructions/s measured on the box).
+    inst = roofline.MEASURED_FP64_INST_PER_CELL.get(kname)
+    if inst is not None:
+        ach_inst = inst * n_cells / (per_launch_ms / 1e3) / 1e9
+        roof["fp64_pipe"] = {"inst_per_cell_ncu": inst, "achieved_ginst_s": round(ach_inst, 1),
+                             "peak_ginst_s": FP64_PIPE_GINST_S, "frac": round(ach_inst / FP64_PIPE_GINST_S, 4)}
 
     # End to end through the public API with host buffers: every step
     # uploads the state from pinned host memory (set_field), advances one
