@@ -159,6 +159,179 @@ def measured_peaks():
 
 
 # --------------------------------------------------------------------------
+# Batched steady solves: 256 NACA 4-digit O-grids (camber 0-6%, thickness
+# 8-18%, 4k-64k cells log-uniform), M 0.3-0.85, AoA -4..8 deg, 2nd-order
+# HLLC + LSQ/Venkatakrishnan, SSP-RK3, local dt at CFL 1.2.
+def batch_workload(n: int, seed: int = 0):
+    from finitevolume_gb300 import meshgen, solvers as S
+    cases = meshgen.batch_cases(n, seed)
+    meshes = [S.Mesh(meshgen.naca_ogrid(c["ni"], c["nj"], shape=c["shape"]), reorder="morton") for c in cases]
+    fss = []
+    for c in cases:
+        a = np.radians(c["aoa_deg"])
+        fss.append((1.0, c["mach"] * np.cos(a), c["mach"] * np.sin(a), 1.0 / GAMMA))
+    return cases, meshes, fss
+
+
+def _plain_solver(mesh, fs, fp32):
+    from finitevolume_gb300 import solvers as S
+    bcs = [S.EulerBoundaryCondition(S.EulerBoundaryType.Wall),
+           S.EulerBoundaryCondition(S.EulerBoundaryType.CharacteristicFarfield, S.from_primitive(*fs, GAMMA))]
+    ic = S.EulerInitialCondition(S.EulerICMode.Freestream, rho=fs[0], u=fs[1], v=fs[2], p=fs[3])
+    return S.EulerFVMSolver(mesh, bcs, GAMMA, CFL, ic, S.NumericalFluxScheme.HLLC, order=2, rk_stages=3,
+                            local_dt=True, gradient=S.GradientScheme.LeastSquares, limiter=S.Limiter.Venkatakrishnan,
+                            venkat_k=VENKAT_K, fp32_flux=fp32)
+
+
+def _batch_solver(meshes, fss, fp32, tol=-1.0):
+    from finitevolume_gb300 import solvers as S
+    return S.BatchSolver(meshes, [S.EulerBoundaryType.Wall, S.EulerBoundaryType.CharacteristicFarfield], fss,
+                         GAMMA, CFL, S.NumericalFluxScheme.HLLC, venkat_k=VENKAT_K, fp32_flux=fp32, tol=tol)
+
+
+def batch_throughput(meshes, fss, fp32: bool, iters: int):
+    """Fixed-iteration rate of the batch vs the same instances one by one.
+
+    Returns (batched Mcell-iters/s, sequential Mcell-iters/s); both timed
+    on the host around direct solver calls ending in a device sync.
+    """
+    import torch
+    from finitevolume_gb300 import capi
+    cells = sum(m.n_cells for m in meshes)
+    b = _batch_solver(meshes, fss, fp32)
+    b.run(3)
+    b.status()
+    t0 = time.perf_counter()
+    b.run(iters)
+    b.status()
+    tb = time.perf_counter() - t0
+    del b
+    ts = 0.0
+    for m, fs in zip(meshes, fss):
+        s = _plain_solver(m, fs, fp32)
+        try:
+            s.run(3)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.run(iters)  # fv_step returns after its stream has drained
+        except capi.FVError:  # a diverged instance: timed up to the raise
+            pass
+        ts += time.perf_counter() - t0
+        del s
+    return cells * iters / tb / 1e6, cells * iters / ts / 1e6
+
+
+def _per_iter_seconds(mesh, fs, fp32: bool, iters: int = 40) -> float:
+    """Per-iteration wall time of one plain (unbatched) solve of a case."""
+    from finitevolume_gb300 import capi
+    s = _plain_solver(mesh, fs, fp32)
+    try:
+        s.run(5)
+        t0 = time.perf_counter()
+        s.run(iters)
+        return (time.perf_counter() - t0) / iters
+    except capi.FVError:
+        return float("nan")
+    finally:
+        del s
+
+
+def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 500, cd_tol: float = 1e-5):
+    """Converged steady solves per second, batched vs plain sequential.
+
+    FP64: the batch runs with per-instance early exit at the density
+    tolerance (capped at ``max_iter``); instance i takes K_i iterations.
+    FP32-flux: an instance counts as converged at the first of two
+    consecutive checkpoints (every ``chunk`` iterations) with
+    |CD - CD_fp64| <= ``cd_tol`` against its converged FP64 drag, and is
+    then frozen; instances without a converged FP64 reference run to the
+    cap and count as not converged.
+    Sequential: each plain solve of the same case performs the same
+    arithmetic as its batch instance (the batch reproduces a standalone
+    solve to round-off), so it takes the same K_i iterations; its time is
+    K_i times the measured per-iteration time of that plain solve.
+    """
+    n = len(meshes)
+    refs = [(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0) for fs in fss]
+    out = {}
+    # FP64 batched, early exit on the residual
+    b = _batch_solver(meshes, fss, False, tol)
+    t0 = time.perf_counter()
+    done = 0
+    while done < max_iter:
+        b.run(chunk)
+        done += chunk
+        act, it, nr = b.status()
+        if not act.any():
+            break
+    t64 = time.perf_counter() - t0
+    conv64 = (~act) & (nr[:, 0] < tol)
+    k64 = it.copy()
+    cd64 = np.array([b.wall_forces(i, *refs[i])["cd_total"] for i in range(n)])
+    del b
+    # FP32-flux batched, drag criterion; the timer stops during the drag reads
+    b = _batch_solver(meshes, fss, True, -1.0)
+    k32 = np.full(n, max_iter, np.int64)
+    hits = np.zeros(n, np.int64)
+    conv32 = np.zeros(n, bool)
+    t32 = 0.0
+    done = 0
+    while done < max_iter:
+        t0 = time.perf_counter()
+        b.run(chunk)
+        b.status()
+        t32 += time.perf_counter() - t0
+        done += chunk
+        for i in np.nonzero(conv64 & ~conv32)[0]:
+            cd = b.wall_forces(int(i), *refs[i])["cd_total"]
+            hits[i] = hits[i] + 1 if abs(cd - cd64[i]) <= cd_tol else 0
+            if hits[i] >= 2:
+                conv32[i] = True
+                k32[i] = done
+                b.set_active(int(i), False)
+        if conv32[conv64].all():
+            break
+    # instances still running at the end ran every checkpoint
+    act32, it32, _ = b.status()
+    k32 = np.where(conv32, k32, it32)
+    del b
+    # plain sequential solves: per-iteration time of each case
+    t_seq64 = np.array([_per_iter_seconds(m, fs, False) for m, fs in zip(meshes, fss)])
+    t_seq32 = np.array([_per_iter_seconds(m, fs, True) for m, fs in zip(meshes, fss)])
+    s64 = float(np.nansum(k64 * t_seq64))
+    s32 = float(np.nansum(k32 * t_seq32))
+    n64, n32 = int(conv64.sum()), int(conv32.sum())
+    out["f64"] = {"batched_solves_per_s": round(n64 / t64, 5), "batched_seconds": round(t64, 2), "converged": n64,
+                  "sequential_solves_per_s": round(n64 / s64, 5), "sequential_seconds": round(s64, 2),
+                  "iterations_median": int(np.median(k64)),
+                  "iterations_converged_median": int(np.median(k64[conv64])) if n64 else None}
+    out["fp32_flux"] = {"batched_solves_per_s": round(n32 / t32, 5), "batched_seconds": round(t32, 2),
+                        "converged": n32, "criterion": f"|CD - CD_fp64| <= {cd_tol} at two checkpoints",
+                        "sequential_solves_per_s": round(n32 / s32, 5), "sequential_seconds": round(s32, 2),
+                        "iterations_converged_median": int(np.median(k32[conv32])) if n32 else None}
+    out["instances"] = n
+    out["sequential_method"] = ("K_i x measured per-iteration time of the plain solve of case i "
+                                "(40 iterations after 5 warm-up), summed over all instances")
+    return out
+
+
+def run_batched(args):
+    """--batched: converged solves/s of the 256-instance family, FP64 and
+    FP32-flux, batched vs plain sequential solves."""
+    import torch
+    torch.cuda.init()
+    cases, meshes, fss = batch_workload(args.instances)
+    out = {"metric": "converged steady solves/s, 256-instance batched Euler (per-instance early exit)",
+           "unit": "solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic (seeded NACA family)",
+           "config": {"workload": "naca4_family_ogrid_batch", "instances": len(meshes),
+                      "cells_total": int(sum(m.n_cells for m in meshes)), "tol_l2_density": args.tol,
+                      "max_iter": args.max_iter, "cfl": CFL},
+           "results": {}}
+    out["results"] = batch_converged(cases, meshes, fss, args.tol, args.max_iter)
+    print(json.dumps(out), flush=True)
+
+
+# --------------------------------------------------------------------------
 def cpu_port_rate(poly, U0, max_seconds: float, threads: int = 0):
     """Time the oracle port (CPU restatement, OpenMP) on the same workload."""
     from oracle import port
@@ -229,7 +402,15 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiler target: build the workload, run --steps iterations with direct launches, exit")
     ap.add_argument("--fp32", action="store_true", help="with --profile: the FP32-flux variant")
+    ap.add_argument("--batched", action="store_true",
+                    help="converged solves/s of the batched airfoil family instead of the headline")
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--max-iter", type=int, default=20000)
     args = ap.parse_args()
+    if args.batched:
+        run_batched(args)
+        return
     if args.profile:
         poly = load_mesh()
         s, _ = make_solver(poly, fp32=args.fp32)
@@ -351,13 +532,34 @@ def main():
         fa, fb = a.wall_forces(*force_ref()), b.wall_forces(*force_ref())
         Ua, Ub = a.field(), b.field()
         v32 = n_cells * args.steps / (float(np.sum(ms32)) / 1e3) / 1e6
+        k32 = int(np.argmax(ms32))
+        kn32 = roofline.KERNEL_NAMES[k32]
+        pl32 = ms32[k32] / max(l32[k32], 1)
+        alg32 = roofline.kernel_bytes(kn32, n_cells, n_faces, n_bf, fp32=True)
         variants["fp32_flux"] = {
             "value": round(v32, 3), "unit": "Mcell-iters/s", "speedup_vs_fp64": round(v32 / value * world, 3),
             "kernel_ms_per_step": {k: round(m / args.steps, 4) for k, m in zip(roofline.KERNEL_NAMES, ms32)},
+            "roofline": {"bound": "hbm", "kernel": kn32, "launch_ms": round(pl32, 4),
+                         "algorithmic_bytes_per_launch": alg32,
+                         "achieved": round(alg32 / (pl32 / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(alg32 / (pl32 / 1e3) / 1e9 / hbm, 4),
+                         "traffic": roofline.measured_traffic(kn32, n_cells, fp32=True)},
             "dCL": abs(fa["cl"] - fb["cl"]), "dCD": abs(fa["cd_total"] - fb["cd_total"]),
             "state_l2_rel": float(np.linalg.norm(Ua - Ub) / np.linalg.norm(Ua)),
             "iterations_compared": args.warmup + args.steps}
         del a, b
+        # Batched steady solves at a fixed iteration count: 256 instances
+        # advanced together vs the same instances one after another.
+        _, bm, bfs = batch_workload(256)
+        it = int(os.environ.get("FV_BATCH_ITERS", "20"))
+        for prec, fp32 in (("f64", False), ("fp32_flux", True)):
+            rb, rs = batch_throughput(bm, bfs, fp32, it)
+            variants[f"batched_256_{prec}"] = {
+                "value": round(rb, 3), "unit": "Mcell-iters/s", "sequential": round(rs, 3),
+                "speedup_vs_sequential": round(rb / rs, 3), "iterations": it,
+                "cells_total": int(sum(m.n_cells for m in bm)),
+                "workload": "256 NACA 4-digit O-grids, 4k-64k cells log-uniform, M 0.3-0.85, AoA -4..8"}
+        del bm
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": world,

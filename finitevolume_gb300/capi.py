@@ -113,6 +113,7 @@ SIGNATURES = {
     "fv_batch_set_tolerance": (C.c_int, [_P, C.c_double]),
     "fv_batch_status": (C.c_int, [_P, _I32, _I32, _D]),
     "fv_batch_wall_forces": (C.c_int, [_P, C.c_int32, _D, _D]),
+    "fv_batch_set_active": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "fv_checkpoint_write": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, C.c_uint64, C.c_int64, _D]),
     "fv_checkpoint_read": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, C.POINTER(C.c_int64),
                                      C.POINTER(C.c_uint64), _D]),

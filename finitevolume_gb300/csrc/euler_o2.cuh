@@ -30,6 +30,7 @@
 #include <type_traits>
 
 #include "euler_o1.cuh"
+#include "fpconv.cuh"
 
 namespace FV_KNS {
 
@@ -94,13 +95,42 @@ template <> struct GStore<float> {
     }
 };
 
-// Face flux storage: double -> St; float -> float4.  Loaded as FP64 in the gather.
+// Flux-precision geometry: the solver stores these arrays as double (FP64
+// mode) or float (FP32-flux mode), so no conversion is issued per use.
+template <typename T> __device__ __forceinline__ T pick(double d, float f) {
+    if constexpr (std::is_same<T, double>::value) return d;
+    else return f;
+}
+template <typename T> __device__ __forceinline__ void ld_pair(const void* p, int i, T& x, T& y) {
+    if constexpr (std::is_same<T, double>::value) {
+        const double2 q = __ldg(static_cast<const double2*>(p) + i);
+        x = q.x; y = q.y;
+    } else {
+        const float2 q = __ldg(static_cast<const float2*>(p) + i);
+        x = q.x; y = q.y;
+    }
+}
+template <typename T> __device__ __forceinline__ void ld_quad(const void* p, int i, T& x, T& y, T& z, T& w) {
+    if constexpr (std::is_same<T, double>::value) {
+        const double4_32a q = static_cast<const double4_32a*>(p)[i];
+        x = q.x; y = q.y; z = q.z; w = q.w;
+    } else {
+        const float4 q = __ldg(static_cast<const float4*>(p) + i);
+        x = q.x; y = q.y; z = q.z; w = q.w;
+    }
+}
+template <typename T> __device__ __forceinline__ T ld_one(const void* p, int i) {
+    return __ldg(static_cast<const T*>(p) + i);
+}
+
+// Face flux storage: double -> St; float -> float4.  Loaded as FP64 in the
+// gather (exact widening on the integer pipe).
 __device__ __forceinline__ void st_flux(St* ff, int f, const V4<double>& F) { st_state(ff, f, st_make(F.r, F.u, F.v, F.p)); }
 __device__ __forceinline__ void st_flux(float4* ff, int f, const V4<float>& F) { ff[f] = make_float4(F.r, F.u, F.v, F.p); }
 __device__ __forceinline__ St ld_flux(const St* ff, int f) { return ld_state(ff, f); }
 __device__ __forceinline__ St ld_flux(const float4* ff, int f) {
     float4 a = __ldg(ff + f);
-    return st_make((double)a.x, (double)a.y, (double)a.z, (double)a.w);
+    return st_make(fvconv::f2d(a.x), fvconv::f2d(a.y), fvconv::f2d(a.z), fvconv::f2d(a.w));
 }
 
 // ---------------------------------------------------------------------------
@@ -211,6 +241,17 @@ __device__ __forceinline__ V4<T> ghost_prim(const BCTable& bc, int patch, const 
 
 using fvgb::O2Args;
 
+// Face normal, length and CFL length in flux precision.
+template <typename T> __device__ __forceinline__ void face_geom(const O2Args& a, int f, T& nx, T& ny, T& ar, T& len) {
+    if constexpr (std::is_same<T, double>::value) {
+        const double4_32a q = a.m.fgeom[f];
+        nx = q.x; ny = q.y; ar = q.z; len = q.w;
+    } else {
+        const float4 q = __ldg(a.fgeom32 + f);
+        nx = q.x; ny = q.y; ar = q.z; len = q.w;
+    }
+}
+
 // Order-preserving integer key of an IEEE value (negative values have their
 // magnitude bits flipped), so that integer compares -- on the integer pipe,
 // not the scarce FP64 pipe -- order values like the floating-point compare
@@ -234,8 +275,10 @@ template <> struct OKey<float> {
 };
 
 // ---------------------------------------------------------------------------
+// Resident blocks per SM: FP32 mode is latency bound (4 blocks, <= 64
+// registers); FP64 mode needs 2 blocks to keep the FP64 pipe fed.
 template <typename T, int GRAD, int LIM>
-__global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
+__global__ void __launch_bounds__(fvgb::kCellBlock, sizeof(T) == 4 ? 4 : 2) k_grad(const O2Args a) {
     using WS = WStore<T>;
     using WT = typename WS::type;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -249,7 +292,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
         fs = a.inst_fs + 4 * inst;
     }
     const WT* W = static_cast<const WT*>(a.W);
-    const T g = (T)a.gamma;
+    const T g = pick<T>(a.gamma, a.gamma32);
     const V4<T> wc = WS::ld(W, c);
     const T* wcv = &wc.r;
     using OK = OKey<T>;
@@ -270,16 +313,17 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
             wn = WS::ld(W, nb);
         } else {
             const int f = -1 - nb;
-            const double4_32a geo = a.m.fgeom[f];
-            V4<T> gh = ghost_prim<T>(a.bc, a.m.fpatch[f], wc, (T)geo.x, (T)geo.y, g, fs);
+            T nx, ny, ar, len;
+            face_geom<T>(a, f, nx, ny, ar, len);
+            V4<T> gh = ghost_prim<T>(a.bc, a.m.fpatch[f], wc, nx, ny, g, fs);
             wn = {T(0.5) * (wc.r + gh.r), T(0.5) * (wc.u + gh.u), T(0.5) * (wc.v + gh.v), T(0.5) * (wc.p + gh.p)};
         }
         const T* wnv = &wn.r;
         if (GRAD == 0) {
             // sum_j a_j (W_j - W_c) = sum_j a_j W_j - (sum_j a_j) W_c; the
             // weight sums are per-cell geometry (lsq_sum).
-            const double2 ab = __ldg(a.lsq + e);
-            const T ax = (T)ab.x, ay = (T)ab.y;
+            T ax, ay;
+            ld_pair<T>(a.lsq, e, ax, ay);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const I kk = OK::key(wnv[k]);
@@ -289,8 +333,8 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
                 gy[k] += ay * wnv[k];
             }
         } else {
-            const double4_32a q = a.gg[e];
-            const T ax = (T)q.x, ay = (T)q.y, wgt = (T)q.z;
+            T ax, ay, wgt, unused;
+            ld_quad<T>(a.gg, e, ax, ay, wgt, unused);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 T d = wnv[k] - wcv[k];
@@ -303,21 +347,18 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
         }
     }
     if (GRAD == 0) {
-        const double2 s = __ldg(a.lsq_sum + c);
+        T sx, sy;
+        ld_pair<T>(a.lsq_sum, c, sx, sy);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            gx[k] -= (T)s.x * wcv[k];
-            gy[k] -= (T)s.y * wcv[k];
+            gx[k] -= sx * wcv[k];
+            gy[k] -= sy * wcv[k];
             dmax[k] = OK::val(kmax[k]) - wcv[k];
             dmin[k] = OK::val(kmin[k]) - wcv[k];
         }
     }
     if (LIM != 0) {
-        T eps2 = T(0);
-        if (LIM == 2) {
-            T kh = (T)(a.venkat_k * a.h[c]);
-            eps2 = kh * kh * kh;
-        }
+        const T eps2 = LIM == 2 ? ld_one<T>(a.eps2, c) : T(0);
         // Per face f the limiter value is psi_f = phi(D1, D2_f) with D2_f the
         // unlimited extrapolation to the face and D1 = dmax (D2_f > 0) or
         // dmin (D2_f < 0).  With D1 fixed per sign, phi only limits
@@ -330,8 +371,8 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_grad(const O2Args a) {
         I pmax[4] = {0, 0, 0, 0}, nmax[4] = {0, 0, 0, 0};
         const I sign = OK::sign_bit();
         for (int e = e0; e < e1; ++e) {
-            const double2 r = __ldg(a.erf + e);
-            const T rx = (T)r.x, ry = (T)r.y;
+            T rx, ry;
+            ld_pair<T>(a.erf, e, rx, ry);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const I b = OK::bits(gx[k] * rx + gy[k] * ry);
@@ -407,38 +448,46 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_face(const O2Args a) {
     const bool live = f < a.m.n_faces && (!a.active || a.active[a.cell_inst[a.m.fl[f]]]);
     if (live) {
         const WT* W = static_cast<const WT*>(a.W);
-        const T g = (T)a.gamma, igm1 = (T)(1.0 / (a.gamma - 1.0));
+        const T g = pick<T>(a.gamma, a.gamma32), igm1 = pick<T>(a.igm1, a.igm1_32);
         const int L = a.m.fl[f], R = a.m.fr[f];
         const double* fs = a.active ? a.inst_fs + 4 * a.cell_inst[L] : nullptr;
-        const double4_32a geo = a.m.fgeom[f];
-        const T nx = (T)geo.x, ny = (T)geo.y;
+        T nx, ny, ar, len;
+        face_geom<T>(a, f, nx, ny, ar, len);
         V4<T> wl = WS::ld(W, L), wr;
         const V4<T> wlc = wl;
         if (ORDER == 2) {
-            const double4_32a rr = a.frf[f];
+            T rxl, ryl, rxr, ryr;
+            ld_quad<T>(a.frf, f, rxl, ryl, rxr, ryr);
             const G8<T> gl = GStore<T>::ld(static_cast<const typename GStore<T>::type*>(a.G), L);
-            wl = recon<T>(wl, gl, (T)rr.x, (T)rr.y);
+            wl = recon<T>(wl, gl, rxl, ryl);
             if (R >= 0) {
                 const G8<T> gr = GStore<T>::ld(static_cast<const typename GStore<T>::type*>(a.G), R);
-                wr = recon<T>(WS::ld(W, R), gr, (T)rr.z, (T)rr.w);
+                wr = recon<T>(WS::ld(W, R), gr, rxr, ryr);
             }
         } else if (R >= 0) {
             wr = WS::ld(W, R);
         }
         if (R < 0) wr = ghost_prim<T>(a.bc, a.m.fpatch[f], wl, nx, ny, g, fs);
         const V4<T> F = num_flux_p<T, FLUX>(wl, wr, nx, ny, g, igm1, a.exact_tol, a.exact_max_iter);
-        const T ar = (T)geo.z;
         st_flux(static_cast<FT*>(a.ff), f, V4<T>{ar * F.r, ar * F.u, ar * F.v, ar * F.p});
         if (DT != 0) {
             // compute_dt's per-face candidate from cell-centred states
-            // (src/EulerFVMSolver.cpp:140-160).
-            double Smax = fabs((double)wlc.u * geo.x + (double)wlc.v * geo.y) + a.cs[L];
+            // (src/EulerFVMSolver.cpp:140-160).  FP32-flux mode forms the
+            // wave speed in FP32 (the sound speed is stored in FP32 there)
+            // and widens it exactly; dt itself is FP64.
+            const T* cs = static_cast<const T*>(a.cs);
+            T Smax = fabs(wlc.u * nx + wlc.v * ny) + cs[L];
             if (R >= 0) {
                 const V4<T> wrc = WS::ld(W, R);
-                Smax = rmax(Smax, fabs((double)wrc.u * geo.x + (double)wrc.v * geo.y) + a.cs[R]);
+                Smax = rmax(Smax, fabs(wrc.u * nx + wrc.v * ny) + cs[R]);
             }
-            if (DT == 2) a.dtf[f] = Smax * geo.z;
-            else cand = a.ctl->cfl * geo.w / Smax;
+            if constexpr (std::is_same<T, double>::value) {
+                if (DT == 2) a.dtf[f] = Smax * ar;
+                else cand = a.ctl->cfl * len / Smax;
+            } else {
+                if (DT == 2) a.dtf[f] = fvconv::f2d(Smax * ar);
+                else cand = a.ctl->cfl * fvconv::f2d(len) / fvconv::f2d(Smax);
+            }
         }
     }
     if (DT == 1) {
@@ -462,10 +511,14 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
     if (c < a.m.n_cells && (!a.active || a.active[a.cell_inst[c]])) {
         const FT* ff = static_cast<const FT*>(a.ff);
-        St R = st_make(0.0, 0.0, 0.0, 0.0);
-        double lam = 0.0;
         const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
-        for (int e = e0; e < e1; ++e) {
+        // Every cell has faces: the sum starts from the first signed flux
+        // instead of 0 + flux (one FP64 add per component less; only the
+        // sign of an exactly-zero sum can differ, and u + dt * (+-0) = u).
+        const int ent0 = a.m.cf[e0];
+        St R = flip_if(ld_flux(ff, ent0 >> 1), ent0);
+        double lam = (STAGE == 0 && DT == 2) ? a.dtf[ent0 >> 1] : 0.0;
+        for (int e = e0 + 1; e < e1; ++e) {
             const int ent = a.m.cf[e];
             const int f = ent >> 1;
             R += flip_if(ld_flux(ff, f), ent);
@@ -497,26 +550,22 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
         st_state(a.U, c, un);
         const double g = a.gamma;
         if constexpr (std::is_same<T, float>::value) {
-            // FP32-flux mode: the primitive copy only feeds FP32 arithmetic,
-            // so it is derived in FP32 (off the FP64 pipe); the sound speed
-            // for the next iteration's time step stays FP64.
-            const float gf = (float)g;
-            const float rf = (float)un.r, irf = 1.0f / rf;
-            const float uf = (float)un.ru * irf, vf = (float)un.rv * irf;
-            const float pf = (gf - 1.0f) * ((float)un.E - 0.5f * rf * (uf * uf + vf * vf));
+            // FP32-flux mode: the primitive copy and the sound speed only
+            // feed FP32 arithmetic (fluxes, the wave speed of the time
+            // step), so they are derived in FP32 from the state rounded on
+            // the integer pipe; nothing here issues on the FP64 pipe.
+            const float gf = a.gamma32;
+            const float rf = fvconv::d2f(un.r), irf = 1.0f / rf;
+            const float uf = fvconv::d2f(un.ru) * irf, vf = fvconv::d2f(un.rv) * irf;
+            const float pf = (gf - 1.0f) * (fvconv::d2f(un.E) - 0.5f * rf * (uf * uf + vf * vf));
             WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{rf, uf, vf, pf});
-            if (STAGE == NST - 1) {
-                const double ir = 1.0 / un.r;
-                const double uu = un.ru * ir, vv = un.rv * ir;
-                const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
-                a.cs[c] = sqrt(g * p * ir);
-            }
+            if (STAGE == NST - 1) static_cast<float*>(a.cs)[c] = sqrtf(gf * pf * irf);
         } else {
             const double ir = 1.0 / un.r;
             const double uu = un.ru * ir, vv = un.rv * ir;
             const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
             WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{un.r, uu, vv, p});
-            if (STAGE == NST - 1) a.cs[c] = sqrt(g * p * ir);
+            if (STAGE == NST - 1) static_cast<double*>(a.cs)[c] = sqrt(g * p * ir);
         }
     }
     // Batched solves reduce per instance instead (k_batch_norms); a.r2 is
@@ -568,7 +617,12 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_prim(const O2Args a) {
     const double uu = un.ru * ir, vv = un.rv * ir;
     const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
     WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{(T)un.r, (T)uu, (T)vv, (T)p});
-    a.cs[c] = sqrt(g * p * ir);
+    if constexpr (std::is_same<T, float>::value) {
+        const float rf = (float)un.r, pf = (float)p;
+        static_cast<float*>(a.cs)[c] = sqrtf(a.gamma32 * pf / rf);
+    } else {
+        static_cast<double*>(a.cs)[c] = sqrt(g * p * ir);
+    }
 }
 
 }  // namespace FV_KNS

@@ -1,0 +1,78 @@
+// float <-> double conversions on the integer pipe.
+//
+// On GB300 a hardware double<->float conversion issues on the FP64 pipe,
+// which runs at about 1.6 thread-operations per SM-clock; in the FP32-flux
+// kernels those conversions, not the FP32 work, set the run time.  These
+// routines produce the IEEE 754 results bit for bit (float -> double is
+// exact; double -> float rounds to nearest, ties to even, with float
+// subnormals, signed zeros, overflow to infinity and NaN handled) using
+// only integer shifts, adds and selects, straight from the binary32 /
+// binary64 encodings:
+//   binary32: sign 1 | exponent 8 (bias 127)  | fraction 23
+//   binary64: sign 1 | exponent 11 (bias 1023) | fraction 52
+// so a normal value keeps its fraction bits (shifted by 29) and has its
+// exponent re-biased by 1023 - 127 = 896.
+#pragma once
+
+#include <cstdint>
+
+namespace fvconv {
+
+__device__ __forceinline__ double f2d(float x) {
+    const uint32_t b = __float_as_uint(x);
+    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+    const uint32_t a = b & 0x7fffffffu;
+    const uint32_t ef = a >> 23;
+    uint64_t r;
+    if (ef - 1u < 254u) {
+        // normal: re-bias the exponent, widen the fraction
+        r = ((uint64_t)a << 29) + ((uint64_t)896 << 52);
+    } else if (ef == 255u) {
+        // infinity / NaN: all-ones exponent, fraction kept (quiet bit stays)
+        r = 0x7ff0000000000000ull | ((uint64_t)(a & 0x7fffffu) << 29);
+    } else if (a == 0u) {
+        r = 0;
+    } else {
+        // subnormal float: value = m * 2^-149 with m < 2^23; normalise so the
+        // leading one (bit p) becomes the implicit bit of a normal double
+        const int p = 31 - __clz((int)a);
+        r = ((uint64_t)(p + 874) << 52) | (((uint64_t)a << (52 - p)) & 0x000fffffffffffffull);
+    }
+    return __longlong_as_double((long long)(sign | r));
+}
+
+__device__ __forceinline__ float d2f(double x) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const uint64_t a = b & 0x7fffffffffffffffull;
+    const uint32_t ed = (uint32_t)(a >> 52);
+    uint32_t r;
+    if (ed - 897u < 254u) {
+        // normal float range: drop 29 fraction bits, round to nearest even;
+        // a carry out of the fraction bumps the exponent (to infinity past
+        // the largest float), as IEEE rounding requires
+        const uint64_t t = a - ((uint64_t)896 << 52);
+        const uint32_t q = (uint32_t)(t >> 29);
+        const uint32_t rem = (uint32_t)t & 0x1fffffffu;
+        r = q + ((rem > 0x10000000u) | ((rem == 0x10000000u) & (q & 1u)));
+    } else if (ed >= 1151u) {
+        // overflow -> infinity; NaN stays NaN (quiet, payload top bits kept)
+        r = a > 0x7ff0000000000000ull ? (0x7fc00000u | (uint32_t)((a >> 29) & 0x3fffffu)) : 0x7f800000u;
+    } else if (ed < 871u) {
+        // below half the smallest float subnormal (2^-150): rounds to zero
+        r = 0;
+    } else {
+        // float subnormal result: m = round(x * 2^149); with the implicit bit,
+        // x * 2^149 = full * 2^(ed - 926), a right shift by s = 926 - ed
+        // (30 <= s <= 55).  m may round up to 2^23 = the smallest normal.
+        const uint64_t full = (a & 0x000fffffffffffffull) | 0x0010000000000000ull;
+        const int s = 926 - (int)ed;
+        const uint64_t q = full >> s;
+        const uint64_t rem = full & ((1ull << s) - 1ull);
+        const uint64_t half = 1ull << (s - 1);
+        r = (uint32_t)(q + ((rem > half) | ((rem == half) & (q & 1ull))));
+    }
+    return __uint_as_float(sign | r);
+}
+
+}  // namespace fvconv

@@ -31,6 +31,7 @@ __device__ __forceinline__ St& operator+=(St& a, const St& b) { a.r += b.r; a.ru
 // std::max / std::min semantics ((a < b) ? b : a and (b < a) ? b : a), so
 // signed zeros and NaNs propagate exactly as in the reference.
 __device__ __forceinline__ double rmax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float rmax(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ double rmin(double a, double b) { return (b < a) ? b : a; }
 
 __device__ __forceinline__ St ld_state(const St* __restrict__ U, int i) {

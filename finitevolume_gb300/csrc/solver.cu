@@ -39,6 +39,12 @@ static T* dalloc(size_t n, std::vector<void*>& owned) {
     return static_cast<T*>(p);
 }
 
+static std::vector<float> to_float(const std::vector<double>& v) {
+    std::vector<float> o(v.size());
+    for (size_t i = 0; i < v.size(); ++i) o[i] = (float)v[i];
+    return o;
+}
+
 template <typename T>
 static T* dupload(const std::vector<T>& v, std::vector<void*>& owned) {
     T* p = dalloc<T>(v.size(), owned);
@@ -166,17 +172,35 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         W = dalloc<char>(wsz * (size_t)N, owned);
         G = dalloc<char>(2 * wsz * (size_t)N, owned);
         if (cfg.fp32) ff = reinterpret_cast<St*>(dalloc<char>(16 * (size_t)F, owned));
-        cs = dalloc<double>(N, owned);
+        cs = dalloc<char>(wsz / 4 * (size_t)N, owned);
         dtv = dalloc<double>(N, owned);
         cnb = dupload(h2.d_cnb, owned);
-        if (cfg.gradient == 0) {
-            lsq = reinterpret_cast<const double2*>(dupload(h2.d_lsq, owned));
-            lsq_sum = reinterpret_cast<const double2*>(dupload(h2.d_lsq_sum, owned));
+        // Venkatakrishnan eps^2 = (K h)^3 per cell, formed as the kernels
+        // formed it before (K h in FP64, rounded to the flux precision,
+        // cubed in that precision).
+        std::vector<double> e64(N);
+        std::vector<float> e32(N);
+        for (int c = 0; c < N; ++c) {
+            const double kh = opt.venkat_k * h2.d_h[c];
+            const float khf = (float)kh;
+            e64[c] = kh * kh * kh;
+            e32[c] = khf * khf * khf;
         }
-        else gg = reinterpret_cast<const double4_32a*>(dupload(h2.d_gg, owned));
-        erf = reinterpret_cast<const double2*>(dupload(h2.d_erf, owned));
-        frf = reinterpret_cast<const double4_32a*>(dupload(h2.d_frf, owned));
-        hcell = dupload(h2.d_h, owned);
+        // The per-entry / per-face reconstruction geometry is stored in the
+        // flux precision: FP32-flux mode then converts nothing per use.
+        auto up = [&](const std::vector<double>& v) -> const void* {
+            return cfg.fp32 ? static_cast<const void*>(dupload(to_float(v), owned))
+                            : static_cast<const void*>(dupload(v, owned));
+        };
+        if (cfg.gradient == 0) {
+            lsq = up(h2.d_lsq);
+            lsq_sum = up(h2.d_lsq_sum);
+        }
+        else gg = up(h2.d_gg);
+        erf = up(h2.d_erf);
+        frf = up(h2.d_frf);
+        eps2 = cfg.fp32 ? static_cast<const void*>(dupload(e32, owned)) : static_cast<const void*>(dupload(e64, owned));
+        if (cfg.fp32) fgeom32 = reinterpret_cast<const float4*>(dupload(to_float(hm.d_fgeom), owned));
     }
 
     if (batch) {
@@ -298,7 +322,8 @@ O2Args Solver::o2_args() const {
     a.gg = gg;
     a.erf = erf;
     a.frf = frf;
-    a.h = hcell;
+    a.eps2 = eps2;
+    a.fgeom32 = fgeom32;
     a.U = U;
     a.U0 = U0;
     a.W = W;
@@ -314,6 +339,9 @@ O2Args Solver::o2_args() const {
     a.bc = bc;
     a.gamma = gamma;
     a.venkat_k = opt.venkat_k;
+    a.igm1 = 1.0 / (gamma - 1.0);
+    a.gamma32 = (float)gamma;
+    a.igm1_32 = (float)a.igm1;
     a.exact_tol = opt.exact_tol;
     a.exact_max_iter = opt.exact_max_iter;
     a.cell_inst = cell_inst;
@@ -849,6 +877,17 @@ int fv_batch_status(fv_solver_t s, int32_t* active, int32_t* iterations, double*
         if (active) FV_CUDA(cudaMemcpy(active, v.active, sizeof(int) * v.n_inst, cudaMemcpyDeviceToHost));
         if (iterations) FV_CUDA(cudaMemcpy(iterations, v.inst_iter, sizeof(int) * v.n_inst, cudaMemcpyDeviceToHost));
         if (norms) FV_CUDA(cudaMemcpy(norms, v.inst_norms, sizeof(double) * 4 * v.n_inst, cudaMemcpyDeviceToHost));
+    });
+}
+
+int fv_batch_set_active(fv_solver_t s, int32_t instance, int32_t active) {
+    return guarded([&] {
+        if (!s || !s->s.batch || instance < 0 || instance >= s->s.n_inst || (active != 0 && active != 1))
+            fvgb::raise(FV_ERR_BAD_ARG, "bad argument");
+        fvgb::Solver& v = s->s;
+        const int a = active;
+        FV_CUDA(cudaMemcpyAsync(v.active + instance, &a, sizeof(int), cudaMemcpyHostToDevice, v.stream));
+        FV_CUDA(cudaStreamSynchronize(v.stream));
     });
 }
 

@@ -65,15 +65,17 @@ struct Solver {
     St* U0 = nullptr;
     void* W = nullptr;
     void* G = nullptr;
-    double* cs = nullptr;
+    void* cs = nullptr;             // sound speed, flux precision
     double* dtv = nullptr;
     const int* cnb = nullptr;
-    const double2* lsq = nullptr;
-    const double2* lsq_sum = nullptr;
-    const double4_32a* gg = nullptr;
-    const double2* erf = nullptr;
-    const double4_32a* frf = nullptr;
-    const double* hcell = nullptr;
+    // reconstruction geometry in flux precision (see O2Args)
+    const void* lsq = nullptr;
+    const void* lsq_sum = nullptr;
+    const void* gg = nullptr;
+    const void* erf = nullptr;
+    const void* frf = nullptr;
+    const void* eps2 = nullptr;
+    const float4* fgeom32 = nullptr;
 
     cudaStream_t stream = nullptr;
     bool own_stream = false;

@@ -69,18 +69,20 @@ struct O1Args {
 struct O2Args {
     DevMesh m;
     const int* cnb;          // per entry: neighbour or -1-face
-    const double2* lsq;      // per entry LSQ weights
-    const double2* lsq_sum;  // per cell sums of the LSQ weights
-    const double4_32a* gg;   // per entry Green-Gauss coefficients
-    const double2* erf;      // per entry face offset
-    const double4_32a* frf;  // per face offsets from the owner / neighbour centroid
-    const double* h;         // per cell sqrt(volume)
+    // Reconstruction geometry in flux precision T (double or float arrays):
+    const void* lsq;         // per entry LSQ weights (2 T)
+    const void* lsq_sum;     // per cell sums of the LSQ weights (2 T)
+    const void* gg;          // per entry Green-Gauss coefficients (4 T; double: double4_32a)
+    const void* erf;         // per entry face offset (2 T)
+    const void* frf;         // per face offsets from the owner / neighbour centroid (4 T)
+    const void* eps2;        // per cell Venkatakrishnan (K h)^3, h = sqrt(volume) (T)
+    const float4* fgeom32;   // FP32 mode: per face nx, ny, area, CFL length
     St* U;
     St* U0;
     void* W;                 // primitive copy: St (FP64) or float4 (FP32 flux)
     void* G;                 // limited gradients: 4 double2 or 2 float4 per cell
     void* ff;                // face fluxes: St or float4
-    double* cs;              // per cell sound speed (cell-centred, for dt)
+    void* cs;                // per cell sound speed (cell-centred, for dt; T)
     double* dtf;             // per face lambda * length (local dt)
     double* dtv;             // per cell dt/volume of the current iteration
     StepCtl* ctl;
@@ -89,6 +91,8 @@ struct O2Args {
     int hist_cap;
     BCTable bc;
     double gamma, venkat_k, exact_tol;
+    double igm1;             // 1 / (gamma - 1)
+    float gamma32, igm1_32;  // the same constants rounded to float
     int exact_max_iter;
     // Batched solves (all null otherwise): instance of each cell, the
     // instance-active flags, per-instance freestream (4 conserved values),

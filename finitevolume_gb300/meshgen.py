@@ -109,13 +109,18 @@ def _ogrid_nodes(ni: int, nj: int, first: float, r_out: float, center=(0.5, 0.0)
 
 
 def naca_ogrid(ni: int = 256, nj: int = 128, first: float = 1e-3, r_far: float = 20.0,
-               code: str = "0012") -> PolyMesh:
+               code: str = "0012", shape=None) -> PolyMesh:
     """NACA 4-digit O-grid: ``ni`` cells around, ``nj`` radially.
 
-    Patches: ``airfoil`` (the wall) and ``farfield`` (circle of radius
-    ``r_far`` chords about mid-chord).
+    ``shape`` = (max camber, camber position, thickness) as chord fractions
+    overrides the 4-digit ``code`` (non-integer sections).  Patches:
+    ``airfoil`` (the wall) and ``farfield`` (circle of radius ``r_far``
+    chords about mid-chord).
     """
-    m, p, t = int(code[0]) / 100.0, int(code[1]) / 10.0, int(code[2:]) / 100.0
+    if shape is not None:
+        m, p, t = (float(x) for x in shape)
+    else:
+        m, p, t = int(code[0]) / 100.0, int(code[1]) / 10.0, int(code[2:]) / 100.0
     nodes3 = _ogrid_nodes(ni, nj, first, r_far, m=m, p=p, t=t)
     nodes = nodes3.reshape(-1, 2)
     jj, ii = np.meshgrid(np.arange(nj), np.arange(ni), indexing="ij")
@@ -437,3 +442,27 @@ def sod_strip(nx: int, ny: int, length: float = 1.0, height: float = None, jitte
     cells = np.stack([t1, t2], 1).reshape(-1, 3)
     quads = _structured(nodes, nx, ny)
     return from_cells(nodes, cells, quads.bedges, quads.bpatch, quads.patch_names)
+
+
+def batch_cases(n: int = 256, seed: int = 0, cells=(4096, 65536)):
+    """Seeded family of steady airfoil cases for batched solves.
+
+    Per instance: NACA 4-digit section with max camber uniform in [0, 6%]
+    (at 40% chord) and thickness uniform in [8%, 18%]; an O-grid whose cell
+    count is log-uniform in ``cells`` (ni = 2 nj); freestream Mach uniform in
+    [0.3, 0.85] and angle of attack uniform in [-4, 8] degrees.  Returns a
+    list of dicts (ni, nj, shape, mach, aoa_deg).
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    lo, hi = np.log(cells[0]), np.log(cells[1])
+    for _ in range(n):
+        camber = rng.uniform(0.0, 0.06)
+        thick = rng.uniform(0.08, 0.18)
+        nc = float(np.exp(rng.uniform(lo, hi)))
+        nj = max(8, int(round(np.sqrt(nc / 2.0))))
+        mach = rng.uniform(0.3, 0.85)
+        aoa = rng.uniform(-4.0, 8.0)
+        out.append({"ni": 2 * nj, "nj": nj, "shape": (camber, 0.4, thick), "mach": mach, "aoa_deg": aoa})
+    return out
+

@@ -12,15 +12,22 @@ of 2nd-order MUSCL with materialised gradient and limiter arrays):
 and first order, forward Euler, local dt:
     B1 = 76 N + 40 F
 
-Per kernel of this implementation (the limiter is fused into the gradient
-kernel, so no limiter array exists; face fluxes are materialised once):
-    gradients  W r (4s N) + G w (8s N) + CSR offsets 4N + entries 4E
-               + LSQ geometry (24 inverse + 16 centroid) N + face midpoints 16F
-               + h 8N
-    faces      W r (4s N) + G r (8s N) + face normal/length 24F + owner/
-               neighbour 8F + midpoints 16F + centroids 16N + fluxes w (4s F)
+Per kernel of this implementation, at an RK stage without time-step work
+(stages 2 and 3; the limiter is fused into the gradient kernel, so no
+limiter array exists; face fluxes are materialised once):
+    gradients  W r (4s N) + G w (8s N) + CSR offsets 4N + per-entry
+               neighbour 4E + LSQ weights 2s E + face offsets 2s E
+               + weight sums 2s N + Venkatakrishnan eps^2 s N
+               = 15s N + 4N + (4 + 4s) E
+    faces      W r (4s N) + G r (8s N) + normal/length/CFL length 4s F
+               + offsets from both centroids 4s F + owner/neighbour 8F
+               + fluxes w (4s F)
+               = 12s N + (12s + 8) F
     update     fluxes r (4s F) + CSR offsets 4N + entries 4E + U r/w 64N
-               + U0 32N + W w (4s N) + dt/V 8N + volume 8N
+               + U0 r 32N + W w (4s N) + dt/V r 8N
+               = 4s F + 4E + (108 + 4s) N
+Arrays an earlier kernel has just written may still sit in the 129 MB L2,
+so a measured DRAM figure can come in below these counts.
 """
 from __future__ import annotations
 
@@ -39,11 +46,11 @@ def kernel_bytes(kind: str, n: int, f: int, fb: int, fp32: bool = False) -> floa
     s = 4.0 if fp32 else 8.0
     e = 2 * f - fb
     if kind == "gradients":
-        return 4 * s * n + 8 * s * n + 4 * n + 4 * e + 40 * n + 16 * f + 8 * n
+        return 15 * s * n + 4 * n + (4 + 4 * s) * e
     if kind == "faces":
-        return 4 * s * n + 8 * s * n + 24 * f + 8 * f + 16 * f + 16 * n + 4 * s * f
+        return 12 * s * n + (12 * s + 8) * f
     if kind == "update":
-        return 4 * s * f + 4 * n + 4 * e + 64 * n + 32 * n + 4 * s * n + 8 * n + 8 * n
+        return 4 * s * f + 4 * e + (108 + 4 * s) * n
     raise ValueError(kind)
 
 

@@ -432,6 +432,10 @@ class BatchSolver:
         capi.check(capi.lib().fv_step_timed(self._h, int(n), capi.dptr(ms), capi.i32ptr(cnt)))
         return ms, cnt
 
+    def set_active(self, instance: int, active: bool) -> None:
+        """Freeze or resume one instance (caller-side convergence tests)."""
+        capi.check(capi.lib().fv_batch_set_active(self._h, int(instance), int(bool(active))))
+
     def status(self):
         """(active[n], iterations[n], norms[n, 4])."""
         act = np.zeros(self.n, np.int32)

@@ -240,6 +240,10 @@ int fv_batch_set_tolerance(fv_solver_t s, double tol_rho);
 int fv_batch_status(fv_solver_t s, int32_t* active, int32_t* iterations, double* norms);
 /* fv_wall_forces restricted to one instance's wall faces. */
 int fv_batch_wall_forces(fv_solver_t s, int32_t instance, const double ref[7], double out[11]);
+/* Freeze (active = 0) or resume (1) one instance, e.g. once the caller's own
+ * convergence test (a force coefficient) holds.  Takes effect at the next
+ * fv_step. */
+int fv_batch_set_active(fv_solver_t s, int32_t instance, int32_t active);
 
 /* ------------------------------------------------------------------------
  * Scalar diffusion solver (UnstructuredFVMSolver)

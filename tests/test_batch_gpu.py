@@ -73,3 +73,25 @@ def test_batch_early_exit_freezes_converged_instances(gpu):
     assert np.array_equal(b.field(k), frozen)
     for i in others:
         assert not np.array_equal(b.field(i), before[i])
+
+
+def test_batch_set_active_freezes_and_resumes_one_instance(gpu):
+    meshes = _meshes()
+    fss = [_fs(M, a) for _, _, _, M, a in CASES]
+    b = S.BatchSolver(meshes, [S.EulerBoundaryType.Wall, S.EulerBoundaryType.CharacteristicFarfield], fss)
+    b.run(10)
+    b.set_active(1, False)
+    frozen = b.field(1).copy()
+    others = {i: b.field(i).copy() for i in (0, 2)}
+    b.run(10)
+    act, it, _ = b.status()
+    assert not act[1] and it[1] == 10 and it[0] == 20
+    assert np.array_equal(b.field(1), frozen)
+    assert all(not np.array_equal(b.field(i), others[i]) for i in (0, 2))
+    b.set_active(1, True)
+    b.run(5)
+    act, it, _ = b.status()
+    assert act[1] and it[1] == 15
+    with pytest.raises(Exception):
+        b.set_active(7, False)
+

@@ -1,0 +1,27 @@
+"""Integer-pipe float<->double conversions (finitevolume_gb300/csrc/fpconv.cuh).
+
+The FP32-flux kernels widen face fluxes and round the state with these
+routines instead of the hardware conversions (which issue on GB300's scarce
+FP64 pipe).  They must agree with the hardware bit for bit: exhaustively
+for float -> double, and on 2^31 double patterns weighted towards the
+rounding and range boundaries for double -> float.
+"""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.gpu
+def test_integer_conversions_match_hardware(gpu, tmp_path):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = str(tmp_path / "fpconv_check")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-I",
+                    os.path.join(ROOT, "finitevolume_gb300", "csrc"), os.path.join(ROOT, "tests", "cuda", "fpconv_check.cu"),
+                    "-o", exe], check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "f2d_mismatch 0 d2f_mismatch 0" in r.stdout
