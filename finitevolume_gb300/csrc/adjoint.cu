@@ -1,0 +1,989 @@
+// Discrete adjoint of the Euler residual (first and second order, FP64).
+//
+// No reference counterpart: the reference has no adjoint.  The residual
+// being differentiated is the one the solver's own kernels evaluate
+// (euler_o2.cuh: k_grad / k_face / k_update, i.e. EulerFVMSolver::step's
+// face and cell passes, src/EulerFVMSolver.cpp:61-111, extended to MUSCL):
+//
+//   W_c   = prim(U_c)
+//   Gu_c  = sum_e a_e nb_e - s_c W_c        nb_e = W_j, or (W_c + ghost(W_c)) / 2
+//   G_c   = psi_c (.) Gu_c                  psi frozen at the linearisation state
+//   w_f^s = W_s + G_s . r_f^s               (W_s where the positivity test fell back)
+//   F_f   = |f| flux(w_f^L, w_f^R or ghost(w_f^L, fs))
+//   R_c   = sum_f -/+ F_f                   owner subtracts, neighbour adds
+//
+// Linearisation (once per state): per face, the flux Jacobians with
+// respect to both reconstructed states (boundary: with respect to the
+// interior state through the ghost state, and to the primitive
+// freestream) are formed by forward-mode dual numbers running the same
+// templated flux and ghost-state code as the residual kernels; per
+// boundary face also the Jacobians of the gradient's boundary value.
+// Then the tangent (forward, JVP) and cotangent (backward, VJP) maps are
+// sparse products with these matrices, written as face passes followed by
+// cell gathers in the residual's own CSR order: every kernel writes only
+// its own face or cell, there are no atomics, and repeated runs are bit
+// identical.  The scatter of a cell's gradient cotangent to its
+// neighbours is turned into a gather through the "twin" of each CSR entry
+// (the entry of the neighbour's row that points back through the same
+// face).
+//
+// The adjoint equation (dR/dU)^T lambda = dJ/dU is solved by SSP-RK3 in
+// pseudo-time on d lambda / d tau = D ((dR/dU)^T lambda - dJ/dU), D the
+// primal's local dt / V: the linear part D (dR/dU)^T has the spectrum of
+// the linearised primal iteration, so it is stable at the primal's CFL
+// number and converges at the primal's asymptotic rate.
+#define FV_KNS adjk
+#include "euler_o2.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "capi_internal.h"
+
+namespace adjk {
+
+// ---------------------------------------------------------------------------
+// Forward-mode dual numbers (value + N partials)
+// ---------------------------------------------------------------------------
+template <int N>
+struct Dual {
+    double v;
+    double d[N];
+    __device__ Dual() {}
+    __device__ Dual(double x) : v(x) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) d[k] = 0.0;
+    }
+};
+using D4 = Dual<4>;
+
+template <int N> __device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
+    Dual<N> r;
+    r.v = a.v + b.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = a.d[k] + b.d[k];
+    return r;
+}
+template <int N> __device__ __forceinline__ Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
+    Dual<N> r;
+    r.v = a.v - b.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = a.d[k] - b.d[k];
+    return r;
+}
+template <int N> __device__ __forceinline__ Dual<N> operator-(const Dual<N>& a) {
+    Dual<N> r;
+    r.v = -a.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = -a.d[k];
+    return r;
+}
+template <int N> __device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
+    Dual<N> r;
+    r.v = a.v * b.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+}
+template <int N> __device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+    Dual<N> r;
+    r.v = a.v / b.v;
+    const double ib = 1.0 / b.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
+    return r;
+}
+template <int N> __device__ __forceinline__ bool operator<(const Dual<N>& a, const Dual<N>& b) { return a.v < b.v; }
+template <int N> __device__ __forceinline__ bool operator<=(const Dual<N>& a, const Dual<N>& b) { return a.v <= b.v; }
+template <int N> __device__ __forceinline__ bool operator>(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
+template <int N> __device__ __forceinline__ bool operator>=(const Dual<N>& a, const Dual<N>& b) { return a.v >= b.v; }
+template <int N> __device__ __forceinline__ Dual<N> fabs(const Dual<N>& a) { return a.v < 0.0 ? -a : a; }
+template <int N> __device__ __forceinline__ Dual<N> fmin(const Dual<N>& a, const Dual<N>& b) { return b.v < a.v ? b : a; }
+template <int N> __device__ __forceinline__ Dual<N> fmax(const Dual<N>& a, const Dual<N>& b) { return b.v > a.v ? b : a; }
+using ::fabs;
+using ::fmax;
+using ::fmin;
+
+template <> __device__ __forceinline__ D4 tsqrt<D4>(D4 x) {
+    D4 r;
+    r.v = sqrt(x.v);
+    const double h = 0.5 / r.v;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r.d[k] = x.d[k] * h;
+    return r;
+}
+template <> __device__ __forceinline__ D4 trsqrt<D4>(D4 x) {
+    D4 r;
+    r.v = 1.0 / sqrt(x.v);
+    const double h = -0.5 * r.v / x.v;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r.d[k] = x.d[k] * h;
+    return r;
+}
+// a^b; the exponent's partials enter through log(a) only when present.
+template <> __device__ __forceinline__ D4 tpow<D4>(D4 a, D4 b) {
+    D4 r;
+    r.v = pow(a.v, b.v);
+    bool bd = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) bd |= b.d[k] != 0.0;
+    const double la = bd ? log(a.v) : 0.0;
+    const double q = b.v * pow(a.v, b.v - 1.0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r.d[k] = q * a.d[k] + (bd ? r.v * la * b.d[k] : 0.0);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+struct AdjArgs {
+    int n_cells, n_faces, n_int_faces, order, flux;
+    const int* fl;
+    const int* fr;
+    const int* fpatch;
+    const double4_32a* fgeom;
+    const int* cf_off;
+    const int* cf;
+    const int* cnb;
+    const double2* lsq;
+    const double2* lsq_sum;
+    const double4_32a* frf;
+    const int* twin;
+    BCTable bc;
+    double gamma, igm1, cfl;
+    // linearisation state
+    const St* W;         // [N] primitives
+    const double2* Gu;   // [4N] unlimited gradients
+    const double* psi;   // [4N] limiter values
+    double* JL;          // [16F] dF/dw_L (boundary: through the ghost state)
+    double* JR;          // [16F] dF/dw_R (boundary: dF/d fs)
+    double* Gb;          // [32 Fb] 0.5 (I + dghost/dw) | 0.5 dghost/dfs of the gradient's boundary value
+    unsigned char* fb;   // [F] bit 0 owner side fell back to the cell value, bit 1 neighbour side
+    St* F;               // [F] flux times length
+    double* D;           // [N] local dt / V
+    // work arrays
+    double* wbar;        // [8F]
+    St* Wbar;            // [N]
+    double2* Gub;        // [4N]
+    double* fsb;         // [4 Fb]
+    St* dW;              // [N]
+    double2* dG;         // [4N]
+    St* dF;              // [F]
+    const double* dfs;   // [4 * kMaxPatches] primitive freestream tangents
+};
+
+__device__ __forceinline__ V4<double> ldW(const St* W, int i) {
+    const St s = ld_state(W, i);
+    return {s.r, s.ru, s.rv, s.E};
+}
+__device__ __forceinline__ double vget(const V4<double>& w, int k) { return (&w.r)[k]; }
+template <int N> __device__ __forceinline__ Dual<N> dget(const V4<Dual<N>>& w, int k) { return (&w.r)[k]; }
+
+template <typename T>
+__device__ __forceinline__ V4<T> flux_of(int flux, const V4<T>& L, const V4<T>& R, T nx, T ny, T g, T igm1) {
+    return flux == FLUX_HLLC ? hllc_p<T>(L, R, nx, ny, g, igm1) : rusanov_p<T>(L, R, nx, ny, g, igm1);
+}
+
+__device__ __forceinline__ V4<D4> seed(const V4<double>& w) {
+    V4<D4> r = {D4(w.r), D4(w.u), D4(w.v), D4(w.p)};
+    r.r.d[0] = 1.0; r.u.d[1] = 1.0; r.v.d[2] = 1.0; r.p.d[3] = 1.0;
+    return r;
+}
+__device__ __forceinline__ V4<D4> cst(const V4<double>& w) { return {D4(w.r), D4(w.u), D4(w.v), D4(w.p)}; }
+
+__device__ __forceinline__ void store_jac(double* J, const V4<D4>& F, double ar) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) J[4 * i + k] = ar * dget(F, i).d[k];
+}
+
+// Per face: reconstruction (with its positivity decisions), flux value and
+// the flux Jacobians.
+__global__ void k_lin_face(const AdjArgs a) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n_faces) return;
+    const int L = a.fl[f], R = a.fr[f];
+    const double4_32a geo = a.fgeom[f];
+    const double nx = geo.x, ny = geo.y, ar = geo.z;
+    const double g = a.gamma;
+    V4<double> wl = ldW(a.W, L), wr = {0, 0, 0, 0};
+    const V4<double> wlc = wl;
+    unsigned char flags = 0;
+    if (a.order == 2) {
+        const double4_32a rr = a.frf[f];
+        V4<double> o;
+        double* ov = &o.r;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double2 q = a.Gu[4 * L + k];
+            const double p = a.psi[4 * L + k];
+            ov[k] = vget(wl, k) + ((p * q.x) * rr.x + (p * q.y) * rr.y);
+        }
+        if (o.r > 0.0 && o.p > 0.0) wl = o;
+        else flags |= 1;
+        if (R >= 0) {
+            wr = ldW(a.W, R);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const double2 q = a.Gu[4 * R + k];
+                const double p = a.psi[4 * R + k];
+                ov[k] = vget(wr, k) + ((p * q.x) * rr.z + (p * q.y) * rr.w);
+            }
+            if (o.r > 0.0 && o.p > 0.0) wr = o;
+            else flags |= 2;
+        }
+    } else if (R >= 0) {
+        wr = ldW(a.W, R);
+    }
+    a.fb[f] = flags;
+    const D4 gD(g), iD(a.igm1), nxD(nx), nyD(ny);
+    double* JL = a.JL + 16 * (size_t)f;
+    double* JR = a.JR + 16 * (size_t)f;
+    V4<D4> F1;
+    if (R >= 0) {
+        F1 = flux_of<D4>(a.flux, seed(wl), cst(wr), nxD, nyD, gD, iD);
+        store_jac(JL, F1, ar);
+        const V4<D4> F2 = flux_of<D4>(a.flux, cst(wl), seed(wr), nxD, nyD, gD, iD);
+        store_jac(JR, F2, ar);
+    } else {
+        const int patch = a.fpatch[f];
+        const int t = a.bc.type[patch];
+        V4<double> fsp = {0, 0, 0, 0};
+        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+        const D4 wu(t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0), wv(t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0);
+        const V4<D4> wlD = seed(wl);
+        F1 = flux_of<D4>(a.flux, wlD, ghost_core<D4>(t, wlD, nxD, nyD, gD, cst(fsp), wu, wv), nxD, nyD, gD, iD);
+        store_jac(JL, F1, ar);
+        const V4<D4> F2 = flux_of<D4>(a.flux, cst(wl), ghost_core<D4>(t, cst(wl), nxD, nyD, gD, seed(fsp), wu, wv),
+                                      nxD, nyD, gD, iD);
+        store_jac(JR, F2, ar);
+        // the gradient's boundary value (W_c + ghost(W_c)) / 2 at the cell-centred state
+        double* Gb = a.Gb + 32 * (size_t)(f - a.n_int_faces);
+        const V4<D4> gw = ghost_core<D4>(t, seed(wlc), nxD, nyD, gD, cst(fsp), wu, wv);
+        const V4<D4> gf = ghost_core<D4>(t, cst(wlc), nxD, nyD, gD, seed(fsp), wu, wv);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                Gb[4 * i + k] = 0.5 * ((i == k ? 1.0 : 0.0) + dget(gw, i).d[k]);
+                Gb[16 + 4 * i + k] = 0.5 * dget(gf, i).d[k];
+            }
+    }
+    st_state(a.F, f, st_make(ar * F1.r.v, ar * F1.u.v, ar * F1.v.v, ar * F1.p.v));
+}
+
+// Per cell: D = cfl / sum_f lambda_f |f| (the primal's local time step over
+// the volume), from the cell-centred states.
+__global__ void k_lin_dt(const AdjArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    double lam = 0.0;
+    const double g = a.gamma;
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int f = a.cf[e] >> 1;
+        const double4_32a geo = a.fgeom[f];
+        const int L = a.fl[f], R = a.fr[f];
+        const V4<double> wl = ldW(a.W, L);
+        double Smax = fabs(wl.u * geo.x + wl.v * geo.y) + sqrt(g * wl.p / wl.r);
+        if (R >= 0) {
+            const V4<double> wr = ldW(a.W, R);
+            Smax = rmax(Smax, fabs(wr.u * geo.x + wr.v * geo.y) + sqrt(g * wr.p / wr.r));
+        }
+        lam += Smax * geo.z;
+    }
+    a.D[c] = a.cfl / lam;
+}
+
+// dW/dU at primitive state w (row i = dW_i / dU).
+__device__ __forceinline__ void prim_jac(const V4<double>& w, double g, double J[16]) {
+    const double ir = 1.0 / w.r, gm1 = g - 1.0;
+    J[0] = 1.0; J[1] = 0.0; J[2] = 0.0; J[3] = 0.0;
+    J[4] = -w.u * ir; J[5] = ir; J[6] = 0.0; J[7] = 0.0;
+    J[8] = -w.v * ir; J[9] = 0.0; J[10] = ir; J[11] = 0.0;
+    J[12] = 0.5 * gm1 * (w.u * w.u + w.v * w.v); J[13] = -gm1 * w.u; J[14] = -gm1 * w.v; J[15] = gm1;
+}
+
+// ---------------------------------------------------------------------------
+// Residual at the linearisation state: R_c = sum -/+ F_f.
+__global__ void k_res_cell(const AdjArgs a, St* __restrict__ R) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    St r = st_make(0.0, 0.0, 0.0, 0.0);
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int ent = a.cf[e];
+        r += flip_if(ld_state(a.F, ent >> 1), ent);
+    }
+    st_state(R, c, r);
+}
+
+// ---------------------------------------------------------------------------
+// Tangent map dR = (dR/dU) dU + (dR/dfs) dfs
+__global__ void k_fwd_cell1(const AdjArgs a, const St* __restrict__ dU) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    double J[16];
+    prim_jac(ldW(a.W, c), a.gamma, J);
+    const St u = ld_state(dU, c);
+    const double x[4] = {u.r, u.ru, u.rv, u.E};
+    double y[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) y[i] = J[4 * i] * x[0] + J[4 * i + 1] * x[1] + J[4 * i + 2] * x[2] + J[4 * i + 3] * x[3];
+    st_state(a.dW, c, st_make(y[0], y[1], y[2], y[3]));
+}
+
+__global__ void k_fwd_cell2(const AdjArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    const St wc = ld_state(a.dW, c);
+    const double dwc[4] = {wc.r, wc.ru, wc.rv, wc.E};
+    const double2 s = a.lsq_sum[c];
+    double gx[4], gy[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { gx[k] = -s.x * dwc[k]; gy[k] = -s.y * dwc[k]; }
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int nb = a.cnb[e];
+        const double2 w = a.lsq[e];
+        double v[4];
+        if (nb >= 0) {
+            const St q = ld_state(a.dW, nb);
+            v[0] = q.r; v[1] = q.ru; v[2] = q.rv; v[3] = q.E;
+        } else {
+            const int f = -1 - nb;
+            const double* Gb = a.Gb + 32 * (size_t)(f - a.n_int_faces);
+            const double* df = a.dfs + 4 * a.fpatch[f];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                double t = 0.0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) t += Gb[4 * i + k] * dwc[k] + Gb[16 + 4 * i + k] * df[k];
+                v[i] = t;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { gx[k] += w.x * v[k]; gy[k] += w.y * v[k]; }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const double p = a.psi[4 * c + k];
+        a.dG[4 * c + k] = make_double2(p * gx[k], p * gy[k]);
+    }
+}
+
+__global__ void k_fwd_face(const AdjArgs a) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n_faces) return;
+    const int L = a.fl[f], R = a.fr[f];
+    const unsigned char fl = a.fb[f];
+    double dl[4], dr[4];
+    {
+        const St q = ld_state(a.dW, L);
+        dl[0] = q.r; dl[1] = q.ru; dl[2] = q.rv; dl[3] = q.E;
+    }
+    double4_32a rr = {0, 0, 0, 0};
+    if (a.order == 2) rr = a.frf[f];
+    if (a.order == 2 && !(fl & 1))
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double2 q = a.dG[4 * L + k];
+            dl[k] += q.x * rr.x + q.y * rr.y;
+        }
+    if (R >= 0) {
+        const St q = ld_state(a.dW, R);
+        dr[0] = q.r; dr[1] = q.ru; dr[2] = q.rv; dr[3] = q.E;
+        if (a.order == 2 && !(fl & 2))
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const double2 g = a.dG[4 * R + k];
+                dr[k] += g.x * rr.z + g.y * rr.w;
+            }
+    } else {
+        const double* df = a.dfs + 4 * a.fpatch[f];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) dr[k] = df[k];
+    }
+    const double* JL = a.JL + 16 * (size_t)f;
+    const double* JR = a.JR + 16 * (size_t)f;
+    double y[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        double t = 0.0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) t += JL[4 * i + k] * dl[k] + JR[4 * i + k] * dr[k];
+        y[i] = t;
+    }
+    st_state(a.dF, f, st_make(y[0], y[1], y[2], y[3]));
+}
+
+__global__ void k_fwd_cell3(const AdjArgs a, St* __restrict__ dR) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    St r = st_make(0.0, 0.0, 0.0, 0.0);
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int ent = a.cf[e];
+        r += flip_if(ld_state(a.dF, ent >> 1), ent);
+    }
+    st_state(dR, c, r);
+}
+
+// ---------------------------------------------------------------------------
+// Cotangent map: Ubar = (dR/dU)^T lam, fsbar = (dR/dfs)^T lam.
+__global__ void k_bwd_face(const AdjArgs a, const St* __restrict__ lam) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n_faces) return;
+    const int L = a.fl[f], R = a.fr[f];
+    // R_L -= F_f, R_R += F_f
+    const St ll = ld_state(lam, L);
+    double fbar[4] = {-ll.r, -ll.ru, -ll.rv, -ll.E};
+    if (R >= 0) {
+        const St lr = ld_state(lam, R);
+        fbar[0] += lr.r; fbar[1] += lr.ru; fbar[2] += lr.rv; fbar[3] += lr.E;
+    }
+    const double* JL = a.JL + 16 * (size_t)f;
+    const double* JR = a.JR + 16 * (size_t)f;
+    double* wb = a.wbar + 8 * (size_t)f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        double tl = 0.0, tr = 0.0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) { tl += JL[4 * i + k] * fbar[i]; tr += JR[4 * i + k] * fbar[i]; }
+        wb[k] = tl;
+        if (R >= 0) wb[4 + k] = tr;
+        else a.fsb[4 * (size_t)(f - a.n_int_faces) + k] = tr;
+    }
+}
+
+// Gather of the face-state cotangents: W-bar and the gradient cotangent.
+// order 1: finishes Ubar here (MODE 0: write Ubar; 1..3: RK stage 0..2).
+__device__ __forceinline__ void finish_cell(const AdjArgs& a, int c, const double wbar[4], int mode,
+                                            St* __restrict__ out, St* __restrict__ lam, St* __restrict__ lam0,
+                                            const St* __restrict__ rhs, double* __restrict__ r2) {
+    double J[16];
+    prim_jac(ldW(a.W, c), a.gamma, J);
+    double u[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) u[k] = J[k] * wbar[0] + J[4 + k] * wbar[1] + J[8 + k] * wbar[2] + J[12 + k] * wbar[3];
+    if (mode == 0) {
+        st_state(out, c, st_make(u[0], u[1], u[2], u[3]));
+        return;
+    }
+    // pseudo-time residual r = (dR/dU)^T lam - dJ/dU
+    const St g = ld_state(rhs, c);
+    const double r[4] = {u[0] - g.r, u[1] - g.ru, u[2] - g.rv, u[3] - g.E};
+    const double d = a.D[c];
+    const St l = ld_state(lam, c);
+    St e = st_make(l.r + d * r[0], l.ru + d * r[1], l.rv + d * r[2], l.E + d * r[3]);
+    St n;
+    if (mode == 1) {
+        st_state(lam0, c, l);
+        n = e;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) r2[k] = r[k] * r[k];
+    } else if (mode == 2) {
+        n = 0.75 * ld_state(lam0, c) + 0.25 * e;
+    } else {
+        n = (1.0 / 3.0) * ld_state(lam0, c) + (2.0 / 3.0) * e;
+    }
+    st_state(lam, c, n);
+}
+
+__device__ __forceinline__ void block_partials(double r2[4], double* partials) {
+    __shared__ double red[8][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r2[k] = warp_sum(r2[k]);
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 4; ++k) red[threadIdx.x >> 5][k] = r2[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 4; ++k) {
+            double v = 0.0;
+            for (int w = 0; w < 8; ++w) v += red[w][k];
+            partials[4 * blockIdx.x + k] = v;
+        }
+}
+
+__global__ void __launch_bounds__(256) k_bwd_cell1(const AdjArgs a, int mode, St* out, St* lam, St* lam0,
+                                                   const St* rhs, double* partials) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double r2[4] = {0.0, 0.0, 0.0, 0.0};
+    if (c < a.n_cells) {
+        double wb[4] = {0.0, 0.0, 0.0, 0.0}, gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+            const int ent = a.cf[e];
+            const int f = ent >> 1;
+            const bool owner = ent & 1;
+            const double* w = a.wbar + 8 * (size_t)f + (owner ? 0 : 4);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) wb[k] += w[k];
+            if (a.order == 2 && !(a.fb[f] & (owner ? 1 : 2))) {
+                const double4_32a rr = a.frf[f];
+                const double rx = owner ? rr.x : rr.z, ry = owner ? rr.y : rr.w;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) { gx[k] += w[k] * rx; gy[k] += w[k] * ry; }
+            }
+        }
+        if (a.order == 2) {
+            St q = st_make(wb[0], wb[1], wb[2], wb[3]);
+            st_state(a.Wbar, c, q);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const double p = a.psi[4 * c + k];
+                a.Gub[4 * c + k] = make_double2(p * gx[k], p * gy[k]);
+            }
+        } else {
+            finish_cell(a, c, wb, mode, out, lam, lam0, rhs, r2);
+        }
+    }
+    if (a.order == 1 && mode == 1) block_partials(r2, partials);
+}
+
+// Gradient cotangent to W-bar (gather through twin entries), then Ubar.
+__global__ void __launch_bounds__(256) k_bwd_cell2(const AdjArgs a, int mode, St* out, St* lam, St* lam0,
+                                                   const St* rhs, double* partials) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double r2[4] = {0.0, 0.0, 0.0, 0.0};
+    if (c < a.n_cells) {
+        const St w0 = ld_state(a.Wbar, c);
+        double wb[4] = {w0.r, w0.ru, w0.rv, w0.E};
+        double2 gc[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) gc[k] = a.Gub[4 * c + k];
+        const double2 s = a.lsq_sum[c];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) wb[k] -= s.x * gc[k].x + s.y * gc[k].y;
+        for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+            const int nb = a.cnb[e];
+            if (nb >= 0) {
+                const double2 w = a.lsq[a.twin[e]];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const double2 q = a.Gub[4 * nb + k];
+                    wb[k] += w.x * q.x + w.y * q.y;
+                }
+            } else {
+                const int f = -1 - nb;
+                const double2 w = a.lsq[e];
+                double v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) v[k] = w.x * gc[k].x + w.y * gc[k].y;
+                const double* Gb = a.Gb + 32 * (size_t)(f - a.n_int_faces);
+                double* fs = a.fsb + 4 * (size_t)(f - a.n_int_faces);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    double tw = 0.0, tf = 0.0;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) { tw += Gb[4 * i + k] * v[i]; tf += Gb[16 + 4 * i + k] * v[i]; }
+                    wb[k] += tw;
+                    fs[k] += tf;
+                }
+            }
+        }
+        finish_cell(a, c, wb, mode, out, lam, lam0, rhs, r2);
+    }
+    if (mode == 1) block_partials(r2, partials);
+}
+
+// Norm of the stage-0 pseudo-time residual: block partials folded in block
+// order by one block (deterministic); appended to the history.
+__global__ void __launch_bounds__(256) k_adj_norms(const double* partials, int nblk, double* hist, int* counter,
+                                                   int cap) {
+    __shared__ double red[256][4];
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nblk; b += 256)
+        for (int k = 0; k < 4; ++k) t[k] += partials[4 * b + k];
+    for (int k = 0; k < 4; ++k) red[threadIdx.x][k] = t[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int k = 0; k < 4; ++k) red[threadIdx.x][k] += red[threadIdx.x + w][k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int it = *counter;
+        if (it < cap)
+            for (int k = 0; k < 4; ++k) hist[4 * it + k] = sqrt(red[0][k]);
+        *counter = it + 1;
+    }
+}
+
+__global__ void k_perm_gather(const St* __restrict__ in_ref, St* __restrict__ out_dev, const int* __restrict__ perm,
+                              int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out_dev[i] = in_ref[perm[i]];
+}
+__global__ void k_perm_scatter(const St* __restrict__ in_dev, St* __restrict__ out_ref, const int* __restrict__ perm,
+                               int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out_ref[perm[i]] = in_dev[i];
+}
+
+}  // namespace adjk
+
+// ===========================================================================
+// Host object and C ABI
+// ===========================================================================
+using adjk::AdjArgs;
+using fvgb::St;
+
+struct fv_adjoint_s {
+    fv_solver_s* solver = nullptr;
+    AdjArgs a{};
+    int N = 0, F = 0, Fb = 0, P = 0;
+    std::vector<void*> owned;
+    St *U = nullptr, *W = nullptr, *stage_ref = nullptr, *stage_dev = nullptr, *lam = nullptr, *lam0 = nullptr,
+       *rhs = nullptr, *Rdev = nullptr;
+    double2 *Gu = nullptr, *G = nullptr;
+    double *psi = nullptr, *cs = nullptr, *partials = nullptr, *hist = nullptr, *dfs_dev = nullptr;
+    int* counter = nullptr;
+    int hist_cap = 0;
+    bool linearised = false;
+    ~fv_adjoint_s() {
+        for (void* p : owned) cudaFree(p);
+        if (hist) cudaFree(hist);
+    }
+    template <typename T>
+    T* alloc(size_t n) {
+        void* p = nullptr;
+        FV_CUDA(cudaMalloc(&p, sizeof(T) * (n ? n : 1)));
+        owned.push_back(p);
+        return static_cast<T*>(p);
+    }
+};
+
+namespace {
+
+constexpr int kB = 256;
+inline int blocks(int n) { return (n + kB - 1) / kB; }
+
+void check_launch() { FV_CUDA(cudaGetLastError()); }
+
+// device-order buffer <- host array in reference order
+void upload_ref(fv_adjoint_s* A, const double* host, St* dev) {
+    fvgb::Solver& s = A->solver->s;
+    FV_CUDA(cudaMemcpyAsync(A->stage_ref, host, sizeof(St) * (size_t)A->N, cudaMemcpyHostToDevice, s.stream));
+    adjk::k_perm_gather<<<blocks(A->N), kB, 0, s.stream>>>(A->stage_ref, dev, s.d_perm, A->N);
+    check_launch();
+}
+
+void download_ref(fv_adjoint_s* A, const St* dev, double* host) {
+    fvgb::Solver& s = A->solver->s;
+    adjk::k_perm_scatter<<<blocks(A->N), kB, 0, s.stream>>>(dev, A->stage_ref, s.d_perm, A->N);
+    check_launch();
+    FV_CUDA(cudaMemcpyAsync(host, A->stage_ref, sizeof(St) * (size_t)A->N, cudaMemcpyDeviceToHost, s.stream));
+    FV_CUDA(cudaStreamSynchronize(s.stream));
+}
+
+// fsbar per patch, summed over boundary faces in face order
+void reduce_fsbar(fv_adjoint_s* A, double* out) {
+    fvgb::Solver& s = A->solver->s;
+    std::vector<double> fb(4 * (size_t)A->Fb);
+    std::vector<int> patch(A->Fb);
+    if (A->Fb) {
+        FV_CUDA(cudaMemcpyAsync(fb.data(), A->a.fsb, sizeof(double) * fb.size(), cudaMemcpyDeviceToHost, s.stream));
+        FV_CUDA(cudaMemcpyAsync(patch.data(), A->a.fpatch + A->a.n_int_faces, sizeof(int) * A->Fb,
+                                cudaMemcpyDeviceToHost, s.stream));
+    }
+    FV_CUDA(cudaStreamSynchronize(s.stream));
+    for (int i = 0; i < 4 * A->P; ++i) out[i] = 0.0;
+    for (int i = 0; i < A->Fb; ++i)
+        for (int k = 0; k < 4; ++k) out[4 * patch[i] + k] += fb[4 * (size_t)i + k];
+}
+
+void linearise(fv_adjoint_s* A) {
+    fvgb::Solver& s = A->solver->s;
+    AdjArgs& a = A->a;
+    fvgb::StepCtl ctl;
+    s.read_ctl(ctl);
+    a.cfl = ctl.cfl;  // the pseudo-time CFL number is the primal's
+    if (a.order == 2) {
+        fvgb::O2Args o = s.o2_args();
+        o.U = A->U;
+        o.W = A->W;
+        o.G = A->G;
+        o.cs = A->cs;
+        o.lim_gu = A->Gu;
+        o.lim_psi = A->psi;
+        o.active = nullptr;
+        fvgb::o2::launch_prim_f64(o, s.stream);
+        check_launch();
+        fvgb::o2::launch_part_f64(o, s.cfg, 0, 0, s.stream);
+        check_launch();
+    } else {
+        fvgb::O2Args o{};
+        o.m = s.dm;
+        o.U = A->U;
+        o.W = A->W;
+        o.cs = A->cs;
+        o.gamma = s.gamma;
+        fvgb::o2::launch_prim_f64(o, s.stream);
+        check_launch();
+    }
+    adjk::k_lin_face<<<blocks(A->F), kB, 0, s.stream>>>(a);
+    check_launch();
+    adjk::k_lin_dt<<<blocks(A->N), kB, 0, s.stream>>>(a);
+    check_launch();
+    A->linearised = true;
+}
+
+void backward(fv_adjoint_s* A, const St* lam, int mode, St* out) {
+    fvgb::Solver& s = A->solver->s;
+    AdjArgs& a = A->a;
+    if (A->Fb) FV_CUDA(cudaMemsetAsync(a.fsb, 0, sizeof(double) * 4 * (size_t)A->Fb, s.stream));
+    adjk::k_bwd_face<<<blocks(A->F), kB, 0, s.stream>>>(a, lam);
+    check_launch();
+    adjk::k_bwd_cell1<<<blocks(A->N), kB, 0, s.stream>>>(a, mode, out, A->lam, A->lam0, A->rhs, A->partials);
+    check_launch();
+    if (a.order == 2) {
+        adjk::k_bwd_cell2<<<blocks(A->N), kB, 0, s.stream>>>(a, mode, out, A->lam, A->lam0, A->rhs, A->partials);
+        check_launch();
+    }
+    if (mode == 1) {
+        adjk::k_adj_norms<<<1, 256, 0, s.stream>>>(A->partials, blocks(A->N), A->hist, A->counter, A->hist_cap);
+        check_launch();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fv_adjoint_create(fv_solver_t solver, fv_adjoint_t* out) {
+    return fvgb::guarded([&] {
+        if (!solver || !out) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        fvgb::Solver& s = solver->s;
+        if (s.viscous || s.batch) fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: Euler solvers only (not NS, not batched)");
+        if (s.opt.precision != FV_PREC_FP64) fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: FP64 solvers only");
+        if (s.opt.flux != FV_FLUX_RUSANOV && s.opt.flux != FV_FLUX_HLLC)
+            fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: Rusanov or HLLC flux");
+        const int order = s.opt.order;
+        if (order == 2 && (!s.general || s.opt.gradient != FV_GRAD_LSQ))
+            fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: second order needs least-squares gradients");
+        auto A = std::make_unique<fv_adjoint_s>();
+        A->solver = solver;
+        A->N = s.N;
+        A->F = s.F;
+        A->Fb = s.F - s.dm.n_int_faces;
+        A->P = s.bc.n;
+        AdjArgs& a = A->a;
+        a.n_cells = s.N;
+        a.n_faces = s.F;
+        a.n_int_faces = s.dm.n_int_faces;
+        a.order = order;
+        a.flux = s.opt.flux;
+        a.fl = s.dm.fl;
+        a.fr = s.dm.fr;
+        a.fpatch = s.dm.fpatch;
+        a.fgeom = s.dm.fgeom;
+        a.cf_off = s.dm.cf_off;
+        a.cf = s.dm.cf;
+        a.bc = s.bc;
+        a.gamma = s.gamma;
+        a.igm1 = 1.0 / (s.gamma - 1.0);
+        const size_t N = s.N, F = s.F, Fb = A->Fb;
+        A->U = A->alloc<St>(N);
+        A->W = A->alloc<St>(N);
+        A->cs = A->alloc<double>(N);
+        A->stage_ref = A->alloc<St>(N);
+        A->stage_dev = A->alloc<St>(N);
+        A->lam = A->alloc<St>(N);
+        A->lam0 = A->alloc<St>(N);
+        A->rhs = A->alloc<St>(N);
+        A->Rdev = A->alloc<St>(N);
+        A->Gu = A->alloc<double2>(4 * N);
+        A->G = A->alloc<double2>(4 * N);
+        A->psi = A->alloc<double>(4 * N);
+        A->partials = A->alloc<double>(4 * (size_t)blocks(s.N));
+        A->counter = A->alloc<int>(1);
+        A->dfs_dev = A->alloc<double>(4 * fvgb::kMaxPatches);
+        a.W = A->W;
+        a.Gu = A->Gu;
+        a.psi = A->psi;
+        a.JL = A->alloc<double>(16 * F);
+        a.JR = A->alloc<double>(16 * F);
+        a.Gb = A->alloc<double>(32 * Fb);
+        a.fb = A->alloc<unsigned char>(F);
+        a.F = A->alloc<St>(F);
+        a.D = A->alloc<double>(N);
+        a.wbar = A->alloc<double>(8 * F);
+        a.Wbar = A->alloc<St>(N);
+        a.Gub = A->alloc<double2>(4 * N);
+        a.fsb = A->alloc<double>(4 * Fb);
+        a.dW = A->alloc<St>(N);
+        a.dG = A->alloc<double2>(4 * N);
+        a.dF = A->alloc<St>(F);
+        a.dfs = A->dfs_dev;
+        if (order == 2) {
+            a.cnb = s.cnb;
+            a.lsq = static_cast<const double2*>(s.lsq);
+            a.lsq_sum = static_cast<const double2*>(s.lsq_sum);
+            a.frf = static_cast<const double4_32a*>(s.frf);
+            // twin entries: the entry of the neighbour's row through the same face
+            const size_t E = (size_t)(2 * s.F - A->Fb);
+            std::vector<int> off(N + 1), cf(E), cnb(E), twin(E, -1);
+            FV_CUDA(cudaMemcpy(off.data(), s.dm.cf_off, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost));
+            FV_CUDA(cudaMemcpy(cf.data(), s.dm.cf, sizeof(int) * E, cudaMemcpyDeviceToHost));
+            FV_CUDA(cudaMemcpy(cnb.data(), s.cnb, sizeof(int) * E, cudaMemcpyDeviceToHost));
+            for (size_t c = 0; c < N; ++c)
+                for (int e = off[c]; e < off[c + 1]; ++e) {
+                    const int f = cf[e] >> 1, nb = cnb[e];
+                    if (nb < 0) {
+                        if (-1 - nb != f) fvgb::raise(FV_ERR_BAD_MESH, "adjoint: CSR and neighbour lists disagree");
+                        continue;
+                    }
+                    for (int e2 = off[nb]; e2 < off[nb + 1]; ++e2)
+                        if ((cf[e2] >> 1) == f) { twin[e] = e2; break; }
+                    if (twin[e] < 0) fvgb::raise(FV_ERR_BAD_MESH, "adjoint: face without a twin entry");
+                }
+            int* d_twin = A->alloc<int>(E);
+            FV_CUDA(cudaMemcpy(d_twin, twin.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
+            a.twin = d_twin;
+        }
+        *out = A.release();
+    });
+}
+
+int fv_adjoint_destroy(fv_adjoint_t adj) {
+    return fvgb::guarded([&] { delete adj; });
+}
+
+int fv_residual_forward(fv_adjoint_t A, const double* U, double* R) {
+    return fvgb::guarded([&] {
+        if (!A) fvgb::raise(FV_ERR_BAD_ARG, "null adjoint");
+        fvgb::Solver& s = A->solver->s;
+        FV_CUDA(cudaStreamSynchronize(s.stream));
+        if (U) upload_ref(A, U, A->U);
+        else FV_CUDA(cudaMemcpyAsync(A->U, s.U, sizeof(St) * (size_t)A->N, cudaMemcpyDeviceToDevice, s.stream));
+        linearise(A);
+        if (R) {
+            adjk::k_res_cell<<<blocks(A->N), kB, 0, s.stream>>>(A->a, A->Rdev);
+            check_launch();
+            download_ref(A, A->Rdev, R);
+        }
+        FV_CUDA(cudaStreamSynchronize(s.stream));
+    });
+}
+
+int fv_residual_jvp(fv_adjoint_t A, const double* dU, const double* dfs, double* dR) {
+    return fvgb::guarded([&] {
+        if (!A || !dU || !dR) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (!A->linearised) fvgb::raise(FV_ERR_BAD_ARG, "call fv_residual_forward first");
+        fvgb::Solver& s = A->solver->s;
+        std::vector<double> d(4 * fvgb::kMaxPatches, 0.0);
+        if (dfs)
+            for (int i = 0; i < 4 * A->P; ++i) d[i] = dfs[i];
+        FV_CUDA(cudaMemcpyAsync(A->dfs_dev, d.data(), sizeof(double) * d.size(), cudaMemcpyHostToDevice, s.stream));
+        upload_ref(A, dU, A->stage_dev);
+        adjk::k_fwd_cell1<<<blocks(A->N), kB, 0, s.stream>>>(A->a, A->stage_dev);
+        check_launch();
+        if (A->a.order == 2) {
+            adjk::k_fwd_cell2<<<blocks(A->N), kB, 0, s.stream>>>(A->a);
+            check_launch();
+        }
+        adjk::k_fwd_face<<<blocks(A->F), kB, 0, s.stream>>>(A->a);
+        check_launch();
+        adjk::k_fwd_cell3<<<blocks(A->N), kB, 0, s.stream>>>(A->a, A->Rdev);
+        check_launch();
+        download_ref(A, A->Rdev, dR);
+    });
+}
+
+int fv_residual_backward(fv_adjoint_t A, const double* Rbar, double* Ubar, double* fsbar) {
+    return fvgb::guarded([&] {
+        if (!A || !Rbar || !Ubar) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (!A->linearised) fvgb::raise(FV_ERR_BAD_ARG, "call fv_residual_forward first");
+        upload_ref(A, Rbar, A->stage_dev);
+        backward(A, A->stage_dev, 0, A->Rdev);
+        download_ref(A, A->Rdev, Ubar);
+        if (fsbar) reduce_fsbar(A, fsbar);
+    });
+}
+
+int fv_adjoint_solve(fv_adjoint_t A, const double* dJdU, int32_t max_iter, double tol, double* lambda,
+                     double* fsbar, double* history, int32_t* iterations) {
+    return fvgb::guarded([&] {
+        if (!A || !dJdU || max_iter < 0) fvgb::raise(FV_ERR_BAD_ARG, "bad argument");
+        if (!A->linearised) fvgb::raise(FV_ERR_BAD_ARG, "call fv_residual_forward first");
+        fvgb::Solver& s = A->solver->s;
+        if (A->hist_cap < max_iter) {
+            if (A->hist) cudaFree(A->hist);
+            A->hist = nullptr;
+            FV_CUDA(cudaMalloc(&A->hist, sizeof(double) * 4 * (size_t)std::max(max_iter, 1)));
+            A->hist_cap = max_iter;
+        }
+        upload_ref(A, dJdU, A->rhs);
+        FV_CUDA(cudaMemsetAsync(A->lam, 0, sizeof(St) * (size_t)A->N, s.stream));
+        FV_CUDA(cudaMemsetAsync(A->counter, 0, sizeof(int), s.stream));
+        // SSP-RK3 in pseudo-time; the stage-0 residual norm is checked every chunk
+        const int chunk = 50;
+        int done = 0;
+        std::vector<double> last(4);
+        while (done < max_iter) {
+            const int n = std::min(chunk, max_iter - done);
+            for (int i = 0; i < n; ++i)
+                for (int st = 1; st <= 3; ++st) backward(A, A->lam, st, nullptr);
+            done += n;
+            FV_CUDA(cudaMemcpyAsync(last.data(), A->hist + 4 * (size_t)(done - 1), sizeof(double) * 4,
+                                    cudaMemcpyDeviceToHost, s.stream));
+            FV_CUDA(cudaStreamSynchronize(s.stream));
+            if (!std::isfinite(last[0])) fvgb::raise(FV_ERR_NONFINITE, "adjoint iteration diverged");
+            if (tol > 0 && last[0] < tol && last[1] < tol && last[2] < tol && last[3] < tol) break;
+        }
+        if (iterations) *iterations = done;
+        if (history && done)
+            FV_CUDA(cudaMemcpy(history, A->hist, sizeof(double) * 4 * (size_t)done, cudaMemcpyDeviceToHost));
+        if (lambda) download_ref(A, A->lam, lambda);
+        if (fsbar) {
+            // lam^T dR/dfs at the converged lam
+            backward(A, A->lam, 0, A->Rdev);
+            reduce_fsbar(A, fsbar);
+        }
+        FV_CUDA(cudaStreamSynchronize(s.stream));
+    });
+}
+
+// dJ/dU of a wall-force coefficient (pressure part, owner-cell pressure as
+// in compute_wall_forces, src/WallTraction.cpp:163-217) at the solver's
+// current state, in reference cell order; returns J.
+int fv_force_gradient(fv_solver_t solver, int32_t objective, const double ref[7], double* value, double* dJdU) {
+    return fvgb::guarded([&] {
+        if (!solver || !ref) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (objective < 0 || objective > 2) fvgb::raise(FV_ERR_BAD_ARG, "objective: 0 drag, 1 lift, 2 moment");
+        fvgb::Solver& s = solver->s;
+        if (s.viscous) fvgb::raise(FV_ERR_UNSUPPORTED, "force gradient: Euler solvers only");
+        std::vector<double> f(4 * (size_t)s.N);
+        s.download_field(f.data());
+        const double vmag = std::hypot(ref[1], ref[2]);
+        const double dx = ref[1] / vmag, dy = ref[2] / vmag, lx = -dy, ly = dx;
+        const double qL = 0.5 * ref[0] * vmag * vmag * ref[4];
+        const double g = s.gamma;
+        if (dJdU) std::memset(dJdU, 0, sizeof(double) * 4 * (size_t)s.N);
+        double J = 0.0;
+        for (const fvgb::WallFace& w : s.wall_faces) {
+            const double* u = f.data() + 4 * (size_t)w.cell;
+            const double uu = u[1] / u[0], vv = u[2] / u[0];
+            const double p = (g - 1.0) * (u[3] - 0.5 * u[0] * (uu * uu + vv * vv));
+            double kx, ky;
+            if (objective == 0) { kx = dx; ky = dy; }
+            else if (objective == 1) { kx = lx; ky = ly; }
+            else {
+                // moment about (ref[5], ref[6]) of the force A p n, over qL * L
+                const double rx = w.xm - ref[5], ry = w.ym - ref[6];
+                kx = -ry / ref[4];
+                ky = rx / ref[4];
+            }
+            const double c = w.area * (w.nx * kx + w.ny * ky) / qL;
+            J += c * p;
+            if (dJdU) {
+                double* d = dJdU + 4 * (size_t)w.cell;
+                d[0] += c * (g - 1.0) * 0.5 * (uu * uu + vv * vv);
+                d[1] += c * (g - 1.0) * (-uu);
+                d[2] += c * (g - 1.0) * (-vv);
+                d[3] += c * (g - 1.0);
+            }
+        }
+        if (value) *value = J;
+    });
+}
+
+}  // extern "C"

@@ -204,20 +204,25 @@ __device__ __forceinline__ V4<T> prim_of(const St& s, T g) {
     return {r, u, v, p};
 }
 
-// Ghost state in primitive form (EulerFVMSolver::ghost_state,
-// src/EulerFVMSolver.cpp:174-193, plus the characteristic farfield).
-// fs, when given, replaces the patch's freestream state (batched solves:
-// one freestream per instance).
+// Primitive freestream of a farfield patch from its conserved state.
 template <typename T>
-__device__ __forceinline__ V4<T> ghost_prim(const BCTable& bc, int patch, const V4<T>& w, T nx, T ny, T g,
-                                            const double* fs = nullptr) {
-    int t = bc.type[patch];
+__device__ __forceinline__ V4<T> fs_prim(const double* st, T g) {
+    T rf = (T)st[0];
+    T uf = (T)(st[1] / st[0]), vf = (T)(st[2] / st[0]);
+    T pf = (T)((g - 1.0) * (st[3] - 0.5 * st[0] * ((st[1] / st[0]) * (st[1] / st[0]) + (st[2] / st[0]) * (st[2] / st[0]))));
+    return {rf, uf, vf, pf};
+}
+
+// Ghost state in primitive form from the patch kind, the interior state w,
+// the primitive freestream fsp (farfield kinds) and the wall velocity
+// (no-slip).  Shared by the residual kernels and, on dual numbers, by the
+// discrete adjoint's linearisation.
+template <typename T>
+__device__ __forceinline__ V4<T> ghost_core(int t, const V4<T>& w, T nx, T ny, T g, const V4<T>& fsp, T wall_u,
+                                            T wall_v) {
     if (t == BC_OUTFLOW) return w;
     if (t == BC_FARFIELD || t == BC_CHAR) {
-        const double* st = fs ? fs : bc.st[patch];
-        T rf = (T)st[0];
-        T uf = (T)(st[1] / st[0]), vf = (T)(st[2] / st[0]);
-        T pf = (T)((g - 1.0) * (st[3] - 0.5 * st[0] * ((st[1] / st[0]) * (st[1] / st[0]) + (st[2] / st[0]) * (st[2] / st[0]))));
+        const T rf = fsp.r, uf = fsp.u, vf = fsp.v, pf = fsp.p;
         if (t == BC_FARFIELD) return {rf, uf, vf, pf};
         T ci = tsqrt<T>(g * w.p / w.r), cf = tsqrt<T>(g * pf / rf);
         T vni = w.u * nx + w.v * ny, vnf = uf * nx + vf * ny;
@@ -234,9 +239,24 @@ __device__ __forceinline__ V4<T> ghost_prim(const BCTable& bc, int patch, const 
         T pb = rb * cb * cb / g;
         return {rb, ut + vnb * nx, vt + vnb * ny, pb};
     }
-    if (t == BC_NOSLIP) return {w.r, T(2) * (T)bc.wall_u[patch] - w.u, T(2) * (T)bc.wall_v[patch] - w.v, w.p};
+    if (t == BC_NOSLIP) return {w.r, T(2) * wall_u - w.u, T(2) * wall_v - w.v, w.p};
     T Vn = w.u * nx + w.v * ny;
     return {w.r, w.u - T(2) * Vn * nx, w.v - T(2) * Vn * ny, w.p};
+}
+
+// Ghost state in primitive form (EulerFVMSolver::ghost_state,
+// src/EulerFVMSolver.cpp:174-193, plus the characteristic farfield).
+// fs, when given, replaces the patch's freestream state (batched solves:
+// one freestream per instance).
+template <typename T>
+__device__ __forceinline__ V4<T> ghost_prim(const BCTable& bc, int patch, const V4<T>& w, T nx, T ny, T g,
+                                            const double* fs = nullptr) {
+    const int t = bc.type[patch];
+    V4<T> fsp = {T(0), T(0), T(0), T(0)};
+    if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<T>(fs ? fs : bc.st[patch], g);
+    T wu = T(0), wv = T(0);
+    if (t == BC_NOSLIP) { wu = (T)bc.wall_u[patch]; wv = (T)bc.wall_v[patch]; }
+    return ghost_core<T>(t, w, nx, ny, g, fsp, wu, wv);
 }
 
 using fvgb::O2Args;
@@ -357,6 +377,14 @@ __global__ void __launch_bounds__(fvgb::kCellBlock, sizeof(T) == 4 ? 4 : 2) k_gr
             dmin[k] = OK::val(kmin[k]) - wcv[k];
         }
     }
+    if constexpr (sizeof(T) == 8) {
+        if (a.lim_gu) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) a.lim_gu[4 * c + k] = make_double2(gx[k], gy[k]);
+            if (LIM == 0)
+                for (int k = 0; k < 4; ++k) a.lim_psi[4 * c + k] = 1.0;
+        }
+    }
     if (LIM != 0) {
         const T eps2 = LIM == 2 ? ld_one<T>(a.eps2, c) : T(0);
         // Per face f the limiter value is psi_f = phi(D1, D2_f) with D2_f the
@@ -404,6 +432,9 @@ __global__ void __launch_bounds__(fvgb::kCellBlock, sizeof(T) == 4 ? 4 : 2) k_gr
                 if (num * dmn < nmin * den) { nmin = num; dmn = den; }
             }
             const T psi = nmin / dmn;
+            if constexpr (sizeof(T) == 8) {
+                if (a.lim_psi) a.lim_psi[4 * c + k] = psi;
+            }
             gx[k] *= psi;
             gy[k] *= psi;
         }

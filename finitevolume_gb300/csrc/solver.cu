@@ -18,6 +18,7 @@
 #include "mesh_host.h"
 #include "solver.h"
 #include "types.h"
+#include "capi_internal.h"
 
 using fvgb::HostMesh;
 
@@ -348,6 +349,8 @@ O2Args Solver::o2_args() const {
     a.active = active;
     a.inst_fs = inst_fs;
     a.r2 = r2;
+    a.lim_gu = nullptr;
+    a.lim_psi = nullptr;
     return a;
 }
 
@@ -579,30 +582,7 @@ void Solver::wall_forces(const double ref[7], double out[11], int instance) {
 // C ABI
 // ===========================================================================
 using fvgb::Solver;
-
-struct fv_solver_s {
-    Solver s;
-};
-
-template <typename Fn>
-static int guarded(Fn&& fn) {
-    try {
-        fn();
-        return FV_OK;
-    } catch (const fvgb::Error& e) {
-        fvgb::set_last_error(e.msg);
-        return e.code;
-    } catch (const fvgb::MeshError& e) {
-        fvgb::set_last_error(e.msg);
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        fvgb::set_last_error("host allocation failed");
-        return FV_ERR_BAD_ARG;
-    } catch (const std::exception& e) {
-        fvgb::set_last_error(e.what());
-        return FV_ERR_BAD_ARG;
-    }
-}
+using fvgb::guarded;
 
 extern "C" {
 

@@ -101,6 +101,11 @@ struct O2Args {
     const int* active;
     const double* inst_fs;
     double4_32a* r2;
+    // Discrete-adjoint linearisation (FP64 only; null otherwise): the
+    // unlimited gradients (4 double2 per cell) and the limiter values
+    // (4 per cell) of k_grad.
+    double2* lim_gu;
+    double* lim_psi;
 };
 
 // Second-order path configuration (validated by the solver).

@@ -298,6 +298,115 @@ class BoundaryType(enum.IntEnum):
     Neumann = 1
 
 
+_MAX_PATCHES = 32  # boundary-condition table size of the C ABI
+
+
+class Objective(enum.IntEnum):
+    """Wall-force coefficients the adjoint differentiates."""
+    Drag = 0
+    Lift = 1
+    Moment = 2
+
+
+def force_gradient(solver: "EulerFVMSolver", objective: Objective, ref) -> tuple:
+    """(J, dJ/dU [N, 4]) of a pressure force coefficient at the solver's state."""
+    r = np.ascontiguousarray(ref, dtype=np.float64)
+    val = C.c_double()
+    g = np.zeros((solver.n_cells, 4))
+    capi.check(capi.lib().fv_force_gradient(solver._h, int(objective), capi.dptr(r), C.byref(val), capi.dptr(g)))
+    return val.value, g
+
+
+class DiscreteAdjoint:
+    """Forward/backward pair of the Euler residual R(U, fs) and its adjoint.
+
+    ``forward(U)`` linearises at U (default: the solver's state) and returns
+    R(U); ``jvp`` and ``vjp`` are the tangent and cotangent maps at that
+    state (limiter values frozen); ``solve`` returns the adjoint lambda of
+    (dR/dU)^T lambda = dJ/dU and fsbar = (dR/dfs)^T lambda, fs being each
+    patch's primitive freestream (rho, u, v, p).
+    """
+
+    def __init__(self, solver: "EulerFVMSolver"):
+        self.solver = solver
+        self.n = solver.n_cells
+        self.n_patches = len(solver.mesh.patch_names)
+        h = C.c_void_p()
+        capi.check(capi.lib().fv_adjoint_create(solver._h, C.byref(h)))
+        self._h = h
+
+    def forward(self, U=None) -> np.ndarray:
+        R = np.zeros((self.n, 4))
+        u = None if U is None else capi.dptr(np.ascontiguousarray(U, dtype=np.float64))
+        capi.check(capi.lib().fv_residual_forward(self._h, u, capi.dptr(R)))
+        return R
+
+    def jvp(self, dU, dfs=None) -> np.ndarray:
+        dR = np.zeros((self.n, 4))
+        d = None
+        if dfs is not None:
+            pad = np.zeros((_MAX_PATCHES, 4))
+            q = np.asarray(dfs, dtype=np.float64).reshape(-1, 4)
+            pad[:q.shape[0]] = q
+            d = capi.dptr(pad)
+        capi.check(capi.lib().fv_residual_jvp(self._h, capi.dptr(np.ascontiguousarray(dU, dtype=np.float64)), d,
+                                              capi.dptr(dR)))
+        return dR
+
+    def vjp(self, Rbar):
+        Ub = np.zeros((self.n, 4))
+        fb = np.zeros((_MAX_PATCHES, 4))
+        capi.check(capi.lib().fv_residual_backward(self._h, capi.dptr(np.ascontiguousarray(Rbar, dtype=np.float64)),
+                                                   capi.dptr(Ub), capi.dptr(fb)))
+        return Ub, fb[:self.n_patches]
+
+    def solve(self, dJdU, max_iter: int = 20000, tol: float = 1e-12):
+        lam = np.zeros((self.n, 4))
+        fb = np.zeros((_MAX_PATCHES, 4))
+        hist = np.zeros((max(max_iter, 1), 4))
+        it = C.c_int32()
+        capi.check(capi.lib().fv_adjoint_solve(self._h, capi.dptr(np.ascontiguousarray(dJdU, dtype=np.float64)),
+                                               int(max_iter), float(tol), capi.dptr(lam), capi.dptr(fb),
+                                               capi.dptr(hist), C.byref(it)))
+        return lam, fb[:self.n_patches], hist[:it.value], it.value
+
+    def freestream_gradient(self, objective: Objective, mach: float, aoa_deg: float, farfield_patches,
+                            max_iter: int = 20000, tol: float = 1e-12) -> dict:
+        """dJ/dM and dJ/dAoA (per degree) of a force coefficient at a
+        converged state whose farfield patches carry the freestream
+        (1, M cos a, M sin a, 1/gamma) and whose force reference is that
+        freestream (q = M^2 / 2, unit chord)."""
+        a = np.radians(aoa_deg)
+        ref = np.array([1.0, mach * np.cos(a), mach * np.sin(a), 1.0 / self.solver.gas_gamma(), 1.0, 0.25, 0.0])
+        self.forward()
+        J, g = force_gradient(self.solver, objective, ref)
+        lam, fb, hist, it = self.solve(g, max_iter, tol)
+        fsb = fb[list(farfield_patches)].sum(axis=0)
+        dfs_dM = np.array([0.0, np.cos(a), np.sin(a), 0.0])
+        dfs_da = np.array([0.0, -mach * np.sin(a), mach * np.cos(a), 0.0])
+        # explicit dependence through the force reference (direction, q)
+        Jd, _ = force_gradient(self.solver, Objective.Drag, ref)
+        Jl, _ = force_gradient(self.solver, Objective.Lift, ref)
+        if objective == Objective.Drag:
+            eM, ea = -2.0 * J / mach, Jl
+        elif objective == Objective.Lift:
+            eM, ea = -2.0 * J / mach, -Jd
+        else:
+            eM, ea = -2.0 * J / mach, 0.0
+        dM = eM - fsb @ dfs_dM
+        da = (ea - fsb @ dfs_da) * np.pi / 180.0
+        return {"J": J, "dJ_dM": dM, "dJ_dAoA_deg": da, "iterations": it,
+                "adjoint_residual": hist[-1].tolist() if len(hist) else None}
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                capi.lib().fv_adjoint_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
 class UnstructuredFVMSolver:
     """GPU scalar diffusion solver with the reference's constructor and methods
     (include/UnstructuredFVMSolver.h:21-92).

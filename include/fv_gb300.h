@@ -246,6 +246,43 @@ int fv_batch_wall_forces(fv_solver_t s, int32_t instance, const double ref[7], d
 int fv_batch_set_active(fv_solver_t s, int32_t instance, int32_t active);
 
 /* ------------------------------------------------------------------------
+ * Discrete adjoint of the Euler residual (no reference counterpart: the
+ * reference has no adjoint).  The adjoint pair differentiates the residual
+ * R(U, fs) that EulerFVMSolver::step drives to zero (the face and cell
+ * passes of src/EulerFVMSolver.cpp:61-111, with the MUSCL / limiter /
+ * characteristic-farfield extensions of this library), linearised at one
+ * state with the limiter values frozen there.  fs is the primitive
+ * freestream (rho, u, v, p) of each farfield patch.  Arrays are [4 N] AoS
+ * in the caller's (reference) cell order; freestream arrays are
+ * [4 n_patches].  FP64 Euler solvers with the Rusanov or HLLC flux (least-
+ * squares gradients at second order).  The adjoint object borrows the
+ * solver's mesh arrays: destroy it before the solver.
+ * --------------------------------------------------------------------- */
+typedef struct fv_adjoint_s* fv_adjoint_t;
+
+int fv_adjoint_create(fv_solver_t s, fv_adjoint_t* out);
+int fv_adjoint_destroy(fv_adjoint_t a);
+/* Forward: linearise at U (NULL: the solver's current state) and return
+ * R(U) (NULL: not returned). */
+int fv_residual_forward(fv_adjoint_t a, const double* U, double* R);
+/* Tangent: dR = dR/dU dU + dR/dfs dfs (dfs may be NULL). */
+int fv_residual_jvp(fv_adjoint_t a, const double* dU, const double* dfs, double* dR);
+/* Backward: Ubar = (dR/dU)^T Rbar, fsbar = (dR/dfs)^T Rbar (fsbar may be NULL). */
+int fv_residual_backward(fv_adjoint_t a, const double* Rbar, double* Ubar, double* fsbar);
+/* Solve (dR/dU)^T lambda = dJdU by SSP-RK3 pseudo-time iteration at the
+ * primal's local time step, until every component of the residual norm is
+ * below tol or max_iter iterations; returns lambda, fsbar = (dR/dfs)^T
+ * lambda, the norm history [4 * iterations] and the iteration count (each
+ * output may be NULL).  Then dJ/dalpha = dJ/dalpha|explicit - fsbar .
+ * dfs/dalpha. */
+int fv_adjoint_solve(fv_adjoint_t a, const double* dJdU, int32_t max_iter, double tol, double* lambda, double* fsbar,
+                     double* history, int32_t* iterations);
+/* Wall-force coefficient J (objective 0 drag, 1 lift, 2 moment; pressure
+ * part with the owner-cell pressure, ref as fv_wall_forces) at the
+ * solver's current state, and dJ/dU (may be NULL). */
+int fv_force_gradient(fv_solver_t s, int32_t objective, const double ref[7], double* value, double* dJdU);
+
+/* ------------------------------------------------------------------------
  * Scalar diffusion solver (UnstructuredFVMSolver)
  * ------------------------------------------------------------------------ */
 typedef struct fv_diffusion_s* fv_diffusion_t;

@@ -1,0 +1,135 @@
+"""Discrete adjoint of the Euler residual (fv_residual_forward / _jvp /
+_backward / fv_adjoint_solve).
+
+No reference counterpart exists; the checks are the ones an adjoint must
+pass against its own primal:
+  * transposition: <Rbar, J dU + Jf dfs> == <J^T Rbar, dU> + <Jf^T Rbar, dfs>
+    to round-off, for first/second order, Rusanov/HLLC, fixed and
+    characteristic farfields (limiter values frozen);
+  * linearisation: the tangent map against central differences of the
+    residual itself (no limiter, so that freezing it changes nothing);
+  * the gradients of drag and lift with respect to Mach number and angle
+    of attack from one adjoint solve against central differences of
+    converged primal solves.
+"""
+import numpy as np
+import pytest
+
+from finitevolume_gb300 import meshgen, solvers as S
+from helpers import GAMMA
+
+pytestmark = pytest.mark.gpu
+
+
+def _fs(M, aoa):
+    a = np.radians(aoa)
+    return np.array([1.0, M * np.cos(a), M * np.sin(a), 1.0 / GAMMA])
+
+
+def _solver(mesh, fs, order, flux, limiter, farfield=S.EulerBoundaryType.CharacteristicFarfield, cfl=1.2):
+    bcs = [S.EulerBoundaryCondition(S.EulerBoundaryType.Wall),
+           S.EulerBoundaryCondition(farfield, S.from_primitive(*fs, GAMMA))]
+    ic = S.EulerInitialCondition(S.EulerICMode.Freestream, rho=fs[0], u=fs[1], v=fs[2], p=fs[3])
+    return S.EulerFVMSolver(mesh, bcs, GAMMA, cfl, ic, flux, order=order, rk_stages=3, local_dt=True,
+                            gradient=S.GradientScheme.LeastSquares, limiter=limiter)
+
+
+def _converge(s, tol, max_iter):
+    done = 0
+    while done < max_iter:
+        h = s.run(1000, history=True)
+        done += 1000
+        if h[:, 0].min() < tol:
+            return h[-1, 0]
+    return h[-1, 0]
+
+
+# (order, flux, limiter, farfield kind, Mach): transonic cases are limited
+CASES = [(1, S.NumericalFluxScheme.Rusanov, S.Limiter.NoLimiter, S.EulerBoundaryType.CharacteristicFarfield, 0.7),
+         (1, S.NumericalFluxScheme.HLLC, S.Limiter.NoLimiter, S.EulerBoundaryType.Farfield, 0.7),
+         (2, S.NumericalFluxScheme.HLLC, S.Limiter.Venkatakrishnan, S.EulerBoundaryType.CharacteristicFarfield, 0.7),
+         (2, S.NumericalFluxScheme.Rusanov, S.Limiter.BarthJespersen, S.EulerBoundaryType.Farfield, 0.7),
+         (2, S.NumericalFluxScheme.HLLC, S.Limiter.NoLimiter, S.EulerBoundaryType.CharacteristicFarfield, 0.5)]
+
+
+def _mesh(order, **kw):
+    # unlimited second order needs the finer grid to stay stable at the nose
+    return S.Mesh(meshgen.naca_ogrid(48, 24, **kw) if order == 1 else meshgen.naca_ogrid(96, 48, **kw))
+
+
+@pytest.mark.parametrize("order,flux,limiter,farfield,mach", CASES)
+def test_backward_is_the_transpose_of_forward(gpu, order, flux, limiter, farfield, mach):
+    mesh = _mesh(order)
+    s = _solver(mesh, _fs(mach, 2.0), order, flux, limiter, farfield)
+    s.run(300)
+    adj = S.DiscreteAdjoint(s)
+    R = adj.forward()
+    assert np.isfinite(R).all()
+    rng = np.random.default_rng(7)
+    U = s.field()
+    dU = rng.standard_normal(U.shape) * np.abs(U).mean(axis=0)
+    dfs = rng.standard_normal((2, 4))
+    Rb = rng.standard_normal(U.shape)
+    lhs = float(np.sum(Rb * adj.jvp(dU, dfs)))
+    Ub, fb = adj.vjp(Rb)
+    rhs = float(np.sum(Ub * dU) + np.sum(fb * dfs))
+    scale = float(np.sum(np.abs(Rb * adj.jvp(dU, dfs))))
+    assert abs(lhs - rhs) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("order,flux", [(1, S.NumericalFluxScheme.HLLC), (2, S.NumericalFluxScheme.HLLC),
+                                        (2, S.NumericalFluxScheme.Rusanov)])
+def test_tangent_matches_central_differences(gpu, order, flux):
+    mesh = _mesh(order)
+    fs = _fs(0.5, 3.0)
+    s = _solver(mesh, fs, order, flux, S.Limiter.NoLimiter)
+    s.run(300)
+    U = s.field()
+    adj = S.DiscreteAdjoint(s)
+    rng = np.random.default_rng(3)
+    dU = rng.standard_normal(U.shape) * np.abs(U).mean(axis=0)
+    h = 1e-6
+    fd = (adj.forward(U + h * dU) - adj.forward(U - h * dU)) / (2 * h)
+    adj.forward(U)
+    jv = adj.jvp(dU)
+    # Rusanov's max(|Vn| + c) has kinks a central difference can straddle
+    assert np.linalg.norm(jv - fd) <= 1e-5 * np.linalg.norm(jv)
+    # freestream direction: residual of solvers built on fs +- h dfs, same state
+    dfs = np.array([0.1, 0.3, -0.2, 0.05])
+    Rp = S.DiscreteAdjoint(_solver(mesh, fs + h * dfs, order, flux, S.Limiter.NoLimiter)).forward(U)
+    Rm = S.DiscreteAdjoint(_solver(mesh, fs - h * dfs, order, flux, S.Limiter.NoLimiter)).forward(U)
+    fdf = (Rp - Rm) / (2 * h)
+    jf = adj.jvp(np.zeros_like(U), np.stack([np.zeros(4), dfs]))
+    assert np.linalg.norm(jf - fdf) <= 1e-6 * np.linalg.norm(jf)
+
+
+def _coefficients(mesh, M, aoa, order, flux, tol, max_iter):
+    s = _solver(mesh, _fs(M, aoa), order, flux, S.Limiter.NoLimiter)
+    res = _converge(s, tol, max_iter)
+    f = s.wall_forces(1.0, M * np.cos(np.radians(aoa)), M * np.sin(np.radians(aoa)), 1.0 / GAMMA, 1.0, 0.25, 0.0)
+    return f["cd_total"], f["cl"], res, s
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_freestream_gradients_match_converged_differences(gpu, order):
+    mesh = _mesh(order, r_far=10.0)
+    M, aoa = 0.5, 2.0
+    flux = S.NumericalFluxScheme.HLLC
+    tol, max_iter = 1e-12, 60000 if order == 1 else 150000
+    cd, cl, res, s = _coefficients(mesh, M, aoa, order, flux, tol, max_iter)
+    assert res < 1e-11, res
+    adj = S.DiscreteAdjoint(s)
+    gd = adj.freestream_gradient(S.Objective.Drag, M, aoa, [1], max_iter=max_iter, tol=1e-12)
+    gl = adj.freestream_gradient(S.Objective.Lift, M, aoa, [1], max_iter=max_iter, tol=1e-12)
+    assert abs(gd["J"] - cd) < 1e-12 and abs(gl["J"] - cl) < 1e-12
+    hM, ha = 1e-4, 1e-3
+    cdp, clp, r1, _ = _coefficients(mesh, M + hM, aoa, order, flux, tol, max_iter)
+    cdm, clm, r2, _ = _coefficients(mesh, M - hM, aoa, order, flux, tol, max_iter)
+    cda, cla, r3, _ = _coefficients(mesh, M, aoa + ha, order, flux, tol, max_iter)
+    cdb, clb, r4, _ = _coefficients(mesh, M, aoa - ha, order, flux, tol, max_iter)
+    assert max(r1, r2, r3, r4) < 1e-11
+    fd = {"cd_M": (cdp - cdm) / (2 * hM), "cl_M": (clp - clm) / (2 * hM),
+          "cd_a": (cda - cdb) / (2 * ha), "cl_a": (cla - clb) / (2 * ha)}
+    ad = {"cd_M": gd["dJ_dM"], "cl_M": gl["dJ_dM"], "cd_a": gd["dJ_dAoA_deg"], "cl_a": gl["dJ_dAoA_deg"]}
+    for k in fd:
+        assert abs(ad[k] - fd[k]) <= 1e-4 * max(abs(fd[k]), 1e-3), (k, ad[k], fd[k])
