@@ -199,17 +199,12 @@ __device__ __forceinline__ void store_jac(double* J, const V4<D4>& F, double ar)
         for (int k = 0; k < 4; ++k) J[4 * i + k] = ar * dget(F, i).d[k];
 }
 
-// Per face: reconstruction (with its positivity decisions), flux value and
-// the flux Jacobians.
-__global__ void k_lin_face(const AdjArgs a) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= a.n_faces) return;
-    const int L = a.fl[f], R = a.fr[f];
-    const double4_32a geo = a.fgeom[f];
-    const double nx = geo.x, ny = geo.y, ar = geo.z;
-    const double g = a.gamma;
-    V4<double> wl = ldW(a.W, L), wr = {0, 0, 0, 0};
-    const V4<double> wlc = wl;
+// Reconstructed face states at the linearisation state and the positivity
+// decisions (bit 0 owner side fell back, bit 1 neighbour side), as k_face.
+__device__ __forceinline__ unsigned char recon_face(const AdjArgs& a, int f, int L, int R, V4<double>& wl,
+                                                    V4<double>& wr) {
+    wl = ldW(a.W, L);
+    wr = {0, 0, 0, 0};
     unsigned char flags = 0;
     if (a.order == 2) {
         const double4_32a rr = a.frf[f];
@@ -237,6 +232,21 @@ __global__ void k_lin_face(const AdjArgs a) {
     } else if (R >= 0) {
         wr = ldW(a.W, R);
     }
+    return flags;
+}
+
+// Per face: reconstruction (with its positivity decisions), flux value and
+// the flux Jacobians.
+__global__ void k_lin_face(const AdjArgs a) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n_faces) return;
+    const int L = a.fl[f], R = a.fr[f];
+    const double4_32a geo = a.fgeom[f];
+    const double nx = geo.x, ny = geo.y, ar = geo.z;
+    const double g = a.gamma;
+    V4<double> wl, wr;
+    const unsigned char flags = recon_face(a, f, L, R, wl, wr);
+    const V4<double> wlc = ldW(a.W, L);
     a.fb[f] = flags;
     const D4 gD(g), iD(a.igm1), nxD(nx), nyD(ny);
     double* JL = a.JL + 16 * (size_t)f;
@@ -607,6 +617,131 @@ __global__ void __launch_bounds__(256) k_adj_norms(const double* partials, int n
     }
 }
 
+// ---------------------------------------------------------------------------
+// Geometry cotangents of lam^T R (shape sensitivities), after a backward
+// pass at lam has filled wbar and Gub.  Per face: the unit normal, the
+// length and the reconstruction offsets (x_f - x_L, x_f - x_R).
+__global__ void k_geo_face(const AdjArgs a, const St* __restrict__ lam, double* __restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n_faces) return;
+    const int L = a.fl[f], R = a.fr[f];
+    const double4_32a geo = a.fgeom[f];
+    const double ar = geo.z, g = a.gamma;
+    const St ll = ld_state(lam, L);
+    double fbar[4] = {-ll.r, -ll.ru, -ll.rv, -ll.E};
+    if (R >= 0) {
+        const St lr = ld_state(lam, R);
+        fbar[0] += lr.r; fbar[1] += lr.ru; fbar[2] += lr.rv; fbar[3] += lr.E;
+    }
+    V4<double> wl, wr;
+    const unsigned char flags = recon_face(a, f, L, R, wl, wr);
+    // d flux / d (nx, ny) by dual numbers (partials 0 and 1)
+    D4 nxD(geo.x), nyD(geo.y);
+    nxD.d[0] = 1.0;
+    nyD.d[1] = 1.0;
+    const D4 gD(g), iD(a.igm1);
+    V4<D4> Fl;
+    if (R >= 0) {
+        Fl = flux_of<D4>(a.flux, cst(wl), cst(wr), nxD, nyD, gD, iD);
+    } else {
+        const int patch = a.fpatch[f];
+        const int t = a.bc.type[patch];
+        V4<double> fsp = {0, 0, 0, 0};
+        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+        const D4 wu(t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0), wv(t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0);
+        Fl = flux_of<D4>(a.flux, cst(wl), ghost_core<D4>(t, cst(wl), nxD, nyD, gD, cst(fsp), wu, wv), nxD, nyD, gD,
+                         iD);
+    }
+    double nbx = 0.0, nby = 0.0, abar = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const D4 q = dget(Fl, i);
+        nbx += fbar[i] * q.d[0];
+        nby += fbar[i] * q.d[1];
+        abar += fbar[i] * q.v;
+    }
+    double* o = out + 8 * (size_t)f;
+    o[0] = ar * nbx;
+    o[1] = ar * nby;
+    o[2] = abar;
+    double rl[2] = {0.0, 0.0}, rrr[2] = {0.0, 0.0};
+    if (a.order == 2) {
+        const double* wb = a.wbar + 8 * (size_t)f;
+        if (!(flags & 1))
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const double2 q = a.Gu[4 * L + k];
+                const double p = a.psi[4 * L + k];
+                rl[0] += wb[k] * p * q.x;
+                rl[1] += wb[k] * p * q.y;
+            }
+        if (R >= 0 && !(flags & 2))
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const double2 q = a.Gu[4 * R + k];
+                const double p = a.psi[4 * R + k];
+                rrr[0] += wb[4 + k] * p * q.x;
+                rrr[1] += wb[4 + k] * p * q.y;
+            }
+    }
+    o[3] = rl[0]; o[4] = rl[1]; o[5] = rrr[0]; o[6] = rrr[1]; o[7] = 0.0;
+}
+
+// Per cell: cotangents of the LSQ weights of each entry (abar, 2 per
+// entry) and of their sums (sbar, 2 per cell); per boundary face the
+// normal cotangent through the gradient's boundary value (nbg).
+__global__ void k_geo_cell(const AdjArgs a, double* __restrict__ abar, double* __restrict__ sbar,
+                           double* __restrict__ nbg) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    const V4<double> wc = ldW(a.W, c);
+    double2 gu[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) gu[k] = a.Gub[4 * c + k];
+    double sx = 0.0, sy = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { sx -= gu[k].x * vget(wc, k); sy -= gu[k].y * vget(wc, k); }
+    sbar[2 * c] = sx;
+    sbar[2 * c + 1] = sy;
+    const double g = a.gamma;
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int nb = a.cnb[e];
+        V4<double> v;
+        if (nb >= 0) {
+            v = ldW(a.W, nb);
+        } else {
+            const int f = -1 - nb;
+            const double4_32a geo = a.fgeom[f];
+            const int patch = a.fpatch[f];
+            const int t = a.bc.type[patch];
+            V4<double> fsp = {0, 0, 0, 0};
+            if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+            const D4 wu(t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0), wv(t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0);
+            D4 nxD(geo.x), nyD(geo.y);
+            nxD.d[0] = 1.0;
+            nyD.d[1] = 1.0;
+            const V4<D4> gh = ghost_core<D4>(t, cst(wc), nxD, nyD, D4(g), cst(fsp), wu, wv);
+            v = {0.5 * (wc.r + gh.r.v), 0.5 * (wc.u + gh.u.v), 0.5 * (wc.v + gh.v.v), 0.5 * (wc.p + gh.p.v)};
+            // cotangent of the boundary value: lsq weight of this entry times Gub
+            const double2 w = a.lsq[e];
+            double bx = 0.0, by = 0.0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const double ci = w.x * gu[i].x + w.y * gu[i].y;
+                bx += 0.5 * ci * dget(gh, i).d[0];
+                by += 0.5 * ci * dget(gh, i).d[1];
+            }
+            nbg[2 * (size_t)(f - a.n_int_faces)] = bx;
+            nbg[2 * (size_t)(f - a.n_int_faces) + 1] = by;
+        }
+        double ax = 0.0, ay = 0.0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { ax += gu[k].x * vget(v, k); ay += gu[k].y * vget(v, k); }
+        abar[2 * (size_t)e] = ax;
+        abar[2 * (size_t)e + 1] = ay;
+    }
+}
+
 __global__ void k_perm_gather(const St* __restrict__ in_ref, St* __restrict__ out_dev, const int* __restrict__ perm,
                               int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -626,6 +761,10 @@ __global__ void k_perm_scatter(const St* __restrict__ in_dev, St* __restrict__ o
 using adjk::AdjArgs;
 using fvgb::St;
 
+namespace fvgb {
+const HostMesh& host_mesh_of(const fv_mesh_s* m);
+}
+
 struct fv_adjoint_s {
     fv_solver_s* solver = nullptr;
     AdjArgs a{};
@@ -638,6 +777,7 @@ struct fv_adjoint_s {
     int* counter = nullptr;
     int hist_cap = 0;
     bool linearised = false;
+    bool solved = false;
     ~fv_adjoint_s() {
         for (void* p : owned) cudaFree(p);
         if (hist) cudaFree(hist);
@@ -855,6 +995,7 @@ int fv_residual_forward(fv_adjoint_t A, const double* U, double* R) {
         if (U) upload_ref(A, U, A->U);
         else FV_CUDA(cudaMemcpyAsync(A->U, s.U, sizeof(St) * (size_t)A->N, cudaMemcpyDeviceToDevice, s.stream));
         linearise(A);
+        A->solved = false;
         if (R) {
             adjk::k_res_cell<<<blocks(A->N), kB, 0, s.stream>>>(A->a, A->Rdev);
             check_launch();
@@ -932,6 +1073,7 @@ int fv_adjoint_solve(fv_adjoint_t A, const double* dJdU, int32_t max_iter, doubl
         if (iterations) *iterations = done;
         if (history && done)
             FV_CUDA(cudaMemcpy(history, A->hist, sizeof(double) * 4 * (size_t)done, cudaMemcpyDeviceToHost));
+        A->solved = true;
         if (lambda) download_ref(A, A->lam, lambda);
         if (fsbar) {
             // lam^T dR/dfs at the converged lam
@@ -939,6 +1081,216 @@ int fv_adjoint_solve(fv_adjoint_t A, const double* dJdU, int32_t max_iter, doubl
             reduce_fsbar(A, fsbar);
         }
         FV_CUDA(cudaStreamSynchronize(s.stream));
+    });
+}
+
+// Shape gradient: dJ/dX over the mesh nodes, X in the caller's node
+// numbering, with J a wall-force coefficient and lam the adjoint of the
+// last fv_adjoint_solve (which must have been solved for the same J).
+// dJ/dX = dJ/dX|explicit - lam^T dR/dX, where R depends on the nodes
+// through the face normals, lengths and midpoints, the cell centroids
+// (shoelace, src/MeshReader.cpp:56-76) and the least-squares weights built
+// from them; the limiter values stay frozen.  The device computes the
+// cotangents of those geometric quantities; this host code runs the
+// reverse pass of the geometry itself.
+int fv_adjoint_shape_gradient(fv_adjoint_t A, fv_mesh_t mesh, int32_t objective, const double ref[7],
+                              double* dJdX) {
+    return fvgb::guarded([&] {
+        if (!A || !mesh || !ref || !dJdX) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (!A->solved) fvgb::raise(FV_ERR_BAD_ARG, "call fv_adjoint_solve first");
+        if (objective < 0 || objective > 2) fvgb::raise(FV_ERR_BAD_ARG, "objective: 0 drag, 1 lift, 2 moment");
+        const fvgb::HostMesh& h = fvgb::host_mesh_of(mesh);
+        fvgb::Solver& s = A->solver->s;
+        if (h.n_cells != A->N || h.n_faces != A->F) fvgb::raise(FV_ERR_BAD_ARG, "mesh does not match the solver");
+        if (h.cnode_off.empty())
+            fvgb::raise(FV_ERR_UNSUPPORTED, "shape gradient: the mesh must be built from cell polygons");
+        const int N = A->N, F = A->F, Fb = A->Fb;
+        const size_t E = (size_t)(2 * F - Fb);
+        AdjArgs& a = A->a;
+        // cotangents on the device
+        backward(A, A->lam, 0, A->Rdev);
+        double* d_face = A->alloc<double>(8 * (size_t)F);
+        double* d_ab = A->alloc<double>(2 * E);
+        double* d_sb = A->alloc<double>(2 * (size_t)N);
+        double* d_nbg = A->alloc<double>(2 * (size_t)std::max(Fb, 1));
+        FV_CUDA(cudaMemsetAsync(d_nbg, 0, sizeof(double) * 2 * (size_t)std::max(Fb, 1), s.stream));
+        FV_CUDA(cudaMemsetAsync(d_ab, 0, sizeof(double) * 2 * E, s.stream));
+        FV_CUDA(cudaMemsetAsync(d_sb, 0, sizeof(double) * 2 * (size_t)N, s.stream));
+        adjk::k_geo_face<<<blocks(F), kB, 0, s.stream>>>(a, A->lam, d_face);
+        check_launch();
+        if (a.order == 2) {
+            adjk::k_geo_cell<<<blocks(N), kB, 0, s.stream>>>(a, d_ab, d_sb, d_nbg);
+            check_launch();
+        }
+        std::vector<double> face(8 * (size_t)F), ab(2 * E), sb(2 * (size_t)N), nbg(2 * (size_t)std::max(Fb, 1));
+        FV_CUDA(cudaMemcpyAsync(face.data(), d_face, sizeof(double) * face.size(), cudaMemcpyDeviceToHost, s.stream));
+        FV_CUDA(cudaMemcpyAsync(ab.data(), d_ab, sizeof(double) * ab.size(), cudaMemcpyDeviceToHost, s.stream));
+        FV_CUDA(cudaMemcpyAsync(sb.data(), d_sb, sizeof(double) * sb.size(), cudaMemcpyDeviceToHost, s.stream));
+        FV_CUDA(cudaMemcpyAsync(nbg.data(), d_nbg, sizeof(double) * nbg.size(), cudaMemcpyDeviceToHost, s.stream));
+        FV_CUDA(cudaStreamSynchronize(s.stream));
+        // cotangents of the geometric quantities, reference numbering
+        std::vector<double> nxb(F, 0.0), nyb(F, 0.0), arb(F, 0.0), fxb(F, 0.0), fyb(F, 0.0), cxb(N, 0.0),
+            cyb(N, 0.0);
+        for (int i = 0; i < F; ++i) {
+            const int f = h.fperm[i];
+            const double* o = face.data() + 8 * (size_t)i;
+            nxb[f] += o[0];
+            nyb[f] += o[1];
+            arb[f] += o[2];
+            if (i >= h.n_int_faces) {
+                nxb[f] += nbg[2 * (size_t)(i - h.n_int_faces)];
+                nyb[f] += nbg[2 * (size_t)(i - h.n_int_faces) + 1];
+            }
+            if (a.order == 2) {
+                // r_L = x_f - x_L, r_R = x_f - x_R
+                fxb[f] += o[3]; fyb[f] += o[4];
+                cxb[h.fl[f]] -= o[3]; cyb[h.fl[f]] -= o[4];
+                if (h.fr[f] >= 0) {
+                    fxb[f] += o[5]; fyb[f] += o[6];
+                    cxb[h.fr[f]] -= o[5]; cyb[h.fr[f]] -= o[6];
+                }
+            }
+        }
+        if (a.order == 2) {
+            // least-squares weights a_e = B w_e d_e, B = M^-1, M = sum w d d^T,
+            // w = 1/|d|^2, d = x_nb - x_c (x_nb: neighbour centroid or the
+            // boundary face midpoint); their sums s_c pass sbar to every a_e
+            for (int i = 0; i < N; ++i) {
+                const int c = h.perm[i];
+                const double xc = h.cx[c], yc = h.cy[c];
+                const int e0 = h.d_cf_off[i], e1 = h.d_cf_off[i + 1];
+                double m00 = 0.0, m01 = 0.0, m11 = 0.0;
+                for (int e = e0; e < e1; ++e) {
+                    const int f = h.fperm[h.d_cf[e] >> 1];
+                    double px, py;
+                    if (h.fr[f] < 0) { px = h.fxm[f]; py = h.fym[f]; }
+                    else { const int nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
+                    const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
+                    m00 += w * dx * dx; m01 += w * dx * dy; m11 += w * dy * dy;
+                }
+                const double det = m00 * m11 - m01 * m01;
+                const double b00 = m11 / det, b01 = -m01 / det, b11 = m00 / det;
+                double B00 = 0.0, B01 = 0.0, B10 = 0.0, B11 = 0.0;  // Bbar
+                for (int e = e0; e < e1; ++e) {
+                    const int f = h.fperm[h.d_cf[e] >> 1];
+                    double px, py;
+                    if (h.fr[f] < 0) { px = h.fxm[f]; py = h.fym[f]; }
+                    else { const int nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
+                    const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
+                    const double ax = ab[2 * (size_t)e] + sb[2 * (size_t)i], ay = ab[2 * (size_t)e + 1] + sb[2 * (size_t)i + 1];
+                    B00 += ax * w * dx; B01 += ax * w * dy; B10 += ay * w * dx; B11 += ay * w * dy;
+                }
+                // Mbar = -B^T Bbar B^T (B symmetric)
+                const double t00 = b00 * B00 + b01 * B10, t01 = b00 * B01 + b01 * B11;
+                const double t10 = b01 * B00 + b11 * B10, t11 = b01 * B01 + b11 * B11;
+                const double M00 = -(t00 * b00 + t01 * b01), M01 = -(t00 * b01 + t01 * b11);
+                const double M10 = -(t10 * b00 + t11 * b01), M11 = -(t10 * b01 + t11 * b11);
+                for (int e = e0; e < e1; ++e) {
+                    const int f = h.fperm[h.d_cf[e] >> 1];
+                    const bool bnd = h.fr[f] < 0;
+                    int nb = -1;
+                    double px, py;
+                    if (bnd) { px = h.fxm[f]; py = h.fym[f]; }
+                    else { nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
+                    const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
+                    const double ax = ab[2 * (size_t)e] + sb[2 * (size_t)i], ay = ab[2 * (size_t)e + 1] + sb[2 * (size_t)i + 1];
+                    // (w d)bar = B a_bar
+                    const double vx = b00 * ax + b01 * ay, vy = b01 * ax + b11 * ay;
+                    // M = sum w d d^T: dbar += w (Mbar + Mbar^T) d, wbar += d^T Mbar d
+                    double ddx = w * ((M00 + M00) * dx + (M01 + M10) * dy) + w * vx;
+                    double ddy = w * ((M10 + M01) * dx + (M11 + M11) * dy) + w * vy;
+                    const double wb = dx * (M00 * dx + M01 * dy) + dy * (M10 * dx + M11 * dy) + dx * vx + dy * vy;
+                    ddx += wb * (-2.0 * w * w * dx);
+                    ddy += wb * (-2.0 * w * w * dy);
+                    if (bnd) { fxb[f] += ddx; fyb[f] += ddy; }
+                    else { cxb[nb] += ddx; cyb[nb] += ddy; }
+                    cxb[c] -= ddx;
+                    cyb[c] -= ddy;
+                }
+            }
+        }
+        // node cotangents of lam^T R
+        const int nn = h.n_nodes;
+        std::vector<double> xb(nn, 0.0), yb(nn, 0.0);
+        for (int c = 0; c < N; ++c) {
+            if (cxb[c] == 0.0 && cyb[c] == 0.0) continue;
+            const int64_t lo = h.cnode_off[c], hi = h.cnode_off[c + 1];
+            const int k = (int)(hi - lo);
+            const int32_t* ids = h.cnodes.data() + lo;
+            double area = 0.0, Sx = 0.0, Sy = 0.0;
+            for (int j = 0; j < k; ++j) {
+                const int p0 = ids[j], p1 = ids[(j + 1) % k];
+                const double cr = h.nx_[p0] * h.ny_[p1] - h.nx_[p1] * h.ny_[p0];
+                area += cr;
+                Sx += (h.nx_[p0] + h.nx_[p1]) * cr;
+                Sy += (h.ny_[p0] + h.ny_[p1]) * cr;
+            }
+            area *= 0.5;
+            // C = S / (6 area)
+            const double Sbx = cxb[c] / (6.0 * area), Sby = cyb[c] / (6.0 * area);
+            const double Ab = -(cxb[c] * Sx + cyb[c] * Sy) / (6.0 * area * area);
+            for (int j = 0; j < k; ++j) {
+                const int p0 = ids[j], p1 = ids[(j + 1) % k];
+                const double x0 = h.nx_[p0], y0 = h.ny_[p0], x1 = h.nx_[p1], y1 = h.ny_[p1];
+                const double cr = x0 * y1 - x1 * y0;
+                xb[p0] += Sbx * cr; xb[p1] += Sbx * cr;
+                yb[p0] += Sby * cr; yb[p1] += Sby * cr;
+                const double crb = Sbx * (x0 + x1) + Sby * (y0 + y1) + 0.5 * Ab;
+                xb[p0] += crb * y1; yb[p1] += crb * x0;
+                xb[p1] -= crb * y0; yb[p0] -= crb * x1;
+            }
+        }
+        for (int f = 0; f < F; ++f) {
+            const int n1 = h.fn1[f], n2 = h.fn2[f];
+            const double dx = h.nx_[n2] - h.nx_[n1], dy = h.ny_[n2] - h.ny_[n1];
+            const double ln = std::sqrt(dx * dx + dy * dy);
+            // n = (dy, -dx) / ln, length ln, midpoint (p1 + p2) / 2
+            const double lb = arb[f] - (nxb[f] * dy - nyb[f] * dx) / (ln * ln);
+            const double dyb = nxb[f] / ln + lb * dy / ln;
+            const double dxb = -nyb[f] / ln + lb * dx / ln;
+            xb[n2] += dxb; xb[n1] -= dxb;
+            yb[n2] += dyb; yb[n1] -= dyb;
+            xb[n1] += 0.5 * fxb[f]; xb[n2] += 0.5 * fxb[f];
+            yb[n1] += 0.5 * fyb[f]; yb[n2] += 0.5 * fyb[f];
+        }
+        // explicit part: J = sum_wall p_c (k . n) |f| / qL at the adjoint's state
+        std::vector<double> U(4 * (size_t)N);
+        download_ref(A, A->U, U.data());
+        const double vmag = std::hypot(ref[1], ref[2]);
+        const double ddx = ref[1] / vmag, ddy = ref[2] / vmag;
+        const double qL = 0.5 * ref[0] * vmag * vmag * ref[4];
+        const double g = s.gamma;
+        std::vector<double> ex(nn, 0.0), ey(nn, 0.0);
+        for (const fvgb::WallFace& w : s.wall_faces) {
+            int f = -1;
+            // the wall face in reference numbering
+            f = h.fperm[w.dev_face];
+            const double* u = U.data() + 4 * (size_t)w.cell;
+            const double uu = u[1] / u[0], vv = u[2] / u[0];
+            const double p = (g - 1.0) * (u[3] - 0.5 * u[0] * (uu * uu + vv * vv));
+            const int n1 = h.fn1[f], n2 = h.fn2[f];
+            const double dx = h.nx_[n2] - h.nx_[n1], dy = h.ny_[n2] - h.ny_[n1];
+            double bdx, bdy, bxm = 0.0, bym = 0.0;
+            if (objective == 0) { bdy = p * ddx / qL; bdx = -p * ddy / qL; }
+            else if (objective == 1) { bdy = p * (-ddy) / qL; bdx = -p * ddx / qL; }
+            else {
+                const double L = ref[4];
+                const double rx = 0.5 * (h.nx_[n1] + h.nx_[n2]) - ref[5], ry = 0.5 * (h.ny_[n1] + h.ny_[n2]) - ref[6];
+                // J = -p (rx dx + ry dy) / (qL L)
+                bdx = -p * rx / (qL * L);
+                bdy = -p * ry / (qL * L);
+                bxm = -p * dx / (qL * L);
+                bym = -p * dy / (qL * L);
+            }
+            ex[n2] += bdx; ex[n1] -= bdx;
+            ey[n2] += bdy; ey[n1] -= bdy;
+            ex[n1] += 0.5 * bxm; ex[n2] += 0.5 * bxm;
+            ey[n1] += 0.5 * bym; ey[n2] += 0.5 * bym;
+        }
+        for (int i = 0; i < nn; ++i) {
+            dJdX[2 * (size_t)i] = ex[i] - xb[i];
+            dJdX[2 * (size_t)i + 1] = ey[i] - yb[i];
+        }
     });
 }
 

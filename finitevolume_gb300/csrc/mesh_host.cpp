@@ -70,6 +70,8 @@ void build_from_polygons(HostMesh& m, int32_t n_nodes, const double* xy, int32_t
             fail(kBadMesh, "mesh: node " + std::to_string(i) + " has a non-finite coordinate");
     }
     if (cell_off[0] != 0) fail(kBadArg, "mesh: cell_off[0] != 0");
+    m.cnode_off.assign(cell_off, cell_off + n_cells + 1);
+    m.cnodes.assign(cell_nodes, cell_nodes + cell_off[n_cells]);
     std::unordered_map<uint64_t, int32_t> edge_to_face;
     edge_to_face.reserve((size_t)(cell_off[n_cells] * 0.6) + 16);
     m.cf_off.assign(n_cells + 1, 0);

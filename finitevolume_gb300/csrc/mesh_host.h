@@ -23,6 +23,10 @@ struct HostMesh {
     std::vector<double> fnx, fny, farea, fxm, fym;
     std::vector<int32_t> cf_off, cf;              // cell -> faces, reference order
     std::vector<double> vol, cx, cy;
+    // cell polygons (CCW node lists) when the mesh was built from them;
+    // empty for meshes given as faces plus cell geometry
+    std::vector<int64_t> cnode_off;
+    std::vector<int32_t> cnodes;
 
     // --- device order (perm[new] = reference cell, fperm[new] = ref face) --
     std::vector<int32_t> perm, iperm, fperm, ifperm;

@@ -370,6 +370,14 @@ class DiscreteAdjoint:
                                                capi.dptr(hist), C.byref(it)))
         return lam, fb[:self.n_patches], hist[:it.value], it.value
 
+    def shape_gradient(self, objective: Objective, ref) -> np.ndarray:
+        """dJ/dX [n_nodes, 2] of the objective the last ``solve`` used."""
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = np.zeros((self.solver.mesh.poly.n_nodes, 2))
+        capi.check(capi.lib().fv_adjoint_shape_gradient(self._h, self.solver.mesh.handle, int(objective),
+                                                        capi.dptr(r), capi.dptr(out)))
+        return out
+
     def freestream_gradient(self, objective: Objective, mach: float, aoa_deg: float, farfield_patches,
                             max_iter: int = 20000, tol: float = 1e-12) -> dict:
         """dJ/dM and dJ/dAoA (per degree) of a force coefficient at a

@@ -277,6 +277,13 @@ int fv_residual_backward(fv_adjoint_t a, const double* Rbar, double* Ubar, doubl
  * dfs/dalpha. */
 int fv_adjoint_solve(fv_adjoint_t a, const double* dJdU, int32_t max_iter, double tol, double* lambda, double* fsbar,
                      double* history, int32_t* iterations);
+/* Shape gradient dJ/dX [2 n_nodes] (x, y per node, the mesh's node
+ * numbering) of the objective the last fv_adjoint_solve was solved for:
+ * dJ/dX|explicit - lambda^T dR/dX through face normals, lengths and
+ * midpoints, shoelace cell centroids and the least-squares weights (limiter
+ * values frozen).  mesh is the mesh the solver was created from; it must
+ * have been built from cell polygons (fv_mesh_create_polygons). */
+int fv_adjoint_shape_gradient(fv_adjoint_t a, fv_mesh_t mesh, int32_t objective, const double ref[7], double* dJdX);
 /* Wall-force coefficient J (objective 0 drag, 1 lift, 2 moment; pressure
  * part with the owner-cell pressure, ref as fv_wall_forces) at the
  * solver's current state, and dJ/dU (may be NULL). */

@@ -133,3 +133,69 @@ def test_freestream_gradients_match_converged_differences(gpu, order):
     ad = {"cd_M": gd["dJ_dM"], "cl_M": gl["dJ_dM"], "cd_a": gd["dJ_dAoA_deg"], "cl_a": gl["dJ_dAoA_deg"]}
     for k in fd:
         assert abs(ad[k] - fd[k]) <= 1e-4 * max(abs(fd[k]), 1e-3), (k, ad[k], fd[k])
+
+
+def _wall_normal_directions(poly, n_dirs, seed, width=20):
+    """Seeded surface-normal displacement fields of the wall (patch 0):
+    white noise on the wall nodes smoothed by a periodic Gaussian over
+    ``width`` nodes, times the unit node normal; each scaled to max 1."""
+    e = poly.bedges[poly.bpatch == 0]
+    order = [int(e[0, 0])]
+    nxt = {int(a): int(b) for a, b in e}
+    while nxt[order[-1]] != order[0]:
+        order.append(nxt[order[-1]])
+    order = np.array(order)
+    P = poly.nodes[order]
+    t = np.roll(P, -1, axis=0) - np.roll(P, 1, axis=0)
+    nrm = np.stack([t[:, 1], -t[:, 0]], 1)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    rng = np.random.default_rng(seed)
+    k = np.arange(-width, width + 1)
+    ker = np.exp(-0.5 * (k / (width / 3.0)) ** 2)
+    out = []
+    for _ in range(n_dirs):
+        w = rng.standard_normal(len(order))
+        a = sum(ker[j] * np.roll(w, k[j]) for j in range(len(k)))
+        a /= np.abs(a).max()
+        d = np.zeros_like(poly.nodes)
+        d[order] = a[:, None] * nrm
+        out.append(d)
+    return out
+
+
+def _moved(poly, d):
+    import dataclasses
+    return dataclasses.replace(poly, nodes=np.ascontiguousarray(poly.nodes + d))
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_shape_gradient_matches_converged_differences(gpu, order):
+    poly = meshgen.naca_ogrid(48, 24, r_far=10.0) if order == 1 else meshgen.naca_ogrid(96, 48, r_far=10.0)
+    M, aoa = 0.5, 2.0
+    fs = _fs(M, aoa)
+    flux = S.NumericalFluxScheme.HLLC
+    tol, max_iter = 1e-12, 60000 if order == 1 else 150000
+    ref = np.array([1.0, fs[1], fs[2], fs[3], 1.0, 0.25, 0.0])
+    s = _solver(S.Mesh(poly), fs, order, flux, S.Limiter.NoLimiter)
+    assert _converge(s, tol, max_iter) < 1e-11
+    adj = S.DiscreteAdjoint(s)
+    adj.forward()
+    grads = {}
+    for obj in (S.Objective.Lift, S.Objective.Drag):
+        _, g = S.force_gradient(s, obj, ref)
+        adj.solve(g, max_iter, 1e-12)
+        grads[obj] = adj.shape_gradient(obj, ref)
+    h = 1e-6
+    for d in _wall_normal_directions(poly, 2, seed=11):
+        vals = {}
+        for sgn in (1, -1):
+            sp = _solver(S.Mesh(_moved(poly, sgn * h * d)), fs, order, flux, S.Limiter.NoLimiter)
+            assert _converge(sp, tol, max_iter) < 1e-11
+            f = sp.wall_forces(*ref)
+            vals[sgn] = (f["cl"], f["cd_total"])
+        fd_cl = (vals[1][0] - vals[-1][0]) / (2 * h)
+        fd_cd = (vals[1][1] - vals[-1][1]) / (2 * h)
+        ad_cl = float(np.sum(grads[S.Objective.Lift] * d))
+        ad_cd = float(np.sum(grads[S.Objective.Drag] * d))
+        assert abs(ad_cl - fd_cl) <= 1e-4 * max(abs(fd_cl), 1e-3), (ad_cl, fd_cl)
+        assert abs(ad_cd - fd_cd) <= 1e-4 * max(abs(fd_cd), 1e-3), (ad_cd, fd_cd)
