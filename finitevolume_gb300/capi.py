@@ -114,7 +114,7 @@ SIGNATURES = {
     "fv_batch_status": (C.c_int, [_P, _I32, _I32, _D]),
     "fv_batch_wall_forces": (C.c_int, [_P, C.c_int32, _D, _D]),
     "fv_batch_set_active": (C.c_int, [_P, C.c_int32, C.c_int32]),
-    "fv_adjoint_create": (C.c_int, [_P, C.POINTER(_P)]),
+    "fv_adjoint_create": (C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
     "fv_adjoint_destroy": (C.c_int, [_P]),
     "fv_residual_forward": (C.c_int, [_P, _D, _D]),
     "fv_residual_jvp": (C.c_int, [_P, _D, _D, _D]),

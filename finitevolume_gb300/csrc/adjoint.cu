@@ -171,6 +171,18 @@ struct AdjArgs {
     double2* dG;         // [4N]
     St* dF;              // [F]
     const double* dfs;   // [4 * kMaxPatches] primitive freestream tangents
+    // full-limiter linearisation (limiter != 0 and full == 1): per cell and
+    // variable the active side (0 none, +1 dmax side, -1 dmin side), the
+    // entry of the extreme neighbour value (-1: the cell itself), the entry
+    // of the extreme face extrapolation, and dpsi/d(d1), dpsi/dy
+    int full, limiter;
+    const double2* erf;  // [E] face midpoint - centroid
+    const double* eps2;  // [N] Venkatakrishnan eps^2
+    signed char* lside;  // [4N]
+    int* led;            // [4N]
+    int* ler;            // [4N]
+    double2* lpd;        // [4N] (dpsi/dd1, dpsi/dy)
+    double* ldb;         // [4N] cotangent of d1 passed to the extreme neighbour
 };
 
 __device__ __forceinline__ V4<double> ldW(const St* W, int i) {
@@ -284,6 +296,80 @@ __global__ void k_lin_face(const AdjArgs a) {
     st_state(a.F, f, st_make(ar * F1.r.v, ar * F1.u.v, ar * F1.v.v, ar * F1.p.v));
 }
 
+// Per cell and variable: the limiter's active branch and its partials,
+// recomputed with k_grad's formulas (neighbour extremes including the cell
+// itself; face extrapolations D2 = Gu . (x_f - x_c); psi = min(1,
+// phi(dmax, max D2 > 0), phi(-dmin, max -D2 over D2 < 0))).
+__global__ void k_lin_lim(const AdjArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    const V4<double> wc = ldW(a.W, c);
+    const double g = a.gamma;
+    const int e0 = a.cf_off[c], e1 = a.cf_off[c + 1];
+    for (int k = 0; k < 4; ++k) {
+        const double w0 = vget(wc, k);
+        double vmax = w0, vmin = w0;
+        int emax = -1, emin = -1;
+        double ypos = 0.0, yneg = 0.0;
+        int epos = -1, eneg = -1;
+        const double2 gu = a.Gu[4 * c + k];
+        for (int e = e0; e < e1; ++e) {
+            const int nb = a.cnb[e];
+            double v;
+            if (nb >= 0) {
+                v = vget(ldW(a.W, nb), k);
+            } else {
+                const int f = -1 - nb;
+                const double4_32a geo = a.fgeom[f];
+                const int patch = a.fpatch[f];
+                const int t = a.bc.type[patch];
+                V4<double> fsp = {0, 0, 0, 0};
+                if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+                const double wu = t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0;
+                const double wv = t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0;
+                const V4<double> gh = ghost_core<double>(t, wc, geo.x, geo.y, g, fsp, wu, wv);
+                v = 0.5 * (w0 + vget(gh, k));
+            }
+            if (v > vmax) { vmax = v; emax = e; }
+            if (v < vmin) { vmin = v; emin = e; }
+            const double2 r = a.erf[e];
+            const double d2 = gu.x * r.x + gu.y * r.y;
+            if (d2 > ypos) { ypos = d2; epos = e; }
+            if (-d2 > yneg) { yneg = -d2; eneg = e; }
+        }
+        const double eps2 = a.limiter == 2 ? a.eps2[c] : 0.0;
+        double nmin = 1.0, dmn = 1.0;
+        int side = 0;
+        double pd1 = 0.0, py = 0.0;
+        for (int sd = 0; sd < 2; ++sd) {
+            const double y = sd == 0 ? ypos : yneg;
+            if (!(y > 0.0)) continue;
+            const double d1 = sd == 0 ? vmax - w0 : w0 - vmin;
+            double num, den, nd1, ny, dd1, dy;
+            if (a.limiter == 1) {
+                num = d1; den = y; nd1 = 1.0; ny = 0.0; dd1 = 0.0; dy = 1.0;
+            } else {
+                const double p = d1 * y, q = d1 * d1 + eps2;
+                num = q + 2.0 * p;
+                den = (y + y) * y + (q + p);
+                nd1 = 2.0 * d1 + 2.0 * y; ny = 2.0 * d1;
+                dd1 = 2.0 * d1 + y; dy = 4.0 * y + d1;
+            }
+            if (num * dmn < nmin * den) {
+                nmin = num; dmn = den;
+                side = sd == 0 ? 1 : -1;
+                pd1 = (nd1 * den - num * dd1) / (den * den);
+                py = (ny * den - num * dy) / (den * den);
+            }
+        }
+        const int i = 4 * c + k;
+        a.lside[i] = (signed char)side;
+        a.led[i] = side == 1 ? emax : (side == -1 ? emin : -1);
+        a.ler[i] = side == 1 ? epos : (side == -1 ? eneg : -1);
+        a.lpd[i] = make_double2(pd1, py);
+    }
+}
+
 // Per cell: D = cfl / sum_f lambda_f |f| (the primal's local time step over
 // the volume), from the cell-centred states.
 __global__ void k_lin_dt(const AdjArgs a) {
@@ -374,10 +460,40 @@ __global__ void k_fwd_cell2(const AdjArgs a) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) { gx[k] += w.x * v[k]; gy[k] += w.y * v[k]; }
     }
+    double dpsi[4] = {0.0, 0.0, 0.0, 0.0};
+    if (a.full) {
+        for (int k = 0; k < 4; ++k) {
+            const int i = 4 * c + k;
+            const int side = a.lside[i];
+            if (!side) continue;
+            const double2 pd = a.lpd[i];
+            const double2 r = a.erf[a.ler[i]];
+            const double dy = side * (gx[k] * r.x + gy[k] * r.y);
+            double dd1 = 0.0;
+            const int ed = a.led[i];
+            if (ed >= 0) {
+                const int nb = a.cnb[ed];
+                double dn;
+                if (nb >= 0) {
+                    const St q = ld_state(a.dW, nb);
+                    dn = (&q.r)[k];
+                } else {
+                    const int f = -1 - nb;
+                    const double* Gb = a.Gb + 32 * (size_t)(f - a.n_int_faces);
+                    const double* df = a.dfs + 4 * a.fpatch[f];
+                    dn = 0.0;
+                    for (int j = 0; j < 4; ++j) dn += Gb[4 * k + j] * dwc[j] + Gb[16 + 4 * k + j] * df[j];
+                }
+                dd1 = side * (dn - dwc[k]);
+            }
+            dpsi[k] = pd.x * dd1 + pd.y * dy;
+        }
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const double p = a.psi[4 * c + k];
-        a.dG[4 * c + k] = make_double2(p * gx[k], p * gy[k]);
+        const double2 gu = a.Gu[4 * c + k];
+        a.dG[4 * c + k] = make_double2(p * gx[k] + dpsi[k] * gu.x, p * gy[k] + dpsi[k] * gu.y);
     }
 }
 
@@ -534,13 +650,50 @@ __global__ void __launch_bounds__(256) k_bwd_cell1(const AdjArgs a, int mode, St
             }
         }
         if (a.order == 2) {
-            St q = st_make(wb[0], wb[1], wb[2], wb[3]);
-            st_state(a.Wbar, c, q);
+            double gux[4], guy[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const double p = a.psi[4 * c + k];
-                a.Gub[4 * c + k] = make_double2(p * gx[k], p * gy[k]);
+                gux[k] = p * gx[k];
+                guy[k] = p * gy[k];
             }
+            if (a.full) {
+                // psi-bar = Gbar . Gu; then through psi = phi(d1, y):
+                // y = side * Gu . r_er, d1 = side * (nb_ed - W_c)
+                for (int k = 0; k < 4; ++k) {
+                    const int i = 4 * c + k;
+                    const int side = a.lside[i];
+                    a.ldb[i] = 0.0;
+                    if (!side) continue;
+                    const double2 gu = a.Gu[i];
+                    const double psib = gx[k] * gu.x + gy[k] * gu.y;
+                    const double2 pd = a.lpd[i];
+                    const double yb = psib * pd.y, d1b = psib * pd.x;
+                    const double2 r = a.erf[a.ler[i]];
+                    gux[k] += side * yb * r.x;
+                    guy[k] += side * yb * r.y;
+                    const int ed = a.led[i];
+                    if (ed < 0) continue;  // the cell's own value: d1 = 0 identically
+                    wb[k] -= side * d1b;
+                    const int nb = a.cnb[ed];
+                    if (nb >= 0) {
+                        a.ldb[i] = side * d1b;  // gathered by the neighbour
+                    } else {
+                        // boundary value (W_c + ghost(W_c)) / 2, row k of its Jacobians
+                        const int f = -1 - nb;
+                        const double* Gb = a.Gb + 32 * (size_t)(f - a.n_int_faces);
+                        double* fs = a.fsb + 4 * (size_t)(f - a.n_int_faces);
+                        for (int j = 0; j < 4; ++j) {
+                            wb[j] += side * d1b * Gb[4 * k + j];
+                            fs[j] += side * d1b * Gb[16 + 4 * k + j];
+                        }
+                    }
+                }
+            }
+            St q = st_make(wb[0], wb[1], wb[2], wb[3]);
+            st_state(a.Wbar, c, q);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) a.Gub[4 * c + k] = make_double2(gux[k], guy[k]);
         } else {
             finish_cell(a, c, wb, mode, out, lam, lam0, rhs, r2);
         }
@@ -565,11 +718,13 @@ __global__ void __launch_bounds__(256) k_bwd_cell2(const AdjArgs a, int mode, St
         for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
             const int nb = a.cnb[e];
             if (nb >= 0) {
-                const double2 w = a.lsq[a.twin[e]];
+                const int tw = a.twin[e];
+                const double2 w = a.lsq[tw];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const double2 q = a.Gub[4 * nb + k];
                     wb[k] += w.x * q.x + w.y * q.y;
+                    if (a.full && a.led[4 * nb + k] == tw) wb[k] += a.ldb[4 * nb + k];
                 }
             } else {
                 const int f = -1 - nb;
@@ -861,6 +1016,10 @@ void linearise(fv_adjoint_s* A) {
     }
     adjk::k_lin_face<<<blocks(A->F), kB, 0, s.stream>>>(a);
     check_launch();
+    if (a.full) {
+        adjk::k_lin_lim<<<blocks(A->N), kB, 0, s.stream>>>(a);
+        check_launch();
+    }
     adjk::k_lin_dt<<<blocks(A->N), kB, 0, s.stream>>>(a);
     check_launch();
     A->linearised = true;
@@ -888,9 +1047,11 @@ void backward(fv_adjoint_s* A, const St* lam, int mode, St* out) {
 
 extern "C" {
 
-int fv_adjoint_create(fv_solver_t solver, fv_adjoint_t* out) {
+int fv_adjoint_create(fv_solver_t solver, int32_t limiter_mode, fv_adjoint_t* out) {
     return fvgb::guarded([&] {
         if (!solver || !out) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (limiter_mode != FV_ADJ_FROZEN_LIMITER && limiter_mode != FV_ADJ_FULL_LIMITER)
+            fvgb::raise(FV_ERR_BAD_ARG, "limiter_mode: FV_ADJ_FROZEN_LIMITER or FV_ADJ_FULL_LIMITER");
         fvgb::Solver& s = solver->s;
         if (s.viscous || s.batch) fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: Euler solvers only (not NS, not batched)");
         if (s.opt.precision != FV_PREC_FP64) fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: FP64 solvers only");
@@ -958,6 +1119,17 @@ int fv_adjoint_create(fv_solver_t solver, fv_adjoint_t* out) {
             a.lsq = static_cast<const double2*>(s.lsq);
             a.lsq_sum = static_cast<const double2*>(s.lsq_sum);
             a.frf = static_cast<const double4_32a*>(s.frf);
+            a.limiter = s.opt.limiter;
+            a.full = limiter_mode == FV_ADJ_FULL_LIMITER && s.opt.limiter != FV_LIM_NONE;
+            if (a.full) {
+                a.erf = static_cast<const double2*>(s.erf);
+                a.eps2 = static_cast<const double*>(s.eps2);
+                a.lside = A->alloc<signed char>(4 * N);
+                a.led = A->alloc<int>(4 * N);
+                a.ler = A->alloc<int>(4 * N);
+                a.lpd = A->alloc<double2>(4 * N);
+                a.ldb = A->alloc<double>(4 * N);
+            }
             // twin entries: the entry of the neighbour's row through the same face
             const size_t E = (size_t)(2 * s.F - A->Fb);
             std::vector<int> off(N + 1), cf(E), cnb(E), twin(E, -1);

@@ -322,17 +322,18 @@ class DiscreteAdjoint:
 
     ``forward(U)`` linearises at U (default: the solver's state) and returns
     R(U); ``jvp`` and ``vjp`` are the tangent and cotangent maps at that
-    state (limiter values frozen); ``solve`` returns the adjoint lambda of
+    state (limiter values frozen, or differentiated with
+    ``full_limiter=True``); ``solve`` returns the adjoint lambda of
     (dR/dU)^T lambda = dJ/dU and fsbar = (dR/dfs)^T lambda, fs being each
     patch's primitive freestream (rho, u, v, p).
     """
 
-    def __init__(self, solver: "EulerFVMSolver"):
+    def __init__(self, solver: "EulerFVMSolver", full_limiter: bool = False):
         self.solver = solver
         self.n = solver.n_cells
         self.n_patches = len(solver.mesh.patch_names)
         h = C.c_void_p()
-        capi.check(capi.lib().fv_adjoint_create(solver._h, C.byref(h)))
+        capi.check(capi.lib().fv_adjoint_create(solver._h, 1 if full_limiter else 0, C.byref(h)))
         self._h = h
 
     def forward(self, U=None) -> np.ndarray:

@@ -260,7 +260,13 @@ int fv_batch_set_active(fv_solver_t s, int32_t instance, int32_t active);
  * --------------------------------------------------------------------- */
 typedef struct fv_adjoint_s* fv_adjoint_t;
 
-int fv_adjoint_create(fv_solver_t s, fv_adjoint_t* out);
+/* FROZEN: the limiter values are held at the linearisation state (the
+ * usual frozen-limiter adjoint); FULL: the limiter is differentiated too,
+ * through its active branch (neighbour extreme, face extrapolation extreme,
+ * Venkatakrishnan / Barth-Jespersen formula).  Shape gradients hold the
+ * limiter's own geometric inputs (face offsets, eps) fixed in both modes. */
+enum { FV_ADJ_FROZEN_LIMITER = 0, FV_ADJ_FULL_LIMITER = 1 };
+int fv_adjoint_create(fv_solver_t s, int32_t limiter_mode, fv_adjoint_t* out);
 int fv_adjoint_destroy(fv_adjoint_t a);
 /* Forward: linearise at U (NULL: the solver's current state) and return
  * R(U) (NULL: not returned). */
