@@ -315,6 +315,50 @@ def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 
     return out
 
 
+def adjoint_cost(iters: int = 200, warm: int = 300):
+    """Discrete adjoint against the primal on the 500k-cell NACA0012 O-grid
+    (1024 x 488), M 0.75, AoA 2 deg, 2nd-order HLLC + LSQ/Venkatakrishnan,
+    SSP-RK3 at CFL 1.2: wall time per primal iteration, per adjoint
+    iteration (frozen and full limiter) and of the linearisation.  The
+    adjoint iteration is the transposed linearised primal iteration, so it
+    converges at the primal's asymptotic rate and the cost of a converged
+    adjoint relative to a converged primal is the ratio at equal iteration
+    counts."""
+    import torch
+    from finitevolume_gb300 import meshgen, solvers as S
+    M, aoa = 0.75, 2.0
+    a = np.radians(aoa)
+    fs = (1.0, M * np.cos(a), M * np.sin(a), 1.0 / GAMMA)
+    mesh = S.Mesh(meshgen.cached("naca_ogrid", ni=1024, nj=488), reorder="morton")
+    s = _plain_solver(mesh, fs, False)
+    s.run(warm)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.run(iters)
+    tp = (time.perf_counter() - t0) / iters
+    ref = np.array([1.0, fs[1], fs[2], fs[3], 1.0, 0.25, 0.0])
+    out = {"workload": "naca0012 O-grid 1024x488, M 0.75, AoA 2, 2nd-order HLLC, Venkatakrishnan K=5",
+           "cells": mesh.n_cells, "primal_ms_per_iter": round(tp * 1e3, 4), "iterations_timed": iters}
+    for full in (False, True):
+        adj = S.DiscreteAdjoint(s, full_limiter=full)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        adj.forward()
+        tl = time.perf_counter() - t0
+        _, g = S.force_gradient(s, S.Objective.Drag, ref)
+        adj.solve(g, 3, 0.0)  # warm-up
+        t0 = time.perf_counter()
+        adj.solve(g, iters, 0.0)
+        ta = (time.perf_counter() - t0) / iters
+        key = "full_limiter" if full else "frozen_limiter"
+        out[key] = {"adjoint_ms_per_iter": round(ta * 1e3, 4), "linearise_ms": round(tl * 1e3, 2),
+                    "cost_vs_primal_per_iter": round(ta / tp, 3),
+                    "cost_vs_primal_1000_iters": round((tl + 1000 * ta) / (1000 * tp), 3)}
+        del adj
+    del s
+    return out
+
+
 def run_batched(args):
     """--batched: converged solves/s of the 256-instance family, FP64 and
     FP32-flux, batched vs plain sequential solves."""
@@ -560,6 +604,7 @@ def main():
                 "cells_total": int(sum(m.n_cells for m in bm)),
                 "workload": "256 NACA 4-digit O-grids, 4k-64k cells log-uniform, M 0.3-0.85, AoA -4..8"}
         del bm
+        variants["adjoint_500k"] = adjoint_cost()
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": world,
