@@ -199,6 +199,7 @@ def batch_throughput(meshes, fss, fp32: bool, iters: int):
     from finitevolume_gb300 import capi
     cells = sum(m.n_cells for m in meshes)
     b = _batch_solver(meshes, fss, fp32)
+    b.autotune(steps=2, cache=False)
     b.run(3)
     b.status()
     t0 = time.perf_counter()
@@ -495,6 +496,7 @@ def main():
     u_ptr, s_ptr = solver.device_state()
     stream = torch.cuda.ExternalStream(s_ptr)
 
+    launch = solver.autotune(steps=3, cache=False)  # launch shapes by timing, state restored
     solver.run(max(args.warmup, 3))  # warm-up through the graph path
 
     if world > 1:
@@ -569,6 +571,7 @@ def main():
         # FP32 flux/gradient arithmetic, FP64 accumulation/update/norms.
         a, _ = make_solver(poly)
         b, _ = make_solver(poly, fp32=True)
+        b.autotune(steps=3, cache=False)
         a.run(args.warmup)
         b.run(args.warmup)
         ms32, l32 = b.step_timed(args.steps)
@@ -614,6 +617,7 @@ def main():
                 "config": {"workload": "naca0012_mixed_1M_o2_hllc_lsq_venkat_rk3", "cells": n_cells,
                            "faces": n_faces, "mach": MACH, "aoa_deg": AOA_DEG, "cfl": CFL,
                            "l2": "inputs larger than L2 (working set > 400 MB), no flush",
+                           "launch_threads_per_block": {k: launch[k] for k in ("gradients", "faces", "cells")},
                            "parallelism": f"replicas{world}" if world > 1 else "single"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": int(np.sum(launches)), "variants": variants}

@@ -92,6 +92,8 @@ SIGNATURES = {
     "fv_set_field": (C.c_int, [_P, _D]),
     "fv_get_residual": (C.c_int, [_P, _D]),
     "fv_set_cfl": (C.c_int, [_P, C.c_double]),
+    "fv_solver_set_launch": (C.c_int, [_P, _I32]),
+    "fv_solver_autotune": (C.c_int, [_P, C.c_int32, _I32]),
     "fv_get_gamma": (C.c_int, [_P, _D]),
     "fv_device_state": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P)]),
     "fv_wall_forces": (C.c_int, [_P, _D, _D]),

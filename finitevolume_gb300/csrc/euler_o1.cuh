@@ -89,15 +89,17 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_face_o1(const O1Args a) {
 // norms, records the history row, and re-arms the control block.
 __device__ __forceinline__ void finish_norms(double s0, double s1, double s2, double s3, StepCtl* ctl,
                                              double* partials, double* hist, int hist_cap) {
-    __shared__ double red[fvgb::kCellBlock / 32][4];
+    // up to 512 threads per block (launch shapes are tunable)
+    __shared__ double red[16][4];
     __shared__ bool last;
+    const int nw = blockDim.x >> 5;
     s0 = warp_sum(s0); s1 = warp_sum(s1); s2 = warp_sum(s2); s3 = warp_sum(s3);
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) { red[w][0] = s0; red[w][1] = s1; red[w][2] = s2; red[w][3] = s3; }
     __syncthreads();
     if (threadIdx.x < 4) {
         double v = 0.0;
-        for (int i = 0; i < fvgb::kCellBlock / 32; ++i) v += red[i][threadIdx.x];
+        for (int i = 0; i < nw; ++i) v += red[i][threadIdx.x];
         partials[blockIdx.x * 4 + threadIdx.x] = v;
     }
     __threadfence();
@@ -121,7 +123,7 @@ __device__ __forceinline__ void finish_norms(double s0, double s1, double s2, do
         int bad = 0;
         for (int k = 0; k < 4; ++k) {
             double v = 0.0;
-            for (int i = 0; i < fvgb::kCellBlock / 32; ++i) v += red[i][k];
+            for (int i = 0; i < nw; ++i) v += red[i][k];
             n[k] = sqrt(v);
             if (!isfinite(n[k])) bad = 1;
             ctl->norms[k] = n[k];

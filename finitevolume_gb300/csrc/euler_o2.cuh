@@ -295,10 +295,10 @@ template <> struct OKey<float> {
 };
 
 // ---------------------------------------------------------------------------
-// Resident blocks per SM: FP32 mode is latency bound (4 blocks, <= 64
-// registers); FP64 mode needs 2 blocks to keep the FP64 pipe fed.
+// Register caps: FP32 mode is latency bound (<= 64 registers, 32 warps per
+// SM); FP64 mode <= 128 (16 warps keep the FP64 pipe fed).
 template <typename T, int GRAD, int LIM>
-__global__ void __launch_bounds__(fvgb::kCellBlock, sizeof(T) == 4 ? 4 : 2) k_grad(const O2Args a) {
+__global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_grad(const O2Args a) {
     using WS = WStore<T>;
     using WT = typename WS::type;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -469,7 +469,7 @@ __device__ __forceinline__ V4<T> num_flux_p(const V4<T>& L, const V4<T>& R, T nx
 
 // DT: 0 = no time step this stage, 1 = global (atomicMin), 2 = local (per face).
 template <typename T, int FLUX, int ORDER, int DT>
-__global__ void __launch_bounds__(fvgb::kFaceBlock) k_face(const O2Args a) {
+__global__ void __launch_bounds__(fvgb::kMaxBlock) k_face(const O2Args a) {
     using WS = WStore<T>;
     using WT = typename WS::type;
     using FT = typename std::conditional<std::is_same<T, double>::value, St, float4>::type;
@@ -522,21 +522,34 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_face(const O2Args a) {
         }
     }
     if (DT == 1) {
-        __shared__ double smin[fvgb::kFaceBlock / 32];
+        __shared__ double smin[fvgb::kMaxBlock / 32];
         cand = warp_min(cand);
         if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = cand;
         __syncthreads();
         if (threadIdx.x == 0) {
             double v = smin[0];
-            for (int w = 1; w < fvgb::kFaceBlock / 32; ++w) v = fmin(v, smin[w]);
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = fmin(v, smin[w]);
             atomicMin(&a.ctl->dt_bits, (unsigned long long)__double_as_longlong(v));
         }
     }
 }
 
+// FP32-flux mode: the primitive copy and the sound speed only feed FP32
+// arithmetic (fluxes, the wave speed of the time step), so they are derived
+// in FP32 from the state rounded on the integer pipe; nothing here issues
+// on the FP64 pipe.  Shared by the update and by the refresh after a state
+// upload, so both leave the same W.
+__device__ __forceinline__ V4<float> prim32(const St& un, float gf, float& cs) {
+    const float rf = fvconv::d2f(un.r), irf = 1.0f / rf;
+    const float uf = fvconv::d2f(un.ru) * irf, vf = fvconv::d2f(un.rv) * irf;
+    const float pf = (gf - 1.0f) * (fvconv::d2f(un.E) - 0.5f * rf * (uf * uf + vf * vf));
+    cs = sqrtf(gf * pf * irf);
+    return {rf, uf, vf, pf};
+}
+
 // STAGE: 0..NST-1; NST: 1 (forward Euler) or 3 (SSP-RK3); DT: 1 global, 2 local.
 template <typename T, int STAGE, int NST, int DT>
-__global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
+__global__ void __launch_bounds__(fvgb::kMaxBlock) k_update(const O2Args a) {
     using FT = typename std::conditional<std::is_same<T, double>::value, St, float4>::type;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
@@ -581,16 +594,9 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_update(const O2Args a) {
         st_state(a.U, c, un);
         const double g = a.gamma;
         if constexpr (std::is_same<T, float>::value) {
-            // FP32-flux mode: the primitive copy and the sound speed only
-            // feed FP32 arithmetic (fluxes, the wave speed of the time
-            // step), so they are derived in FP32 from the state rounded on
-            // the integer pipe; nothing here issues on the FP64 pipe.
-            const float gf = a.gamma32;
-            const float rf = fvconv::d2f(un.r), irf = 1.0f / rf;
-            const float uf = fvconv::d2f(un.ru) * irf, vf = fvconv::d2f(un.rv) * irf;
-            const float pf = (gf - 1.0f) * (fvconv::d2f(un.E) - 0.5f * rf * (uf * uf + vf * vf));
-            WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{rf, uf, vf, pf});
-            if (STAGE == NST - 1) static_cast<float*>(a.cs)[c] = sqrtf(gf * pf * irf);
+            float cs;
+            WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, prim32(un, a.gamma32, cs));
+            if (STAGE == NST - 1) static_cast<float*>(a.cs)[c] = cs;
         } else {
             const double ir = 1.0 / un.r;
             const double uu = un.ru * ir, vv = un.rv * ir;
@@ -647,11 +653,12 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_prim(const O2Args a) {
     const double ir = 1.0 / un.r;
     const double uu = un.ru * ir, vv = un.rv * ir;
     const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
-    WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{(T)un.r, (T)uu, (T)vv, (T)p});
     if constexpr (std::is_same<T, float>::value) {
-        const float rf = (float)un.r, pf = (float)p;
-        static_cast<float*>(a.cs)[c] = sqrtf(a.gamma32 * pf / rf);
+        float cs;
+        WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, prim32(un, a.gamma32, cs));
+        static_cast<float*>(a.cs)[c] = cs;
     } else {
+        WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{(T)un.r, (T)uu, (T)vv, (T)p});
         static_cast<double*>(a.cs)[c] = sqrt(g * p * ir);
     }
 }

@@ -9,24 +9,24 @@ using fvgb::O2Args;
 using fvgb::O2Config;
 
 template <int GRAD, int LIM>
-void grad(const O2Args& a, cudaStream_t s) {
-    const int cb = (a.m.n_cells + fvgb::kCellBlock - 1) / fvgb::kCellBlock;
-    k_grad<R, GRAD, LIM><<<cb, fvgb::kCellBlock, 0, s>>>(a);
+void grad(const O2Args& a, int bs, cudaStream_t s) {
+    const int cb = (a.m.n_cells + bs - 1) / bs;
+    k_grad<R, GRAD, LIM><<<cb, bs, 0, s>>>(a);
 }
 
 template <int FLUX, int ORDER>
-void face(const O2Args& a, int dt, cudaStream_t s) {
-    const int fb = (a.m.n_faces + fvgb::kFaceBlock - 1) / fvgb::kFaceBlock;
-    if (dt == 1) k_face<R, FLUX, ORDER, 1><<<fb, fvgb::kFaceBlock, 0, s>>>(a);
-    else if (dt == 2) k_face<R, FLUX, ORDER, 2><<<fb, fvgb::kFaceBlock, 0, s>>>(a);
-    else k_face<R, FLUX, ORDER, 0><<<fb, fvgb::kFaceBlock, 0, s>>>(a);
+void face(const O2Args& a, int dt, int bs, cudaStream_t s) {
+    const int fb = (a.m.n_faces + bs - 1) / bs;
+    if (dt == 1) k_face<R, FLUX, ORDER, 1><<<fb, bs, 0, s>>>(a);
+    else if (dt == 2) k_face<R, FLUX, ORDER, 2><<<fb, bs, 0, s>>>(a);
+    else k_face<R, FLUX, ORDER, 0><<<fb, bs, 0, s>>>(a);
 }
 
 template <int ST, int NST>
-void update(const O2Args& a, int local, cudaStream_t s) {
-    const int cb = (a.m.n_cells + fvgb::kCellBlock - 1) / fvgb::kCellBlock;
-    if (local) k_update<R, ST, NST, 2><<<cb, fvgb::kCellBlock, 0, s>>>(a);
-    else k_update<R, ST, NST, 1><<<cb, fvgb::kCellBlock, 0, s>>>(a);
+void update(const O2Args& a, int local, int bs, cudaStream_t s) {
+    const int cb = (a.m.n_cells + bs - 1) / bs;
+    if (local) k_update<R, ST, NST, 2><<<cb, bs, 0, s>>>(a);
+    else k_update<R, ST, NST, 1><<<cb, bs, 0, s>>>(a);
 }
 }  // namespace
 
@@ -42,28 +42,28 @@ void launch_part_f32(const O2Args& a, const O2Config& c, int stage, int part, cu
     if (part == 0) {
         if (c.order != 2) return;
         switch (c.gradient * 3 + c.limiter) {
-            case 0: grad<0, 0>(a, s); break;
-            case 1: grad<0, 1>(a, s); break;
-            case 2: grad<0, 2>(a, s); break;
-            case 3: grad<1, 0>(a, s); break;
-            case 4: grad<1, 1>(a, s); break;
-            default: grad<1, 2>(a, s); break;
+            case 0: grad<0, 0>(a, c.blk_grad, s); break;
+            case 1: grad<0, 1>(a, c.blk_grad, s); break;
+            case 2: grad<0, 2>(a, c.blk_grad, s); break;
+            case 3: grad<1, 0>(a, c.blk_grad, s); break;
+            case 4: grad<1, 1>(a, c.blk_grad, s); break;
+            default: grad<1, 2>(a, c.blk_grad, s); break;
         }
     } else if (part == 1) {
         const int dt = stage == 0 ? (c.local_dt ? 2 : 1) : 0;
         switch (c.flux * 2 + (c.order == 2 ? 1 : 0)) {
-            case 0: face<0, 1>(a, dt, s); break;
-            case 1: face<0, 2>(a, dt, s); break;
-            case 2: face<1, 1>(a, dt, s); break;
-            case 3: face<1, 2>(a, dt, s); break;
-            case 4: face<2, 1>(a, dt, s); break;
-            default: face<2, 2>(a, dt, s); break;
+            case 0: face<0, 1>(a, dt, c.blk_face, s); break;
+            case 1: face<0, 2>(a, dt, c.blk_face, s); break;
+            case 2: face<1, 1>(a, dt, c.blk_face, s); break;
+            case 3: face<1, 2>(a, dt, c.blk_face, s); break;
+            case 4: face<2, 1>(a, dt, c.blk_face, s); break;
+            default: face<2, 2>(a, dt, c.blk_face, s); break;
         }
     } else {
-        if (c.stages == 1) update<0, 1>(a, c.local_dt, s);
-        else if (stage == 0) update<0, 3>(a, c.local_dt, s);
-        else if (stage == 1) update<1, 3>(a, c.local_dt, s);
-        else update<2, 3>(a, c.local_dt, s);
+        if (c.stages == 1) update<0, 1>(a, c.local_dt, c.blk_cell, s);
+        else if (stage == 0) update<0, 3>(a, c.local_dt, c.blk_cell, s);
+        else if (stage == 1) update<1, 3>(a, c.local_dt, c.blk_cell, s);
+        else update<2, 3>(a, c.local_dt, c.blk_cell, s);
     }
 }
 

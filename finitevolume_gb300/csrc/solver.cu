@@ -102,6 +102,7 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     cfg.limiter = opt.limiter;
     cfg.stages = opt.rk_stages;
     cfg.local_dt = opt.dt_mode == FV_DT_LOCAL;
+    cfg.blk_grad = cfg.blk_face = cfg.blk_cell = 256;
     gamma = g;
     N = hm.n_cells;
     F = hm.n_faces;
@@ -155,7 +156,8 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     if (!(general && cfg.fp32)) ff = dalloc<St>(F, owned);
     dtf = dalloc<double>(F, owned);
     n_cell_blocks = (N + kCellBlock - 1) / kCellBlock;
-    partials = dalloc<double>(4 * (size_t)n_cell_blocks, owned);
+    // sized for the smallest tunable cell block
+    partials = dalloc<double>(4 * (size_t)((N + kMinBlock - 1) / kMinBlock), owned);
     ctl = dalloc<StepCtl>(1, owned);
     StepCtl c0;
     std::memset(&c0, 0, sizeof(c0));
@@ -503,6 +505,62 @@ void Solver::upload_field(const void* in_ref_order) {
     FV_CUDA(cudaStreamSynchronize(stream));
 }
 
+void Solver::set_launch(int bg, int bf, int bc) {
+    for (int b : {bg, bf, bc})
+        if (b < kMinBlock || b > kMaxBlock || b % 32 != 0)
+            raise(FV_ERR_BAD_ARG, "launch shape: 128..512 threads per block, a multiple of 32");
+    if (!general || viscous) raise(FV_ERR_UNSUPPORTED, "launch shapes apply to the second-order / multi-stage path");
+    FV_CUDA(cudaStreamSynchronize(stream));
+    cfg.blk_grad = bg;
+    cfg.blk_face = bf;
+    cfg.blk_cell = bc;
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+}
+
+void Solver::autotune(int n, int out[3]) {
+    if (n <= 0) raise(FV_ERR_BAD_ARG, "autotune needs n > 0");
+    if (!general || viscous) raise(FV_ERR_UNSUPPORTED, "autotune applies to the second-order / multi-stage path");
+    // save the state the trial steps change
+    FV_CUDA(cudaStreamSynchronize(stream));
+    StepCtl c0;
+    read_ctl(c0);
+    FV_CUDA(cudaMemcpyAsync(staging, U, sizeof(St) * (size_t)N, cudaMemcpyDeviceToDevice, stream));
+    std::vector<int> act, it;
+    std::vector<double> nrm;
+    if (batch) {
+        act.resize(n_inst); it.resize(n_inst); nrm.resize(4 * (size_t)n_inst);
+        FV_CUDA(cudaMemcpy(act.data(), active, sizeof(int) * n_inst, cudaMemcpyDeviceToHost));
+        FV_CUDA(cudaMemcpy(it.data(), inst_iter, sizeof(int) * n_inst, cudaMemcpyDeviceToHost));
+        FV_CUDA(cudaMemcpy(nrm.data(), inst_norms, sizeof(double) * nrm.size(), cudaMemcpyDeviceToHost));
+    }
+    const int cand[3] = {128, 256, 512};
+    double best[3] = {1e300, 1e300, 1e300};
+    int pick[3] = {256, 256, 256};
+    for (int b : cand) {
+        set_launch(b, b, b);
+        double ms[3];
+        int l[3];
+        step_timed(1, ms, l);  // warm-up at this shape
+        step_timed(n, ms, l);
+        for (int k = 0; k < 3; ++k)
+            if (l[k] > 0 && ms[k] < best[k]) { best[k] = ms[k]; pick[k] = b; }
+    }
+    set_launch(pick[0], pick[1], pick[2]);
+    // restore
+    FV_CUDA(cudaMemcpyAsync(U, staging, sizeof(St) * (size_t)N, cudaMemcpyDeviceToDevice, stream));
+    FV_CUDA(cudaMemcpyAsync(ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice, stream));
+    if (batch) {
+        FV_CUDA(cudaMemcpyAsync(active, act.data(), sizeof(int) * n_inst, cudaMemcpyHostToDevice, stream));
+        FV_CUDA(cudaMemcpyAsync(inst_iter, it.data(), sizeof(int) * n_inst, cudaMemcpyHostToDevice, stream));
+        FV_CUDA(cudaMemcpyAsync(inst_norms, nrm.data(), sizeof(double) * nrm.size(), cudaMemcpyHostToDevice, stream));
+    }
+    refresh_primitives();
+    FV_CUDA(cudaStreamSynchronize(stream));
+    steps_taken -= (long long)3 * (n + 1);
+    for (int k = 0; k < 3; ++k) out[k] = pick[k];
+}
+
 void Solver::set_cfl(double cfl) {
     FV_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(ctl) + offsetof(StepCtl, cfl), &cfl, sizeof(cfl),
                             cudaMemcpyHostToDevice, stream));
@@ -777,6 +835,23 @@ int fv_get_residual(fv_solver_t s, double norms[4]) {
         fvgb::StepCtl c;
         s->s.read_ctl(c);
         for (int k = 0; k < 4; ++k) norms[k] = c.norms[k];
+    });
+}
+
+int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]) {
+    return guarded([&] {
+        if (!s || !blocks) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        s->s.set_launch(blocks[0], blocks[1], blocks[2]);
+    });
+}
+
+int fv_solver_autotune(fv_solver_t s, int32_t steps, int32_t blocks[3]) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        int b[3];
+        s->s.autotune(steps, b);
+        if (blocks)
+            for (int k = 0; k < 3; ++k) blocks[k] = b[k];
     });
 }
 

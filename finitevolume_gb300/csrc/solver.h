@@ -99,6 +99,11 @@ struct Solver {
     void download_field(double* out);
     void upload_field(const void* in_ref_order);
     void set_cfl(double cfl);
+    // launch shapes of the second-order kernels (gradients, faces, cells)
+    void set_launch(int bg, int bf, int bc);
+    // time each kernel class at 128/256/512 threads per block for n steps
+    // (state restored afterwards) and keep the fastest shape per class
+    void autotune(int n, int out[3]);
     void set_stream(void* s);
     void wall_forces(const double ref[7], double out[11], int instance = -1);
 };

@@ -117,10 +117,15 @@ struct O2Config {
     int limiter;   // 0 none, 1 Barth-Jespersen, 2 Venkatakrishnan
     int stages;    // 1 or 3
     int local_dt;  // 1 local, 0 global
+    // launch shapes (threads per block, 128..512, multiple of 32), chosen by
+    // the autotuner; 256 by default
+    int blk_grad, blk_face, blk_cell;
 };
 
 constexpr int kCellBlock = 256;
 constexpr int kFaceBlock = 256;
+constexpr int kMaxBlock = 512;  // largest tunable block of the second-order kernels
+constexpr int kMinBlock = 128;  // smallest (sizes the norm partials)
 
 namespace o2 {
 void launch_prim_f64(const O2Args& a, cudaStream_t s);

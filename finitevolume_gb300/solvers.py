@@ -171,6 +171,45 @@ def _ic_struct(ic: EulerInitialCondition) -> capi.IC:
     return s
 
 
+def _launch_cache_path() -> str:
+    import os
+    root = os.environ.get("FV_MESH_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "finitevolume_gb300"))
+    return os.path.join(root, "launch_shapes.json")
+
+
+def _autotune(handle, key: str, steps: int, cache: bool) -> dict:
+    """Launch shapes from the cache, or tuned on this solver and cached."""
+    import json
+    import os
+    path = _launch_cache_path()
+    table = {}
+    if cache and os.path.exists(path):
+        try:
+            with open(path) as f:
+                table = json.load(f)
+        except (OSError, ValueError):
+            table = {}
+    if cache and key in table:
+        b = np.array(table[key], dtype=np.int32)
+        capi.check(capi.lib().fv_solver_set_launch(handle, capi.i32ptr(b)))
+        return {"gradients": int(b[0]), "faces": int(b[1]), "cells": int(b[2]), "cached": True}
+    b = np.zeros(3, np.int32)
+    capi.check(capi.lib().fv_solver_autotune(handle, int(steps), capi.i32ptr(b)))
+    if cache:
+        table[key] = b.tolist()
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + f".{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
+            json.dump(table, f)
+        os.replace(tmp, path)
+    return {"gradients": int(b[0]), "faces": int(b[1]), "cells": int(b[2]), "cached": False}
+
+
+def _shape_key(o, n_cells: int, batch: bool) -> str:
+    return (f"p{o.precision}-o{o.order}-f{o.flux}-g{o.gradient}-l{o.limiter}-rk{o.rk_stages}-dt{o.dt_mode}"
+            f"-b{int(batch)}-n{int(np.log2(max(n_cells, 1)))}")
+
+
 class EulerFVMSolver:
     """GPU explicit Euler solver with the reference's constructor and methods."""
 
@@ -246,6 +285,16 @@ class EulerFVMSolver:
         return g.value
 
     # -- extensions ----------------------------------------------------------
+    def set_launch(self, gradients: int, faces: int, cells: int) -> None:
+        """Threads per block of the gradient, face and cell kernels."""
+        b = np.array([gradients, faces, cells], np.int32)
+        capi.check(capi.lib().fv_solver_set_launch(self._h, capi.i32ptr(b)))
+
+    def autotune(self, steps: int = 5, cache: bool = True) -> dict:
+        """Pick the launch shapes by timing (state preserved); results are
+        cached per scheme and mesh-size octave."""
+        return _autotune(self._h, _shape_key(self._opt, self.n_cells, False), steps, cache)
+
     def step_async(self, n: int) -> None:
         capi.check(capi.lib().fv_step_async(self._h, int(n)))
 
@@ -532,6 +581,7 @@ class BatchSolver:
         o.flux, o.order, o.rk_stages, o.dt_mode = int(flux_scheme), int(order), int(rk_stages), 1
         o.gradient, o.limiter, o.venkat_k = int(gradient), int(limiter), float(venkat_k)
         o.precision = 1 if fp32_flux else 0
+        self._opt = o
         h = C.c_void_p()
         capi.check(capi.lib().fv_batch_create(self.mesh.handle, bc, len(boundary_types), capi.dptr(fs), float(gamma),
                                               float(cfl), C.byref(o), C.byref(h)))
@@ -540,6 +590,10 @@ class BatchSolver:
 
     def set_tolerance(self, tol: float) -> None:
         capi.check(capi.lib().fv_batch_set_tolerance(self._h, float(tol)))
+
+    def autotune(self, steps: int = 5, cache: bool = True) -> dict:
+        """Launch shapes of the batched kernels chosen by timing (state preserved)."""
+        return _autotune(self._h, _shape_key(self._opt, self.mesh.n_cells, True), steps, cache)
 
     def run(self, n: int) -> None:
         capi.check(capi.lib().fv_step(self._h, int(n), None))

@@ -194,6 +194,16 @@ int fv_step_timed(fv_solver_t s, int32_t n, double kernel_ms[3], int32_t launche
 /* Copy the last n residual-norm rows recorded on the device (n x 4). */
 int fv_get_history(fv_solver_t s, int32_t n, double* history);
 
+/* Launch shapes (threads per block of the gradient, face and cell kernels:
+ * 128..512, multiples of 32) of the second-order / multi-stage path, and
+ * the autotuner that picks them: each kernel class is timed over `steps`
+ * steps at 128, 256 and 512 threads per block (CUDA events on the solver's
+ * stream), the fastest shape per class is kept, and the solver's state is
+ * restored afterwards.  No reference counterpart (the reference's loops are
+ * OpenMP). */
+int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]);
+int fv_solver_autotune(fv_solver_t s, int32_t steps, int32_t blocks[3]);
+
 /* EulerFVMSolver::field / set_field / residual / set_cfl / gas_gamma
  * (include/EulerFVMSolver.h:121-160). */
 int fv_get_field(fv_solver_t s, double* U);
