@@ -32,7 +32,7 @@ class FVError(RuntimeError):
 
 class BC(C.Structure):
     _fields_ = [("type", C.c_int32), ("isothermal", C.c_int32), ("state", C.c_double * 4),
-                ("wall_u", C.c_double), ("wall_v", C.c_double), ("wall_T", C.c_double)]
+                ("wall_u", C.c_double), ("wall_v", C.c_double), ("wall_T", C.c_double), ("nut", C.c_double)]
 
 
 class IC(C.Structure):
@@ -48,7 +48,8 @@ class Options(C.Structure):
                 ("venkat_k", C.c_double), ("rk_stages", C.c_int32), ("dt_mode", C.c_int32),
                 ("precision", C.c_int32), ("strict", C.c_int32), ("exact_tol", C.c_double),
                 ("exact_max_iter", C.c_int32), ("viscous", C.c_int32), ("gas_constant", C.c_double),
-                ("mu", C.c_double), ("prandtl", C.c_double)]
+                ("mu", C.c_double), ("prandtl", C.c_double), ("prandtl_t", C.c_double),
+                ("initial_nut", C.c_double), ("sa", C.c_double * 9)]
 
 
 class NoAllocMesh(C.Structure):
@@ -92,6 +93,10 @@ SIGNATURES = {
     "fv_set_field": (C.c_int, [_P, _D]),
     "fv_get_residual": (C.c_int, [_P, _D]),
     "fv_set_cfl": (C.c_int, [_P, C.c_double]),
+    "fv_get_nut": (C.c_int, [_P, _D]),
+    "fv_set_nut": (C.c_int, [_P, _D]),
+    "fv_get_nut_residual": (C.c_int, [_P, _D]),
+    "fv_get_wall_distance": (C.c_int, [_P, _D]),
     "fv_solver_set_launch": (C.c_int, [_P, _I32]),
     "fv_solver_autotune": (C.c_int, [_P, C.c_int32, _I32]),
     "fv_get_gamma": (C.c_int, [_P, _D]),

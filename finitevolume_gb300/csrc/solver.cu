@@ -58,6 +58,7 @@ Solver::~Solver() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     for (void* p : owned) cudaFree(p);
     if (hist) cudaFree(hist);
+    if (nut_hist) cudaFree(nut_hist);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -90,7 +91,11 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
                                   "global dt, FP64");
     if (opt.viscous && !(opt.gas_constant > 0.0 && opt.prandtl > 0.0 && opt.mu >= 0.0))
         raise(FV_ERR_BAD_ARG, "viscous solver needs gas_constant > 0, prandtl > 0, mu >= 0");
+    if (opt.viscous < 0 || opt.viscous > 2) raise(FV_ERR_BAD_ARG, "viscous: 0 Euler, 1 Navier-Stokes, 2 RANS-SA");
+    if (opt.viscous == 2 && !(opt.mu > 0.0 && opt.prandtl_t > 0.0 && opt.initial_nut >= 0.0))
+        raise(FV_ERR_BAD_ARG, "RANS-SA needs mu > 0, prandtl_t > 0, initial_nut >= 0");
     viscous = opt.viscous != 0;
+    rans = opt.viscous == 2;
     general = batch || (!viscous && !(opt.order == 1 && opt.rk_stages == 1 && opt.precision == FV_PREC_FP64));
     if (general && opt.strict) raise(FV_ERR_UNSUPPORTED, "strict mode covers the reference's first-order scheme only");
     if (general && opt.precision == FV_PREC_FP32_FLUX && opt.flux == FV_FLUX_EXACT)
@@ -259,6 +264,48 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         ns_wall_out = dalloc<double2>(wf.size(), owned);
     }
 
+    if (rans) {
+        // RANSTurbulenceSASolver ctor: uniform initial nu-tilde, the wall
+        // distance from the no-slip faces (compute_wall_distance), model
+        // constants and effective-conductivity factors.
+        RansArgs& r = rs;
+        r.cf_off = m.cf_off;
+        r.cf = m.cf;
+        r.vol = m.vol;
+        r.cxy = m.cxy;
+        r.nut = dupload(std::vector<double>(N, opt.initial_nut), owned);
+        r.nut_ff = dalloc<double>(F, owned);
+        r.nu = dalloc<double2>(N, owned);
+        r.grad = dalloc<double2>(4 * (size_t)N, owned);
+        r.walld = dalloc<double>(N, owned);
+        r.partials = dalloc<double>(5 * (size_t)n_cell_blocks, owned);
+        r.nut_norm = dupload(std::vector<double>(1, 0.0), owned);
+        for (int p = 0; p < kMaxPatches; ++p) r.farfield_nut[p] = p < hm.n_patches ? bcs[p].nut : 0.0;
+        for (int i = 0; i < 9; ++i) r.sa[i] = opt.sa[i];
+        r.cp = gamma * opt.gas_constant / (gamma - 1.0);
+        r.prandtl = opt.prandtl;
+        r.prandtl_t = opt.prandtl_t;
+        std::vector<double4_32a> seg;
+        for (int f = 0; f < F; ++f) {
+            if (hm.fr[f] >= 0 || bc.type[hm.fpatch[f]] != FV_BC_NOSLIP) continue;
+            double4_32a q;
+            q.x = hm.nx_[hm.fn1[f]]; q.y = hm.ny_[hm.fn1[f]];
+            q.z = hm.nx_[hm.fn2[f]]; q.w = hm.ny_[hm.fn2[f]];
+            seg.push_back(q);
+        }
+        if (seg.empty()) {
+            // no wall: infinite distance, as compute_wall_distance
+            FV_CUDA(cudaMemcpy(r.walld, std::vector<double>(N, INFINITY).data(), sizeof(double) * N,
+                               cudaMemcpyHostToDevice));
+        } else {
+            double4_32a* d_seg = dupload(seg, owned);
+            RansArgs tmp = rans_args();
+            rans_wall_distance(tmp, d_seg, (int)seg.size(), stream);
+            FV_CUDA(cudaGetLastError());
+            FV_CUDA(cudaStreamSynchronize(stream));
+        }
+    }
+
     // Initial condition, reference numbering then device order
     // (src/EulerFVMSolver.cpp:24-37).
     std::vector<St> u0(N);
@@ -293,8 +340,24 @@ void Solver::ensure_history(int n) {
     if (hist) cudaFree(hist);
     hist = h;
     hist_cap = cap;
+    if (rans) {
+        double* nh = nullptr;
+        FV_CUDA(cudaMalloc(&nh, sizeof(double) * (size_t)cap));
+        FV_CUDA(cudaMemset(nh, 0, sizeof(double) * (size_t)cap));
+        if (nut_hist) cudaFree(nut_hist);
+        nut_hist = nh;
+    }
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
+}
+
+RansArgs Solver::rans_args() const {
+    RansArgs r = rs;
+    r.ns = ns;
+    r.hist = hist;
+    r.hist_cap = hist_cap;
+    r.nut_hist = nut_hist;
+    return r;
 }
 
 O1Args Solver::o1_args() const {
@@ -371,6 +434,11 @@ void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* ev
         if (classes) classes->push_back(cls);
         if (events) FV_CUDA(cudaEventRecord((*events)[++*ev_pos], stream));
     };
+    if (rans) {
+        rans_launch_step(rans_args(), stream);
+        mark(1);
+        return;
+    }
     if (viscous) {
         // NS step: prim + gradients + face fluxes + cell pass, timed as one.
         ns_launch_step(ns, o1_args(), stream);
@@ -591,7 +659,8 @@ void Solver::wall_forces(const double ref[7], double out[11], int instance) {
     std::vector<double> tau(nw, 0.0), pw(nw, 0.0);
     if (viscous) {
         std::vector<double2> tp(nw);
-        ns_launch_wall(ns, ns_wall_faces, (int)nw, ns_wall_out, stream);
+        if (rans) rans_launch_wall(rans_args(), ns_wall_faces, (int)nw, ns_wall_out, stream);
+        else ns_launch_wall(ns, ns_wall_faces, (int)nw, ns_wall_out, stream);
         FV_CUDA(cudaGetLastError());
         if (nw) FV_CUDA(cudaMemcpyAsync(tp.data(), ns_wall_out, sizeof(double2) * nw, cudaMemcpyDeviceToHost, stream));
         FV_CUDA(cudaStreamSynchronize(stream));
@@ -750,6 +819,11 @@ void fv_options_default(fv_options_t* o) {
     o->gas_constant = 287.0;
     o->mu = 0.0;
     o->prandtl = 0.72;
+    o->prandtl_t = 0.9;
+    o->initial_nut = 0.0;
+    // SAModelConstants defaults (include/SpalartAllmaras.h:13-23)
+    const double sa[9] = {0.1355, 0.622, 2.0 / 3.0, 0.41, 0.3, 2.0, 7.1, 0.7, 0.9};
+    for (int i = 0; i < 9; ++i) o->sa[i] = sa[i];
 }
 
 int fv_solver_create(fv_mesh_t mesh, const fv_bc_t* bcs, int32_t n_bcs, double gamma, double cfl, const fv_ic_t* ic,
@@ -852,6 +926,52 @@ int fv_solver_autotune(fv_solver_t s, int32_t steps, int32_t blocks[3]) {
         s->s.autotune(steps, b);
         if (blocks)
             for (int k = 0; k < 3; ++k) blocks[k] = b[k];
+    });
+}
+
+static void get_cell_scalar(Solver& v, const double* dev, double* out) {
+    std::vector<double> d(v.N);
+    FV_CUDA(cudaStreamSynchronize(v.stream));
+    FV_CUDA(cudaMemcpy(d.data(), dev, sizeof(double) * v.N, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < v.N; ++i) out[v.perm[i]] = d[i];
+}
+
+int fv_get_nut(fv_solver_t s, double* nut) {
+    return guarded([&] {
+        if (!s || !nut) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (!s->s.rans) fvgb::raise(FV_ERR_UNSUPPORTED, "not a RANS-SA solver");
+        get_cell_scalar(s->s, s->s.rs.nut, nut);
+    });
+}
+
+int fv_set_nut(fv_solver_t s, const double* nut) {
+    return guarded([&] {
+        if (!s || !nut) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        Solver& v = s->s;
+        if (!v.rans) fvgb::raise(FV_ERR_UNSUPPORTED, "not a RANS-SA solver");
+        std::vector<double> d(v.N);
+        for (int i = 0; i < v.N; ++i) d[i] = nut[v.perm[i]];
+        FV_CUDA(cudaStreamSynchronize(v.stream));
+        FV_CUDA(cudaMemcpy(v.rs.nut, d.data(), sizeof(double) * v.N, cudaMemcpyHostToDevice));
+        const double z = 0.0;
+        FV_CUDA(cudaMemcpy(v.rs.nut_norm, &z, sizeof(z), cudaMemcpyHostToDevice));
+    });
+}
+
+int fv_get_nut_residual(fv_solver_t s, double* norm) {
+    return guarded([&] {
+        if (!s || !norm) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (!s->s.rans) fvgb::raise(FV_ERR_UNSUPPORTED, "not a RANS-SA solver");
+        FV_CUDA(cudaStreamSynchronize(s->s.stream));
+        FV_CUDA(cudaMemcpy(norm, s->s.rs.nut_norm, sizeof(double), cudaMemcpyDeviceToHost));
+    });
+}
+
+int fv_get_wall_distance(fv_solver_t s, double* d) {
+    return guarded([&] {
+        if (!s || !d) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (!s->s.rans) fvgb::raise(FV_ERR_UNSUPPORTED, "not a RANS-SA solver");
+        get_cell_scalar(s->s, s->s.rs.walld, d);
     });
 }
 

@@ -7,6 +7,7 @@
 #include "../../include/fv_gb300.h"
 #include "mesh_host.h"
 #include "ns.h"
+#include "rans.h"
 #include "types.h"
 
 namespace fvgb {
@@ -53,8 +54,11 @@ struct Solver {
     double4_32a* r2 = nullptr;
     double tol = -1.0;                // density-norm tolerance; < 0 never freezes
 
-    // Navier-Stokes path
+    // Navier-Stokes path (and RANS-SA on top of it)
     bool viscous = false;
+    bool rans = false;
+    RansArgs rs{};
+    double* nut_hist = nullptr;
     NSArgs ns{};
     int* ns_wall_faces = nullptr;   // device indices of the wall faces, reference order
     double2* ns_wall_out = nullptr; // (tau_wall, p) per wall face
@@ -88,6 +92,7 @@ struct Solver {
               const fv_options_t& o, const double* batch_freestream = nullptr);
     void ensure_history(int n);
     O1Args o1_args() const;
+    RansArgs rans_args() const;
     O2Args o2_args() const;
     void refresh_primitives();
     void launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos);

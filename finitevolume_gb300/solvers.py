@@ -218,7 +218,7 @@ class EulerFVMSolver:
                  flux_scheme: NumericalFluxScheme = NumericalFluxScheme.Rusanov, exact_riemann_tol: float = 1e-6,
                  exact_riemann_max_iter: int = 20, *, order: int = 1, rk_stages: int = 1, local_dt: bool = False,
                  gradient: GradientScheme = GradientScheme.LeastSquares, limiter: Limiter = Limiter.Venkatakrishnan,
-                 venkat_k: float = 5.0, fp32_flux: bool = False, strict: bool = False, _viscous=None):
+                 venkat_k: float = 5.0, fp32_flux: bool = False, strict: bool = False, _viscous=None, _rans=None):
         if not isinstance(input_mesh, Mesh):
             input_mesh = Mesh(input_mesh)
         self.mesh = input_mesh
@@ -227,6 +227,12 @@ class EulerFVMSolver:
         if _viscous is not None:
             o.viscous = 1
             o.gas_constant, o.mu, o.prandtl = (float(x) for x in _viscous)
+        if _rans is not None:
+            o.viscous = 2
+            o.prandtl_t = float(_rans["prandtl_t"])
+            o.initial_nut = float(_rans["initial_nut"])
+            for i, v in enumerate(_rans["sa"]):
+                o.sa[i] = float(v)
         o.flux = int(flux_scheme)
         o.exact_tol = float(exact_riemann_tol)
         o.exact_max_iter = int(exact_riemann_max_iter)
@@ -682,6 +688,77 @@ class NavierStokesFVMSolver(EulerFVMSolver):
                 arr[i].state[k] = float(b.farfield_state[k])
         super().__init__(input_mesh, arr, gamma, cfl, initial_condition, flux_scheme, exact_riemann_tol,
                          exact_riemann_max_iter, gradient=gradient_scheme, _viscous=(gas_constant, mu, prandtl))
+
+
+@dataclasses.dataclass
+class SAModelConstants:
+    """SA-noft2 model constants (include/SpalartAllmaras.h:13-23)."""
+    cb1: float = 0.1355
+    cb2: float = 0.622
+    sigma: float = 2.0 / 3.0
+    kappa: float = 0.41
+    cw2: float = 0.3
+    cw3: float = 2.0
+    cv1: float = 7.1
+    cv2: float = 0.7
+    cv3: float = 0.9
+
+    def as_list(self):
+        return [self.cb1, self.cb2, self.sigma, self.kappa, self.cw2, self.cw3, self.cv1, self.cv2, self.cv3]
+
+
+@dataclasses.dataclass
+class RANSBoundaryConditionSA:
+    """include/RANSTurbulenceSASolver.h: the mean-flow condition plus the
+    freestream nu-tilde of a farfield patch."""
+    ns: NSBoundaryCondition = dataclasses.field(default_factory=NSBoundaryCondition)
+    farfield_nut: float = 0.0
+
+
+class RANSTurbulenceSASolver(EulerFVMSolver):
+    """GPU RANS solver with the Spalart-Allmaras model and the reference's
+    constructor and methods (include/RANSTurbulenceSASolver.h): the
+    Navier-Stokes scheme with mu + rho nu_t, plus the transported nu-tilde."""
+
+    def __init__(self, input_mesh: Mesh, boundary_conditions: Sequence[RANSBoundaryConditionSA], gamma: float,
+                 gas_constant: float, mu: float, prandtl: float, prandtl_t: float, cfl: float,
+                 initial_condition: EulerInitialCondition, initial_nut: float,
+                 flux_scheme: NumericalFluxScheme = NumericalFluxScheme.Rusanov,
+                 gradient_scheme: GradientScheme = GradientScheme.LeastSquares, exact_riemann_tol: float = 1e-6,
+                 exact_riemann_max_iter: int = 20, sa_constants: SAModelConstants = None):
+        arr = (capi.BC * max(1, len(boundary_conditions)))()
+        for i, rb in enumerate(boundary_conditions):
+            b = rb.ns
+            arr[i].type = _NS_TO_ABI[NSBoundaryType(b.type)]
+            arr[i].isothermal = 1 if b.is_isothermal_wall else 0
+            arr[i].wall_u, arr[i].wall_v, arr[i].wall_T = float(b.wall_u), float(b.wall_v), float(b.wall_temperature)
+            for k in range(4):
+                arr[i].state[k] = float(b.farfield_state[k])
+            arr[i].nut = float(rb.farfield_nut)
+        sa = (sa_constants or SAModelConstants()).as_list()
+        super().__init__(input_mesh, arr, gamma, cfl, initial_condition, flux_scheme, exact_riemann_tol,
+                         exact_riemann_max_iter, gradient=gradient_scheme, _viscous=(gas_constant, mu, prandtl),
+                         _rans={"prandtl_t": prandtl_t, "initial_nut": initial_nut, "sa": sa})
+
+    def nut_field(self) -> np.ndarray:
+        out = np.zeros(self.n_cells)
+        capi.check(capi.lib().fv_get_nut(self._h, capi.dptr(out)))
+        return out
+
+    def set_field(self, new_U: np.ndarray, new_nut: np.ndarray = None) -> None:
+        super().set_field(new_U)
+        if new_nut is not None:
+            capi.check(capi.lib().fv_set_nut(self._h, capi.dptr(np.ascontiguousarray(new_nut, dtype=np.float64))))
+
+    def nut_residual(self) -> float:
+        r = C.c_double()
+        capi.check(capi.lib().fv_get_nut_residual(self._h, C.byref(r)))
+        return r.value
+
+    def wall_distance(self) -> np.ndarray:
+        out = np.zeros(self.n_cells)
+        capi.check(capi.lib().fv_get_wall_distance(self._h, capi.dptr(out)))
+        return out
 
 
 class GradientCalculator:

@@ -126,6 +126,7 @@ typedef struct {
     int32_t isothermal;  /* NOSLIP: 1 = isothermal at wall_T, 0 = adiabatic     */
     double state[4];     /* FARFIELD / CHAR_FARFIELD: conserved freestream state */
     double wall_u, wall_v, wall_T;
+    double nut;          /* RANS-SA, FARFIELD: freestream nu-tilde               */
 } fv_bc_t;
 
 /* EulerInitialCondition (include/EulerFVMSolver.h:59-67), primitive form. */
@@ -150,8 +151,13 @@ typedef struct {
     int32_t strict;        /* 1: IEEE op-for-op with the reference (no FMA)    */
     double exact_tol;      /* exact Riemann Newton relative tolerance          */
     int32_t exact_max_iter;
-    int32_t viscous;       /* 1: Navier-Stokes viscous + heat flux             */
+    int32_t viscous;       /* 1: Navier-Stokes viscous + heat flux; 2: RANS with
+                              the Spalart-Allmaras (SA-noft2) model             */
     double gas_constant, mu, prandtl;
+    double prandtl_t;      /* RANS: turbulent Prandtl number                   */
+    double initial_nut;    /* RANS: uniform initial nu-tilde                   */
+    double sa[9];          /* RANS: cb1, cb2, sigma, kappa, cw2, cw3, cv1, cv2, cv3
+                              (SAModelConstants, include/SpalartAllmaras.h:13-23) */
 } fv_options_t;
 
 /* Fill *opt with the reference's defaults: Rusanov, order 1, forward Euler,
@@ -210,6 +216,14 @@ int fv_get_field(fv_solver_t s, double* U);
 int fv_set_field(fv_solver_t s, const double* U);
 int fv_get_residual(fv_solver_t s, double norms[4]);
 int fv_set_cfl(fv_solver_t s, double cfl);
+/* RANSTurbulenceSASolver::nut_field / set_field(U, nut) / nut_residual
+ * (include/RANSTurbulenceSASolver.h): nu-tilde per cell in the caller's
+ * order, and the wall distance the SA model uses (compute_wall_distance,
+ * include/WallDistance.h:38). */
+int fv_get_nut(fv_solver_t s, double* nut);
+int fv_set_nut(fv_solver_t s, const double* nut);
+int fv_get_nut_residual(fv_solver_t s, double* norm);
+int fv_get_wall_distance(fv_solver_t s, double* d);
 int fv_get_gamma(fv_solver_t s, double* gamma);
 /* Device pointer to the AoS state in device cell order, and the solver's
  * stream (for callers that time or chain work on it). */

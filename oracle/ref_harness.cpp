@@ -6,7 +6,7 @@
 // that the parity tests and the golden-fixture script read.
 //
 // Usage: fvref <mode> mesh=<file.fvmesh> out=<dir> [key=value ...]
-//   mode = mesh | euler | ns | diff | grad | walldist
+//   mode = mesh | euler | ns | rans | diff | grad | walldist
 // Reference interfaces driven here:
 //   MeshReader::read               include/MeshReader.h:81
 //   EulerFVMSolver                 include/EulerFVMSolver.h:107-160
@@ -32,6 +32,7 @@
 #include "MeshReader.h"
 #include "NavierStokesFVMSolver.h"
 #include "UnstructuredFVMSolver.h"
+#include "RANSTurbulenceSASolver.h"
 #include "WallDistance.h"
 #include "WallTraction.h"
 
@@ -227,6 +228,79 @@ int run_ns(const UnstructuredMesh& m, const std::string& out) {
     return 0;
 }
 
+// RANSTurbulenceSASolver (include/RANSTurbulenceSASolver.h:1-233): bc specs
+// as run_ns, farfield specs carry the freestream nut as a 7th field.
+int run_rans(const UnstructuredMesh& m, const std::string& out) {
+    double gamma = argd("gamma", 1.4);
+    std::vector<RANSBoundaryConditionSA> bcs(m.patches.size());
+    std::vector<int> wall_faces;
+    for (const std::string& spec : g_args["bc"]) {
+        std::vector<std::string> p = split(spec, ':');
+        int pid = patch_index(m, p[0]);
+        if (pid < 0) { std::fprintf(stderr, "unknown patch %s\n", p[0].c_str()); return 2; }
+        NSBoundaryCondition& bc = bcs[pid].ns;
+        if (p[1] == "noslip") {
+            bc.type = NSBoundaryType::NoSlipWall;
+            if (p.size() > 2) bc.wall_u = std::stod(p[2]);
+            if (p.size() > 3) bc.wall_v = std::stod(p[3]);
+            if (p.size() > 4) { bc.is_isothermal_wall = true; bc.wall_temperature = std::stod(p[4]); }
+        } else if (p[1] == "outflow") {
+            bc.type = NSBoundaryType::Outflow;
+        } else {
+            bc.type = NSBoundaryType::Farfield;
+            bc.farfield_state = from_primitive(std::stod(p[2]), std::stod(p[3]), std::stod(p[4]),
+                                               std::stod(p[5]), gamma);
+            if (p.size() > 6) bcs[pid].farfield_nut = std::stod(p[6]);
+        }
+    }
+    for (size_t f = 0; f < m.faces.size(); ++f) {
+        const Face& face = m.faces[f];
+        if (face.cell_right == -1 && bcs[face.patch_id].ns.type == NSBoundaryType::NoSlipWall)
+            wall_faces.push_back((int)f);
+    }
+    GradientScheme gs = arg("grad", "lsq") == "gg" ? GradientScheme::GreenGauss : GradientScheme::LeastSquares;
+    RANSTurbulenceSASolver solver(m, bcs, gamma, argd("R", 287.0), argd("mu", 1e-3), argd("Pr", 0.72),
+                                  argd("Prt", 0.9), argd("cfl", 0.5), ic_from_args(), argd("nut0", 0.0),
+                                  flux_of(arg("flux", "rusanov")), gs, argd("tol", 1e-6), (int)argi("maxit", 20));
+    long steps = argi("steps", 10);
+    std::vector<double> hist;
+    auto t0 = std::chrono::steady_clock::now();
+    for (long s = 0; s < steps; ++s) {
+        solver.step();
+        const EulerResidualNorms& r = solver.residual();
+        hist.insert(hist.end(), {r.rho, r.rho_u, r.rho_v, r.E, solver.nut_residual()});
+    }
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::vector<double> field;
+    for (const EulerState& s : solver.field()) field.insert(field.end(), {s.rho, s.rho_u, s.rho_v, s.E});
+    dump(out + "/field.f64", field);
+    dump(out + "/nut.f64", solver.nut_field());
+    std::vector<WallFaceSample> samples = solver.compute_wall_traction_samples(wall_faces);
+    UnstructuredMesh mg = m;
+    mg.compute_geometry();
+    WallReferenceQuantities ref;
+    ref.rho_ref = argd("ref_rho", 1.0);
+    ref.velocity_x_ref = argd("ref_u", 1.0);
+    ref.velocity_y_ref = argd("ref_v", 0.0);
+    ref.p_ref = argd("ref_p", 0.0);
+    ref.length_ref = argd("ref_len", 1.0);
+    ref.moment_reference_x = argd("ref_mx", 0.25);
+    ref.moment_reference_y = argd("ref_my", 0.0);
+    std::vector<double> forces;
+    for (const WallForceReport& r : compute_wall_forces(mg, samples, ref))
+        forces.insert(forces.end(), {(double)r.patch_id, r.friction_drag, r.pressure_drag, r.total_drag, r.lift,
+                                     r.moment, r.cd_friction, r.cd_pressure, r.cd_total, r.cl, r.cm});
+    dump(out + "/forces.f64", forces);
+    dump(out + "/walld.f64", compute_wall_distance(mg, wall_faces));
+    std::vector<double> hist5(hist);
+    {
+        FILE* f = std::fopen((out + "/history.f64").c_str(), "wb");
+        if (f) { std::fwrite(hist5.data(), sizeof(double), hist5.size(), f); std::fclose(f); }
+    }
+    std::printf("{\"steps\": %ld, \"cells\": %zu, \"seconds\": %.6f}\n", steps, m.cells.size(), secs);
+    return 0;
+}
+
 int run_diff(UnstructuredMesh m, const std::string& out) {
     for (const std::string& spec : g_args["bc"]) {
         std::vector<std::string> p = split(spec, ':');
@@ -338,7 +412,7 @@ int run_ckpt() {
 
 int main(int argc, char** argv) {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: fvref <mesh|euler|ns|diff|grad|walldist> mesh=<f> out=<dir> [k=v...]\n");
+        std::fprintf(stderr, "usage: fvref <mesh|euler|ns|rans|diff|grad|walldist> mesh=<f> out=<dir> [k=v...]\n");
         return 2;
     }
     std::string mode = argv[1];
@@ -354,6 +428,7 @@ int main(int argc, char** argv) {
     if (mode == "mesh") { mesh.compute_geometry(); return run_mesh(mesh, out); }
     if (mode == "euler") return run_euler(mesh, out);
     if (mode == "ns") return run_ns(mesh, out);
+    if (mode == "rans") return run_rans(mesh, out);
     if (mode == "diff") return run_diff(mesh, out);
     if (mode == "grad") return run_grad(mesh, out);
     if (mode == "walldist") return run_walldist(mesh, out);

@@ -82,12 +82,64 @@ def ns_case(name, mesh, case, tmp, steps):
                         case=np.array(json.dumps({**case, "steps": steps})))
 
 
+def rans_case(name, mesh, case, tmp, steps):
+    path = os.path.join(tmp, name + ".fvmesh")
+    fvmesh.write_fvmesh(mesh, path)
+    out = os.path.join(tmp, name)
+    os.makedirs(out, exist_ok=True)
+    ref = case["ref"]
+    res = {}
+    for flux in case["fluxes"]:
+        for grad in case["grads"]:
+            fvref("rans", path, out, flux=flux, grad=grad, cfl=case["cfl"], ic=case["ic"], bc=case["bc"], steps=steps,
+                  gamma=GAMMA, R=case["R"], mu=case["mu"], Pr=case["Pr"], Prt=case["Prt"], nut0=case["nut0"],
+                  ref_rho=ref[0], ref_u=ref[1], ref_v=ref[2], ref_p=ref[3], ref_len=ref[4], ref_mx=ref[5],
+                  ref_my=ref[6])
+            tag = f"{flux}_{grad}"
+            res[f"field_{tag}"] = np.fromfile(os.path.join(out, "field.f64")).reshape(-1, 4)
+            res[f"nut_{tag}"] = np.fromfile(os.path.join(out, "nut.f64"))
+            res[f"hist_{tag}"] = np.fromfile(os.path.join(out, "history.f64")).reshape(-1, 5)
+            res[f"forces_{tag}"] = np.fromfile(os.path.join(out, "forces.f64")).reshape(-1, 11)
+    res["walld"] = np.fromfile(os.path.join(out, "walld.f64"))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **mesh_arrays(mesh), **res,
+                        case=np.array(json.dumps({**case, "steps": steps})))
+
+
+def rans_fixtures(tmp):
+    """Spalart-Allmaras RANS (RANSTurbulenceSASolver): a no-slip NACA0012 in
+    a farfield with freestream nu-tilde = 3 nu, and a channel between an
+    isothermal still wall and a moving wall with outflow ends."""
+    R = 287.0
+    M, aoa = 0.5, np.radians(2.0)
+    u, v, p = M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA
+    mu = 1e-3
+    og = meshgen.naca_ogrid(64, 32)
+    rans_case("rans_naca_og64", og, {
+        "fluxes": ["rusanov", "hllc"], "grads": ["lsq", "gg"], "cfl": 0.5, "R": R, "mu": mu, "Pr": 0.72,
+        "Prt": 0.9, "nut0": 3 * mu, "ic": "free:" + prim_str(1.0, u, v, p),
+        "bc": ["airfoil:noslip", "farfield:farfield:" + prim_str(1.0, u, v, p) + ":" + repr(3 * mu)],
+        "ref": [1.0, float(u), float(v), float(p), 1.0, 0.25, 0.0]}, tmp, 150)
+    T_inf = (1.0 / GAMMA) / R
+    ch = meshgen.sod_strip(24, 8, length=2.0, height=1.0, jitter=0.15, seed=3)
+    rans_case("rans_channel_tri", ch, {
+        "fluxes": ["rusanov"], "grads": ["lsq", "gg"], "cfl": 0.4, "R": R, "mu": 5e-3, "Pr": 0.72, "Prt": 0.9,
+        "nut0": 2e-2, "ic": "free:" + prim_str(1.0, 0.05, 0.0, 1.0 / GAMMA),
+        "bc": ["bottom:noslip:0:0:" + repr(T_inf), "top:noslip:0.2:0", "left:outflow", "right:outflow"],
+        "ref": [1.0, 0.2, 0.0, 1.0 / GAMMA, 2.0, 1.0, 0.5]}, tmp, 200)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", choices=["rans"], default=None, help="regenerate one group of fixtures")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
+    if a.only == "rans":
+        with tempfile.TemporaryDirectory() as tmp:
+            rans_fixtures(tmp)
+        return
     with tempfile.TemporaryDirectory() as tmp:
+        rans_fixtures(tmp)
         # NACA0012 O-grid, M=0.5, AoA=2 deg, slip wall + fixed farfield.
         M, aoa = 0.5, np.radians(2.0)
         u, v, p = M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA
