@@ -360,6 +360,36 @@ def adjoint_cost(iters: int = 200, warm: int = 300):
     return out
 
 
+def rans_sa_rate(steps: int = 20, warm: int = 3):
+    """RANS with the Spalart-Allmaras model on the ~2M-cell NACA4412 hybrid
+    mesh (40 wall-clustered quad layers, y+ ~ 1 at Re_c 6e6, growth 1.15,
+    seeded random triangles to 30 chords): M 0.15, AoA 4 deg, Re_c 6e6,
+    Pr 0.72, Pr_t 0.9, freestream nu-tilde = 3 nu, HLLC with Green-Gauss
+    viscous gradients, the reference's forward-Euler global-dt scheme."""
+    import torch
+    from finitevolume_gb300 import meshgen, solvers as S
+    M, aoa, Re = 0.15, 4.0, 6e6
+    a = np.radians(aoa)
+    rho, u, v, p = 1.0, M * np.cos(a), M * np.sin(a), 1.0 / GAMMA
+    mu = rho * M * 1.0 / Re
+    R = 287.0
+    mesh = S.Mesh(meshgen.cached("naca_hybrid"), reorder="morton")
+    far = S.NSBoundaryCondition(S.NSBoundaryType.Farfield, farfield_state=list(S.from_primitive(rho, u, v, p, GAMMA)))
+    bcs = [S.RANSBoundaryConditionSA(S.NSBoundaryCondition(S.NSBoundaryType.NoSlipWall)),
+           S.RANSBoundaryConditionSA(far, 3.0 * mu / rho)]
+    ic = S.EulerInitialCondition(S.EulerICMode.Freestream, rho=rho, u=u, v=v, p=p)
+    s = S.RANSTurbulenceSASolver(mesh, bcs, GAMMA, R, mu, 0.72, 0.9, 0.5, ic, 3.0 * mu / rho,
+                                 S.NumericalFluxScheme.HLLC, S.GradientScheme.GreenGauss)
+    s.run(warm)
+    torch.cuda.synchronize()
+    ms, launches = s.step_timed(steps)
+    t = float(np.sum(ms))
+    return {"workload": "naca4412 hybrid, 40 quad layers + random triangles, M 0.15, AoA 4, Re 6e6, SA-noft2",
+            "cells": mesh.n_cells, "faces": mesh.n_faces, "value": round(mesh.n_cells * steps / (t / 1e3) / 1e6, 3),
+            "unit": "Mcell-iters/s", "ms_per_step": round(t / steps, 4), "steps": steps,
+            "nut_residual": s.nut_residual()}
+
+
 def run_batched(args):
     """--batched: converged solves/s of the 256-instance family, FP64 and
     FP32-flux, batched vs plain sequential solves."""
@@ -608,6 +638,7 @@ def main():
                 "workload": "256 NACA 4-digit O-grids, 4k-64k cells log-uniform, M 0.3-0.85, AoA -4..8"}
         del bm
         variants["adjoint_500k"] = adjoint_cost()
+        variants["rans_sa_2M"] = rans_sa_rate()
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": world,

@@ -350,6 +350,104 @@ def naca_mixed(ni: int = 1024, nj: int = 512, first: float = 1e-3, r_core: float
     return mesh
 
 
+def naca_hybrid(ni: int = 1024, n_layers: int = 40, first: float = 4.5e-6, growth: float = 1.15,
+                r_far: float = 30.0, code: str = "4412", tri_rows: int = 955, jitter: float = 0.3,
+                seed: int = 0) -> PolyMesh:
+    """Hybrid RANS mesh about a NACA 4-digit section.
+
+    ``n_layers`` wall-clustered quad layers (first spacing ``first`` chords,
+    geometric ``growth``) along the smoothed surface normals, then seeded
+    random triangles out to a farfield circle of radius ``r_far`` about
+    mid-chord.  The triangles are a Delaunay triangulation, in the index
+    space of an auxiliary O-grid of ``tri_rows`` rows (periodic around),
+    of its nodes moved by seeded uniform offsets of up to ``jitter`` cells;
+    mapped back bilinearly, they fill the annulus between the outermost
+    quad layer and the farfield and share its nodes on both rings.  The
+    default (1024 around, 40 layers, 955 rows) has 1.99M cells; the first
+    spacing is y+ ~ 1 at Re_c = 6e6 by the flat-plate estimate.
+
+    Patches: ``airfoil`` (wall), ``farfield``.
+    """
+    from scipy.spatial import Delaunay
+
+    rng = np.random.default_rng(seed)
+    m, p, t = int(code[0]) / 100.0, int(code[1]) / 10.0, int(code[2:]) / 100.0
+    s0 = airfoil_loop(ni, m, p, t)
+    tang = np.roll(s0, -1, axis=0) - np.roll(s0, 1, axis=0)
+    nrm = np.stack([tang[:, 1], -tang[:, 0]], 1)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    d = first * (growth ** np.arange(n_layers + 1) - 1.0) / (growth - 1.0)
+    quad = s0[None, :, :] + d[:, None, None] * nrm[None, :, :]          # [L+1, ni, 2]
+    # auxiliary O-grid from the outermost layer to the farfield circle
+    inner = quad[-1]
+    center = np.array([0.5, 0.0])
+    theta = 2.0 * np.pi * np.arange(ni) / ni
+    circ = center + r_far * np.stack([np.cos(theta), np.sin(theta)], 1)
+    dist = np.linalg.norm(circ - inner, axis=1)
+    k_first = (d[-1] - d[-2]) * growth
+    e = _stretch(tri_rows, k_first, float(dist.mean()))
+    f = e / e[-1]
+    w = f ** 0.5
+    aux = np.empty((tri_rows + 1, ni, 2))
+    for k in range(tri_rows + 1):
+        pn = inner + (e[k] * dist / e[-1])[:, None] * nrm
+        ps = inner + f[k] * (circ - inner)
+        aux[k] = (1.0 - w[k]) * pn + w[k] * ps
+    aux[0] = inner
+    aux[-1] = circ
+    # index-space points: fixed rings, jittered interior, ghost rows outside
+    K = tri_rows
+    ii, kk = np.meshgrid(np.arange(ni, dtype=np.float64), np.arange(1, K, dtype=np.float64))
+    free = np.stack([kk.ravel() + rng.uniform(-jitter, jitter, kk.size),
+                     (ii.ravel() + rng.uniform(-jitter, jitter, ii.size)) % ni], 1)
+    ring0 = np.stack([np.zeros(ni), np.arange(ni, dtype=np.float64)], 1)
+    ringK = np.stack([np.full(ni, float(K)), np.arange(ni, dtype=np.float64)], 1)
+    g0 = np.stack([np.full(ni, -1.0), (np.arange(ni) + 0.5) % ni], 1)
+    gK = np.stack([np.full(ni, K + 1.0), (np.arange(ni) + 0.5) % ni], 1)
+    fixed = np.concatenate([ring0, ringK, g0, gK], 0)
+    tri, ids, ext = _periodic_delaunay(fixed, free, float(ni), 3.0)
+    keep = (ext[tri, 0].mean(1) > 0.0) & (ext[tri, 0].mean(1) < K)
+    tri = ids[tri[keep]]
+    base = np.concatenate([free, fixed], 0)
+    nf = free.shape[0]
+    # bilinear map (k, i) -> physical, periodic in i
+    kq, iq = base[:, 0], base[:, 1]
+    k0 = np.clip(np.floor(kq).astype(np.int64), 0, K - 1)
+    i0 = np.floor(iq).astype(np.int64) % ni
+    a_, b_ = kq - k0, iq - np.floor(iq)
+    i1 = (i0 + 1) % ni
+    xy = ((1 - a_)[:, None] * ((1 - b_)[:, None] * aux[k0, i0] + b_[:, None] * aux[k0, i1])
+          + a_[:, None] * ((1 - b_)[:, None] * aux[k0 + 1, i0] + b_[:, None] * aux[k0 + 1, i1]))
+    # node numbering: quad layers (rows 0..L, ring L = aux ring 0), then the
+    # free triangle nodes, then the farfield ring
+    L = n_layers
+    n_quad_nodes = (L + 1) * ni
+    nodes = np.concatenate([quad.reshape(-1, 2), xy[:nf], circ], 0)
+    # base id -> node id
+    bmap = np.empty(base.shape[0], np.int64)
+    bmap[:nf] = n_quad_nodes + np.arange(nf)
+    bmap[nf:nf + ni] = L * ni + np.arange(ni)                 # ring 0 = outermost quad ring
+    bmap[nf + ni:nf + 2 * ni] = n_quad_nodes + nf + np.arange(ni)  # farfield ring
+    bmap[nf + 2 * ni:] = -1                                    # ghosts never survive
+    tris = bmap[tri]
+    if (tris < 0).any():
+        raise RuntimeError("naca_hybrid: a ghost point survived the triangulation")
+    P = nodes[tris]
+    area2 = (P[:, 1, 0] - P[:, 0, 0]) * (P[:, 2, 1] - P[:, 0, 1]) - (P[:, 2, 0] - P[:, 0, 0]) * (P[:, 1, 1] - P[:, 0, 1])
+    tris[area2 < 0] = tris[area2 < 0][:, ::-1]
+    jj, ii2 = np.meshgrid(np.arange(L), np.arange(ni), indexing="ij")
+    a0 = jj * ni + ii2
+    b0 = jj * ni + (ii2 + 1) % ni
+    quads = np.stack([a0, b0, b0 + ni, a0 + ni], -1).reshape(-1, 4)
+    cells = [list(q) for q in quads] + [list(t) for t in tris]
+    wall = np.stack([np.arange(ni), (np.arange(ni) + 1) % ni], 1)
+    far = n_quad_nodes + nf + np.stack([np.arange(ni), (np.arange(ni) + 1) % ni], 1)
+    mesh = from_cells(nodes, cells, np.concatenate([wall, far]),
+                      np.r_[np.zeros(ni, np.int32), np.ones(ni, np.int32)], ["airfoil", "farfield"])
+    _orient(mesh)
+    return mesh
+
+
 def cached(name: str, **kw) -> PolyMesh:
     """Generate ``name(**kw)`` once and keep it as .npz in a cache folder.
 
