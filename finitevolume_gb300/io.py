@@ -47,11 +47,12 @@ def read_checkpoint(path: str, equation: Optional[str], cell_count: int) -> Tupl
 class ResidualCSV:
     """Residual history file of the reference's run loop."""
 
-    def __init__(self, path: str, interval: int = 1, precision: int = 6):
+    def __init__(self, path: str, interval: int = 1, precision: int = 6, extra=()):
         self.f: TextIO = open(path, "w")
         self.interval = max(1, int(interval))
         self.precision = precision
-        self.f.write("step,residual_rho,residual_rho_u,residual_rho_v,residual_E\n")
+        cols = ["residual_rho", "residual_rho_u", "residual_rho_v", "residual_E"] + [f"residual_{x}" for x in extra]
+        self.f.write("step," + ",".join(cols) + "\n")
         self.f.flush()
 
     def record(self, step_index: int, norms) -> None:

@@ -26,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "CflRamp.h"
 #include "Checkpoint.h"
 #include "EulerFVMSolver.h"
 #include "GradientReconstruction.h"
@@ -301,6 +302,29 @@ int run_rans(const UnstructuredMesh& m, const std::string& out) {
     return 0;
 }
 
+// next_cfl (src/CflRamp.cpp:7-27) on the sequences of a binary file:
+// per record [cfl, cfl_max, cfl_min, growth, shrink, divergence, window, n,
+// history[n]] -> one output double each.
+int run_cflramp() {
+    std::ifstream in(arg("in"), std::ios::binary);
+    std::vector<double> out;
+    double head[8];
+    while (in.read(reinterpret_cast<char*>(head), sizeof(head))) {
+        std::vector<double> h((size_t)head[7]);
+        in.read(reinterpret_cast<char*>(h.data()), sizeof(double) * h.size());
+        CflRampParams p;
+        p.cfl_min = head[2];
+        p.growth_factor = head[3];
+        p.shrink_factor = head[4];
+        p.divergence_threshold = head[5];
+        p.window = (int)head[6];
+        out.push_back(next_cfl(head[0], head[1], h, p));
+    }
+    dump(arg("out"), out);
+    std::printf("{\"records\": %zu}\n", out.size());
+    return 0;
+}
+
 int run_diff(UnstructuredMesh m, const std::string& out) {
     for (const std::string& spec : g_args["bc"]) {
         std::vector<std::string> p = split(spec, ':');
@@ -422,6 +446,7 @@ int main(int argc, char** argv) {
         g_args[std::string(argv[i], eq - argv[i])].push_back(eq + 1);
     }
     if (mode == "ckpt") return run_ckpt();
+    if (mode == "cflramp") return run_cflramp();
     UnstructuredMesh mesh;
     if (!MeshReader::read(arg("mesh"), mesh)) return 1;
     std::string out = arg("out", ".");

@@ -128,18 +128,57 @@ def rans_fixtures(tmp):
         "ref": [1.0, 0.2, 0.0, 1.0 / GAMMA, 2.0, 1.0, 0.5]}, tmp, 200)
 
 
+def cfl_ramp_fixture(tmp):
+    """next_cfl on seeded residual windows: falling, rising, flat, noisy and
+    divergent sequences, several ramp parameter sets."""
+    rng = np.random.default_rng(5)
+    recs, rows = [], []
+    for i in range(400):
+        window = int(rng.integers(3, 20))
+        n = int(rng.integers(1, window + 1)) if i % 7 == 0 else window
+        kind = i % 5
+        steps = np.arange(n)
+        if kind == 0:
+            h = 10.0 ** (-0.1 * steps * rng.uniform(0.1, 2.0))
+        elif kind == 1:
+            h = 10.0 ** (0.01 * steps * rng.uniform(0.5, 20.0))
+        elif kind == 2:
+            h = np.full(n, rng.uniform(1e-6, 1.0)) * (1.0 + rng.uniform(-0.02, 0.02, n))
+        elif kind == 3:
+            h = 10.0 ** rng.normal(-3.0, 0.3, n)
+        else:
+            h = 10.0 ** (0.5 * steps * rng.uniform(0.5, 2.0))
+        head = [rng.uniform(0.05, 3.0), rng.uniform(0.5, 5.0), rng.uniform(0.01, 0.2), rng.uniform(1.05, 2.0),
+                rng.uniform(0.2, 0.9), rng.uniform(0.5, 3.0), float(window), float(n)]
+        recs.append(np.concatenate([head, h]))
+        rows.append((head, h))
+    path = os.path.join(tmp, "ramp.bin")
+    np.concatenate(recs).astype(np.float64).tofile(path)
+    out = os.path.join(tmp, "ramp.out")
+    subprocess.run([os.path.join(ROOT, "oracle", "_ref", "fvref"), "cflramp", f"in={path}", f"out={out}"],
+                   check=True, capture_output=True)
+    np.savez_compressed(os.path.join(HERE, "cfl_ramp.npz"), heads=np.array([r[0] for r in rows]),
+                        hist=np.array([np.pad(r[1], (0, 20 - len(r[1])), constant_values=np.nan) for r in rows]),
+                        out=np.fromfile(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["rans"], default=None, help="regenerate one group of fixtures")
+    ap.add_argument("--only", choices=["rans", "cfl"], default=None, help="regenerate one group of fixtures")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
+    if a.only == "cfl":
+        with tempfile.TemporaryDirectory() as tmp:
+            cfl_ramp_fixture(tmp)
+        return
     if a.only == "rans":
         with tempfile.TemporaryDirectory() as tmp:
             rans_fixtures(tmp)
         return
     with tempfile.TemporaryDirectory() as tmp:
         rans_fixtures(tmp)
+        cfl_ramp_fixture(tmp)
         # NACA0012 O-grid, M=0.5, AoA=2 deg, slip wall + fixed farfield.
         M, aoa = 0.5, np.radians(2.0)
         u, v, p = M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA
