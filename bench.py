@@ -390,6 +390,35 @@ def rans_sa_rate(steps: int = 20, warm: int = 3):
             "nut_residual": s.nut_residual()}
 
 
+def sod_layout(nx: int = 1000, ny: int = 500, steps: int = 50):
+    """Sod shock tube (rho 1/0.125, p 1/0.1) on a 1M-cell randomly perturbed
+    triangle strip, 2nd-order HLLC + LSQ/Venkatakrishnan, SSP-RK3, global
+    dt: the fields after ``steps`` steps in identity, Morton and RCM cell
+    order must be bit-identical; also the Morton run's rate."""
+    from finitevolume_gb300 import meshgen, solvers as S
+    poly = meshgen.sod_strip(nx, ny, seed=0)
+    out = {"workload": f"sod strip {nx}x{ny}x2 triangles, 2nd-order HLLC, SSP-RK3, global dt",
+           "cells": int(poly.n_cells), "steps": steps}
+    fields = {}
+    for reorder in ("none", "morton", "rcm"):
+        mesh = S.Mesh(poly, reorder=reorder)
+        bcs = [S.EulerBoundaryCondition(S.EulerBoundaryType.Wall),
+               S.EulerBoundaryCondition(S.EulerBoundaryType.Outflow),
+               S.EulerBoundaryCondition(S.EulerBoundaryType.Wall),
+               S.EulerBoundaryCondition(S.EulerBoundaryType.Outflow)]
+        ic = S.EulerInitialCondition(S.EulerICMode.TwoRegion, rho_l=1.0, u_l=0.0, v_l=0.0, p_l=1.0, rho_r=0.125,
+                                     u_r=0.0, v_r=0.0, p_r=0.1, x0=0.5)
+        sv = S.EulerFVMSolver(mesh, bcs, GAMMA, 0.5, ic, S.NumericalFluxScheme.HLLC, order=2, rk_stages=3,
+                              local_dt=False)
+        ms, _ = sv.step_timed(steps)
+        fields[reorder] = sv.field()
+        out[f"{reorder}_Mcell_iters_s"] = round(poly.n_cells * steps / (float(np.sum(ms)) / 1e3) / 1e6, 3)
+        del sv
+    out["bitwise_identical"] = bool(np.array_equal(fields["none"], fields["morton"]) and
+                                    np.array_equal(fields["none"], fields["rcm"]))
+    return out
+
+
 def run_batched(args):
     """--batched: converged solves/s of the 256-instance family, FP64 and
     FP32-flux, batched vs plain sequential solves."""
@@ -639,6 +668,7 @@ def main():
         del bm
         variants["adjoint_500k"] = adjoint_cost()
         variants["rans_sa_2M"] = rans_sa_rate()
+        variants["sod_layout_1M"] = sod_layout()
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": world,

@@ -157,33 +157,33 @@ __device__ __forceinline__ V4<T> rusanov_p(const V4<T>& L, const V4<T>& R, T nx,
             T(0.5) * (FL.p + FR.p) - h * (ER - EL)};
 }
 
-// HLLC on primitive inputs (HllcFlux.h:35-76), rearranged to four divisions:
-// with q = 1/(S_K - S*), the star factor is rho_K (S_K - Vn_K) q and the
-// pressure term of E* reduces to (S* - Vn_K) p_K q.
+// HLLC on primitive inputs (HllcFlux.h:35-76), rearranged for the FP64
+// pipe: the sound speeds come from one reciprocal square root each
+// (c = g p / sqrt(g p rho)), the energy and 1/rho only of the upwind side
+// that the flux uses, and with q = 1/(S_K - S*) the star factor is
+// rho_K (S_K - Vn_K) q and the pressure term of E* is (S* - Vn_K) p_K q.
 template <typename T> __device__ __forceinline__ T trsqrt(T x);
 template <> __device__ __forceinline__ double trsqrt<double>(double x) { return rsqrt(x); }
 template <> __device__ __forceinline__ float trsqrt<float>(float x) { return rsqrtf(x); }
 
 template <typename T>
 __device__ __forceinline__ V4<T> hllc_p(const V4<T>& L, const V4<T>& R, T nx, T ny, T g, T igm1) {
-    T irL = T(1) / L.r, irR = T(1) / R.r;
-    // c = sqrt(t) computed as t * rsqrt(t): cheaper than sqrt on the FP64 pipe.
-    const T tL = g * L.p * irL, tR = g * R.p * irR;
-    T cL = tL * trsqrt<T>(tL), cR = tR * trsqrt<T>(tR);
+    const T gpL = g * L.p, gpR = g * R.p;
+    T cL = gpL * trsqrt<T>(gpL * L.r), cR = gpR * trsqrt<T>(gpR * R.r);
     T VnL = L.u * nx + L.v * ny, VnR = R.u * nx + R.v * ny;
-    T EL = L.p * igm1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
-    T ER = R.p * igm1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
     T SL = fmin(VnL - cL, VnR - cR), SR = fmax(VnL + cL, VnR + cR);
-    if (SL >= T(0)) return phys_flux_p(L, EL, VnL, nx, ny);
-    if (SR <= T(0)) return phys_flux_p(R, ER, VnR, nx, ny);
+    if (SL >= T(0)) return phys_flux_p(L, L.p * igm1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v), VnL, nx, ny);
+    if (SR <= T(0)) return phys_flux_p(R, R.p * igm1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v), VnR, nx, ny);
     T mL = L.r * (SL - VnL), mR = R.r * (SR - VnR);
     // A reciprocal plus a multiply issues fewer FP64 instructions than a
     // general division on this part.
     T Ss = (R.p - L.p + mL * VnL - mR * VnR) * (T(1) / (mL - mR));
     bool left = Ss >= T(0);
-    T SK = left ? SL : SR, VnK = left ? VnL : VnR, EK = left ? EL : ER, irK = left ? irL : irR;
+    T SK = left ? SL : SR, VnK = left ? VnL : VnR;
     T mK = left ? mL : mR;
     V4<T> K = left ? L : R;
+    const T EK = K.p * igm1 + T(0.5) * K.r * (K.u * K.u + K.v * K.v);
+    const T irK = T(1) / K.r;
     T q = T(1) / (SK - Ss);
     T fac = mK * q;
     T VtK = -K.u * ny + K.v * nx;
@@ -412,6 +412,7 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             T nmin = T(1), dmn = T(1);
+            bool lim = false;
 #pragma unroll
             for (int side = 0; side < 2; ++side) {
                 const I yb = side == 0 ? pmax[k] : nmax[k];
@@ -429,14 +430,17 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
                     num = q + T(2) * p;
                     den = (y + y) * y + (q + p);
                 }
-                if (num * dmn < nmin * den) { nmin = num; dmn = den; }
+                if (num * dmn < nmin * den) { nmin = num; dmn = den; lim = true; }
             }
-            const T psi = nmin / dmn;
+            // psi = 1 needs no division or scaling
+            const T psi = lim ? nmin / dmn : T(1);
             if constexpr (sizeof(T) == 8) {
                 if (a.lim_psi) a.lim_psi[4 * c + k] = psi;
             }
-            gx[k] *= psi;
-            gy[k] *= psi;
+            if (lim) {
+                gx[k] *= psi;
+                gy[k] *= psi;
+            }
         }
     }
     G8<T> out;
