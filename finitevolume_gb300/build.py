@@ -32,7 +32,8 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xc
               "-I" + os.path.join(ROOT, "include")]
 # Per-file extra flags: the strict kernels are built without FMA contraction.
 EXTRA = {"kernels_strict.cu": ["--fmad=false"], "diffusion.cu": ["--fmad=false"], "gradients.cu": ["--fmad=false"],
-         "ns.cu": ["--fmad=false"], "rans.cu": ["--fmad=false"]}
+         "ns.cu": ["--fmad=false"], "rans.cu": ["--fmad=false"],
+         "geometry.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 
 

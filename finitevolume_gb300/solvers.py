@@ -296,6 +296,12 @@ class EulerFVMSolver:
         b = np.array([gradients, faces, cells], np.int32)
         capi.check(capi.lib().fv_solver_set_launch(self._h, capi.i32ptr(b)))
 
+    def update_nodes(self, nodes) -> None:
+        """Move the mesh nodes ([n_nodes, 2]) and recompute the geometry on
+        the device (the state is kept)."""
+        xy = np.ascontiguousarray(nodes, dtype=np.float64)
+        capi.check(capi.lib().fv_solver_update_nodes(self._h, self.mesh.handle, capi.dptr(xy)))
+
     def autotune(self, steps: int = 5, cache: bool = True) -> dict:
         """Pick the launch shapes by timing (state preserved); results are
         cached per scheme and mesh-size octave."""

@@ -208,6 +208,17 @@ int fv_get_history(fv_solver_t s, int32_t n, double* history);
  * restored afterwards.  No reference counterpart (the reference's loops are
  * OpenMP). */
 int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]);
+/* Move the mesh nodes (xy [2 n_nodes], the mesh's node numbering) and
+ * recompute on the device every geometric quantity the Euler solver uses:
+ * face normals, lengths, midpoints and CFL lengths, shoelace cell areas and
+ * centroids (UnstructuredMesh::compute_geometry,
+ * include/UnstructuredMesh.h:89-105; src/MeshReader.cpp:56-76) and the
+ * second-order reconstruction geometry, in place (captured graphs stay
+ * valid).  mesh is the mesh the solver was created from (built from cell
+ * polygons); the mesh handle itself keeps its original nodes.  Gives the
+ * geometry of a solver built on the moved mesh bit for bit (Green-Gauss
+ * interpolation weights: to the last bit of hypot). */
+int fv_solver_update_nodes(fv_solver_t s, fv_mesh_t mesh, const double* xy);
 int fv_solver_autotune(fv_solver_t s, int32_t steps, int32_t blocks[3]);
 
 /* EulerFVMSolver::field / set_field / residual / set_cfl / gas_gamma
