@@ -15,6 +15,7 @@
 
 #include "EulerFVMSolver.h"
 #include "NavierStokesFVMSolver.h"
+#include "RANSTurbulenceSASolver.h"
 #include "UnstructuredFVMSolver.h"
 
 static UnstructuredMesh read_mesh(const char* path) {
@@ -83,6 +84,20 @@ int main(int argc, char** argv) {
         for (const EulerState& q : s.field()) out.insert(out.end(), {q.rho, q.rho_u, q.rho_v, q.E});
         const EulerResidualNorms& r = s.residual();
         out.insert(out.end(), {r.rho, r.rho_u, r.rho_v, r.E});
+    } else if (kind == 3) {
+        std::vector<RANSBoundaryConditionSA> bcs(mesh.patches.size());
+        bcs[0].ns.type = NSBoundaryType::NoSlipWall;
+        bcs[1].ns.type = NSBoundaryType::Farfield;
+        bcs[1].ns.farfield_state = fs;
+        bcs[1].farfield_nut = kv["nut_far"];
+        RANSTurbulenceSASolver s(mesh, bcs, g, kv["R"], kv["mu"], kv["Pr"], kv["Prt"], kv["cfl"], ic, kv["nut0"],
+                                 (NumericalFluxScheme)(int)kv["flux"], GradientScheme::LeastSquares, 1e-6, 20);
+        s.run(steps);
+        for (const EulerState& q : s.field()) out.insert(out.end(), {q.rho, q.rho_u, q.rho_v, q.E});
+        const std::vector<double>& nut = s.nut_field();
+        out.insert(out.end(), nut.begin(), nut.end());
+        const EulerResidualNorms& r = s.residual();
+        out.insert(out.end(), {r.rho, r.rho_u, r.rho_v, r.E, s.nut_residual()});
     } else {
         UnstructuredFVMSolver s(mesh, kv["alpha"], kv["dt"], kv["v0"], kv["r0"]);
         s.run(steps);

@@ -90,6 +90,20 @@ def test_driver_reproduces_reference(gpu, tmp_path):
                                                    rho=ic["rho"], u=ic["u"], v=ic["v"], p=ic["p"], R=case["R"],
                                                    mu=case["mu"], Pr=case["Pr"]), str(tmp_path / "n.f64"))
     assert rel_err(out[:-4].reshape(-1, 4), g["field_rusanov_lsq"]) < 1e-10
+    # RANS with Spalart-Allmaras, HLLC + LSQ
+    g = load_golden("rans_naca_og64")
+    case = case_of(g)
+    ic = parse_ic(case["ic"])
+    m = S.Mesh(poly_of(g))
+    write_mesh(m, str(tmp_path / "rans.txt"))
+    nut_far = float(case["bc"][1].split(":")[6])
+    out = _run(exe, str(tmp_path / "rans.txt"), dict(kind=3, flux=1, cfl=case["cfl"], steps=case["steps"],
+                                                     rho=ic["rho"], u=ic["u"], v=ic["v"], p=ic["p"], R=case["R"],
+                                                     mu=case["mu"], Pr=case["Pr"], Prt=case["Prt"],
+                                                     nut0=case["nut0"], nut_far=nut_far), str(tmp_path / "r.f64"))
+    n = m.n_cells
+    assert rel_err(out[:4 * n].reshape(-1, 4), g["field_hllc_lsq"]) < 1e-10
+    assert rel_err(out[4 * n:5 * n], g["nut_hllc_lsq"]) < 1e-10
     # Diffusion: patch kinds come from mesh.patches, as in the reference
     g = load_golden("diffusion_cart")
     case = case_of(g)
