@@ -572,6 +572,7 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_update(const O2Args a) {
             R += flip_if(ld_flux(ff, f), ent);
             if (STAGE == 0 && DT == 2) lam += a.dtf[f];
         }
+        if (a.forcing) R += ld_state(a.forcing, c);
         double dtv;
         if (STAGE == 0) {
             // Local: dt_i = cfl V_i / sum_f lambda_f A_f, so dt_i / V_i = cfl / sum;
@@ -612,6 +613,25 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_update(const O2Args a) {
     // Batched solves reduce per instance instead (k_batch_norms); a.r2 is
     // uniform over the grid, so the block-wide reduction is all-or-nothing.
     if (STAGE == 0 && !a.r2) finish_norms(s0, s1, s2, s3, a.ctl, a.partials, a.hist, a.hist_cap);
+}
+
+// Residual only (multigrid restriction): the same signed gather as
+// k_update, plus the forcing term, stored per cell.
+template <typename T>
+__global__ void __launch_bounds__(fvgb::kMaxBlock) k_residual(const O2Args a) {
+    using FT = typename std::conditional<std::is_same<T, double>::value, St, float4>::type;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.m.n_cells) return;
+    const FT* ff = static_cast<const FT*>(a.ff);
+    const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
+    const int ent0 = a.m.cf[e0];
+    St R = flip_if(ld_flux(ff, ent0 >> 1), ent0);
+    for (int e = e0 + 1; e < e1; ++e) {
+        const int ent = a.m.cf[e];
+        R += flip_if(ld_flux(ff, ent >> 1), ent);
+    }
+    if (a.forcing) R += ld_state(a.forcing, c);
+    st_state(a.resid, c, R);
 }
 
 // Per-instance residual norms of a batched solve: one block per instance

@@ -43,6 +43,11 @@ void launch_prim_f64(const O2Args& a, cudaStream_t s) {
     ::fast::k_prim<R><<<cb, kCellBlock, 0, s>>>(a);
 }
 
+void launch_residual_f64(const O2Args& a, cudaStream_t s) {
+    const int cb = (a.m.n_cells + kCellBlock - 1) / kCellBlock;
+    ::fast::k_residual<R><<<cb, kCellBlock, 0, s>>>(a);
+}
+
 void launch_part_f64(const O2Args& a, const O2Config& c, int stage, int part, cudaStream_t s) {
     if (part == 0) {
         if (c.order != 2) return;

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <numeric>
 #include <queue>
 #include <unordered_map>
@@ -570,6 +571,139 @@ void concat_meshes(const std::vector<const HostMesh*>& parts, HostMesh& out) {
     out.n_nodes = node0;
     out.n_cells = cell0;
     out.n_faces = face0;
+}
+
+// Agglomeration: seeds in the fine mesh's device order (space-filling
+// curve); each seed takes its unassigned face neighbours by decreasing
+// shared face length up to four cells, then the unassigned neighbours of
+// those; leftover single cells join the neighbouring agglomerate they share
+// the longest face with.
+void agglomerate(const HostMesh& f, std::vector<int32_t>& agg, HostMesh& c) {
+    const int N = f.n_cells;
+    agg.assign(N, -1);
+    std::vector<int32_t> size;
+    auto neighbours = [&](int cell, std::vector<std::pair<double, int>>& out) {
+        out.clear();
+        for (int k = f.cf_off[cell]; k < f.cf_off[cell + 1]; ++k) {
+            const int fc = f.cf[k];
+            const int nb = f.fl[fc] == cell ? f.fr[fc] : f.fl[fc];
+            if (nb >= 0) out.push_back({f.farea[fc], nb});
+        }
+        std::sort(out.begin(), out.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
+            return a.first > b.first || (a.first == b.first && a.second < b.second);
+        });
+    };
+    std::vector<std::pair<double, int>> nb1, nb2;
+    const int32_t* order = f.perm.empty() ? nullptr : f.perm.data();
+    for (int ii = 0; ii < N; ++ii) {
+        const int seed = order ? order[ii] : ii;
+        if (agg[seed] >= 0) continue;
+        const int id = (int)size.size();
+        std::vector<int> mem = {seed};
+        agg[seed] = id;
+        neighbours(seed, nb1);
+        for (auto& q : nb1)
+            if ((int)mem.size() < 4 && agg[q.second] < 0) { agg[q.second] = id; mem.push_back(q.second); }
+        for (size_t m = 1; m < mem.size() && (int)mem.size() < 4; ++m) {
+            neighbours(mem[m], nb2);
+            for (auto& q : nb2)
+                if ((int)mem.size() < 4 && agg[q.second] < 0) { agg[q.second] = id; mem.push_back(q.second); }
+        }
+        size.push_back((int)mem.size());
+    }
+    // merge singletons into the neighbour agglomerate across their longest face
+    for (int cell = 0; cell < N; ++cell) {
+        const int id = agg[cell];
+        if (size[id] != 1) continue;
+        neighbours(cell, nb1);
+        for (auto& q : nb1) {
+            const int t = agg[q.second];
+            if (t != id && size[t] < 6) {
+                agg[cell] = t;
+                size[t] += 1;
+                size[id] = 0;
+                break;
+            }
+        }
+    }
+    // compact ids
+    std::vector<int32_t> remap(size.size(), -1);
+    int nc = 0;
+    for (int cell = 0; cell < N; ++cell)
+        if (remap[agg[cell]] < 0) remap[agg[cell]] = nc++;
+    for (int cell = 0; cell < N; ++cell) agg[cell] = remap[agg[cell]];
+    // coarse cells
+    c = HostMesh{};
+    c.n_cells = nc;
+    c.n_patches = f.n_patches;
+    c.vol.assign(nc, 0.0);
+    c.cx.assign(nc, 0.0);
+    c.cy.assign(nc, 0.0);
+    for (int cell = 0; cell < N; ++cell) {
+        const int a = agg[cell];
+        c.vol[a] += f.vol[cell];
+        c.cx[a] += f.vol[cell] * f.cx[cell];
+        c.cy[a] += f.vol[cell] * f.cy[cell];
+    }
+    for (int a = 0; a < nc; ++a) { c.cx[a] /= c.vol[a]; c.cy[a] /= c.vol[a]; }
+    // coarse faces: (owner, neighbour or -1-patch) -> accumulated n A, A, x A
+    std::map<std::pair<int, int>, int> key;
+    std::vector<double> sx, sy, sa, smx, smy;
+    for (int fc = 0; fc < f.n_faces; ++fc) {
+        const int A = agg[f.fl[fc]];
+        const int B = f.fr[fc] >= 0 ? agg[f.fr[fc]] : -1;
+        if (B == A) continue;
+        int o, n;
+        double sgn = 1.0;
+        if (B >= 0) {
+            o = std::min(A, B);
+            n = std::max(A, B);
+            if (o != A) sgn = -1.0;
+        } else {
+            o = A;
+            n = -1 - f.fpatch[fc];
+        }
+        auto it = key.find({o, n});
+        int k;
+        if (it == key.end()) {
+            k = (int)sx.size();
+            key.emplace(std::make_pair(o, n), k);
+            sx.push_back(0.0); sy.push_back(0.0); sa.push_back(0.0); smx.push_back(0.0); smy.push_back(0.0);
+            c.fl.push_back(o);
+            c.fr.push_back(n >= 0 ? n : -1);
+            c.fpatch.push_back(n >= 0 ? -1 : f.fpatch[fc]);
+        } else {
+            k = it->second;
+        }
+        sx[k] += sgn * f.fnx[fc] * f.farea[fc];
+        sy[k] += sgn * f.fny[fc] * f.farea[fc];
+        sa[k] += f.farea[fc];
+        smx[k] += f.farea[fc] * f.fxm[fc];
+        smy[k] += f.farea[fc] * f.fym[fc];
+    }
+    const int nf = (int)sx.size();
+    c.n_faces = nf;
+    c.fnx.resize(nf); c.fny.resize(nf); c.farea.resize(nf); c.fxm.resize(nf); c.fym.resize(nf);
+    c.fn1.assign(nf, 0); c.fn2.assign(nf, 0);
+    for (int k = 0; k < nf; ++k) {
+        // merged faces whose normals cancel (|sum n A| = 0) carry no flux
+        const double len = std::max(std::sqrt(sx[k] * sx[k] + sy[k] * sy[k]), 1e-300);
+        c.farea[k] = len;
+        c.fnx[k] = sx[k] / len;
+        c.fny[k] = sy[k] / len;
+        c.fxm[k] = smx[k] / sa[k];
+        c.fym[k] = smy[k] / sa[k];
+    }
+    // cell -> faces
+    std::vector<std::vector<int>> cf(nc);
+    for (int k = 0; k < nf; ++k) {
+        cf[c.fl[k]].push_back(k);
+        if (c.fr[k] >= 0) cf[c.fr[k]].push_back(k);
+    }
+    c.cf_off.assign(nc + 1, 0);
+    for (int a = 0; a < nc; ++a) c.cf_off[a + 1] = c.cf_off[a] + (int)cf[a].size();
+    c.cf.reserve(c.cf_off[nc]);
+    for (int a = 0; a < nc; ++a) c.cf.insert(c.cf.end(), cf[a].begin(), cf[a].end());
 }
 
 }  // namespace fvgb

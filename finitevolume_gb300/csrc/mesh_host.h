@@ -71,6 +71,15 @@ void build_grad_geom(const HostMesh& m, HostGradGeom& g);
 // are shared (every part must have the same patch count).
 void concat_meshes(const std::vector<const HostMesh*>& parts, HostMesh& out);
 
+// Agglomeration multigrid: the next coarser level of `fine`.  agg[c] is
+// the agglomerate of fine cell c (reference numbering of both).  Each
+// coarse face merges the fine faces between two agglomerates (or one
+// agglomerate and one patch): area-weighted normal and midpoint, length
+// |sum n_f A_f|; coarse cells carry the summed volume and the
+// volume-weighted centroid.  The result has no nodes and needs
+// build_device_layout before use.
+void agglomerate(const HostMesh& fine, std::vector<int32_t>& agg, HostMesh& coarse);
+
 // src/MeshReader.cpp:317-456 (+ validate_mesh_geometry :125-288).
 // Throws MeshError on invalid input.
 void build_from_polygons(HostMesh& m, int32_t n_nodes, const double* xy, int32_t n_cells, const int64_t* cell_off,

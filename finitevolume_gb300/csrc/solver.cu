@@ -416,6 +416,8 @@ O2Args Solver::o2_args() const {
     a.r2 = r2;
     a.lim_gu = nullptr;
     a.lim_psi = nullptr;
+    a.forcing = forcing;
+    a.resid = nullptr;
     return a;
 }
 
@@ -512,6 +514,17 @@ cudaGraphExec_t Solver::graph_for(int k) {
 void Solver::step_async(int n) {
     if (n < 0) raise(FV_ERR_BAD_ARG, "negative step count");
     ensure_history(std::min(n, 1 << 20));
+    if (!mg.empty()) {
+        // multigrid V-cycles: one smoothing iteration on this level, then
+        // the coarse-grid correction (direct launches)
+        for (int i = 0; i < n; ++i) {
+            launch_step(nullptr, nullptr, nullptr);
+            mg_cycle(0);
+        }
+        FV_CUDA(cudaGetLastError());
+        steps_taken += n;
+        return;
+    }
     const int chunk = kGraphChunk;
     int q = n / chunk, r = n % chunk;
     if (q) {
@@ -647,6 +660,7 @@ void Solver::set_stream(void* s) {
         FV_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         own_stream = true;
     }
+    for (MGLevel& L : mg) L.s->set_stream(stream);  // coarse levels run on this stream
 }
 
 // compute_wall_traction + compute_wall_forces (src/WallTraction.cpp:95-217),

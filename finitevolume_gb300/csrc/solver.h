@@ -2,9 +2,13 @@
 #pragma once
 
 #include <map>
+#include <memory>
 #include <vector>
 
+#include <algorithm>
+
 #include "../../include/fv_gb300.h"
+#include "errors.h"
 #include "mesh_host.h"
 #include "ns.h"
 #include "rans.h"
@@ -16,6 +20,23 @@ struct WallFace {
     int cell;  // owner cell, reference numbering
     double nx, ny, area, xm, ym;
     int dev_face;  // the face's device index
+};
+
+struct Solver;
+
+// One coarse level of the agglomeration multigrid (full approximation
+// scheme): its own first-order solver on the agglomerated mesh and the
+// transfer maps to the next finer level (device numbering of both).
+struct MGLevel {
+    std::unique_ptr<Solver> s;
+    int n_fine = 0;
+    int* fine_off = nullptr;   // [N_c + 1] CSR: coarse cell -> finer cells
+    int* fine = nullptr;
+    int* coarse_of = nullptr;  // [N_f] finer cell -> coarse cell
+    St* U0 = nullptr;          // restricted state
+    St* Rr = nullptr;          // restricted finer residual
+    St* P = nullptr;           // forcing
+    St* Rc = nullptr;          // coarse residual at the restricted state
 };
 
 struct Solver {
@@ -80,6 +101,7 @@ struct Solver {
     const void* frf = nullptr;
     const void* eps2 = nullptr;
     const float4* fgeom32 = nullptr;
+    const St* forcing = nullptr;    // multigrid coarse levels: FAS forcing term
 
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -87,7 +109,6 @@ struct Solver {
     std::vector<void*> owned;
     std::vector<cudaEvent_t> events;  // step_timed event pool
 
-    ~Solver();
     void init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, double cfl, const fv_ic_t& ic,
               const fv_options_t& o, const double* batch_freestream = nullptr);
     void ensure_history(int n);
@@ -111,6 +132,31 @@ struct Solver {
     void autotune(int n, int out[3]);
     void set_stream(void* s);
     void wall_forces(const double ref[7], double out[11], int instance = -1);
+
+    // Agglomeration multigrid (steady solves with local time stepping):
+    // `levels` coarse levels below this solver, smoothed `smooth` RK
+    // iterations each per V-cycle; corrections scaled by `relax`.
+    std::vector<MGLevel> mg;
+    St* mg_resid = nullptr;
+    int mg_smooth = 1;
+    double mg_relax = 1.0;
+    void enable_multigrid(const HostMesh& hm, int levels, int smooth, double relax);
+    template <typename T>
+    T* dalloc_owned(size_t n) {
+        void* p = nullptr;
+        FV_CUDA(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+        owned.push_back(p);
+        return static_cast<T*>(p);
+    }
+    template <typename T>
+    T* upload_owned(const std::vector<T>& v) {
+        T* p = dalloc_owned<T>(v.size());
+        if (!v.empty()) FV_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return p;
+    }
+    void eval_residual(St* out);
+    void mg_cycle(size_t level);
+    ~Solver();
 };
 
 }  // namespace fvgb

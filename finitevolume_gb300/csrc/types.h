@@ -106,6 +106,11 @@ struct O2Args {
     // (4 per cell) of k_grad.
     double2* lim_gu;
     double* lim_psi;
+    // Multigrid (null otherwise): a forcing term added to every cell's
+    // residual (coarse levels of the full-approximation scheme), and the
+    // output of the residual-only pass.
+    const St* forcing;
+    St* resid;
 };
 
 // Second-order path configuration (validated by the solver).
@@ -133,6 +138,10 @@ void launch_prim_f32(const O2Args& a, cudaStream_t s);
 // part 0: gradients + limiter (order 2 only), 1: face fluxes, 2: update.
 void launch_part_f64(const O2Args& a, const O2Config& c, int stage, int part, cudaStream_t s);
 void launch_part_f32(const O2Args& a, const O2Config& c, int stage, int part, cudaStream_t s);
+// residual R(U) (+ forcing) per cell into a.resid, from the face fluxes of
+// the last face pass; no update
+void launch_residual_f64(const O2Args& a, cudaStream_t s);
+void launch_residual_f32(const O2Args& a, cudaStream_t s);
 void launch_batch_norms(const O2Args& a, int n_inst, const int* inst_off, double* inst_norms, int* inst_iter,
                         int* active, double tol, cudaStream_t s);
 }  // namespace o2

@@ -296,6 +296,11 @@ class EulerFVMSolver:
         b = np.array([gradients, faces, cells], np.int32)
         capi.check(capi.lib().fv_solver_set_launch(self._h, capi.i32ptr(b)))
 
+    def multigrid(self, levels: int = 4, smooth: int = 1, relax: float = 0.7) -> None:
+        """Agglomeration multigrid V-cycles (steady solves, local dt): each
+        step becomes one smoothing iteration plus one V-cycle."""
+        capi.check(capi.lib().fv_solver_multigrid(self._h, self.mesh.handle, int(levels), int(smooth), float(relax)))
+
     def update_nodes(self, nodes) -> None:
         """Move the mesh nodes ([n_nodes, 2]) and recompute the geometry on
         the device (the state is kept)."""

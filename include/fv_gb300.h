@@ -220,6 +220,14 @@ int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]);
  * interpolation weights: to the last bit of hypot). */
 int fv_solver_update_nodes(fv_solver_t s, fv_mesh_t mesh, const double* xy);
 int fv_solver_autotune(fv_solver_t s, int32_t steps, int32_t blocks[3]);
+/* Agglomeration multigrid (full approximation scheme) for steady solves
+ * with local time stepping: `levels` coarse levels agglomerated from mesh
+ * (the solver's own mesh), first order, SSP-RK3, `smooth` iterations per
+ * level per V-cycle, corrections scaled by `relax` (0 < relax <= 1).  Every
+ * fv_step is then one smoothing iteration plus one V-cycle; the converged
+ * solution is the scheme's own.  levels = 0 turns it off.  No reference
+ * counterpart. */
+int fv_solver_multigrid(fv_solver_t s, fv_mesh_t mesh, int32_t levels, int32_t smooth, double relax);
 
 /* EulerFVMSolver::field / set_field / residual / set_cfl / gas_gamma
  * (include/EulerFVMSolver.h:121-160). */
