@@ -222,11 +222,13 @@ def batch_throughput(meshes, fss, fp32: bool, iters: int):
     return cells * iters / tb / 1e6, cells * iters / ts / 1e6
 
 
-def _per_iter_seconds(mesh, fs, fp32: bool, iters: int = 40) -> float:
+def _per_iter_seconds(mesh, fs, fp32: bool, mg: bool, iters: int = 40) -> float:
     """Per-iteration wall time of one plain (unbatched) solve of a case."""
     from finitevolume_gb300 import capi
     s = _plain_solver(mesh, fs, fp32)
     try:
+        if mg:
+            s.multigrid()
         s.run(5)
         t0 = time.perf_counter()
         s.run(iters)
@@ -237,26 +239,10 @@ def _per_iter_seconds(mesh, fs, fp32: bool, iters: int = 40) -> float:
         del s
 
 
-def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 500, cd_tol: float = 1e-5):
-    """Converged steady solves per second, batched vs plain sequential.
-
-    FP64: the batch runs with per-instance early exit at the density
-    tolerance (capped at ``max_iter``); instance i takes K_i iterations.
-    FP32-flux: an instance counts as converged at the first of two
-    consecutive checkpoints (every ``chunk`` iterations) with
-    |CD - CD_fp64| <= ``cd_tol`` against its converged FP64 drag, and is
-    then frozen; instances without a converged FP64 reference run to the
-    cap and count as not converged.
-    Sequential: each plain solve of the same case performs the same
-    arithmetic as its batch instance (the batch reproduces a standalone
-    solve to round-off), so it takes the same K_i iterations; its time is
-    K_i times the measured per-iteration time of that plain solve.
-    """
-    n = len(meshes)
-    refs = [(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0) for fs in fss]
-    out = {}
-    # FP64 batched, early exit on the residual
-    b = _batch_solver(meshes, fss, False, tol)
+def _batch_to_tolerance(meshes, fss, fp32, tol, max_iter, mg, chunk=500):
+    b = _batch_solver(meshes, fss, fp32, tol)
+    if mg:
+        b.multigrid()
     t0 = time.perf_counter()
     done = 0
     while done < max_iter:
@@ -265,13 +251,40 @@ def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 
         act, it, nr = b.status()
         if not act.any():
             break
-    t64 = time.perf_counter() - t0
-    conv64 = (~act) & (nr[:, 0] < tol)
-    k64 = it.copy()
-    cd64 = np.array([b.wall_forces(i, *refs[i])["cd_total"] for i in range(n)])
-    del b
-    # FP32-flux batched, drag criterion; the timer stops during the drag reads
+    t = time.perf_counter() - t0
+    return b, t, (~act) & (nr[:, 0] < tol), it.copy()
+
+
+def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 500, cd_tol: float = 1e-5):
+    """Converged steady solves per second, batched vs plain sequential, with
+    and without agglomeration multigrid.
+
+    FP64: the batch runs with per-instance early exit at the density
+    tolerance (capped at ``max_iter``); instance i takes K_i iterations.
+    FP32-flux (with multigrid): an instance counts as converged at the first
+    of two consecutive checkpoints (every ``chunk`` iterations) with
+    |CD - CD_fp64| <= ``cd_tol`` against its converged FP64 (multigrid)
+    drag, and is then frozen; instances without a converged FP64 reference
+    run to the cap and count as not converged.
+    Sequential: each plain solve of the same case performs the same
+    arithmetic as its batch instance (the batch reproduces a standalone
+    solve to round-off), so it takes the same K_i iterations; its time is
+    K_i times the measured per-iteration time of that solve on its own.
+    """
+    n = len(meshes)
+    refs = [(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0) for fs in fss]
+    out = {"instances": n}
+    res = {}
+    for tag, mg in (("f64_plain", False), ("f64_multigrid", True)):
+        b, t, conv, k = _batch_to_tolerance(meshes, fss, False, tol, max_iter, mg, chunk)
+        cd = np.array([b.wall_forces(i, *refs[i])["cd_total"] for i in range(n)])
+        del b
+        res[tag] = (t, conv, k, cd)
+    # FP32-flux with multigrid, drag criterion against the FP64 multigrid drag
+    cd64 = res["f64_multigrid"][3]
+    conv64 = res["f64_multigrid"][1]
     b = _batch_solver(meshes, fss, True, -1.0)
+    b.multigrid()
     k32 = np.full(n, max_iter, np.int64)
     hits = np.zeros(n, np.int64)
     conv32 = np.zeros(n, bool)
@@ -292,27 +305,30 @@ def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 
                 b.set_active(int(i), False)
         if conv32[conv64].all():
             break
-    # instances still running at the end ran every checkpoint
-    act32, it32, _ = b.status()
+    _, it32, _ = b.status()
     k32 = np.where(conv32, k32, it32)
     del b
     # plain sequential solves: per-iteration time of each case
-    t_seq64 = np.array([_per_iter_seconds(m, fs, False) for m, fs in zip(meshes, fss)])
-    t_seq32 = np.array([_per_iter_seconds(m, fs, True) for m, fs in zip(meshes, fss)])
-    s64 = float(np.nansum(k64 * t_seq64))
-    s32 = float(np.nansum(k32 * t_seq32))
-    n64, n32 = int(conv64.sum()), int(conv32.sum())
-    out["f64"] = {"batched_solves_per_s": round(n64 / t64, 5), "batched_seconds": round(t64, 2), "converged": n64,
-                  "sequential_solves_per_s": round(n64 / s64, 5), "sequential_seconds": round(s64, 2),
-                  "iterations_median": int(np.median(k64)),
-                  "iterations_converged_median": int(np.median(k64[conv64])) if n64 else None}
-    out["fp32_flux"] = {"batched_solves_per_s": round(n32 / t32, 5), "batched_seconds": round(t32, 2),
-                        "converged": n32, "criterion": f"|CD - CD_fp64| <= {cd_tol} at two checkpoints",
-                        "sequential_solves_per_s": round(n32 / s32, 5), "sequential_seconds": round(s32, 2),
-                        "iterations_converged_median": int(np.median(k32[conv32])) if n32 else None}
-    out["instances"] = n
-    out["sequential_method"] = ("K_i x measured per-iteration time of the plain solve of case i "
+    t_plain = np.array([_per_iter_seconds(m, fs, False, False) for m, fs in zip(meshes, fss)])
+    t_mg = np.array([_per_iter_seconds(m, fs, False, True) for m, fs in zip(meshes, fss)])
+    t_mg32 = np.array([_per_iter_seconds(m, fs, True, True) for m, fs in zip(meshes, fss)])
+    for tag, tseq in (("f64_plain", t_plain), ("f64_multigrid", t_mg)):
+        t, conv, k, _ = res[tag]
+        s_seq = float(np.nansum(k * tseq))
+        nconv = int(conv.sum())
+        out[tag] = {"batched_solves_per_s": round(nconv / t, 5), "batched_seconds": round(t, 2), "converged": nconv,
+                    "sequential_solves_per_s": round(nconv / s_seq, 5), "sequential_seconds": round(s_seq, 2),
+                    "iterations_median": int(np.median(k)),
+                    "iterations_converged_median": int(np.median(k[conv])) if nconv else None}
+    s32 = float(np.nansum(k32 * t_mg32))
+    n32 = int(conv32.sum())
+    out["fp32_flux_multigrid"] = {"batched_solves_per_s": round(n32 / t32, 5), "batched_seconds": round(t32, 2),
+                                  "converged": n32, "criterion": f"|CD - CD_fp64| <= {cd_tol} at two checkpoints",
+                                  "sequential_solves_per_s": round(n32 / s32, 5), "sequential_seconds": round(s32, 2),
+                                  "iterations_converged_median": int(np.median(k32[conv32])) if n32 else None}
+    out["sequential_method"] = ("K_i x measured per-iteration time of the solve of case i on its own "
                                 "(40 iterations after 5 warm-up), summed over all instances")
+    out["multigrid"] = "4 agglomerated levels, 1 smoothing iteration per level, correction relaxation 0.7"
     return out
 
 

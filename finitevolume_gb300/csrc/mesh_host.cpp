@@ -632,9 +632,19 @@ void agglomerate(const HostMesh& f, std::vector<int32_t>& agg, HostMesh& c) {
     for (int cell = 0; cell < N; ++cell)
         if (remap[agg[cell]] < 0) remap[agg[cell]] = nc++;
     for (int cell = 0; cell < N; ++cell) agg[cell] = remap[agg[cell]];
-    // coarse cells
     c = HostMesh{};
     c.n_cells = nc;
+    // batched meshes: agglomerates never cross instances (no faces join
+    // them) and the ids follow the cell order, so each instance keeps a
+    // contiguous range
+    if (f.group_off.size() >= 2) {
+        const size_t ni = f.group_off.size() - 1;
+        std::vector<int32_t> go(ni + 1, nc);
+        for (size_t i = 0; i < ni; ++i) go[i] = f.group_off[i] < N ? agg[f.group_off[i]] : nc;
+        c.group_off.assign(go.begin(), go.end());
+    }
+    // coarse cells
+
     c.n_patches = f.n_patches;
     c.vol.assign(nc, 0.0);
     c.cx.assign(nc, 0.0);

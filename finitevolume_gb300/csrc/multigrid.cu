@@ -63,9 +63,11 @@ __global__ void k_forcing(int nc, const St* __restrict__ Rr, const St* __restric
 }
 
 __global__ void k_prolong(int nf, const int* __restrict__ coarse_of, const St* __restrict__ Uc,
-                          const St* __restrict__ U0, St* __restrict__ Uf, double relax, double gamma) {
+                          const St* __restrict__ U0, St* __restrict__ Uf, double relax, double gamma,
+                          const int* __restrict__ cell_inst, const int* __restrict__ active) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nf) return;
+    if (active && !active[cell_inst[i]]) return;  // frozen batch instance
     const int c = coarse_of[i];
     const St a = Uc[c], b = U0[c], u = Uf[i];
     const double p0 = (gamma - 1.0) * (u.E - 0.5 * (u.ru * u.ru + u.rv * u.rv) / u.r);
@@ -111,6 +113,9 @@ void Solver::mg_cycle(size_t level) {
     MGLevel& L = mg[level];
     Solver& c = *L.s;
     const int B = 256;
+    // batched: the coarse level skips the instances frozen on this level
+    if (batch)
+        FV_CUDA(cudaMemcpyAsync(c.active, active, sizeof(int) * n_inst, cudaMemcpyDeviceToDevice, stream));
     // finer residual at the smoothed state (with its own forcing)
     eval_residual(mg_resid);
     mgk::k_restrict<<<(c.N + B - 1) / B, B, 0, stream>>>(c.N, L.fine_off, L.fine, U, mg_resid, dm.vol, c.dm.vol,
@@ -126,13 +131,14 @@ void Solver::mg_cycle(size_t level) {
         c.launch_step(nullptr, nullptr, nullptr);
         c.mg_cycle(0);
     }
-    mgk::k_prolong<<<(N + B - 1) / B, B, 0, stream>>>(N, L.coarse_of, c.U, L.U0, U, mg_relax, gamma);
+    mgk::k_prolong<<<(N + B - 1) / B, B, 0, stream>>>(N, L.coarse_of, c.U, L.U0, U, mg_relax, gamma, cell_inst,
+                                                      active);
     FV_CUDA(cudaGetLastError());
     refresh_primitives();
 }
 
 void Solver::enable_multigrid(const HostMesh& hm, int levels, int smooth, double relax) {
-    if (!general || viscous || batch) raise(FV_ERR_UNSUPPORTED, "multigrid: Euler solves on the second-order / multi-stage path");
+    if (!general || viscous) raise(FV_ERR_UNSUPPORTED, "multigrid: Euler solves on the second-order / multi-stage path");
     if (!cfg.local_dt) raise(FV_ERR_UNSUPPORTED, "multigrid: steady solves with local time stepping");
     if (levels < 0 || levels > 8 || smooth < 1 || !(relax > 0.0 && relax <= 1.0))
         raise(FV_ERR_BAD_ARG, "multigrid: 0..8 levels, smooth >= 1, 0 < relax <= 1");
@@ -177,7 +183,7 @@ void Solver::enable_multigrid(const HostMesh& hm, int levels, int smooth, double
         keep[l].build_device_layout(FV_REORDER_MORTON);
         MGLevel L;
         L.s.reset(new Solver());
-        L.s->init(keep[l], bcs.data(), bc.n, gamma, c0.cfl, ic, o);
+        L.s->init(keep[l], bcs.data(), bc.n, gamma, c0.cfl, ic, o, batch ? inst_fs_host.data() : nullptr);
         L.s->set_stream(stream);
         Solver& cs = *L.s;
         const int nf = finer->N;

@@ -221,7 +221,8 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         inst_off = dupload(std::vector<int>(group_off.begin(), group_off.end()), owned);
         active = dupload(std::vector<int>(n_inst, 1), owned);
         inst_iter = dupload(std::vector<int>(n_inst, 0), owned);
-        inst_fs = dupload(std::vector<double>(batch_freestream, batch_freestream + 4 * (size_t)n_inst), owned);
+        inst_fs_host.assign(batch_freestream, batch_freestream + 4 * (size_t)n_inst);
+        inst_fs = dupload(inst_fs_host, owned);
         inst_norms = dupload(std::vector<double>(4 * (size_t)n_inst, 0.0), owned);
         r2 = dalloc<double4_32a>(N, owned);
     }

@@ -71,6 +71,7 @@ struct Solver {
     int* inst_off = nullptr;
     int* inst_iter = nullptr;
     double* inst_fs = nullptr;
+    std::vector<double> inst_fs_host;   // the same, host copy (coarse multigrid levels)
     double* inst_norms = nullptr;
     double4_32a* r2 = nullptr;
     double tol = -1.0;                // density-norm tolerance; < 0 never freezes

@@ -608,6 +608,11 @@ class BatchSolver:
     def set_tolerance(self, tol: float) -> None:
         capi.check(capi.lib().fv_batch_set_tolerance(self._h, float(tol)))
 
+    def multigrid(self, levels: int = 4, smooth: int = 1, relax: float = 0.7) -> None:
+        """Agglomeration multigrid for every instance (agglomerates never
+        cross instances; frozen instances get no corrections)."""
+        capi.check(capi.lib().fv_solver_multigrid(self._h, self.mesh.handle, int(levels), int(smooth), float(relax)))
+
     def autotune(self, steps: int = 5, cache: bool = True) -> dict:
         """Launch shapes of the batched kernels chosen by timing (state preserved)."""
         return _autotune(self._h, _shape_key(self._opt, self.mesh.n_cells, True), steps, cache)

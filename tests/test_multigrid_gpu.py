@@ -56,3 +56,39 @@ def test_multigrid_converges_faster_to_the_same_solution(gpu, order):
     ref = (1.0, fs[1], fs[2], fs[3], 1.0, 0.25, 0.0)
     fa, fb = plain.wall_forces(*ref), mg.wall_forces(*ref)
     assert abs(fa["cl"] - fb["cl"]) < 1e-7 and abs(fa["cd_total"] - fb["cd_total"]) < 1e-7
+
+
+def test_batched_multigrid_converges_every_instance(gpu):
+    # unlimited second order: grids fine enough to stay stable at the nose
+    cases = [(96, 48, 0.5, 2.0), (80, 40, 0.4, -1.0), (112, 56, 0.45, 3.0)]
+    meshes = [S.Mesh(meshgen.naca_ogrid(ni, nj, r_far=10.0)) for ni, nj, _, _ in cases]
+    fss = []
+    for _, _, M, aoa in cases:
+        a = np.radians(aoa)
+        fss.append((1.0, M * np.cos(a), M * np.sin(a), 1.0 / GAMMA))
+    kinds = [S.EulerBoundaryType.Wall, S.EulerBoundaryType.CharacteristicFarfield]
+    tol = 1e-10
+
+    def run(mg):
+        b = S.BatchSolver(meshes, kinds, fss, order=2, limiter=S.Limiter.NoLimiter, tol=tol)
+        if mg:
+            b.multigrid(levels=3)
+        n = 0
+        while n < 200000:
+            b.run(500)
+            n += 500
+            act, it, _ = b.status()
+            if not act.any():
+                break
+        return b, it
+    plain, it_plain = run(False)
+    act, _, nr = plain.status()
+    assert not act.any() and (nr[:, 0] < tol).all()
+    mg, it_mg = run(True)
+    act, _, nr = mg.status()
+    assert not act.any() and (nr[:, 0] < tol).all()
+    assert (it_mg * 2 < it_plain).all(), (it_mg, it_plain)
+    for i, fs in enumerate(fss):
+        ref = (1.0, fs[1], fs[2], fs[3], 1.0, 0.25, 0.0)
+        fa, fb = plain.wall_forces(i, *ref), mg.wall_forces(i, *ref)
+        assert abs(fa["cl"] - fb["cl"]) < 1e-6 and abs(fa["cd_total"] - fb["cd_total"]) < 1e-6
