@@ -159,6 +159,26 @@ def measured_peaks():
 
 
 # --------------------------------------------------------------------------
+# Replicas (N GPUs, one independent solve each; the path has no exchange step)
+def max_over_ranks(x: float, world: int, device: str) -> float:
+    """The slowest rank's value (timed regions end at a barrier)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def replica_rate(n_cells: int, steps: int, max_ms: float, world: int) -> float:
+    """Whole-job Mcell-iters/s: every rank advanced its own n_cells for
+    ``steps`` iterations within the slowest rank's time."""
+    return world * n_cells * steps / (max_ms / 1e3) / 1e6
+
+
+# --------------------------------------------------------------------------
 # Batched steady solves: 256 NACA 4-digit O-grids (camber 0-6%, thickness
 # 8-18%, 4k-64k cells log-uniform), M 0.3-0.85, AoA -4..8 deg, 2nd-order
 # HLLC + LSQ/Venkatakrishnan, SSP-RK3, local dt at CFL 1.2.
@@ -435,6 +455,34 @@ def sod_layout(nx: int = 1000, ny: int = 500, steps: int = 50):
     return out
 
 
+def config1_rate(steps: int = 3000):
+    """The reference's own scheme at small scale: NACA0012 O-grid 256 x 128
+    (32,768 cells, first spacing 1e-3, farfield at 20 chords), first-order
+    Rusanov, forward Euler with local time stepping at CFL 0.5, slip wall
+    and characteristic farfield, M 0.5, AoA 2 deg, 3,000 iterations; CL, CD
+    and the final density residual."""
+    import torch
+    from finitevolume_gb300 import meshgen, solvers as S
+    M, aoa = 0.5, 2.0
+    a = np.radians(aoa)
+    fs = (1.0, M * np.cos(a), M * np.sin(a), 1.0 / GAMMA)
+    mesh = S.Mesh(meshgen.naca_ogrid(256, 128), reorder="morton")
+    bcs = [S.EulerBoundaryCondition(S.EulerBoundaryType.Wall),
+           S.EulerBoundaryCondition(S.EulerBoundaryType.CharacteristicFarfield, S.from_primitive(*fs, GAMMA))]
+    ic = S.EulerInitialCondition(S.EulerICMode.Freestream, rho=fs[0], u=fs[1], v=fs[2], p=fs[3])
+    s = S.EulerFVMSolver(mesh, bcs, GAMMA, 0.5, ic, S.NumericalFluxScheme.Rusanov, local_dt=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h = s.run(steps, history=True)
+    t = time.perf_counter() - t0
+    f = s.wall_forces(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0)
+    return {"workload": "naca0012 O-grid 256x128, 1st-order Rusanov, forward Euler, local dt, CFL 0.5, M 0.5, AoA 2",
+            "cells": mesh.n_cells, "steps": steps, "seconds": round(t, 4),
+            "value": round(mesh.n_cells * steps / t / 1e6, 3), "unit": "Mcell-iters/s (wall clock, graph path)",
+            "cl": f["cl"], "cd": f["cd_total"], "residual_rho_first": float(h[0, 0]),
+            "residual_rho_last": float(h[-1, 0])}
+
+
 def run_batched(args):
     """--batched: converged solves/s of the 256-instance family, FP64 and
     FP32-flux, batched vs plain sequential solves."""
@@ -584,14 +632,9 @@ def main():
         ev1.record(stream)
         ev1.synchronize()
     torch.cuda.synchronize()
-    elapsed_ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-        dist.barrier()
+    elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1), world, "cuda")
     clocks = clk.summary()
-    value = world * n_cells * args.steps / (elapsed_ms / 1e3) / 1e6
+    value = replica_rate(n_cells, args.steps, elapsed_ms, world)
 
     # Roofline of the dominant kernel class (largest summed device time).
     hbm, peak_src = measured_peaks()
@@ -685,6 +728,7 @@ def main():
         variants["adjoint_500k"] = adjoint_cost()
         variants["rans_sa_2M"] = rans_sa_rate()
         variants["sod_layout_1M"] = sod_layout()
+        variants["config1_o1_rusanov_32k"] = config1_rate()
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": world,
