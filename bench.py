@@ -483,6 +483,35 @@ def config1_rate(steps: int = 3000):
             "residual_rho_last": float(h[-1, 0])}
 
 
+def profile_target(target: str, steps: int) -> dict:
+    """Profiler targets beside the headline: the adjoint iteration on the
+    500k-cell O-grid, the RANS-SA step on the 2M-cell hybrid mesh, and a
+    multigrid V-cycle on the 1M-cell mixed mesh (direct launches)."""
+    import torch
+    from finitevolume_gb300 import meshgen, solvers as S
+    t0 = time.perf_counter()
+    if target == "adjoint":
+        M, aoa = 0.75, 2.0
+        a = np.radians(aoa)
+        fs = (1.0, M * np.cos(a), M * np.sin(a), 1.0 / GAMMA)
+        mesh = S.Mesh(meshgen.cached("naca_ogrid", ni=1024, nj=488), reorder="morton")
+        s = _plain_solver(mesh, fs, False)
+        s.run(20)
+        adj = S.DiscreteAdjoint(s)
+        adj.forward()
+        _, g = S.force_gradient(s, S.Objective.Drag, np.array([1.0, fs[1], fs[2], fs[3], 1.0, 0.25, 0.0]))
+        adj.solve(g, steps, 0.0)
+    elif target == "rans":
+        rans_sa_rate(steps=steps, warm=1)
+    else:
+        poly = load_mesh()
+        s, _ = make_solver(poly)
+        s.multigrid()
+        s.run(steps)
+    torch.cuda.synchronize()
+    return {"steps": steps, "seconds": round(time.perf_counter() - t0, 3)}
+
+
 def run_batched(args):
     """--batched: converged solves/s of the 256-instance family, FP64 and
     FP32-flux, batched vs plain sequential solves."""
@@ -570,6 +599,8 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiler target: build the workload, run --steps iterations with direct launches, exit")
     ap.add_argument("--fp32", action="store_true", help="with --profile: the FP32-flux variant")
+    ap.add_argument("--profile-target", choices=["euler", "adjoint", "rans", "multigrid"], default="euler",
+                    help="with --profile: which kernels to run (profiler target)")
     ap.add_argument("--batched", action="store_true",
                     help="converged solves/s of the batched airfoil family instead of the headline")
     ap.add_argument("--instances", type=int, default=256)
@@ -580,10 +611,13 @@ def main():
         run_batched(args)
         return
     if args.profile:
-        poly = load_mesh()
-        s, _ = make_solver(poly, fp32=args.fp32)
-        ms, launches = s.step_timed(args.steps)
-        print(json.dumps({"profile_steps": args.steps, "kernel_ms": ms.tolist(), "launches": launches.tolist()}))
+        if args.profile_target == "euler":
+            poly = load_mesh()
+            s, _ = make_solver(poly, fp32=args.fp32)
+            ms, launches = s.step_timed(args.steps)
+            print(json.dumps({"profile_steps": args.steps, "kernel_ms": ms.tolist(), "launches": launches.tolist()}))
+        else:
+            print(json.dumps({"profile": args.profile_target, **profile_target(args.profile_target, args.steps)}))
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
