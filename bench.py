@@ -396,6 +396,120 @@ def adjoint_cost(iters: int = 200, warm: int = 300):
     return out
 
 
+def _converge(s, tol: float, max_iter: int, chunk: int = 250):
+    """Run until the density residual norm falls below tol (or max_iter)."""
+    done, last = 0, float("nan")
+    while done < max_iter:
+        h = s.run(min(chunk, max_iter - done), history=True)
+        done += len(h)
+        last = float(h[-1, 0])
+        if not np.isfinite(last) or last < tol:
+            break
+    return done, last
+
+
+def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, max_cycles: int = 30000,
+                  adj_iters: int = 40000, adj_tol: float = 1e-12):
+    """Gradients of the 500k-cell NACA0012 O-grid case (1024 x 488, M 0.75,
+    AoA 2 deg, 2nd-order HLLC + LSQ/Venkatakrishnan K=5, SSP-RK3, local dt,
+    CFL 1.2) from the discrete adjoint (frozen and full limiter) against
+    central differences of converged primal solves: dCD/dM and dCD/dAoA,
+    and dCL/dX along ``n_dirs`` seeded wall-normal displacement fields
+    smoothed over 20 wall nodes, step h.  Primal solves use the
+    agglomeration multigrid; perturbed solves start from the base state."""
+    import torch
+    from finitevolume_gb300 import meshgen, solvers as S
+    M, aoa = 0.75, 2.0
+
+    def fs_of(m, al):
+        a = np.radians(al)
+        return (1.0, m * np.cos(a), m * np.sin(a), 1.0 / GAMMA)
+
+    def ref_of(m, al):
+        return np.array([*fs_of(m, al), 1.0, 0.25, 0.0])
+
+    poly = meshgen.cached("naca_ogrid", ni=1024, nj=488)
+    mesh = S.Mesh(poly, reorder="morton")
+    fs = fs_of(M, aoa)
+    out = {"workload": "naca0012 O-grid 1024x488, M 0.75, AoA 2, 2nd-order HLLC, LSQ + Venkatakrishnan K=5, "
+                       "SSP-RK3, local dt, CFL 1.2",
+           "cells": mesh.n_cells, "tol_l2_density": tol, "h_shape": h, "directions": n_dirs}
+    s = _plain_solver(mesh, fs, False)
+    s.multigrid()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cyc, res = _converge(s, tol, max_cycles)
+    tprimal = time.perf_counter() - t0
+    out["primal"] = {"cycles": cyc, "residual": res, "seconds": round(tprimal, 2)}
+    U0 = s.field()
+    f0 = s.wall_forces(*ref_of(M, aoa))
+    out["cl"], out["cd"] = f0["cl"], f0["cd_total"]
+
+    # adjoint gradients
+    dirs = meshgen.wall_normal_directions(poly, n_dirs, seed=0, width=20)
+    for full in (False, True):
+        adj = S.DiscreteAdjoint(s, full_limiter=full)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gd = adj.freestream_gradient(S.Objective.Drag, M, aoa, [1], max_iter=adj_iters, tol=adj_tol)
+        _, g = S.force_gradient(s, S.Objective.Lift, ref_of(M, aoa))
+        _, _, hist, it = adj.solve(g, adj_iters, adj_tol)
+        gl = adj.shape_gradient(S.Objective.Lift, ref_of(M, aoa))
+        torch.cuda.synchronize()
+        ta = time.perf_counter() - t0
+        out["full_limiter" if full else "frozen_limiter"] = {
+            "dCD_dM": gd["dJ_dM"], "dCD_dAoA_deg": gd["dJ_dAoA_deg"], "drag_iterations": gd["iterations"],
+            "drag_adjoint_residual": gd["adjoint_residual"], "lift_iterations": it,
+            "lift_adjoint_residual": hist[-1].tolist() if len(hist) else None,
+            "dCL_dX_dirs": [float(np.sum(gl * d)) for d in dirs], "seconds": round(ta, 2),
+            "seconds_vs_primal": round(ta / tprimal, 3)}
+        del adj
+
+    # central differences: freestream
+    hM, ha = 1e-6, 1e-5
+    fd = {}
+    for key, (m, al) in {"M+": (M + hM, aoa), "M-": (M - hM, aoa), "a+": (M, aoa + ha), "a-": (M, aoa - ha)}.items():
+        sp = _plain_solver(mesh, fs_of(m, al), False)
+        sp.set_field(U0)
+        sp.multigrid()
+        c, r = _converge(sp, tol, max_cycles)
+        fd[key] = (sp.wall_forces(*ref_of(m, al))["cd_total"], c, r)
+        del sp
+    out["fd_freestream"] = {"dCD_dM": (fd["M+"][0] - fd["M-"][0]) / (2 * hM),
+                            "dCD_dAoA_deg": (fd["a+"][0] - fd["a-"][0]) / (2 * ha),
+                            "h_M": hM, "h_aoa_deg": ha,
+                            "cycles": [fd[k][1] for k in fd], "residuals": [fd[k][2] for k in fd]}
+    # central differences: shape (one solver, geometry moved on the device)
+    sp = _plain_solver(mesh, fs, False)
+    sp.multigrid()
+    X = poly.nodes.copy()
+    fd_cl, cycles, resids = [], [], []
+    for d in dirs:
+        v = {}
+        for sgn in (1, -1):
+            sp.update_nodes(X + sgn * h * d)
+            sp.set_field(U0)
+            c, r = _converge(sp, tol, max_cycles)
+            cycles.append(c)
+            resids.append(r)
+            v[sgn] = sp.wall_forces(*ref_of(M, aoa))["cl"]
+        fd_cl.append((v[1] - v[-1]) / (2 * h))
+    sp.update_nodes(X)
+    out["fd_shape"] = {"dCL_dX_dirs": fd_cl, "cycles_median": float(np.median(cycles)),
+                       "residual_max": float(np.max(resids))}
+    fdv = np.array(fd_cl)
+    for key in ("frozen_limiter", "full_limiter"):
+        ad = np.array(out[key]["dCL_dX_dirs"])
+        rel = np.abs(ad - fdv) / np.maximum(np.abs(fdv), 1e-3)
+        o = out[key]
+        o["shape_rel_err_max"] = float(rel.max())
+        o["shape_rel_err_median"] = float(np.median(rel))
+        o["dCD_dM_rel_err"] = abs(o["dCD_dM"] - out["fd_freestream"]["dCD_dM"]) / abs(out["fd_freestream"]["dCD_dM"])
+        o["dCD_dAoA_rel_err"] = (abs(o["dCD_dAoA_deg"] - out["fd_freestream"]["dCD_dAoA_deg"]) /
+                                 abs(out["fd_freestream"]["dCD_dAoA_deg"]))
+    return out
+
+
 def rans_sa_rate(steps: int = 20, warm: int = 3):
     """RANS with the Spalart-Allmaras model on the ~2M-cell NACA4412 hybrid
     mesh (40 wall-clustered quad layers, y+ ~ 1 at Re_c 6e6, growth 1.15,
@@ -601,6 +715,8 @@ def main():
     ap.add_argument("--fp32", action="store_true", help="with --profile: the FP32-flux variant")
     ap.add_argument("--profile-target", choices=["euler", "adjoint", "rans", "multigrid"], default="euler",
                     help="with --profile: which kernels to run (profiler target)")
+    ap.add_argument("--adjoint-check", action="store_true",
+                    help="adjoint gradients of the 500k-cell case against central differences of converged solves")
     ap.add_argument("--batched", action="store_true",
                     help="converged solves/s of the batched airfoil family instead of the headline")
     ap.add_argument("--instances", type=int, default=256)
@@ -609,6 +725,11 @@ def main():
     args = ap.parse_args()
     if args.batched:
         run_batched(args)
+        return
+    if args.adjoint_check:
+        import torch
+        torch.cuda.init()
+        print(json.dumps({"adjoint_check": adjoint_check()}), flush=True)
         return
     if args.profile:
         if args.profile_target == "euler":

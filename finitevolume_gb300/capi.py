@@ -131,6 +131,7 @@ SIGNATURES = {
     "fv_adjoint_solve": (C.c_int, [_P, _D, C.c_int32, C.c_double, _D, _D, _D, C.POINTER(C.c_int32)]),
     "fv_force_gradient": (C.c_int, [_P, C.c_int32, _D, _D, _D]),
     "fv_adjoint_shape_gradient": (C.c_int, [_P, _P, C.c_int32, _D, _D]),
+    "fv_residual_shape_vjp": (C.c_int, [_P, _P, _D, _D]),
     "fv_checkpoint_write": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, C.c_uint64, C.c_int64, _D]),
     "fv_checkpoint_read": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, C.POINTER(C.c_int64),
                                      C.POINTER(C.c_uint64), _D]),

@@ -182,6 +182,7 @@ struct AdjArgs {
     int* led;            // [4N]
     int* ler;            // [4N]
     double2* lpd;        // [4N] (dpsi/dd1, dpsi/dy)
+    double* lpe;         // [4N] dpsi/d eps^2 (Venkatakrishnan; 0 otherwise)
     double* ldb;         // [4N] cotangent of d1 passed to the extreme neighbour
 };
 
@@ -340,7 +341,7 @@ __global__ void k_lin_lim(const AdjArgs a) {
         const double eps2 = a.limiter == 2 ? a.eps2[c] : 0.0;
         double nmin = 1.0, dmn = 1.0;
         int side = 0;
-        double pd1 = 0.0, py = 0.0;
+        double pd1 = 0.0, py = 0.0, pe = 0.0;
         for (int sd = 0; sd < 2; ++sd) {
             const double y = sd == 0 ? ypos : yneg;
             if (!(y > 0.0)) continue;
@@ -360,6 +361,8 @@ __global__ void k_lin_lim(const AdjArgs a) {
                 side = sd == 0 ? 1 : -1;
                 pd1 = (nd1 * den - num * dd1) / (den * den);
                 py = (ny * den - num * dy) / (den * den);
+                // eps^2 enters num and den with unit weight
+                pe = a.limiter == 1 ? 0.0 : (den - num) / (den * den);
             }
         }
         const int i = 4 * c + k;
@@ -367,6 +370,7 @@ __global__ void k_lin_lim(const AdjArgs a) {
         a.led[i] = side == 1 ? emax : (side == -1 ? emin : -1);
         a.ler[i] = side == 1 ? epos : (side == -1 ? eneg : -1);
         a.lpd[i] = make_double2(pd1, py);
+        a.lpe[i] = pe;
     }
 }
 
@@ -897,6 +901,68 @@ __global__ void k_geo_cell(const AdjArgs a, double* __restrict__ abar, double* _
     }
 }
 
+// Full-limiter linearisation: geometry cotangents of the limiter values.
+// psi depends on the nodes through the active face extrapolation
+// y = side Gu . (x_f - x_c) (erb, per entry: added to the entry's offset),
+// through eps^2 = (K sqrt(V))^3 (epb, per cell: the eps^2 cotangent) and,
+// when the extreme neighbour value is a boundary value
+// (W_c + ghost(W_c, n)) / 2, through the face normal (added to nbg).
+// Runs after a backward pass at the same lam (wbar, fb in place) and after
+// k_geo_cell (which writes nbg).
+__global__ void k_geo_lim(const AdjArgs a, double* __restrict__ erb, double* __restrict__ epb,
+                          double* __restrict__ nbg) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    double gx[4] = {0.0, 0.0, 0.0, 0.0}, gy[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int ent = a.cf[e];
+        const int f = ent >> 1;
+        const bool owner = ent & 1;
+        if (a.fb[f] & (owner ? 1 : 2)) continue;
+        const double* w = a.wbar + 8 * (size_t)f + (owner ? 0 : 4);
+        const double4_32a rr = a.frf[f];
+        const double rx = owner ? rr.x : rr.z, ry = owner ? rr.y : rr.w;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { gx[k] += w[k] * rx; gy[k] += w[k] * ry; }
+    }
+    const V4<double> wc = ldW(a.W, c);
+    const double g = a.gamma;
+    double eb = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        const int i = 4 * c + k;
+        const int side = a.lside[i];
+        if (!side) continue;
+        const double2 gu = a.Gu[i];
+        const double psib = gx[k] * gu.x + gy[k] * gu.y;
+        const double2 pd = a.lpd[i];
+        const double yb = psib * pd.y, d1b = psib * pd.x;
+        const int er = a.ler[i];
+        erb[2 * (size_t)er] += side * yb * gu.x;
+        erb[2 * (size_t)er + 1] += side * yb * gu.y;
+        eb += psib * a.lpe[i];
+        const int ed = a.led[i];
+        if (ed < 0) continue;
+        const int nb = a.cnb[ed];
+        if (nb >= 0) continue;
+        const int f = -1 - nb;
+        const double4_32a geo = a.fgeom[f];
+        const int patch = a.fpatch[f];
+        const int t = a.bc.type[patch];
+        V4<double> fsp = {0, 0, 0, 0};
+        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+        const D4 wu(t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0), wv(t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0);
+        D4 nxD(geo.x), nyD(geo.y);
+        nxD.d[0] = 1.0;
+        nyD.d[1] = 1.0;
+        const V4<D4> gh = ghost_core<D4>(t, cst(wc), nxD, nyD, D4(g), cst(fsp), wu, wv);
+        // d1 = side (v - W_c), v = (W_c + ghost) / 2
+        const size_t j = 2 * (size_t)(f - a.n_int_faces);
+        nbg[j] += side * d1b * 0.5 * dget(gh, k).d[0];
+        nbg[j + 1] += side * d1b * 0.5 * dget(gh, k).d[1];
+    }
+    epb[c] = eb;
+}
+
 __global__ void k_perm_gather(const St* __restrict__ in_ref, St* __restrict__ out_dev, const int* __restrict__ perm,
                               int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -930,6 +996,9 @@ struct fv_adjoint_s {
     double2 *Gu = nullptr, *G = nullptr;
     double *psi = nullptr, *cs = nullptr, *partials = nullptr, *hist = nullptr, *dfs_dev = nullptr;
     int* counter = nullptr;
+    // shape-gradient work arrays (allocated on first use)
+    double *geo_face = nullptr, *geo_ab = nullptr, *geo_sb = nullptr, *geo_nbg = nullptr, *geo_er = nullptr,
+           *geo_ep = nullptr;
     int hist_cap = 0;
     bool linearised = false;
     bool solved = false;
@@ -1043,6 +1112,202 @@ void backward(fv_adjoint_s* A, const St* lam, int mode, St* out) {
     }
 }
 
+// lam^T dR/dX over the mesh nodes (reference node numbering), lam a
+// residual cotangent in device order.  The device computes the cotangents
+// of the geometric quantities R depends on (face normals, lengths and
+// midpoints, reconstruction offsets, least-squares weights, and with the
+// full-limiter linearisation the limiter's offsets, eps^2 and boundary
+// extremes); this host code runs the reverse pass of the geometry itself.
+void residual_geometry_vjp(fv_adjoint_s* A, const fvgb::HostMesh& h, const St* lam, std::vector<double>& xb,
+                           std::vector<double>& yb) {
+    fvgb::Solver& s = A->solver->s;
+    const int N = A->N, F = A->F, Fb = A->Fb;
+    const size_t E = (size_t)(2 * F - Fb);
+    AdjArgs& a = A->a;
+    const bool lim = a.order == 2 && a.full;
+    // cotangents on the device
+    backward(A, lam, 0, A->Rdev);
+    if (!A->geo_face) {
+        A->geo_face = A->alloc<double>(8 * (size_t)F);
+        A->geo_ab = A->alloc<double>(2 * E);
+        A->geo_sb = A->alloc<double>(2 * (size_t)N);
+        A->geo_nbg = A->alloc<double>(2 * (size_t)std::max(Fb, 1));
+        A->geo_er = A->alloc<double>(2 * E);
+        A->geo_ep = A->alloc<double>((size_t)N);
+    }
+    double *d_face = A->geo_face, *d_ab = A->geo_ab, *d_sb = A->geo_sb, *d_nbg = A->geo_nbg;
+    FV_CUDA(cudaMemsetAsync(d_nbg, 0, sizeof(double) * 2 * (size_t)std::max(Fb, 1), s.stream));
+    FV_CUDA(cudaMemsetAsync(d_ab, 0, sizeof(double) * 2 * E, s.stream));
+    FV_CUDA(cudaMemsetAsync(d_sb, 0, sizeof(double) * 2 * (size_t)N, s.stream));
+    adjk::k_geo_face<<<blocks(F), kB, 0, s.stream>>>(a, lam, d_face);
+    check_launch();
+    if (a.order == 2) {
+        adjk::k_geo_cell<<<blocks(N), kB, 0, s.stream>>>(a, d_ab, d_sb, d_nbg);
+        check_launch();
+    }
+    if (lim) {
+        FV_CUDA(cudaMemsetAsync(A->geo_er, 0, sizeof(double) * 2 * E, s.stream));
+        adjk::k_geo_lim<<<blocks(N), kB, 0, s.stream>>>(a, A->geo_er, A->geo_ep, d_nbg);
+        check_launch();
+    }
+    std::vector<double> face(8 * (size_t)F), ab(2 * E), sb(2 * (size_t)N), nbg(2 * (size_t)std::max(Fb, 1));
+    FV_CUDA(cudaMemcpyAsync(face.data(), d_face, sizeof(double) * face.size(), cudaMemcpyDeviceToHost, s.stream));
+    FV_CUDA(cudaMemcpyAsync(ab.data(), d_ab, sizeof(double) * ab.size(), cudaMemcpyDeviceToHost, s.stream));
+    FV_CUDA(cudaMemcpyAsync(sb.data(), d_sb, sizeof(double) * sb.size(), cudaMemcpyDeviceToHost, s.stream));
+    FV_CUDA(cudaMemcpyAsync(nbg.data(), d_nbg, sizeof(double) * nbg.size(), cudaMemcpyDeviceToHost, s.stream));
+    std::vector<double> er(lim ? 2 * E : 0), ep(lim ? (size_t)N : 0);
+    if (lim) {
+        FV_CUDA(cudaMemcpyAsync(er.data(), A->geo_er, sizeof(double) * er.size(), cudaMemcpyDeviceToHost, s.stream));
+        FV_CUDA(cudaMemcpyAsync(ep.data(), A->geo_ep, sizeof(double) * ep.size(), cudaMemcpyDeviceToHost, s.stream));
+    }
+    FV_CUDA(cudaStreamSynchronize(s.stream));
+    // cotangents of the geometric quantities, reference numbering
+    std::vector<double> nxb(F, 0.0), nyb(F, 0.0), arb(F, 0.0), fxb(F, 0.0), fyb(F, 0.0), cxb(N, 0.0),
+        cyb(N, 0.0);
+    for (int i = 0; i < F; ++i) {
+        const int f = h.fperm[i];
+        const double* o = face.data() + 8 * (size_t)i;
+        nxb[f] += o[0];
+        nyb[f] += o[1];
+        arb[f] += o[2];
+        if (i >= h.n_int_faces) {
+            nxb[f] += nbg[2 * (size_t)(i - h.n_int_faces)];
+            nyb[f] += nbg[2 * (size_t)(i - h.n_int_faces) + 1];
+        }
+        if (a.order == 2) {
+            // r_L = x_f - x_L, r_R = x_f - x_R
+            fxb[f] += o[3]; fyb[f] += o[4];
+            cxb[h.fl[f]] -= o[3]; cyb[h.fl[f]] -= o[4];
+            if (h.fr[f] >= 0) {
+                fxb[f] += o[5]; fyb[f] += o[6];
+                cxb[h.fr[f]] -= o[5]; cyb[h.fr[f]] -= o[6];
+            }
+        }
+    }
+    if (a.order == 2) {
+        // least-squares weights a_e = B w_e d_e, B = M^-1, M = sum w d d^T,
+        // w = 1/|d|^2, d = x_nb - x_c (x_nb: neighbour centroid or the
+        // boundary face midpoint); their sums s_c pass sbar to every a_e
+        for (int i = 0; i < N; ++i) {
+            const int c = h.perm[i];
+            const double xc = h.cx[c], yc = h.cy[c];
+            const int e0 = h.d_cf_off[i], e1 = h.d_cf_off[i + 1];
+            double m00 = 0.0, m01 = 0.0, m11 = 0.0;
+            for (int e = e0; e < e1; ++e) {
+                const int f = h.fperm[h.d_cf[e] >> 1];
+                double px, py;
+                if (h.fr[f] < 0) { px = h.fxm[f]; py = h.fym[f]; }
+                else { const int nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
+                const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
+                m00 += w * dx * dx; m01 += w * dx * dy; m11 += w * dy * dy;
+            }
+            const double det = m00 * m11 - m01 * m01;
+            const double b00 = m11 / det, b01 = -m01 / det, b11 = m00 / det;
+            double B00 = 0.0, B01 = 0.0, B10 = 0.0, B11 = 0.0;  // Bbar
+            for (int e = e0; e < e1; ++e) {
+                const int f = h.fperm[h.d_cf[e] >> 1];
+                double px, py;
+                if (h.fr[f] < 0) { px = h.fxm[f]; py = h.fym[f]; }
+                else { const int nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
+                const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
+                const double ax = ab[2 * (size_t)e] + sb[2 * (size_t)i], ay = ab[2 * (size_t)e + 1] + sb[2 * (size_t)i + 1];
+                B00 += ax * w * dx; B01 += ax * w * dy; B10 += ay * w * dx; B11 += ay * w * dy;
+            }
+            // Mbar = -B^T Bbar B^T (B symmetric)
+            const double t00 = b00 * B00 + b01 * B10, t01 = b00 * B01 + b01 * B11;
+            const double t10 = b01 * B00 + b11 * B10, t11 = b01 * B01 + b11 * B11;
+            const double M00 = -(t00 * b00 + t01 * b01), M01 = -(t00 * b01 + t01 * b11);
+            const double M10 = -(t10 * b00 + t11 * b01), M11 = -(t10 * b01 + t11 * b11);
+            for (int e = e0; e < e1; ++e) {
+                const int f = h.fperm[h.d_cf[e] >> 1];
+                const bool bnd = h.fr[f] < 0;
+                int nb = -1;
+                double px, py;
+                if (bnd) { px = h.fxm[f]; py = h.fym[f]; }
+                else { nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
+                const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
+                const double ax = ab[2 * (size_t)e] + sb[2 * (size_t)i], ay = ab[2 * (size_t)e + 1] + sb[2 * (size_t)i + 1];
+                // (w d)bar = B a_bar
+                const double vx = b00 * ax + b01 * ay, vy = b01 * ax + b11 * ay;
+                // M = sum w d d^T: dbar += w (Mbar + Mbar^T) d, wbar += d^T Mbar d
+                double ddx = w * ((M00 + M00) * dx + (M01 + M10) * dy) + w * vx;
+                double ddy = w * ((M10 + M01) * dx + (M11 + M11) * dy) + w * vy;
+                const double wb = dx * (M00 * dx + M01 * dy) + dy * (M10 * dx + M11 * dy) + dx * vx + dy * vy;
+                ddx += wb * (-2.0 * w * w * dx);
+                ddy += wb * (-2.0 * w * w * dy);
+                if (bnd) { fxb[f] += ddx; fyb[f] += ddy; }
+                else { cxb[nb] += ddx; cyb[nb] += ddy; }
+                cxb[c] -= ddx;
+                cyb[c] -= ddy;
+            }
+        }
+    }
+    // limiter: extrapolation offsets x_f - x_c of the active entries, eps^2
+    std::vector<double> epsb(lim ? N : 0, 0.0);
+    if (lim) {
+        for (int i = 0; i < N; ++i) {
+            const int c = h.perm[i];
+            for (int e = h.d_cf_off[i]; e < h.d_cf_off[i + 1]; ++e) {
+                const double bx = er[2 * (size_t)e], by = er[2 * (size_t)e + 1];
+                if (bx == 0.0 && by == 0.0) continue;
+                const int f = h.fperm[h.d_cf[e] >> 1];
+                fxb[f] += bx; fyb[f] += by;
+                cxb[c] -= bx; cyb[c] -= by;
+            }
+            epsb[c] = ep[i];
+        }
+    }
+    const double K3 = s.opt.venkat_k * s.opt.venkat_k * s.opt.venkat_k;
+    // node cotangents of lam^T R
+    const int nn = h.n_nodes;
+    xb.assign(nn, 0.0);
+    yb.assign(nn, 0.0);
+    for (int c = 0; c < N; ++c) {
+        const double eb = lim ? epsb[c] : 0.0;
+        if (cxb[c] == 0.0 && cyb[c] == 0.0 && eb == 0.0) continue;
+        const int64_t lo = h.cnode_off[c], hi = h.cnode_off[c + 1];
+        const int k = (int)(hi - lo);
+        const int32_t* ids = h.cnodes.data() + lo;
+        double area = 0.0, Sx = 0.0, Sy = 0.0;
+        for (int j = 0; j < k; ++j) {
+            const int p0 = ids[j], p1 = ids[(j + 1) % k];
+            const double cr = h.nx_[p0] * h.ny_[p1] - h.nx_[p1] * h.ny_[p0];
+            area += cr;
+            Sx += (h.nx_[p0] + h.nx_[p1]) * cr;
+            Sy += (h.ny_[p0] + h.ny_[p1]) * cr;
+        }
+        area *= 0.5;
+        // C = S / (6 area)
+        const double Sbx = cxb[c] / (6.0 * area), Sby = cyb[c] / (6.0 * area);
+        double Ab = -(cxb[c] * Sx + cyb[c] * Sy) / (6.0 * area * area);
+        // eps^2 = K^3 V^1.5 with V = |area|
+        if (eb != 0.0) Ab += eb * 1.5 * K3 * std::sqrt(std::fabs(area)) * (area < 0.0 ? -1.0 : 1.0);
+        for (int j = 0; j < k; ++j) {
+            const int p0 = ids[j], p1 = ids[(j + 1) % k];
+            const double x0 = h.nx_[p0], y0 = h.ny_[p0], x1 = h.nx_[p1], y1 = h.ny_[p1];
+            const double cr = x0 * y1 - x1 * y0;
+            xb[p0] += Sbx * cr; xb[p1] += Sbx * cr;
+            yb[p0] += Sby * cr; yb[p1] += Sby * cr;
+            const double crb = Sbx * (x0 + x1) + Sby * (y0 + y1) + 0.5 * Ab;
+            xb[p0] += crb * y1; yb[p1] += crb * x0;
+            xb[p1] -= crb * y0; yb[p0] -= crb * x1;
+        }
+    }
+    for (int f = 0; f < F; ++f) {
+        const int n1 = h.fn1[f], n2 = h.fn2[f];
+        const double dx = h.nx_[n2] - h.nx_[n1], dy = h.ny_[n2] - h.ny_[n1];
+        const double ln = std::sqrt(dx * dx + dy * dy);
+        // n = (dy, -dx) / ln, length ln, midpoint (p1 + p2) / 2
+        const double lb = arb[f] - (nxb[f] * dy - nyb[f] * dx) / (ln * ln);
+        const double dyb = nxb[f] / ln + lb * dy / ln;
+        const double dxb = -nyb[f] / ln + lb * dx / ln;
+        xb[n2] += dxb; xb[n1] -= dxb;
+        yb[n2] += dyb; yb[n1] -= dyb;
+        xb[n1] += 0.5 * fxb[f]; xb[n2] += 0.5 * fxb[f];
+        yb[n1] += 0.5 * fyb[f]; yb[n2] += 0.5 * fyb[f];
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1128,6 +1393,7 @@ int fv_adjoint_create(fv_solver_t solver, int32_t limiter_mode, fv_adjoint_t* ou
                 a.led = A->alloc<int>(4 * N);
                 a.ler = A->alloc<int>(4 * N);
                 a.lpd = A->alloc<double2>(4 * N);
+                a.lpe = A->alloc<double>(4 * N);
                 a.ldb = A->alloc<double>(4 * N);
             }
             // twin entries: the entry of the neighbour's row through the same face
@@ -1261,10 +1527,8 @@ int fv_adjoint_solve(fv_adjoint_t A, const double* dJdU, int32_t max_iter, doubl
 // last fv_adjoint_solve (which must have been solved for the same J).
 // dJ/dX = dJ/dX|explicit - lam^T dR/dX, where R depends on the nodes
 // through the face normals, lengths and midpoints, the cell centroids
-// (shoelace, src/MeshReader.cpp:56-76) and the least-squares weights built
-// from them; the limiter values stay frozen.  The device computes the
-// cotangents of those geometric quantities; this host code runs the
-// reverse pass of the geometry itself.
+// (shoelace, src/MeshReader.cpp:56-76), the least-squares weights built
+// from them and (full-limiter linearisation only) the limiter values.
 int fv_adjoint_shape_gradient(fv_adjoint_t A, fv_mesh_t mesh, int32_t objective, const double ref[7],
                               double* dJdX) {
     return fvgb::guarded([&] {
@@ -1276,155 +1540,9 @@ int fv_adjoint_shape_gradient(fv_adjoint_t A, fv_mesh_t mesh, int32_t objective,
         if (h.n_cells != A->N || h.n_faces != A->F) fvgb::raise(FV_ERR_BAD_ARG, "mesh does not match the solver");
         if (h.cnode_off.empty())
             fvgb::raise(FV_ERR_UNSUPPORTED, "shape gradient: the mesh must be built from cell polygons");
-        const int N = A->N, F = A->F, Fb = A->Fb;
-        const size_t E = (size_t)(2 * F - Fb);
-        AdjArgs& a = A->a;
-        // cotangents on the device
-        backward(A, A->lam, 0, A->Rdev);
-        double* d_face = A->alloc<double>(8 * (size_t)F);
-        double* d_ab = A->alloc<double>(2 * E);
-        double* d_sb = A->alloc<double>(2 * (size_t)N);
-        double* d_nbg = A->alloc<double>(2 * (size_t)std::max(Fb, 1));
-        FV_CUDA(cudaMemsetAsync(d_nbg, 0, sizeof(double) * 2 * (size_t)std::max(Fb, 1), s.stream));
-        FV_CUDA(cudaMemsetAsync(d_ab, 0, sizeof(double) * 2 * E, s.stream));
-        FV_CUDA(cudaMemsetAsync(d_sb, 0, sizeof(double) * 2 * (size_t)N, s.stream));
-        adjk::k_geo_face<<<blocks(F), kB, 0, s.stream>>>(a, A->lam, d_face);
-        check_launch();
-        if (a.order == 2) {
-            adjk::k_geo_cell<<<blocks(N), kB, 0, s.stream>>>(a, d_ab, d_sb, d_nbg);
-            check_launch();
-        }
-        std::vector<double> face(8 * (size_t)F), ab(2 * E), sb(2 * (size_t)N), nbg(2 * (size_t)std::max(Fb, 1));
-        FV_CUDA(cudaMemcpyAsync(face.data(), d_face, sizeof(double) * face.size(), cudaMemcpyDeviceToHost, s.stream));
-        FV_CUDA(cudaMemcpyAsync(ab.data(), d_ab, sizeof(double) * ab.size(), cudaMemcpyDeviceToHost, s.stream));
-        FV_CUDA(cudaMemcpyAsync(sb.data(), d_sb, sizeof(double) * sb.size(), cudaMemcpyDeviceToHost, s.stream));
-        FV_CUDA(cudaMemcpyAsync(nbg.data(), d_nbg, sizeof(double) * nbg.size(), cudaMemcpyDeviceToHost, s.stream));
-        FV_CUDA(cudaStreamSynchronize(s.stream));
-        // cotangents of the geometric quantities, reference numbering
-        std::vector<double> nxb(F, 0.0), nyb(F, 0.0), arb(F, 0.0), fxb(F, 0.0), fyb(F, 0.0), cxb(N, 0.0),
-            cyb(N, 0.0);
-        for (int i = 0; i < F; ++i) {
-            const int f = h.fperm[i];
-            const double* o = face.data() + 8 * (size_t)i;
-            nxb[f] += o[0];
-            nyb[f] += o[1];
-            arb[f] += o[2];
-            if (i >= h.n_int_faces) {
-                nxb[f] += nbg[2 * (size_t)(i - h.n_int_faces)];
-                nyb[f] += nbg[2 * (size_t)(i - h.n_int_faces) + 1];
-            }
-            if (a.order == 2) {
-                // r_L = x_f - x_L, r_R = x_f - x_R
-                fxb[f] += o[3]; fyb[f] += o[4];
-                cxb[h.fl[f]] -= o[3]; cyb[h.fl[f]] -= o[4];
-                if (h.fr[f] >= 0) {
-                    fxb[f] += o[5]; fyb[f] += o[6];
-                    cxb[h.fr[f]] -= o[5]; cyb[h.fr[f]] -= o[6];
-                }
-            }
-        }
-        if (a.order == 2) {
-            // least-squares weights a_e = B w_e d_e, B = M^-1, M = sum w d d^T,
-            // w = 1/|d|^2, d = x_nb - x_c (x_nb: neighbour centroid or the
-            // boundary face midpoint); their sums s_c pass sbar to every a_e
-            for (int i = 0; i < N; ++i) {
-                const int c = h.perm[i];
-                const double xc = h.cx[c], yc = h.cy[c];
-                const int e0 = h.d_cf_off[i], e1 = h.d_cf_off[i + 1];
-                double m00 = 0.0, m01 = 0.0, m11 = 0.0;
-                for (int e = e0; e < e1; ++e) {
-                    const int f = h.fperm[h.d_cf[e] >> 1];
-                    double px, py;
-                    if (h.fr[f] < 0) { px = h.fxm[f]; py = h.fym[f]; }
-                    else { const int nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
-                    const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
-                    m00 += w * dx * dx; m01 += w * dx * dy; m11 += w * dy * dy;
-                }
-                const double det = m00 * m11 - m01 * m01;
-                const double b00 = m11 / det, b01 = -m01 / det, b11 = m00 / det;
-                double B00 = 0.0, B01 = 0.0, B10 = 0.0, B11 = 0.0;  // Bbar
-                for (int e = e0; e < e1; ++e) {
-                    const int f = h.fperm[h.d_cf[e] >> 1];
-                    double px, py;
-                    if (h.fr[f] < 0) { px = h.fxm[f]; py = h.fym[f]; }
-                    else { const int nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
-                    const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
-                    const double ax = ab[2 * (size_t)e] + sb[2 * (size_t)i], ay = ab[2 * (size_t)e + 1] + sb[2 * (size_t)i + 1];
-                    B00 += ax * w * dx; B01 += ax * w * dy; B10 += ay * w * dx; B11 += ay * w * dy;
-                }
-                // Mbar = -B^T Bbar B^T (B symmetric)
-                const double t00 = b00 * B00 + b01 * B10, t01 = b00 * B01 + b01 * B11;
-                const double t10 = b01 * B00 + b11 * B10, t11 = b01 * B01 + b11 * B11;
-                const double M00 = -(t00 * b00 + t01 * b01), M01 = -(t00 * b01 + t01 * b11);
-                const double M10 = -(t10 * b00 + t11 * b01), M11 = -(t10 * b01 + t11 * b11);
-                for (int e = e0; e < e1; ++e) {
-                    const int f = h.fperm[h.d_cf[e] >> 1];
-                    const bool bnd = h.fr[f] < 0;
-                    int nb = -1;
-                    double px, py;
-                    if (bnd) { px = h.fxm[f]; py = h.fym[f]; }
-                    else { nb = h.fl[f] == c ? h.fr[f] : h.fl[f]; px = h.cx[nb]; py = h.cy[nb]; }
-                    const double dx = px - xc, dy = py - yc, w = 1.0 / (dx * dx + dy * dy);
-                    const double ax = ab[2 * (size_t)e] + sb[2 * (size_t)i], ay = ab[2 * (size_t)e + 1] + sb[2 * (size_t)i + 1];
-                    // (w d)bar = B a_bar
-                    const double vx = b00 * ax + b01 * ay, vy = b01 * ax + b11 * ay;
-                    // M = sum w d d^T: dbar += w (Mbar + Mbar^T) d, wbar += d^T Mbar d
-                    double ddx = w * ((M00 + M00) * dx + (M01 + M10) * dy) + w * vx;
-                    double ddy = w * ((M10 + M01) * dx + (M11 + M11) * dy) + w * vy;
-                    const double wb = dx * (M00 * dx + M01 * dy) + dy * (M10 * dx + M11 * dy) + dx * vx + dy * vy;
-                    ddx += wb * (-2.0 * w * w * dx);
-                    ddy += wb * (-2.0 * w * w * dy);
-                    if (bnd) { fxb[f] += ddx; fyb[f] += ddy; }
-                    else { cxb[nb] += ddx; cyb[nb] += ddy; }
-                    cxb[c] -= ddx;
-                    cyb[c] -= ddy;
-                }
-            }
-        }
-        // node cotangents of lam^T R
-        const int nn = h.n_nodes;
-        std::vector<double> xb(nn, 0.0), yb(nn, 0.0);
-        for (int c = 0; c < N; ++c) {
-            if (cxb[c] == 0.0 && cyb[c] == 0.0) continue;
-            const int64_t lo = h.cnode_off[c], hi = h.cnode_off[c + 1];
-            const int k = (int)(hi - lo);
-            const int32_t* ids = h.cnodes.data() + lo;
-            double area = 0.0, Sx = 0.0, Sy = 0.0;
-            for (int j = 0; j < k; ++j) {
-                const int p0 = ids[j], p1 = ids[(j + 1) % k];
-                const double cr = h.nx_[p0] * h.ny_[p1] - h.nx_[p1] * h.ny_[p0];
-                area += cr;
-                Sx += (h.nx_[p0] + h.nx_[p1]) * cr;
-                Sy += (h.ny_[p0] + h.ny_[p1]) * cr;
-            }
-            area *= 0.5;
-            // C = S / (6 area)
-            const double Sbx = cxb[c] / (6.0 * area), Sby = cyb[c] / (6.0 * area);
-            const double Ab = -(cxb[c] * Sx + cyb[c] * Sy) / (6.0 * area * area);
-            for (int j = 0; j < k; ++j) {
-                const int p0 = ids[j], p1 = ids[(j + 1) % k];
-                const double x0 = h.nx_[p0], y0 = h.ny_[p0], x1 = h.nx_[p1], y1 = h.ny_[p1];
-                const double cr = x0 * y1 - x1 * y0;
-                xb[p0] += Sbx * cr; xb[p1] += Sbx * cr;
-                yb[p0] += Sby * cr; yb[p1] += Sby * cr;
-                const double crb = Sbx * (x0 + x1) + Sby * (y0 + y1) + 0.5 * Ab;
-                xb[p0] += crb * y1; yb[p1] += crb * x0;
-                xb[p1] -= crb * y0; yb[p0] -= crb * x1;
-            }
-        }
-        for (int f = 0; f < F; ++f) {
-            const int n1 = h.fn1[f], n2 = h.fn2[f];
-            const double dx = h.nx_[n2] - h.nx_[n1], dy = h.ny_[n2] - h.ny_[n1];
-            const double ln = std::sqrt(dx * dx + dy * dy);
-            // n = (dy, -dx) / ln, length ln, midpoint (p1 + p2) / 2
-            const double lb = arb[f] - (nxb[f] * dy - nyb[f] * dx) / (ln * ln);
-            const double dyb = nxb[f] / ln + lb * dy / ln;
-            const double dxb = -nyb[f] / ln + lb * dx / ln;
-            xb[n2] += dxb; xb[n1] -= dxb;
-            yb[n2] += dyb; yb[n1] -= dyb;
-            xb[n1] += 0.5 * fxb[f]; xb[n2] += 0.5 * fxb[f];
-            yb[n1] += 0.5 * fyb[f]; yb[n2] += 0.5 * fyb[f];
-        }
+        std::vector<double> xb, yb;
+        residual_geometry_vjp(A, h, A->lam, xb, yb);
+        const int N = A->N, nn = h.n_nodes;
         // explicit part: J = sum_wall p_c (k . n) |f| / qL at the adjoint's state
         std::vector<double> U(4 * (size_t)N);
         download_ref(A, A->U, U.data());
@@ -1462,6 +1580,25 @@ int fv_adjoint_shape_gradient(fv_adjoint_t A, fv_mesh_t mesh, int32_t objective,
         for (int i = 0; i < nn; ++i) {
             dJdX[2 * (size_t)i] = ex[i] - xb[i];
             dJdX[2 * (size_t)i + 1] = ey[i] - yb[i];
+        }
+    });
+}
+
+// (dR/dX)^T Rbar over the mesh nodes at the linearisation state.
+int fv_residual_shape_vjp(fv_adjoint_t A, fv_mesh_t mesh, const double* Rbar, double* Xbar) {
+    return fvgb::guarded([&] {
+        if (!A || !mesh || !Rbar || !Xbar) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (!A->linearised) fvgb::raise(FV_ERR_BAD_ARG, "call fv_residual_forward first");
+        const fvgb::HostMesh& h = fvgb::host_mesh_of(mesh);
+        if (h.n_cells != A->N || h.n_faces != A->F) fvgb::raise(FV_ERR_BAD_ARG, "mesh does not match the solver");
+        if (h.cnode_off.empty())
+            fvgb::raise(FV_ERR_UNSUPPORTED, "shape cotangent: the mesh must be built from cell polygons");
+        upload_ref(A, Rbar, A->stage_dev);
+        std::vector<double> xb, yb;
+        residual_geometry_vjp(A, h, A->stage_dev, xb, yb);
+        for (int i = 0; i < h.n_nodes; ++i) {
+            Xbar[2 * (size_t)i] = xb[i];
+            Xbar[2 * (size_t)i + 1] = yb[i];
         }
     });
 }

@@ -448,6 +448,36 @@ def naca_hybrid(ni: int = 1024, n_layers: int = 40, first: float = 4.5e-6, growt
     return mesh
 
 
+def wall_normal_directions(poly: PolyMesh, n_dirs: int, seed: int = 0, width: int = 20, patch: int = 0):
+    """Seeded surface-normal displacement fields of one closed wall loop
+    (boundary patch ``patch``): white noise on the wall nodes smoothed by a
+    periodic Gaussian over ``width`` nodes (sigma width/3), times the unit
+    node normal; each field [n_nodes, 2] scaled to a maximum of 1 and zero
+    off the wall."""
+    e = poly.bedges[poly.bpatch == patch]
+    nxt = {int(a): int(b) for a, b in e}
+    order = [int(e[0, 0])]
+    while nxt[order[-1]] != order[0]:
+        order.append(nxt[order[-1]])
+    order = np.array(order)
+    P = poly.nodes[order]
+    t = np.roll(P, -1, axis=0) - np.roll(P, 1, axis=0)
+    nrm = np.stack([t[:, 1], -t[:, 0]], 1)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    rng = np.random.default_rng(seed)
+    k = np.arange(-width, width + 1)
+    ker = np.exp(-0.5 * (k / (width / 3.0)) ** 2)
+    out = []
+    for _ in range(n_dirs):
+        w = rng.standard_normal(len(order))
+        a = sum(ker[j] * np.roll(w, k[j]) for j in range(len(k)))
+        a /= np.abs(a).max()
+        d = np.zeros_like(poly.nodes)
+        d[order] = a[:, None] * nrm
+        out.append(d)
+    return out
+
+
 def cached(name: str, **kw) -> PolyMesh:
     """Generate ``name(**kw)`` once and keep it as .npz in a cache folder.
 

@@ -445,6 +445,14 @@ class DiscreteAdjoint:
                                                         capi.dptr(r), capi.dptr(out)))
         return out
 
+    def shape_vjp(self, Rbar) -> np.ndarray:
+        """(dR/dX)^T Rbar [n_nodes, 2] at the linearisation state."""
+        out = np.zeros((self.solver.mesh.poly.n_nodes, 2))
+        capi.check(capi.lib().fv_residual_shape_vjp(self._h, self.solver.mesh.handle,
+                                                    capi.dptr(np.ascontiguousarray(Rbar, dtype=np.float64)),
+                                                    capi.dptr(out)))
+        return out
+
     def freestream_gradient(self, objective: Objective, mach: float, aoa_deg: float, farfield_patches,
                             max_iter: int = 20000, tol: float = 1e-12) -> dict:
         """dJ/dM and dJ/dAoA (per degree) of a force coefficient at a

@@ -306,8 +306,8 @@ typedef struct fv_adjoint_s* fv_adjoint_t;
 /* FROZEN: the limiter values are held at the linearisation state (the
  * usual frozen-limiter adjoint); FULL: the limiter is differentiated too,
  * through its active branch (neighbour extreme, face extrapolation extreme,
- * Venkatakrishnan / Barth-Jespersen formula).  Shape gradients hold the
- * limiter's own geometric inputs (face offsets, eps) fixed in both modes. */
+ * Venkatakrishnan / Barth-Jespersen formula), including its geometric
+ * inputs (face offsets, eps^2, boundary extremes) in shape gradients. */
 enum { FV_ADJ_FROZEN_LIMITER = 0, FV_ADJ_FULL_LIMITER = 1 };
 int fv_adjoint_create(fv_solver_t s, int32_t limiter_mode, fv_adjoint_t* out);
 int fv_adjoint_destroy(fv_adjoint_t a);
@@ -329,10 +329,14 @@ int fv_adjoint_solve(fv_adjoint_t a, const double* dJdU, int32_t max_iter, doubl
 /* Shape gradient dJ/dX [2 n_nodes] (x, y per node, the mesh's node
  * numbering) of the objective the last fv_adjoint_solve was solved for:
  * dJ/dX|explicit - lambda^T dR/dX through face normals, lengths and
- * midpoints, shoelace cell centroids and the least-squares weights (limiter
- * values frozen).  mesh is the mesh the solver was created from; it must
- * have been built from cell polygons (fv_mesh_create_polygons). */
+ * midpoints, shoelace cell centroids, the least-squares weights and (FULL
+ * mode) the limiter values.  mesh is the mesh the solver was created from;
+ * it must have been built from cell polygons (fv_mesh_create_polygons). */
 int fv_adjoint_shape_gradient(fv_adjoint_t a, fv_mesh_t mesh, int32_t objective, const double ref[7], double* dJdX);
+/* Geometric cotangent Xbar = (dR/dX)^T Rbar [2 n_nodes] at the
+ * linearisation state (the residual's node sensitivities alone; the same
+ * map the shape gradient applies to lambda). */
+int fv_residual_shape_vjp(fv_adjoint_t a, fv_mesh_t mesh, const double* Rbar, double* Xbar);
 /* Wall-force coefficient J (objective 0 drag, 1 lift, 2 moment; pressure
  * part with the owner-cell pressure, ref as fv_wall_forces) at the
  * solver's current state, and dJ/dU (may be NULL). */

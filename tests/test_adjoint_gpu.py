@@ -163,31 +163,7 @@ def test_freestream_gradients_match_converged_differences(gpu, order):
 
 
 def _wall_normal_directions(poly, n_dirs, seed, width=20):
-    """Seeded surface-normal displacement fields of the wall (patch 0):
-    white noise on the wall nodes smoothed by a periodic Gaussian over
-    ``width`` nodes, times the unit node normal; each scaled to max 1."""
-    e = poly.bedges[poly.bpatch == 0]
-    order = [int(e[0, 0])]
-    nxt = {int(a): int(b) for a, b in e}
-    while nxt[order[-1]] != order[0]:
-        order.append(nxt[order[-1]])
-    order = np.array(order)
-    P = poly.nodes[order]
-    t = np.roll(P, -1, axis=0) - np.roll(P, 1, axis=0)
-    nrm = np.stack([t[:, 1], -t[:, 0]], 1)
-    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
-    rng = np.random.default_rng(seed)
-    k = np.arange(-width, width + 1)
-    ker = np.exp(-0.5 * (k / (width / 3.0)) ** 2)
-    out = []
-    for _ in range(n_dirs):
-        w = rng.standard_normal(len(order))
-        a = sum(ker[j] * np.roll(w, k[j]) for j in range(len(k)))
-        a /= np.abs(a).max()
-        d = np.zeros_like(poly.nodes)
-        d[order] = a[:, None] * nrm
-        out.append(d)
-    return out
+    return meshgen.wall_normal_directions(poly, n_dirs, seed, width)
 
 
 def _moved(poly, d):
@@ -226,3 +202,39 @@ def test_shape_gradient_matches_converged_differences(gpu, order):
         ad_cd = float(np.sum(grads[S.Objective.Drag] * d))
         assert abs(ad_cl - fd_cl) <= 1e-4 * max(abs(fd_cl), 1e-3), (ad_cl, fd_cl)
         assert abs(ad_cd - fd_cd) <= 1e-4 * max(abs(fd_cd), 1e-3), (ad_cd, fd_cd)
+
+
+@pytest.mark.parametrize("limiter,full", [(S.Limiter.NoLimiter, False), (S.Limiter.Venkatakrishnan, True)])
+def test_residual_shape_cotangent_matches_central_differences(gpu, limiter, full):
+    """(dR/dX)^T Rbar against central differences of the residual under a
+    smooth displacement of every node (geometry recomputed on the device),
+    transonic flow; with the limiter active the full-limiter map includes
+    the limiter's geometric inputs and the frozen one misses them."""
+    poly = meshgen.naca_ogrid(96, 48, r_far=10.0)
+    mesh = S.Mesh(poly)
+    s = _solver(mesh, _fs(0.75, 2.0), 2, S.NumericalFluxScheme.HLLC, limiter)
+    s.run(400)
+    U = s.field()
+    X = poly.nodes.copy()
+    x, y = X[:, 0], X[:, 1]
+    d = 0.1 * np.stack([np.sin(0.7 * x + 0.3 * y), np.cos(0.5 * x - 0.9 * y)], 1)
+    d += _wall_normal_directions(poly, 1, seed=4)[0]
+    rng = np.random.default_rng(9)
+    Rb = rng.standard_normal(U.shape)
+    adj = S.DiscreteAdjoint(s, full_limiter=full)
+    h = 1e-7
+    s.update_nodes(X + h * d)
+    Rp = adj.forward(U)
+    s.update_nodes(X - h * d)
+    Rm = adj.forward(U)
+    s.update_nodes(X)
+    adj.forward(U)
+    fd = float(np.sum(Rb * (Rp - Rm))) / (2 * h)
+    scale = float(np.sum(np.abs(Rb * (Rp - Rm)))) / (2 * h)
+    e = abs(float(np.sum(adj.shape_vjp(Rb) * d)) - fd) / scale
+    assert e < 1e-6, (e, fd, scale)
+    if full:
+        frozen = S.DiscreteAdjoint(s)
+        frozen.forward(U)
+        e_frozen = abs(float(np.sum(frozen.shape_vjp(Rb) * d)) - fd) / scale
+        assert e_frozen > 10 * e, (e, e_frozen)

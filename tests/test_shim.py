@@ -58,6 +58,14 @@ def test_driver_compiles_against_reference_headers(tmp_path):
     assert os.path.exists(compile_driver(str(tmp_path), inc))
 
 
+def test_driver_compiles_against_stand_in_declarations(tmp_path):
+    """The GPU test compiles the driver with tests/shim/ref_decls (the
+    reference is not installed there): those stand-ins must cover every
+    reference type the drop-in headers use."""
+    build.build_library()
+    assert os.path.exists(compile_driver(str(tmp_path), os.path.join(SHIM, "ref_decls")))
+
+
 def _run(exe, mesh_txt, case, out):
     with open(out + ".case", "w") as f:
         f.write("\n".join(f"{k} {float(v)!r}" for k, v in case.items()) + "\n")
