@@ -129,6 +129,8 @@ SIGNATURES = {
     "fv_residual_jvp": (C.c_int, [_P, _D, _D, _D]),
     "fv_residual_backward": (C.c_int, [_P, _D, _D, _D]),
     "fv_adjoint_solve": (C.c_int, [_P, _D, C.c_int32, C.c_double, _D, _D, _D, C.POINTER(C.c_int32)]),
+    "fv_adjoint_solve_gmres": (C.c_int, [_P, _D, C.c_int32, C.c_int32, C.c_double, _D, _D, _D,
+                                         C.POINTER(C.c_int32), _D]),
     "fv_force_gradient": (C.c_int, [_P, C.c_int32, _D, _D, _D]),
     "fv_adjoint_shape_gradient": (C.c_int, [_P, _P, C.c_int32, _D, _D]),
     "fv_residual_shape_vjp": (C.c_int, [_P, _P, _D, _D]),

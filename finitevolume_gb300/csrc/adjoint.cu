@@ -974,6 +974,76 @@ __global__ void k_perm_scatter(const St* __restrict__ in_dev, St* __restrict__ o
     if (i < n) out_ref[perm[i]] = in_dev[i];
 }
 
+
+// ---------------------------------------------------------------------------
+// Krylov vector kernels (GMRES on the fixed point of the pseudo-time
+// iteration).  Vectors are flat double arrays (n = 4 N); a dot product is
+// block partials over a fixed grid folded in block order by one block, so
+// every reduction is deterministic.
+constexpr int kKB = 256;
+constexpr int kKGrid = 1024;
+
+__device__ __forceinline__ double block_sum(double t) {
+    __shared__ double red[kKB / 32];
+    t = warp_sum(t);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+    __syncthreads();
+    double v = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < kKB / 32; ++w) v += red[w];
+    return v;
+}
+
+__global__ void __launch_bounds__(kKB) k_dot(const double* __restrict__ x, const double* __restrict__ y, size_t n,
+                                             double* __restrict__ partials) {
+    double t = 0.0;
+    for (size_t i = blockIdx.x * (size_t)kKB + threadIdx.x; i < n; i += (size_t)gridDim.x * kKB) t += x[i] * y[i];
+    const double v = block_sum(t);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+}
+
+// out[0] = sum of the partials (its square root when sq)
+__global__ void __launch_bounds__(kKB) k_fold(const double* __restrict__ partials, int nblk, double* __restrict__ out,
+                                              int sq) {
+    double t = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += kKB) t += partials[b];
+    const double v = block_sum(t);
+    if (threadIdx.x == 0) out[0] = sq ? sqrt(v) : v;
+}
+
+// y -= alpha[0] x
+__global__ void k_axmy_dev(double* __restrict__ y, const double* __restrict__ x, const double* __restrict__ alpha,
+                           size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] -= alpha[0] * x[i];
+}
+
+// out = x / nrm[0]
+__global__ void k_div_dev(double* __restrict__ out, const double* __restrict__ x, const double* __restrict__ nrm,
+                          size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = x[i] / nrm[0];
+}
+
+// w = v - p + c  ((I - M) v for the affine map p = M v + c)
+__global__ void k_fp_apply(double* __restrict__ w, const double* __restrict__ v, const double* __restrict__ p,
+                           const double* __restrict__ c, size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) w[i] = (v[i] - p[i]) + c[i];
+}
+
+// w = p - x
+__global__ void k_sub(double* __restrict__ w, const double* __restrict__ p, const double* __restrict__ x, size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) w[i] = p[i] - x[i];
+}
+
+// y += a x
+__global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, double a, size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] += a * x[i];
+}
+
 }  // namespace adjk
 
 // ===========================================================================
@@ -996,6 +1066,11 @@ struct fv_adjoint_s {
     double2 *Gu = nullptr, *G = nullptr;
     double *psi = nullptr, *cs = nullptr, *partials = nullptr, *hist = nullptr, *dfs_dev = nullptr;
     int* counter = nullptr;
+    // GMRES work arrays (allocated on first use): restart + 1 basis vectors,
+    // the affine part c, the work vector, the iterate, reduction partials
+    // and device scalars
+    double *kV = nullptr, *kc = nullptr, *kw = nullptr, *kx = nullptr, *kpart = nullptr, *kh = nullptr;
+    int k_restart = 0;
     // shape-gradient work arrays (allocated on first use)
     double *geo_face = nullptr, *geo_ab = nullptr, *geo_sb = nullptr, *geo_nbg = nullptr, *geo_er = nullptr,
            *geo_ep = nullptr;
@@ -1308,6 +1383,22 @@ void residual_geometry_vjp(fv_adjoint_s* A, const fvgb::HostMesh& h, const St* l
     }
 }
 
+// One SSP-RK3 pseudo-time iteration of the adjoint, in place on A->lam:
+// lam <- P(lam) = M lam + c, affine with c = P(0).
+void rk_step(fv_adjoint_s* A) {
+    for (int st = 1; st <= 3; ++st) backward(A, A->lam, st, nullptr);
+}
+
+// sqrt(<x, y>) or <x, y> into the device scalar *out
+void kdot(fv_adjoint_s* A, const double* x, const double* y, double* out, bool sq) {
+    fvgb::Solver& s = A->solver->s;
+    const size_t n = 4 * (size_t)A->N;
+    const int grid = (int)std::min<size_t>(adjk::kKGrid, (n + adjk::kKB - 1) / adjk::kKB);
+    adjk::k_dot<<<grid, adjk::kKB, 0, s.stream>>>(x, y, n, A->kpart);
+    adjk::k_fold<<<1, adjk::kKB, 0, s.stream>>>(A->kpart, grid, out, sq ? 1 : 0);
+    check_launch();
+}
+
 }  // namespace
 
 extern "C" {
@@ -1515,6 +1606,154 @@ int fv_adjoint_solve(fv_adjoint_t A, const double* dJdU, int32_t max_iter, doubl
         if (lambda) download_ref(A, A->lam, lambda);
         if (fsbar) {
             // lam^T dR/dfs at the converged lam
+            backward(A, A->lam, 0, A->Rdev);
+            reduce_fsbar(A, fsbar);
+        }
+        FV_CUDA(cudaStreamSynchronize(s.stream));
+    });
+}
+
+// Restarted GMRES on the fixed point of the pseudo-time iteration:
+// lam = P(lam) = M lam + c  <=>  (I - M) lam = c, each application of
+// (I - M) one SSP-RK3 pseudo-time iteration.  The fixed point is the
+// adjoint solution whatever the spectral radius of M: GMRES converges
+// where the iteration itself diverges (a primal whose explicit iteration
+// limit-cycles at the converged state, or a frozen-limiter linearisation
+// with growing modes).  Arnoldi with modified Gram-Schmidt; the Hessenberg
+// columns come to the host once per matvec for the Givens rotations.
+int fv_adjoint_solve_gmres(fv_adjoint_t A, const double* dJdU, int32_t restart, int32_t max_matvec, double rtol,
+                           double* lambda, double* fsbar, double* history, int32_t* matvecs, double residual[4]) {
+    return fvgb::guarded([&] {
+        if (!A || !dJdU || restart < 1 || max_matvec < 1 || !(rtol > 0.0)) fvgb::raise(FV_ERR_BAD_ARG, "bad argument");
+        if (!A->linearised) fvgb::raise(FV_ERR_BAD_ARG, "call fv_residual_forward first");
+        fvgb::Solver& s = A->solver->s;
+        const size_t n = 4 * (size_t)A->N;
+        const int m = restart;
+        if (A->k_restart < m) {
+            // a larger basis replaces the smaller one (the old buffers stay owned until destroy)
+            A->kV = A->alloc<double>((size_t)(m + 1) * n);
+            A->kh = A->alloc<double>((size_t)m + 2);
+            A->k_restart = m;
+        }
+        if (!A->kc) {
+            A->kc = A->alloc<double>(n);
+            A->kw = A->alloc<double>(n);
+            A->kx = A->alloc<double>(n);
+            A->kpart = A->alloc<double>(adjk::kKGrid);
+        }
+        const int vb = (int)((n + 255) / 256);
+        double* lam = reinterpret_cast<double*>(A->lam);
+        auto V = [&](int i) { return A->kV + (size_t)i * n; };
+        upload_ref(A, dJdU, A->rhs);
+        // c = P(0)
+        FV_CUDA(cudaMemsetAsync(A->lam, 0, sizeof(St) * (size_t)A->N, s.stream));
+        FV_CUDA(cudaMemsetAsync(A->counter, 0, sizeof(int), s.stream));
+        rk_step(A);
+        FV_CUDA(cudaMemcpyAsync(A->kc, lam, sizeof(double) * n, cudaMemcpyDeviceToDevice, s.stream));
+        FV_CUDA(cudaMemsetAsync(A->kx, 0, sizeof(double) * n, s.stream));
+        double beta0 = 0.0;
+        kdot(A, A->kc, A->kc, A->kh, true);
+        FV_CUDA(cudaMemcpyAsync(&beta0, A->kh, sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+        FV_CUDA(cudaStreamSynchronize(s.stream));
+        if (!std::isfinite(beta0)) fvgb::raise(FV_ERR_NONFINITE, "adjoint GMRES: non-finite right-hand side");
+        int mv = 1;  // c = P(0) took one pseudo-time iteration
+        std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hcol(m + 2);
+        std::vector<double> hh((size_t)max_matvec, -1.0);  // relative residual after each matvec
+        hh[0] = 1.0;
+        bool done = beta0 == 0.0;
+        while (!done && mv < max_matvec) {
+            // r = c - (I - M) x = P(x) - x
+            FV_CUDA(cudaMemcpyAsync(lam, A->kx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s.stream));
+            rk_step(A);
+            ++mv;
+            adjk::k_sub<<<vb, 256, 0, s.stream>>>(V(0), lam, A->kx, n);
+            kdot(A, V(0), V(0), A->kh, true);
+            double beta = 0.0;
+            FV_CUDA(cudaMemcpyAsync(&beta, A->kh, sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+            FV_CUDA(cudaStreamSynchronize(s.stream));
+            if (!std::isfinite(beta)) fvgb::raise(FV_ERR_NONFINITE, "adjoint GMRES diverged");
+            hh[mv - 1] = beta / beta0;
+            if (beta <= rtol * beta0) break;
+            adjk::k_div_dev<<<vb, 256, 0, s.stream>>>(V(0), V(0), A->kh, n);
+            check_launch();
+            std::fill(g.begin(), g.end(), 0.0);
+            g[0] = beta;
+            int k = 0;
+            for (int j = 0; j < m && mv < max_matvec; ++j) {
+                // w = (I - M) V_j = V_j - P(V_j) + c
+                FV_CUDA(cudaMemcpyAsync(lam, V(j), sizeof(double) * n, cudaMemcpyDeviceToDevice, s.stream));
+                rk_step(A);
+                ++mv;
+                adjk::k_fp_apply<<<vb, 256, 0, s.stream>>>(A->kw, V(j), lam, A->kc, n);
+                for (int i = 0; i <= j; ++i) {
+                    kdot(A, A->kw, V(i), A->kh + i, false);
+                    adjk::k_axmy_dev<<<vb, 256, 0, s.stream>>>(A->kw, V(i), A->kh + i, n);
+                }
+                kdot(A, A->kw, A->kw, A->kh + j + 1, true);
+                FV_CUDA(cudaMemcpyAsync(hcol.data(), A->kh, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost,
+                                        s.stream));
+                FV_CUDA(cudaStreamSynchronize(s.stream));
+                for (int i = 0; i <= j + 1; ++i)
+                    if (!std::isfinite(hcol[i])) fvgb::raise(FV_ERR_NONFINITE, "adjoint GMRES diverged");
+                const double hnext = hcol[j + 1];
+                if (hnext > 0.0) {
+                    adjk::k_div_dev<<<vb, 256, 0, s.stream>>>(V(j + 1), A->kw, A->kh + j + 1, n);
+                    check_launch();
+                }
+                // Givens rotations of column j
+                for (int i = 0; i < j; ++i) {
+                    const double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+                    hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+                    hcol[i] = t;
+                }
+                const double den = std::hypot(hcol[j], hcol[j + 1]);
+                cs[j] = den > 0.0 ? hcol[j] / den : 1.0;
+                sn[j] = den > 0.0 ? hcol[j + 1] / den : 0.0;
+                hcol[j] = den;
+                g[j + 1] = -sn[j] * g[j];
+                g[j] = cs[j] * g[j];
+                for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hcol[i];
+                k = j + 1;
+                const double res = std::fabs(g[j + 1]);
+                hh[mv - 1] = res / beta0;
+                if (res <= rtol * beta0 || !(hnext > 0.0)) {
+                    done = true;
+                    break;
+                }
+            }
+            // x += V y, H y = g (upper triangular, k x k)
+            for (int i = k - 1; i >= 0; --i) {
+                double t = g[i];
+                for (int l = i + 1; l < k; ++l) t -= H[(size_t)i * m + l] * y[l];
+                y[i] = t / H[(size_t)i * m + i];
+            }
+            for (int i = 0; i < k; ++i) {
+                adjk::k_axpy<<<vb, 256, 0, s.stream>>>(A->kx, V(i), y[i], n);
+                check_launch();
+            }
+        }
+        if (matvecs) *matvecs = mv;
+        if (history)
+            for (int i = 0; i < mv && i < max_matvec; ++i) history[i] = hh[i] >= 0.0 ? hh[i] : (i ? history[i - 1] : 1.0);
+        // lam = x; the adjoint residual norms (dR/dU)^T lam - dJdU of one stage-0 evaluation
+        if (A->hist_cap < 1) {
+            if (A->hist) cudaFree(A->hist);
+            A->hist = nullptr;
+            FV_CUDA(cudaMalloc(&A->hist, sizeof(double) * 4));
+            A->hist_cap = 1;
+        }
+        FV_CUDA(cudaMemcpyAsync(lam, A->kx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s.stream));
+        FV_CUDA(cudaMemsetAsync(A->counter, 0, sizeof(int), s.stream));
+        backward(A, A->lam, 1, nullptr);
+        double r4[4];
+        FV_CUDA(cudaMemcpyAsync(r4, A->hist, sizeof(double) * 4, cudaMemcpyDeviceToHost, s.stream));
+        FV_CUDA(cudaMemcpyAsync(lam, A->kx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s.stream));
+        FV_CUDA(cudaStreamSynchronize(s.stream));
+        if (residual)
+            for (int q = 0; q < 4; ++q) residual[q] = r4[q];
+        A->solved = true;
+        if (lambda) download_ref(A, A->lam, lambda);
+        if (fsbar) {
             backward(A, A->lam, 0, A->Rdev);
             reduce_fsbar(A, fsbar);
         }

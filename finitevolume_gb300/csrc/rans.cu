@@ -35,10 +35,13 @@ __device__ __forceinline__ double sa_fv1(double nut, double nu, const double* c)
 }
 __device__ __forceinline__ double sa_nut(double nut, double nu, const double* c) { return nut * sa_fv1(nut, nu, c); }
 
-// constants c[]: cb1, cb2, sigma, kappa, cw2, cw3, cv1, cv2, cv3
+// constants c[]: cb1, cb2, sigma, kappa, cw2, cw3, cv1, cv2, cv3; cw3_6 = cw3^6.
+// The model's integer powers r^6, g^6 are formed by three multiplies and
+// its sixth root as cbrt(sqrt(.)): within a few ulp of pow(), at a small
+// fraction of its FP64-pipe cost.
 __device__ __forceinline__ double sa_source(double nut, double nu, double omega, double d, double gx, double gy,
-                                            const double* c) {
-    const double cb1 = c[0], cb2 = c[1], sigma = c[2], kappa = c[3], cw2 = c[4], cw3 = c[5], cv2 = c[7], cv3 = c[8];
+                                            const double* c, double cw3_6) {
+    const double cb1 = c[0], cb2 = c[1], sigma = c[2], kappa = c[3], cw2 = c[4], cv2 = c[7], cv3 = c[8];
     double chi = (nut > 0.0) ? nut / nu : 0.0;
     double fv1 = sa_fv1(nut, nu, c);
     double fv2 = 1.0 - chi / (1.0 + chi * fv1);
@@ -52,8 +55,10 @@ __device__ __forceinline__ double sa_source(double nut, double nu, double omega,
     if (nut > 0.0) {
         double s_tilde_safe = rmax(s_tilde, 1e-10);
         double r = rmin(nut / (s_tilde_safe * kappa * kappa * d2), 10.0);
-        double g = r + cw2 * (pow(r, 6.0) - r);
-        double fw = g * pow((1.0 + pow(cw3, 6.0)) / (pow(g, 6.0) + pow(cw3, 6.0)), 1.0 / 6.0);
+        const double r2 = r * r;
+        double g = r + cw2 * (r2 * r2 * r2 - r);
+        const double g2 = g * g;
+        double fw = g * cbrt(sqrt((1.0 + cw3_6) / (g2 * g2 * g2 + cw3_6)));
         double nut_over_d = nut / d;
         const double cw1 = cb1 / (kappa * kappa) + (1.0 + cb2) / sigma;
         destruction = cw1 * fw * nut_over_d * nut_over_d;
@@ -143,36 +148,38 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_sa_face(const RansArgs a) 
         const St UL = ld_state(n.U, cl);
         const St UR = bnd ? ghost_state(n.bc, n.fpatch[f], UL, nx, ny, n.gamma) : ld_state(n.U, cr);
         const double2 nuL = a.nu[cl];
+        const double4_32a wl = n.prim[cl];
+        // interior neighbour's primitives and (nu, nu_t); the cell pass
+        // formed them from the same U by the same operations (u = ru / r,
+        // nu = mu / r, nu_t = sa_nut(nut, nu)), so reading them is exact
+        const double4_32a wr = bnd ? wl : n.prim[cr];
+        const double2 nuR = bnd ? nuL : a.nu[cr];
 
         // compute_dt (src/RANSTurbulenceSASolver.cpp, nu + nu_t diffusion limit)
         {
-            double uL = UL.ru / UL.r;
-            double vL = UL.rv / UL.r;
-            double VnL = uL * nx + vL * ny;
+            double VnL = wl.x * nx + wl.y * ny;
             double Smax = fabs(VnL) + sound_speed(UL, n.gamma);
-            double rho_min = UL.r;
-            double nu_t_max = sa_nut(a.nut[cl], n.mu / UL.r, a.sa);
+            double nu_t_max = nuL.y;
+            // mu / min(rho_L, rho_R) = max(mu / rho_L, mu / rho_R) (rounding is monotone)
+            double nu_max = nuL.x;
             if (!bnd) {
-                double uR = UR.ru / UR.r;
-                double vR = UR.rv / UR.r;
-                double VnR = uR * nx + vR * ny;
+                double VnR = wr.x * nx + wr.y * ny;
                 Smax = rmax(Smax, fabs(VnR) + sound_speed(UR, n.gamma));
-                rho_min = rmin(rho_min, UR.r);
-                nu_t_max = rmax(nu_t_max, sa_nut(a.nut[cr], n.mu / UR.r, a.sa));
+                nu_max = rmax(nu_max, nuR.x);
+                nu_t_max = rmax(nu_t_max, nuR.y);
             }
             const double length = fg[5];
-            const double nu_lam = (n.mu > 0.0) ? n.mu / rho_min : 0.0;
+            const double nu_lam = (n.mu > 0.0) ? nu_max : 0.0;
             const double nu_eff = nu_lam + nu_t_max;
             const double Smax_total = Smax + 2.0 * nu_eff / length;
             cand = n.ctl->cfl * length / Smax_total;
         }
 
         const St inv = num_flux<FLUX>(UL, UR, nx, ny, n.gamma, n.exact_tol, n.exact_max_iter);
-        const double4_32a wl = n.prim[cl];
         const double nut_L = wl.w;
-        const double nut_R = bnd ? boundary_field(a, f, cl, 3) : a.nut[cr];
+        const double nut_R = bnd ? boundary_field(a, f, cl, 3) : wr.w;
         // advection with the face-averaged velocity of the inviscid state pair
-        const double u_R_ghost = UR.ru / UR.r, v_R_ghost = UR.rv / UR.r;
+        const double u_R_ghost = bnd ? UR.ru / UR.r : wr.x, v_R_ghost = bnd ? UR.rv / UR.r : wr.y;
         const double Vn = 0.5 * ((wl.x + u_R_ghost) * nx + (wl.y + v_R_ghost) * ny);
         const double nut_upwind = (Vn >= 0.0) ? nut_L : nut_R;
         const double nut_adv = Vn * nut_upwind * area;
@@ -188,7 +195,6 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_sa_face(const RansArgs a) 
                 for (int k = 0; k < 3; ++k) pR[k] = boundary_field(a, f, cl, k);
                 for (int k = 0; k < 4; ++k) gR[k] = make_double2(0.0, 0.0);
             } else {
-                const double4_32a wr = n.prim[cr];
                 pR[0] = wr.x; pR[1] = wr.y; pR[2] = wr.z;
                 for (int k = 0; k < 4; ++k) gR[k] = a.grad[4 * cr + k];
             }
@@ -198,12 +204,12 @@ __global__ void __launch_bounds__(fvgb::kFaceBlock) k_sa_face(const RansArgs a) 
                 const double2 gL = a.grad[4 * cl + k];
                 fgv[k] = fvgb::face_gradient(fg, bnd, pL[k], pR[k], gL.x, gL.y, gR[k].x, gR[k].y);
             }
-            const double nu_lam_R = bnd ? nuL.x : a.nu[cr].x;
-            const double nu_t_R = bnd ? sa_nut(nut_R, nu_lam_R, a.sa) : a.nu[cr].y;
+            const double nu_lam_R = nuR.x;
+            const double nu_t_R = bnd ? sa_nut(nut_R, nu_lam_R, a.sa) : nuR.y;
             const double rho_R = bnd ? UL.r : UR.r;
             const double turb = 0.5 * (UL.r * nuL.y + rho_R * nu_t_R);
             const double mu_eff = n.mu + turb;
-            const double k_eff = a.cp * n.mu / a.prandtl + a.cp * turb / a.prandtl_t;
+            const double k_eff = a.k_lam + a.cp * turb / a.prandtl_t;
             const double u_face = bnd ? pR[0] : 0.5 * (wl.x + pR[0]);
             const double v_face = bnd ? pR[1] : 0.5 * (wl.y + pR[1]);
             const double div_v = fgv[0].gx + fgv[1].gy;
@@ -260,7 +266,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_sa_cell(const RansArgs a) 
         const double2 gu = a.grad[4 * c], gv = a.grad[4 * c + 1], gn = a.grad[4 * c + 3];
         const double omega = fabs(gv.x - gu.y);
         const double vol = a.vol[c];
-        Rn += vol * sa_source(a.nut[c], a.nu[c].x, omega, a.walld[c], gn.x, gn.y, a.sa);
+        Rn += vol * sa_source(a.nut[c], a.nu[c].x, omega, a.walld[c], gn.x, gn.y, a.sa, a.cw3_6);
         s[0] = R.r * R.r; s[1] = R.ru * R.ru; s[2] = R.rv * R.rv; s[3] = R.E * R.E; s[4] = Rn * Rn;
         const double dt = __longlong_as_double((long long)ctl->dt_bits);
         const double k = dt / vol;

@@ -23,7 +23,9 @@ struct RansArgs {
     int hist_cap;
     double farfield_nut[kMaxPatches];
     double sa[9];          // cb1, cb2, sigma, kappa, cw2, cw3, cv1, cv2, cv3
+    double cw3_6;          // cw3^6, formed on the host by std::pow
     double cp, prandtl, prandtl_t;
+    double k_lam;          // cp * mu / Pr, formed on the host in that order
 };
 
 void rans_wall_distance(const RansArgs& a, const double4_32a* seg, int n_seg, cudaStream_t s);

@@ -283,9 +283,11 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         r.nut_norm = dupload(std::vector<double>(1, 0.0), owned);
         for (int p = 0; p < kMaxPatches; ++p) r.farfield_nut[p] = p < hm.n_patches ? bcs[p].nut : 0.0;
         for (int i = 0; i < 9; ++i) r.sa[i] = opt.sa[i];
+        r.cw3_6 = std::pow(opt.sa[5], 6.0);
         r.cp = gamma * opt.gas_constant / (gamma - 1.0);
         r.prandtl = opt.prandtl;
         r.prandtl_t = opt.prandtl_t;
+        r.k_lam = r.cp * opt.mu / opt.prandtl;
         std::vector<double4_32a> seg;
         for (int f = 0; f < F; ++f) {
             if (hm.fr[f] >= 0 || bc.type[hm.fpatch[f]] != FV_BC_NOSLIP) continue;

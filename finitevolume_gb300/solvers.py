@@ -427,14 +427,32 @@ class DiscreteAdjoint:
                                                    capi.dptr(Ub), capi.dptr(fb)))
         return Ub, fb[:self.n_patches]
 
-    def solve(self, dJdU, max_iter: int = 20000, tol: float = 1e-12):
+    def solve(self, dJdU, max_iter: int = 20000, tol: float = 1e-12, method: str = "rk", restart: int = 40):
+        """Solve (dR/dU)^T lambda = dJdU.  method "rk": SSP-RK3 pseudo-time
+        iteration until every residual-norm component is below tol (history
+        [iterations, 4] of those norms); "gmres": GMRES(restart) on the
+        fixed point of that iteration until its residual falls by the
+        factor tol, max_iter matvecs (history [matvecs] of the relative
+        GMRES residual).  Returns lambda, fsbar, history, iterations; the
+        final residual norms are kept in ``last_residual`` for "gmres"."""
         lam = np.zeros((self.n, 4))
         fb = np.zeros((_MAX_PATCHES, 4))
-        hist = np.zeros((max(max_iter, 1), 4))
         it = C.c_int32()
-        capi.check(capi.lib().fv_adjoint_solve(self._h, capi.dptr(np.ascontiguousarray(dJdU, dtype=np.float64)),
-                                               int(max_iter), float(tol), capi.dptr(lam), capi.dptr(fb),
-                                               capi.dptr(hist), C.byref(it)))
+        g = np.ascontiguousarray(dJdU, dtype=np.float64)
+        if method == "gmres":
+            hist = np.zeros(max(max_iter, 1))
+            res = np.zeros(4)
+            capi.check(capi.lib().fv_adjoint_solve_gmres(self._h, capi.dptr(g), int(restart), int(max_iter),
+                                                         float(tol), capi.dptr(lam), capi.dptr(fb), capi.dptr(hist),
+                                                         C.byref(it), capi.dptr(res)))
+            self.last_residual = res
+            return lam, fb[:self.n_patches], hist[:it.value], it.value
+        if method != "rk":
+            raise ValueError("method: 'rk' or 'gmres'")
+        hist = np.zeros((max(max_iter, 1), 4))
+        capi.check(capi.lib().fv_adjoint_solve(self._h, capi.dptr(g), int(max_iter), float(tol), capi.dptr(lam),
+                                               capi.dptr(fb), capi.dptr(hist), C.byref(it)))
+        self.last_residual = hist[it.value - 1] if it.value else None
         return lam, fb[:self.n_patches], hist[:it.value], it.value
 
     def shape_gradient(self, objective: Objective, ref) -> np.ndarray:
@@ -454,7 +472,7 @@ class DiscreteAdjoint:
         return out
 
     def freestream_gradient(self, objective: Objective, mach: float, aoa_deg: float, farfield_patches,
-                            max_iter: int = 20000, tol: float = 1e-12) -> dict:
+                            max_iter: int = 20000, tol: float = 1e-12, method: str = "rk") -> dict:
         """dJ/dM and dJ/dAoA (per degree) of a force coefficient at a
         converged state whose farfield patches carry the freestream
         (1, M cos a, M sin a, 1/gamma) and whose force reference is that
@@ -463,7 +481,7 @@ class DiscreteAdjoint:
         ref = np.array([1.0, mach * np.cos(a), mach * np.sin(a), 1.0 / self.solver.gas_gamma(), 1.0, 0.25, 0.0])
         self.forward()
         J, g = force_gradient(self.solver, objective, ref)
-        lam, fb, hist, it = self.solve(g, max_iter, tol)
+        lam, fb, hist, it = self.solve(g, max_iter, tol, method)
         fsb = fb[list(farfield_patches)].sum(axis=0)
         dfs_dM = np.array([0.0, np.cos(a), np.sin(a), 0.0])
         dfs_da = np.array([0.0, -mach * np.sin(a), mach * np.cos(a), 0.0])
@@ -478,8 +496,9 @@ class DiscreteAdjoint:
             eM, ea = -2.0 * J / mach, 0.0
         dM = eM - fsb @ dfs_dM
         da = (ea - fsb @ dfs_da) * np.pi / 180.0
+        r = self.last_residual
         return {"J": J, "dJ_dM": dM, "dJ_dAoA_deg": da, "iterations": it,
-                "adjoint_residual": hist[-1].tolist() if len(hist) else None}
+                "adjoint_residual": None if r is None else np.asarray(r).tolist()}
 
     def __del__(self):
         try:

@@ -326,6 +326,16 @@ int fv_residual_backward(fv_adjoint_t a, const double* Rbar, double* Ubar, doubl
  * dfs/dalpha. */
 int fv_adjoint_solve(fv_adjoint_t a, const double* dJdU, int32_t max_iter, double tol, double* lambda, double* fsbar,
                      double* history, int32_t* iterations);
+/* The same system by restarted GMRES(restart) on the fixed point of that
+ * pseudo-time iteration (one pseudo-time iteration per matvec), until the
+ * GMRES residual is below rtol times its initial value or max_matvec
+ * matvecs: converges where the pseudo-time iteration diverges (a primal
+ * whose explicit iteration limit-cycles, a frozen limiter with growing
+ * modes).  history [max_matvec]: relative GMRES residual after each
+ * matvec; residual[4]: norms of (dR/dU)^T lambda - dJdU at the result.
+ * Other outputs as fv_adjoint_solve; each may be NULL. */
+int fv_adjoint_solve_gmres(fv_adjoint_t a, const double* dJdU, int32_t restart, int32_t max_matvec, double rtol,
+                           double* lambda, double* fsbar, double* history, int32_t* matvecs, double residual[4]);
 /* Shape gradient dJ/dX [2 n_nodes] (x, y per node, the mesh's node
  * numbering) of the objective the last fv_adjoint_solve was solved for:
  * dJ/dX|explicit - lambda^T dR/dX through face normals, lengths and

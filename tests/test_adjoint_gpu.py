@@ -238,3 +238,21 @@ def test_residual_shape_cotangent_matches_central_differences(gpu, limiter, full
         frozen.forward(U)
         e_frozen = abs(float(np.sum(frozen.shape_vjp(Rb) * d)) - fd) / scale
         assert e_frozen > 10 * e, (e, e_frozen)
+
+
+def test_gmres_adjoint_matches_pseudo_time_solution(gpu):
+    """Where the pseudo-time iteration converges, GMRES on its fixed point
+    reaches the same adjoint."""
+    mesh = _mesh(2, r_far=10.0)
+    fs = _fs(0.5, 2.0)
+    s = _solver(mesh, fs, 2, S.NumericalFluxScheme.HLLC, S.Limiter.NoLimiter)
+    assert _converge(s, 1e-12, 150000) < 1e-11
+    adj = S.DiscreteAdjoint(s)
+    adj.forward()
+    _, g = S.force_gradient(s, S.Objective.Drag, np.array([1.0, fs[1], fs[2], fs[3], 1.0, 0.25, 0.0]))
+    lam_rk, fb_rk, _, _ = adj.solve(g, 150000, 1e-13)
+    lam_gm, fb_gm, hist, mv = adj.solve(g, 20000, 1e-10, method="gmres", restart=60)
+    assert hist[-1] <= 1e-10 and mv < 20000, (hist[-1], mv)
+    assert np.linalg.norm(lam_gm - lam_rk) <= 1e-7 * np.linalg.norm(lam_rk)
+    assert np.allclose(fb_gm, fb_rk, rtol=1e-7, atol=1e-10 * np.abs(fb_rk).max())
+
