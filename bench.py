@@ -408,19 +408,22 @@ def _converge(s, tol: float, max_iter: int, chunk: int = 250):
     return done, last
 
 
-def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, max_cycles: int = 30000,
-                  adj_matvecs: int = 6000, adj_rtol: float = 1e-10, restart: int = 60):
+def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, freeze_after: int = 3000,
+                  max_cycles: int = 30000, adj_iters: int = 60000, adj_tol: float = 1e-13):
     """Gradients of the 500k-cell NACA0012 O-grid case (1024 x 488, M 0.75,
     AoA 2 deg, 2nd-order HLLC + LSQ/Venkatakrishnan K=5, SSP-RK3, local dt,
-    CFL 1.2) from the discrete adjoint (frozen and full limiter) against
-    central differences of converged primal solves: dCD/dM and dCD/dAoA,
-    and dCL/dX along ``n_dirs`` seeded wall-normal displacement fields
-    smoothed over 20 wall nodes, step h.  Primal solves use the
-    agglomeration multigrid; perturbed solves start from the base state.
-    The adjoint systems are solved by GMRES on the pseudo-time fixed point
-    (the plain pseudo-time iteration diverges at this transonic state)."""
+    CFL 1.2) from the discrete adjoint against central differences of
+    converged primal solves: dCD/dM, dCD/dAoA, and dCL/dX along ``n_dirs``
+    seeded wall-normal displacement fields smoothed over 20 wall nodes,
+    step h.  The primal limit-cycles through the limiter's switching (its
+    residual stalls near 1e-3 even with multigrid), so the limiter is
+    frozen after ``freeze_after`` multigrid cycles and the frozen-limiter
+    scheme is converged to ``tol``; the differences are taken with the
+    limiter frozen at those values, so the frozen-limiter adjoint is the
+    exact linearisation and the full-limiter one differs by the limiter's
+    sensitivity."""
     import torch
-    from finitevolume_gb300 import meshgen, solvers as S
+    from finitevolume_gb300 import capi, meshgen, solvers as S
     M, aoa = 0.75, 2.0
 
     def fs_of(m, al):
@@ -430,64 +433,80 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, max_cyc
     def ref_of(m, al):
         return np.array([*fs_of(m, al), 1.0, 0.25, 0.0])
 
+    def log(d):
+        print(json.dumps(d), file=sys.stderr, flush=True)
+
     poly = meshgen.cached("naca_ogrid", ni=1024, nj=488)
     mesh = S.Mesh(poly, reorder="morton")
     fs = fs_of(M, aoa)
     out = {"workload": "naca0012 O-grid 1024x488, M 0.75, AoA 2, 2nd-order HLLC, LSQ + Venkatakrishnan K=5, "
-                       "SSP-RK3, local dt, CFL 1.2",
+                       "SSP-RK3, local dt, CFL 1.2, 4-level multigrid",
            "cells": mesh.n_cells, "tol_l2_density": tol, "h_shape": h, "directions": n_dirs}
     s = _plain_solver(mesh, fs, False)
     s.multigrid()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    cyc, res = _converge(s, tol, max_cycles)
+    c1, r1 = _converge(s, tol, freeze_after)
+    s.freeze_limiter()
+    c2, r2 = _converge(s, tol, max_cycles)
     tprimal = time.perf_counter() - t0
-    out["primal"] = {"cycles": cyc, "residual": res, "seconds": round(tprimal, 2)}
+    psi = s.limiter_values()
+    out["primal"] = {"cycles_before_freeze": c1, "residual_at_freeze": r1, "cycles_frozen": c2, "residual": r2,
+                     "seconds": round(tprimal, 2), "cells_limited": int((psi < 1.0).any(axis=1).sum())}
+    log({"primal": out["primal"]})
     U0 = s.field()
     f0 = s.wall_forces(*ref_of(M, aoa))
     out["cl"], out["cd"] = f0["cl"], f0["cd_total"]
 
-    # adjoint gradients
     dirs = meshgen.wall_normal_directions(poly, n_dirs, seed=0, width=20)
-    print(json.dumps({"primal": out["primal"]}), file=sys.stderr, flush=True)
     for full in (False, True):
+        key = "full_limiter" if full else "frozen_limiter"
         adj = S.DiscreteAdjoint(s, full_limiter=full)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        gd = adj.freestream_gradient(S.Objective.Drag, M, aoa, [1], max_iter=adj_matvecs, tol=adj_rtol,
-                                     method="gmres")
-        _, g = S.force_gradient(s, S.Objective.Lift, ref_of(M, aoa))
-        _, _, hist, it = adj.solve(g, adj_matvecs, adj_rtol, method="gmres", restart=restart)
-        gl = adj.shape_gradient(S.Objective.Lift, ref_of(M, aoa))
+        try:
+            gd = adj.freestream_gradient(S.Objective.Drag, M, aoa, [1], max_iter=adj_iters, tol=adj_tol)
+            _, g = S.force_gradient(s, S.Objective.Lift, ref_of(M, aoa))
+            _, _, hist, it = adj.solve(g, adj_iters, adj_tol)
+            gl = adj.shape_gradient(S.Objective.Lift, ref_of(M, aoa))
+        except capi.FVError as e:
+            out[key] = {"error": str(e)}
+            log({key: out[key]})
+            del adj
+            continue
         torch.cuda.synchronize()
         ta = time.perf_counter() - t0
-        key = "full_limiter" if full else "frozen_limiter"
         out[key] = {
-            "dCD_dM": gd["dJ_dM"], "dCD_dAoA_deg": gd["dJ_dAoA_deg"], "drag_matvecs": gd["iterations"],
-            "drag_adjoint_residual": gd["adjoint_residual"], "lift_matvecs": it,
-            "lift_gmres_rel_residual": float(hist[-1]) if len(hist) else None,
-            "lift_adjoint_residual": adj.last_residual.tolist(),
+            "dCD_dM": gd["dJ_dM"], "dCD_dAoA_deg": gd["dJ_dAoA_deg"], "drag_iterations": gd["iterations"],
+            "drag_adjoint_residual": gd["adjoint_residual"], "lift_iterations": it,
+            "lift_adjoint_residual": hist[-1].tolist() if len(hist) else None,
             "dCL_dX_dirs": [float(np.sum(gl * d)) for d in dirs], "seconds": round(ta, 2),
             "seconds_vs_primal": round(ta / tprimal, 3)}
-        print(json.dumps({key: out[key]}), file=sys.stderr, flush=True)
+        log({key: out[key]})
         del adj
 
-    # central differences: freestream
+    def frozen_solve(sp):
+        sp.set_field(U0)
+        return _converge(sp, tol, max_cycles)
+
+    # central differences, limiter frozen at psi: freestream
     hM, ha = 1e-6, 1e-5
     fd = {}
     for key, (m, al) in {"M+": (M + hM, aoa), "M-": (M - hM, aoa), "a+": (M, aoa + ha), "a-": (M, aoa - ha)}.items():
         sp = _plain_solver(mesh, fs_of(m, al), False)
-        sp.set_field(U0)
+        sp.set_limiter_values(psi)
         sp.multigrid()
-        c, r = _converge(sp, tol, max_cycles)
+        c, r = frozen_solve(sp)
         fd[key] = (sp.wall_forces(*ref_of(m, al))["cd_total"], c, r)
         del sp
     out["fd_freestream"] = {"dCD_dM": (fd["M+"][0] - fd["M-"][0]) / (2 * hM),
                             "dCD_dAoA_deg": (fd["a+"][0] - fd["a-"][0]) / (2 * ha),
                             "h_M": hM, "h_aoa_deg": ha,
                             "cycles": [fd[k][1] for k in fd], "residuals": [fd[k][2] for k in fd]}
-    # central differences: shape (one solver, geometry moved on the device)
+    log({"fd_freestream": out["fd_freestream"]})
+    # shape (one solver, geometry moved on the device)
     sp = _plain_solver(mesh, fs, False)
+    sp.set_limiter_values(psi)
     sp.multigrid()
     X = poly.nodes.copy()
     fd_cl, cycles, resids = [], [], []
@@ -495,8 +514,7 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, max_cyc
         v = {}
         for sgn in (1, -1):
             sp.update_nodes(X + sgn * h * d)
-            sp.set_field(U0)
-            c, r = _converge(sp, tol, max_cycles)
+            c, r = frozen_solve(sp)
             cycles.append(c)
             resids.append(r)
             v[sgn] = sp.wall_forces(*ref_of(M, aoa))["cl"]
@@ -506,9 +524,11 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, max_cyc
                        "residual_max": float(np.max(resids))}
     fdv = np.array(fd_cl)
     for key in ("frozen_limiter", "full_limiter"):
-        ad = np.array(out[key]["dCL_dX_dirs"])
-        rel = np.abs(ad - fdv) / np.maximum(np.abs(fdv), 1e-3)
         o = out[key]
+        if "error" in o:
+            continue
+        ad = np.array(o["dCL_dX_dirs"])
+        rel = np.abs(ad - fdv) / np.maximum(np.abs(fdv), 1e-3)
         o["shape_rel_err_max"] = float(rel.max())
         o["shape_rel_err_median"] = float(np.median(rel))
         o["dCD_dM_rel_err"] = abs(o["dCD_dM"] - out["fd_freestream"]["dCD_dM"]) / abs(out["fd_freestream"]["dCD_dM"])

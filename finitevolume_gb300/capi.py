@@ -98,6 +98,8 @@ SIGNATURES = {
     "fv_get_nut_residual": (C.c_int, [_P, _D]),
     "fv_get_wall_distance": (C.c_int, [_P, _D]),
     "fv_solver_set_launch": (C.c_int, [_P, _I32]),
+    "fv_solver_freeze_limiter": (C.c_int, [_P, C.c_int32]),
+    "fv_solver_limiter_values": (C.c_int, [_P, _D, _D]),
     "fv_solver_update_nodes": (C.c_int, [_P, _P, _D]),
     "fv_solver_multigrid": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_double]),
     "fv_solver_autotune": (C.c_int, [_P, C.c_int32, _I32]),

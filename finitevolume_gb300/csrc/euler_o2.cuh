@@ -385,7 +385,19 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
                 for (int k = 0; k < 4; ++k) a.lim_psi[4 * c + k] = 1.0;
         }
     }
-    if (LIM != 0) {
+    if (LIM != 0 && a.psi_mode == 2) {
+        // frozen limiter: the values captured earlier (psi = 1 scales exactly)
+        const T* pb = static_cast<const T*>(a.psi_buf) + 4 * (size_t)c;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const T psi = pb[k];
+            if constexpr (sizeof(T) == 8) {
+                if (a.lim_psi) a.lim_psi[4 * c + k] = psi;
+            }
+            gx[k] *= psi;
+            gy[k] *= psi;
+        }
+    } else if (LIM != 0) {
         const T eps2 = LIM == 2 ? ld_one<T>(a.eps2, c) : T(0);
         // Per face f the limiter value is psi_f = phi(D1, D2_f) with D2_f the
         // unlimited extrapolation to the face and D1 = dmax (D2_f > 0) or
@@ -437,6 +449,7 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
             if constexpr (sizeof(T) == 8) {
                 if (a.lim_psi) a.lim_psi[4 * c + k] = psi;
             }
+            if (a.psi_mode == 1) static_cast<T*>(a.psi_buf)[4 * (size_t)c + k] = psi;
             if (lim) {
                 gx[k] *= psi;
                 gy[k] *= psi;

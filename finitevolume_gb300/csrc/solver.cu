@@ -419,6 +419,8 @@ O2Args Solver::o2_args() const {
     a.r2 = r2;
     a.lim_gu = nullptr;
     a.lim_psi = nullptr;
+    a.psi_buf = psi_buf;
+    a.psi_mode = psi_mode;
     a.forcing = forcing;
     a.resid = nullptr;
     return a;
@@ -600,6 +602,67 @@ void Solver::set_launch(int bg, int bf, int bc) {
     cfg.blk_cell = bc;
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
+}
+
+void Solver::freeze_limiter(bool on) {
+    if (viscous) raise(FV_ERR_UNSUPPORTED, "limiter freezing: Euler solvers");
+    if (!general || opt.order != 2 || opt.limiter == FV_LIM_NONE) return;  // no limiter to freeze
+    FV_CUDA(cudaStreamSynchronize(stream));
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    if (!on) {
+        psi_mode = 0;
+        return;
+    }
+    if (!psi_buf) psi_buf = dalloc_owned<char>(4 * (size_t)N * (cfg.fp32 ? sizeof(float) : sizeof(double)));
+    // capture: one gradient evaluation at the current state stores psi
+    refresh_primitives();
+    O2Args a = o2_args();
+    a.psi_mode = 1;
+    if (cfg.fp32) o2::launch_part_f32(a, cfg, 0, 0, stream);
+    else o2::launch_part_f64(a, cfg, 0, 0, stream);
+    FV_CUDA(cudaGetLastError());
+    FV_CUDA(cudaStreamSynchronize(stream));
+    psi_mode = 2;
+}
+
+void Solver::limiter_values(double* out_ref, const double* in_ref) {
+    if (!general || opt.order != 2 || opt.limiter == FV_LIM_NONE)
+        raise(FV_ERR_UNSUPPORTED, "limiter values: second order with a limiter");
+    if (in_ref) {
+        // import: freeze at the given values
+        FV_CUDA(cudaStreamSynchronize(stream));
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+        const size_t esz = cfg.fp32 ? sizeof(float) : sizeof(double);
+        if (!psi_buf) psi_buf = dalloc_owned<char>(4 * (size_t)N * esz);
+        std::vector<double> d(4 * (size_t)N);
+        std::vector<float> f(cfg.fp32 ? 4 * (size_t)N : 0);
+        for (int i = 0; i < N; ++i)
+            for (int k = 0; k < 4; ++k) {
+                const double v = in_ref[4 * (size_t)perm[i] + k];
+                if (!(v >= 0.0 && v <= 1.0)) raise(FV_ERR_BAD_ARG, "limiter values must lie in [0, 1]");
+                if (cfg.fp32) f[4 * (size_t)i + k] = (float)v;
+                else d[4 * (size_t)i + k] = v;
+            }
+        FV_CUDA(cudaMemcpy(psi_buf, cfg.fp32 ? static_cast<const void*>(f.data()) : static_cast<const void*>(d.data()),
+                           4 * (size_t)N * esz, cudaMemcpyHostToDevice));
+        psi_mode = 2;
+    }
+    if (out_ref) {
+        if (psi_mode != 2) raise(FV_ERR_BAD_ARG, "limiter values: the limiter is not frozen");
+        FV_CUDA(cudaStreamSynchronize(stream));
+        std::vector<double> d(4 * (size_t)N);
+        if (cfg.fp32) {
+            std::vector<float> f(4 * (size_t)N);
+            FV_CUDA(cudaMemcpy(f.data(), psi_buf, sizeof(float) * f.size(), cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < f.size(); ++i) d[i] = f[i];
+        } else {
+            FV_CUDA(cudaMemcpy(d.data(), psi_buf, sizeof(double) * d.size(), cudaMemcpyDeviceToHost));
+        }
+        for (int i = 0; i < N; ++i)
+            for (int k = 0; k < 4; ++k) out_ref[4 * (size_t)perm[i] + k] = d[4 * (size_t)i + k];
+    }
 }
 
 void Solver::autotune(int n, int out[3]) {
@@ -933,6 +996,20 @@ int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]) {
     return guarded([&] {
         if (!s || !blocks) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
         s->s.set_launch(blocks[0], blocks[1], blocks[2]);
+    });
+}
+
+int fv_solver_freeze_limiter(fv_solver_t s, int32_t on) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        s->s.freeze_limiter(on != 0);
+    });
+}
+
+int fv_solver_limiter_values(fv_solver_t s, double* psi_out, const double* psi_in) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        s->s.limiter_values(psi_out, psi_in);
     });
 }
 

@@ -103,6 +103,8 @@ struct Solver {
     const void* eps2 = nullptr;
     const float4* fgeom32 = nullptr;
     const St* forcing = nullptr;    // multigrid coarse levels: FAS forcing term
+    void* psi_buf = nullptr;        // frozen limiter values [4N], flux precision
+    int psi_mode = 0;               // 0 evaluated, 2 frozen (see O2Args)
 
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -132,6 +134,12 @@ struct Solver {
     // (state restored afterwards) and keep the fastest shape per class
     void autotune(int n, int out[3]);
     void set_stream(void* s);
+    // Freeze the limiter at the current state (its values are captured and
+    // reused by every later gradient evaluation) or release it.
+    void freeze_limiter(bool on);
+    // Frozen limiter values [N x 4], reference cell order: copy out (out_ref)
+    // and/or freeze at given values (in_ref, each in [0, 1]).
+    void limiter_values(double* out_ref, const double* in_ref);
     void wall_forces(const double ref[7], double out[11], int instance = -1);
 
     // Agglomeration multigrid (steady solves with local time stepping):

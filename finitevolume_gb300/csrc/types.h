@@ -106,6 +106,11 @@ struct O2Args {
     // (4 per cell) of k_grad.
     double2* lim_gu;
     double* lim_psi;
+    // Limiter freezing: psi_mode 1 stores the limiter values ([4N], flux
+    // precision) in psi_buf as they are computed; 2 reads them from there
+    // instead of evaluating the limiter; 0 neither.
+    void* psi_buf;
+    int psi_mode;
     // Multigrid (null otherwise): a forcing term added to every cell's
     // residual (coarse levels of the full-approximation scheme), and the
     // output of the residual-only pass.

@@ -301,6 +301,22 @@ class EulerFVMSolver:
         step becomes one smoothing iteration plus one V-cycle."""
         capi.check(capi.lib().fv_solver_multigrid(self._h, self.mesh.handle, int(levels), int(smooth), float(relax)))
 
+    def freeze_limiter(self, on: bool = True) -> None:
+        """Capture the limiter values at the current state and reuse them in
+        every later step (on=False: evaluate the limiter again)."""
+        capi.check(capi.lib().fv_solver_freeze_limiter(self._h, 1 if on else 0))
+
+    def limiter_values(self) -> np.ndarray:
+        """The frozen limiter values [n_cells, 4] (rho, u, v, p)."""
+        out = np.zeros((self.mesh.n_cells, 4))
+        capi.check(capi.lib().fv_solver_limiter_values(self._h, capi.dptr(out), None))
+        return out
+
+    def set_limiter_values(self, psi) -> None:
+        """Freeze the limiter at the given values [n_cells, 4]."""
+        capi.check(capi.lib().fv_solver_limiter_values(self._h, None,
+                                                       capi.dptr(np.ascontiguousarray(psi, dtype=np.float64))))
+
     def update_nodes(self, nodes) -> None:
         """Move the mesh nodes ([n_nodes, 2]) and recompute the geometry on
         the device (the state is kept)."""

@@ -208,6 +208,18 @@ int fv_get_history(fv_solver_t s, int32_t n, double* history);
  * restored afterwards.  No reference counterpart (the reference's loops are
  * OpenMP). */
 int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]);
+/* Limiter freezing (second order with a limiter; a no-op otherwise): on=1
+ * evaluates the limiter once at the current state and reuses those values
+ * in every later step (the scheme becomes smooth, so steady solves that
+ * limit-cycle through the limiter's switching converge to machine
+ * precision, and the frozen-limiter adjoint is its exact linearisation);
+ * on=0 evaluates the limiter again.  No reference counterpart. */
+int fv_solver_freeze_limiter(fv_solver_t s, int32_t on);
+/* The frozen limiter values [4 n_cells] (per cell: rho, u, v, p; reference
+ * cell order): psi_out (may be NULL) receives them; psi_in (may be NULL,
+ * each value in [0, 1]) freezes the limiter at the given values, e.g. those
+ * of another solver on the same mesh. */
+int fv_solver_limiter_values(fv_solver_t s, double* psi_out, const double* psi_in);
 /* Move the mesh nodes (xy [2 n_nodes], the mesh's node numbering) and
  * recompute on the device every geometric quantity the Euler solver uses:
  * face normals, lengths, midpoints and CFL lengths, shoelace cell areas and
