@@ -133,6 +133,45 @@ __device__ __forceinline__ St ld_flux(const float4* ff, int f) {
     return st_make(fvconv::f2d(a.x), fvconv::f2d(a.y), fvconv::f2d(a.z), fvconv::f2d(a.w));
 }
 
+// FP32-flux gather: the float face fluxes of a cell are summed in
+// float-float (Knuth's TwoSum per addition, the rounding errors collected
+// in a second float) on the FP32 pipe, and hi + lo is widened and added
+// once in FP64.  Each addition is error-free and the error collector rounds
+// at 2^-24 of the errors, so the sum is exact to about 2^-48 relative (the
+// FP64 sum of the widened fluxes: 2^-53).  With LAM the per-face wave-speed
+// terms of the local time step (stored as floats) are summed in FP32.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+}
+__device__ __forceinline__ float4 flipf(const float4& F, int neg) {
+    const unsigned m = (unsigned)(neg & 1) << 31;
+    return make_float4(__uint_as_float(__float_as_uint(F.x) ^ m), __uint_as_float(__float_as_uint(F.y) ^ m),
+                       __uint_as_float(__float_as_uint(F.z) ^ m), __uint_as_float(__float_as_uint(F.w) ^ m));
+}
+template <bool LAM>
+__device__ __forceinline__ St gather32(const float4* __restrict__ ff, const float* __restrict__ lamf_face,
+                                       const int* __restrict__ cf, int e0, int e1, float& lam) {
+    const int ent0 = cf[e0];
+    float4 h = flipf(__ldg(ff + (ent0 >> 1)), ent0);
+    float4 l = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (LAM) lam = __ldg(lamf_face + (ent0 >> 1));
+    for (int e = e0 + 1; e < e1; ++e) {
+        const int ent = cf[e];
+        const int f = ent >> 1;
+        const float4 q = flipf(__ldg(ff + f), ent);
+        two_sum_acc(h.x, l.x, q.x);
+        two_sum_acc(h.y, l.y, q.y);
+        two_sum_acc(h.z, l.z, q.z);
+        two_sum_acc(h.w, l.w, q.w);
+        if (LAM) lam += __ldg(lamf_face + f);
+    }
+    return st_make(fvconv::f2d(h.x) + fvconv::f2d(l.x), fvconv::f2d(h.y) + fvconv::f2d(l.y),
+                   fvconv::f2d(h.z) + fvconv::f2d(l.z), fvconv::f2d(h.w) + fvconv::f2d(l.w));
+}
+
 // ---------------------------------------------------------------------------
 // Primitive-input physics
 // ---------------------------------------------------------------------------
@@ -521,8 +560,9 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_face(const O2Args a) {
         if (DT != 0) {
             // compute_dt's per-face candidate from cell-centred states
             // (src/EulerFVMSolver.cpp:140-160).  FP32-flux mode forms the
-            // wave speed in FP32 (the sound speed is stored in FP32 there)
-            // and widens it exactly; dt itself is FP64.
+            // wave speed in FP32 (the sound speed is stored in FP32 there):
+            // local dt keeps lambda * A as a float for k_update's FP32 sum;
+            // the global-dt candidate is widened exactly and formed in FP64.
             const T* cs = static_cast<const T*>(a.cs);
             T Smax = fabs(wlc.u * nx + wlc.v * ny) + cs[L];
             if (R >= 0) {
@@ -533,7 +573,7 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_face(const O2Args a) {
                 if (DT == 2) a.dtf[f] = Smax * ar;
                 else cand = a.ctl->cfl * len / Smax;
             } else {
-                if (DT == 2) a.dtf[f] = fvconv::f2d(Smax * ar);
+                if (DT == 2) reinterpret_cast<float*>(a.dtf)[f] = Smax * ar;
                 else cand = a.ctl->cfl * fvconv::f2d(len) / fvconv::f2d(Smax);
             }
         }
@@ -573,25 +613,37 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_update(const O2Args a) {
     if (c < a.m.n_cells && (!a.active || a.active[a.cell_inst[c]])) {
         const FT* ff = static_cast<const FT*>(a.ff);
         const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
-        // Every cell has faces: the sum starts from the first signed flux
-        // instead of 0 + flux (one FP64 add per component less; only the
-        // sign of an exactly-zero sum can differ, and u + dt * (+-0) = u).
-        const int ent0 = a.m.cf[e0];
-        St R = flip_if(ld_flux(ff, ent0 >> 1), ent0);
-        double lam = (STAGE == 0 && DT == 2) ? a.dtf[ent0 >> 1] : 0.0;
-        for (int e = e0 + 1; e < e1; ++e) {
-            const int ent = a.m.cf[e];
-            const int f = ent >> 1;
-            R += flip_if(ld_flux(ff, f), ent);
-            if (STAGE == 0 && DT == 2) lam += a.dtf[f];
+        St R;
+        double lam = 0.0;
+        float lamf = 0.0f;
+        if constexpr (std::is_same<T, float>::value) {
+            R = gather32<STAGE == 0 && DT == 2>(ff, reinterpret_cast<const float*>(a.dtf), a.m.cf, e0, e1, lamf);
+        } else {
+            // Every cell has faces: the sum starts from the first signed flux
+            // instead of 0 + flux (one FP64 add per component less; only the
+            // sign of an exactly-zero sum can differ, and u + dt * (+-0) = u).
+            const int ent0 = a.m.cf[e0];
+            R = flip_if(ld_flux(ff, ent0 >> 1), ent0);
+            if (STAGE == 0 && DT == 2) lam = a.dtf[ent0 >> 1];
+            for (int e = e0 + 1; e < e1; ++e) {
+                const int ent = a.m.cf[e];
+                const int f = ent >> 1;
+                R += flip_if(ld_flux(ff, f), ent);
+                if (STAGE == 0 && DT == 2) lam += a.dtf[f];
+            }
         }
         if (a.forcing) R += ld_state(a.forcing, c);
         double dtv;
         if (STAGE == 0) {
-            // Local: dt_i = cfl V_i / sum_f lambda_f A_f, so dt_i / V_i = cfl / sum;
-            // global: the min over faces, divided by the volume.
-            if (DT == 2) dtv = a.ctl->cfl / lam;
-            else dtv = __longlong_as_double((long long)a.ctl->dt_bits) / a.m.vol[c];
+            // Local: dt_i = cfl V_i / sum_f lambda_f A_f, so dt_i / V_i = cfl / sum
+            // (FP32-flux mode: in FP32; the step size only sets the path to the
+            // steady state); global: the min over faces, divided by the volume.
+            if (DT == 2) {
+                if constexpr (std::is_same<T, float>::value) dtv = fvconv::f2d(fvconv::d2f(a.ctl->cfl) / lamf);
+                else dtv = a.ctl->cfl / lam;
+            } else {
+                dtv = __longlong_as_double((long long)a.ctl->dt_bits) / a.m.vol[c];
+            }
             if (NST > 1) a.dtv[c] = dtv;
             s0 = R.r * R.r; s1 = R.ru * R.ru; s2 = R.rv * R.rv; s3 = R.E * R.E;
             if (a.r2) {
@@ -637,11 +689,17 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_residual(const O2Args a) {
     if (c >= a.m.n_cells) return;
     const FT* ff = static_cast<const FT*>(a.ff);
     const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
-    const int ent0 = a.m.cf[e0];
-    St R = flip_if(ld_flux(ff, ent0 >> 1), ent0);
-    for (int e = e0 + 1; e < e1; ++e) {
-        const int ent = a.m.cf[e];
-        R += flip_if(ld_flux(ff, ent >> 1), ent);
+    St R;
+    if constexpr (std::is_same<T, float>::value) {
+        float unused;
+        R = gather32<false>(ff, nullptr, a.m.cf, e0, e1, unused);
+    } else {
+        const int ent0 = a.m.cf[e0];
+        R = flip_if(ld_flux(ff, ent0 >> 1), ent0);
+        for (int e = e0 + 1; e < e1; ++e) {
+            const int ent = a.m.cf[e];
+            R += flip_if(ld_flux(ff, ent >> 1), ent);
+        }
     }
     if (a.forcing) R += ld_state(a.forcing, c);
     st_state(a.resid, c, R);

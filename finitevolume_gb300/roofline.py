@@ -61,7 +61,7 @@ KERNEL_NAMES = ("gradients", "faces", "update")
 # dram__bytes_write.sum, one launch of each kernel class) on the 968,870-cell
 # NACA0012 mixed mesh; the captures are summarised under profiles/.
 MEASURED_TRAFFIC_PER_CELL = {"gradients": 283.4, "faces": 331.2, "update": 206.5}
-MEASURED_TRAFFIC_PER_CELL_FP32 = {"gradients": 146.7, "faces": 168.0, "update": 153.0}
+MEASURED_TRAFFIC_PER_CELL_FP32 = {"gradients": 146.5, "faces": 168.5, "update": 150.3}
 
 # FP64-pipe thread instructions per cell and per launch from the same
 # captures (smsp__inst_executed_pipe_fp64.sum x 32 / cells).  On GB300 the

@@ -254,5 +254,7 @@ def test_gmres_adjoint_matches_pseudo_time_solution(gpu):
     lam_gm, fb_gm, hist, mv = adj.solve(g, 20000, 1e-10, method="gmres", restart=60)
     assert hist[-1] <= 1e-10 and mv < 20000, (hist[-1], mv)
     assert np.linalg.norm(lam_gm - lam_rk) <= 1e-7 * np.linalg.norm(lam_rk)
-    assert np.allclose(fb_gm, fb_rk, rtol=1e-7, atol=1e-10 * np.abs(fb_rk).max())
+    # fsbar = lambda^T dR/dfs inherits lambda's 1e-7 relative agreement
+    # (small components to 1e-7 of the largest)
+    assert np.allclose(fb_gm, fb_rk, rtol=1e-7, atol=1e-7 * np.abs(fb_rk).max())
 
