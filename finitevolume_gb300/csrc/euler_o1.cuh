@@ -35,6 +35,23 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+// Warp sums of four values at once, transposed: the first exchange leaves
+// each lane two partial sums (values 0,1 or 2,3, by lane bit 4), the second
+// one (by lane bit 3), and three ordinary butterfly steps finish it.  Lane
+// l returns the sum of value (l >> 3) & 3: 6 FP64 additions per lane
+// instead of 20 for four separate warp_sum calls (the selects run on the
+// integer pipe).  Deterministic; the addition order differs from warp_sum.
+__device__ __forceinline__ double warp_sum4(double v0, double v1, double v2, double v3) {
+    const int lane = threadIdx.x & 31;
+    const bool b4 = lane & 16, b3 = lane & 8;
+    const double k0 = b4 ? v2 : v0, k1 = b4 ? v3 : v1;
+    const double a = k0 + __shfl_xor_sync(0xffffffffu, b4 ? v0 : v2, 16);
+    const double b = k1 + __shfl_xor_sync(0xffffffffu, b4 ? v1 : v3, 16);
+    double v = (b3 ? b : a) + __shfl_xor_sync(0xffffffffu, b3 ? a : b, 8);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 
 // Per-face wave-speed estimate max(|Vn|+c) of EulerFVMSolver::compute_dt
 // (src/EulerFVMSolver.cpp:140-150).
@@ -93,9 +110,9 @@ __device__ __forceinline__ void finish_norms(double s0, double s1, double s2, do
     __shared__ double red[16][4];
     __shared__ bool last;
     const int nw = blockDim.x >> 5;
-    s0 = warp_sum(s0); s1 = warp_sum(s1); s2 = warp_sum(s2); s3 = warp_sum(s3);
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { red[w][0] = s0; red[w][1] = s1; red[w][2] = s2; red[w][3] = s3; }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double ws = warp_sum4(s0, s1, s2, s3);
+    if ((lane & 7) == 0) red[w][lane >> 3] = ws;
     __syncthreads();
     if (threadIdx.x < 4) {
         double v = 0.0;
@@ -113,10 +130,9 @@ __device__ __forceinline__ void finish_norms(double s0, double s1, double s2, do
         const volatile double* p = partials + 4 * b;
         t[0] += p[0]; t[1] += p[1]; t[2] += p[2]; t[3] += p[3];
     }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) t[k] = warp_sum(t[k]);
+    const double ts = warp_sum4(t[0], t[1], t[2], t[3]);
     __syncthreads();
-    if ((threadIdx.x & 31) == 0) { red[w][0] = t[0]; red[w][1] = t[1]; red[w][2] = t[2]; red[w][3] = t[3]; }
+    if ((lane & 7) == 0) red[w][lane >> 3] = ts;
     __syncthreads();
     if (threadIdx.x == 0) {
         double n[4];

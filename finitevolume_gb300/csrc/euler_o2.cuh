@@ -11,7 +11,7 @@
 //            with the inverse normal matrix, one pair per CSR entry) or
 //            Green-Gauss, then Barth-Jespersen or Venkatakrishnan limiting.
 //            The per-face limiter values are min-reduced by
-//            cross-multiplication, so each variable costs one division.
+//            cross-multiplication, so each variable costs one reciprocal.
 //   k_face   one thread per face: linear reconstruction to the face
 //            midpoint (positivity fallback to the cell value), ghost state
 //            from the reconstructed owner state, numerical flux on
@@ -204,6 +204,15 @@ __device__ __forceinline__ V4<T> rusanov_p(const V4<T>& L, const V4<T>& R, T nx,
 template <typename T> __device__ __forceinline__ T trsqrt(T x);
 template <> __device__ __forceinline__ double trsqrt<double>(double x) { return rsqrt(x); }
 template <> __device__ __forceinline__ float trsqrt<float>(float x) { return rsqrtf(x); }
+
+// a / b where only the quotient's value matters to within an ulp (the
+// limiter, the local time step): FP64 as a times fvconv::rcp_nr3(b), which
+// issues fewer FP64-pipe instructions on this part than the correctly
+// rounded division or the built-in reciprocal (ncu counts per cell); FP32
+// as the division.  HLLC keeps the built-in reciprocal, which measured
+// fewer there.
+template <typename T> __device__ __forceinline__ T tdiv(T a, T b) { return a / b; }
+template <> __device__ __forceinline__ double tdiv<double>(double a, double b) { return a * fvconv::rcp_nr3(b); }
 
 template <typename T>
 __device__ __forceinline__ V4<T> hllc_p(const V4<T>& L, const V4<T>& R, T nx, T ny, T g, T igm1) {
@@ -484,7 +493,7 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
                 if (num * dmn < nmin * den) { nmin = num; dmn = den; lim = true; }
             }
             // psi = 1 needs no division or scaling
-            const T psi = lim ? nmin / dmn : T(1);
+            const T psi = lim ? tdiv<T>(nmin, dmn) : T(1);
             if constexpr (sizeof(T) == 8) {
                 if (a.lim_psi) a.lim_psi[4 * c + k] = psi;
             }
@@ -640,7 +649,7 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_update(const O2Args a) {
             // steady state); global: the min over faces, divided by the volume.
             if (DT == 2) {
                 if constexpr (std::is_same<T, float>::value) dtv = fvconv::f2d(fvconv::d2f(a.ctl->cfl) / lamf);
-                else dtv = a.ctl->cfl / lam;
+                else dtv = tdiv<double>(a.ctl->cfl, lam);
             } else {
                 dtv = __longlong_as_double((long long)a.ctl->dt_bits) / a.m.vol[c];
             }
@@ -668,7 +677,7 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_update(const O2Args a) {
             WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, prim32(un, a.gamma32, cs));
             if (STAGE == NST - 1) static_cast<float*>(a.cs)[c] = cs;
         } else {
-            const double ir = 1.0 / un.r;
+            const double ir = fvconv::rcp_nr3(un.r);  // same as k_prim / k_update
             const double uu = un.ru * ir, vv = un.rv * ir;
             const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
             WStore<T>::st(static_cast<typename WStore<T>::type*>(a.W), c, V4<T>{un.r, uu, vv, p});
@@ -745,7 +754,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_prim(const O2Args a) {
     if (c >= a.m.n_cells) return;
     const St un = ld_state(a.U, c);
     const double g = a.gamma;
-    const double ir = 1.0 / un.r;
+    const double ir = fvconv::rcp_nr3(un.r);  // same as k_prim / k_update
     const double uu = un.ru * ir, vv = un.rv * ir;
     const double p = (g - 1.0) * (un.E - 0.5 * un.r * (uu * uu + vv * vv));
     if constexpr (std::is_same<T, float>::value) {

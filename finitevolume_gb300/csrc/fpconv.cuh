@@ -12,6 +12,9 @@
 //   binary64: sign 1 | exponent 11 (bias 1023) | fraction 52
 // so a normal value keeps its fraction bits (shifted by 29) and has its
 // exponent re-biased by 1023 - 127 = 896.
+//
+// rcp_nr3 (an FP64 reciprocal with three FP64-pipe instructions) uses the
+// same encodings to seed its iteration from the FP32 reciprocal.
 #pragma once
 
 #include <cstdint>
@@ -73,6 +76,26 @@ __device__ __forceinline__ float d2f(double x) {
         r = (uint32_t)(q + ((rem > half) | ((rem == half) & (q & 1ull))));
     }
     return __uint_as_float(sign | r);
+}
+
+// FP64 reciprocal with three DFMA: the FP32 approximate reciprocal of x
+// (x truncated to float on the integer pipe, rcp.approx.f32, widened on
+// the integer pipe) is a seed y with relative error e <= 2^-22, i.e.
+// r = 1 - x y = e; one step of the third-order Newton-Raphson iteration for
+// 1/x (the Taylor series 1/x = y (1 + r + r^2 + ...) truncated after r^2)
+// leaves x y' = 1 - e^3 ~ 1 - 2^-66, so the single rounding of the final
+// FMA gives 1/x to within about half an ulp.  Values outside the float
+// normal range (and 0, inf, NaN) take the IEEE division.
+__device__ __forceinline__ double rcp_nr3(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    if (e - 898u > 250u) return 1.0 / x;  // |x| outside [2^-125, 2^126)
+    const unsigned fb = ((unsigned)(b >> 32) & 0x80000000u) | ((e - 896u) << 23) | ((unsigned)(b >> 29) & 0x7fffffu);
+    float s;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"(__uint_as_float(fb)));
+    const double y = f2d(s);
+    const double r = fma(-x, y, 1.0);
+    return fma(y, fma(r, r, r), y);
 }
 
 }  // namespace fvconv

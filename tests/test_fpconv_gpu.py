@@ -25,3 +25,22 @@ def test_integer_conversions_match_hardware(gpu, tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "f2d_mismatch 0 d2f_mismatch 0" in r.stdout
+
+
+@pytest.mark.gpu
+def test_fp64_reciprocal_within_an_ulp(gpu, tmp_path):
+    """fvconv::rcp_nr3, the FP64 reciprocal of the second-order kernels
+    (limiter quotient, local time step, 1/rho of the primitive copy): within
+    one ulp of the IEEE reciprocal on 2^30 inputs (equal to it on at least
+    99%), and the IEEE result itself outside the float normal range."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = str(tmp_path / "rcp_check")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-I",
+                    os.path.join(ROOT, "finitevolume_gb300", "csrc"), os.path.join(ROOT, "tests", "cuda", "rcp_check.cu"),
+                    "-o", exe], check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    f = r.stdout.split()
+    vals = dict(zip(f[0:8:2], map(int, f[1:8:2])))
+    assert vals["rcp_bad"] == 0 and vals["rcp_max_ulp"] <= 1
+    assert vals["rcp_inexact"] <= vals["rcp_checked"] // 100, r.stdout
