@@ -198,9 +198,9 @@ __device__ __forceinline__ V4<T> rusanov_p(const V4<T>& L, const V4<T>& R, T nx,
 
 // HLLC on primitive inputs (HllcFlux.h:35-76), rearranged for the FP64
 // pipe: the sound speeds come from one reciprocal square root each
-// (c = g p / sqrt(g p rho)), the energy and 1/rho only of the upwind side
-// that the flux uses, and with q = 1/(S_K - S*) the star factor is
-// rho_K (S_K - Vn_K) q and the pressure term of E* is (S* - Vn_K) p_K q.
+// (c = g p / sqrt(g p rho)), the energy only of the upwind side that the
+// flux uses, and with q = 1/(S_K - S*) the star factor is
+// rho_K (S_K - Vn_K) q and the star energy needs no 1/rho_K (below).
 template <typename T> __device__ __forceinline__ T trsqrt(T x);
 template <> __device__ __forceinline__ double trsqrt<double>(double x) { return rsqrt(x); }
 template <> __device__ __forceinline__ float trsqrt<float>(float x) { return rsqrtf(x); }
@@ -222,21 +222,24 @@ __device__ __forceinline__ V4<T> hllc_p(const V4<T>& L, const V4<T>& R, T nx, T 
     T SL = fmin(VnL - cL, VnR - cR), SR = fmax(VnL + cL, VnR + cR);
     if (SL >= T(0)) return phys_flux_p(L, L.p * igm1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v), VnL, nx, ny);
     if (SR <= T(0)) return phys_flux_p(R, R.p * igm1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v), VnR, nx, ny);
-    T mL = L.r * (SL - VnL), mR = R.r * (SR - VnR);
+    const T dL = SL - VnL, dR = SR - VnR;
+    T mL = L.r * dL, mR = R.r * dR;
     // A reciprocal plus a multiply issues fewer FP64 instructions than a
     // general division on this part.
     T Ss = (R.p - L.p + mL * VnL - mR * VnR) * (T(1) / (mL - mR));
     bool left = Ss >= T(0);
     T SK = left ? SL : SR, VnK = left ? VnL : VnR;
-    T mK = left ? mL : mR;
+    T mK = left ? mL : mR, dK = left ? dL : dR;
     V4<T> K = left ? L : R;
     const T EK = K.p * igm1 + T(0.5) * K.r * (K.u * K.u + K.v * K.v);
-    const T irK = T(1) / K.r;
     T q = T(1) / (SK - Ss);
     T fac = mK * q;
     T VtK = -K.u * ny + K.v * nx;
     T mn = fac * Ss, mt = fac * VtK;
-    T Es = fac * (EK * irK + (Ss - VnK) * Ss) + (Ss - VnK) * K.p * q;
+    // E* = rho*_K [E_K / rho_K + (S* - Vn_K)(S* + p_K / (rho_K (S_K - Vn_K)))]
+    // with rho*_K = m_K q: the 1/rho_K cancels, leaving
+    // E* = q [(S_K - Vn_K) E_K + (S* - Vn_K)(m_K S* + p_K)].
+    T Es = q * (dK * EK + (Ss - VnK) * (mK * Ss + K.p));
     V4<T> FK = phys_flux_p(K, EK, VnK, nx, ny);
     return {FK.r + SK * (fac - K.r),
             FK.u + SK * ((mn * nx - mt * ny) - K.r * K.u),
@@ -512,8 +515,9 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
 
 template <typename T>
 __device__ __forceinline__ V4<T> recon(const V4<T>& w, const G8<T>& g, T rx, T ry) {
-    V4<T> o = {w.r + (g.gx[0] * rx + g.gy[0] * ry), w.u + (g.gx[1] * rx + g.gy[1] * ry),
-               w.v + (g.gx[2] * rx + g.gy[2] * ry), w.p + (g.gx[3] * rx + g.gy[3] * ry)};
+    // w + gx rx + gy ry as two multiply-adds (contracted to FMA)
+    V4<T> o = {g.gx[0] * rx + (g.gy[0] * ry + w.r), g.gx[1] * rx + (g.gy[1] * ry + w.u),
+               g.gx[2] * rx + (g.gy[2] * ry + w.v), g.gx[3] * rx + (g.gy[3] * ry + w.p)};
     // Positivity fallback; "x > 0" tested on the integer pipe (sign bit clear
     // and not +0).
     if (OKey<T>::bits(o.r) <= 0 || OKey<T>::bits(o.p) <= 0) return w;

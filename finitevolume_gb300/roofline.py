@@ -60,13 +60,13 @@ KERNEL_NAMES = ("gradients", "faces", "update")
 # DRAM bytes per cell per launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum, one launch of each kernel class) on the 968,870-cell
 # NACA0012 mixed mesh; the captures are summarised under profiles/.
-MEASURED_TRAFFIC_PER_CELL = {"gradients": 283.1, "faces": 330.9, "update": 207.3}
+MEASURED_TRAFFIC_PER_CELL = {"gradients": 283.1, "faces": 331.2, "update": 206.8}
 MEASURED_TRAFFIC_PER_CELL_FP32 = {"gradients": 146.5, "faces": 168.5, "update": 150.3}
 
 # FP64-pipe thread instructions per cell and per launch from the same
 # captures (smsp__inst_executed_pipe_fp64.sum x 32 / cells).  On GB300 the
 # FP64 pipe, not HBM, bounds the FP64 kernels.
-MEASURED_FP64_INST_PER_CELL = {"gradients": 259.4, "faces": 291.0, "update": 44.4}
+MEASURED_FP64_INST_PER_CELL = {"gradients": 259.4, "faces": 254.1, "update": 44.4}
 
 
 def measured_traffic(kind: str, n_cells: int, fp32: bool = False):
