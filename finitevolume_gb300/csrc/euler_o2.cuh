@@ -333,6 +333,7 @@ template <> struct OKey<double> {
     __device__ static I bits(double x) { return __double_as_longlong(x); }
     __device__ static double from_bits(I b) { return __longlong_as_double(b); }
     __device__ static I sign_bit() { return (I)0x8000000000000000ULL; }
+    __device__ static I one_exp() { return (I)1 << 52; }  // +1 in the exponent field
     __device__ static I key(double x) { I b = __double_as_longlong(x); return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
     __device__ static double val(I k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL)); }
 };
@@ -341,6 +342,7 @@ template <> struct OKey<float> {
     __device__ static I bits(float x) { return __float_as_int(x); }
     __device__ static float from_bits(I b) { return __int_as_float(b); }
     __device__ static I sign_bit() { return (I)0x80000000u; }
+    __device__ static I one_exp() { return (I)1 << 23; }
     __device__ static I key(float x) { I b = __float_as_int(x); return b ^ ((b >> 31) & 0x7fffffff); }
     __device__ static float val(I k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
 };
@@ -491,7 +493,13 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
                     const T p = d1 * y;
                     const T q = d1 * d1 + eps2;
                     num = q + T(2) * p;
-                    den = (y + y) * y + (q + p);
+                    // 2y by incrementing the exponent of y's bit pattern
+                    // (integer pipe; y > 0: exact for normal y, infinity
+                    // past the largest binade as 2y would be; a subnormal
+                    // y gives a value below twice the smallest normal, as
+                    // 2y is, which only scales an already negligible 2y^2)
+                    const T y2 = OK::from_bits(yb + OK::one_exp());
+                    den = y2 * y + (q + p);
                 }
                 if (num * dmn < nmin * den) { nmin = num; dmn = den; lim = true; }
             }

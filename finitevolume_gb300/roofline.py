@@ -66,7 +66,7 @@ MEASURED_TRAFFIC_PER_CELL_FP32 = {"gradients": 146.5, "faces": 168.5, "update": 
 # FP64-pipe thread instructions per cell and per launch from the same
 # captures (smsp__inst_executed_pipe_fp64.sum x 32 / cells).  On GB300 the
 # FP64 pipe, not HBM, bounds the FP64 kernels.
-MEASURED_FP64_INST_PER_CELL = {"gradients": 259.4, "faces": 254.1, "update": 44.4}
+MEASURED_FP64_INST_PER_CELL = {"gradients": 251.4, "faces": 254.1, "update": 44.4}
 
 
 def measured_traffic(kind: str, n_cells: int, fp32: bool = False):
