@@ -876,6 +876,34 @@ int fv_mesh_permutation(fv_mesh_t mesh, int32_t* perm) {
     });
 }
 
+int fv_mesh_agglomerate(fv_mesh_t mesh, int32_t counts[2], int32_t* agg, double* coarse_cell_f64,
+                        int32_t* coarse_face_i32, double* coarse_face_f64) {
+    return guarded([&] {
+        if (!mesh || !counts) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        std::vector<int32_t> a;
+        HostMesh c;
+        agglomerate(mesh->h, a, c);
+        counts[0] = c.n_cells;
+        counts[1] = c.n_faces;
+        if (agg) std::copy(a.begin(), a.end(), agg);
+        for (int32_t k = 0; k < c.n_cells && coarse_cell_f64; ++k) {
+            coarse_cell_f64[3 * (size_t)k] = c.vol[k];
+            coarse_cell_f64[3 * (size_t)k + 1] = c.cx[k];
+            coarse_cell_f64[3 * (size_t)k + 2] = c.cy[k];
+        }
+        for (int32_t f = 0; f < c.n_faces; ++f) {
+            if (coarse_face_i32) {
+                int32_t* o = coarse_face_i32 + 3 * (size_t)f;
+                o[0] = c.fl[f]; o[1] = c.fr[f]; o[2] = c.fpatch[f];
+            }
+            if (coarse_face_f64) {
+                double* o = coarse_face_f64 + 3 * (size_t)f;
+                o[0] = c.fnx[f]; o[1] = c.fny[f]; o[2] = c.farea[f];
+            }
+        }
+    });
+}
+
 int fv_mesh_destroy(fv_mesh_t mesh) {
     delete mesh;
     return FV_OK;

@@ -144,6 +144,24 @@ class Mesh:
         capi.check(capi.lib().fv_mesh_permutation(self._h, capi.i32ptr(p)))
         return p
 
+    def agglomerate(self):
+        """The first coarse level multigrid builds from this mesh (host
+        side): dict with ``agg`` (agglomerate of each fine cell), coarse
+        ``cells_f64`` (volume, cx, cy), ``faces_i32`` (left, right, patch)
+        and ``faces_f64`` (nx, ny, length)."""
+        n = np.zeros(2, np.int32)
+        null = C.POINTER(C.c_int32)()
+        dnull = C.POINTER(C.c_double)()
+        capi.check(capi.lib().fv_mesh_agglomerate(self._h, capi.i32ptr(n), null, dnull, null, dnull))
+        nc, nf = int(n[0]), int(n[1])
+        agg = np.zeros(self.n_cells, np.int32)
+        cd = np.zeros((nc, 3), np.float64)
+        fi = np.zeros((nf, 3), np.int32)
+        fd = np.zeros((nf, 3), np.float64)
+        capi.check(capi.lib().fv_mesh_agglomerate(self._h, capi.i32ptr(n), capi.i32ptr(agg), capi.dptr(cd),
+                                                  capi.i32ptr(fi), capi.dptr(fd)))
+        return {"agg": agg, "cells_f64": cd, "faces_i32": fi, "faces_f64": fd}
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:

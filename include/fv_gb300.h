@@ -100,6 +100,17 @@ int fv_mesh_export(fv_mesh_t mesh, int32_t* face_i32, double* face_f64, double* 
                    int32_t* cell_face_off, int32_t* cell_faces);
 /* Device-order permutation: perm[new] = reference cell index. */
 int fv_mesh_permutation(fv_mesh_t mesh, int32_t* perm);
+/* The first coarse level that fv_solver_multigrid builds from this mesh
+ * (host only; inspection and test helper; no reference counterpart).
+ * counts[2] receives the coarse cell and face counts; any other pointer may
+ * be NULL: agg [N] the agglomerate of each fine cell (reference
+ * numbering), coarse_cell_f64 [3*Nc] volume,cx,cy, coarse_face_i32 [3*Fc]
+ * left,right (-1 on boundary),patch (-1 inside), coarse_face_f64 [3*Fc]
+ * nx,ny,length (the unit normal and length of the summed n A of the fine
+ * faces merged into it, oriented out of `left`).  Call once with NULL
+ * arrays to size them; the result is deterministic. */
+int fv_mesh_agglomerate(fv_mesh_t mesh, int32_t counts[2], int32_t* agg, double* coarse_cell_f64,
+                        int32_t* coarse_face_i32, double* coarse_face_f64);
 int fv_mesh_destroy(fv_mesh_t mesh);
 
 /* ------------------------------------------------------------------------
