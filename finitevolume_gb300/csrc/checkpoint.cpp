@@ -76,7 +76,9 @@ int fv_checkpoint_write(const char* path, int32_t equation, int64_t step_index, 
 int fv_checkpoint_read(const char* path, int32_t expected_equation, int64_t expected_cell_count, int64_t* step_index,
                        uint64_t* build_number, double* payload) {
     return guard([&] {
-        if (!path || !payload || expected_cell_count < 0) fvgb::raise(FV_ERR_BAD_ARG, "fv_checkpoint_read: bad argument");
+        if (!path || !payload || expected_cell_count < 0 ||
+            (expected_equation >= 0 && doubles_per_cell(expected_equation) < 0))
+            fvgb::raise(FV_ERR_BAD_ARG, "fv_checkpoint_read: bad argument");
         File f(std::fopen(path, "rb"));
         if (!f.f) fvgb::raise(FV_ERR_BAD_ARG, std::string("fv_checkpoint_read: cannot open ") + path);
         char magic[8];

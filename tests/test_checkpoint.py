@@ -68,3 +68,16 @@ def test_residual_csv(tmp_path):
     lines = open(p).read().splitlines()
     assert lines[0] == "step,residual_rho,residual_rho_u,residual_rho_v,residual_E"
     assert [l.split(",")[0] for l in lines[1:]] == ["2", "4"]
+
+
+def test_read_rejects_unknown_equation_tag(tmp_path):
+    """An equation tag the format does not define is rejected before any
+    payload is read, even when the file carries the same tag."""
+    src = bytearray(_ref("ckpt_euler_ref.bin"))
+    src[12:16] = (99).to_bytes(4, "little")
+    path = str(tmp_path / "tag99.bin")
+    open(path, "wb").write(bytes(src))
+    out = np.zeros(40)
+    st = capi.lib().fv_checkpoint_read(path.encode(), 99, 10, None, None, capi.dptr(out))
+    assert st == capi.FV_ERR_BAD_ARG
+    assert not out.any()
