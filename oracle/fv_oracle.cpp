@@ -749,6 +749,19 @@ void* orc_euler_create(void* mp, const int* bc_type, const double* bc_state, con
     return e;
 }
 void orc_euler_free(void* e) { delete static_cast<orc::Euler*>(e); }
+// One numerical flux (0 Rusanov, 1 HLLC, 2 exact Riemann; 3 the physical
+// flux of UL) of conserved states UL, UR [4] through the unit normal
+// (nx, ny): out [4].  For the flux known-answer tests.
+void orc_flux(int flux, const double* UL, const double* UR, double nx, double ny, double g, double tol, int maxit,
+              double* out) {
+    const orc::State L{UL[0], UL[1], UL[2], UL[3]}, R{UR[0], UR[1], UR[2], UR[3]};
+    orc::State F;
+    if (flux == 0) F = orc::rusanov(L, R, nx, ny, g);
+    else if (flux == 1) F = orc::hllc(L, R, nx, ny, g);
+    else if (flux == 2) F = orc::exact(L, R, nx, ny, g, tol, maxit);
+    else F = orc::phys_flux(L, nx, ny, g);
+    out[0] = F.rho; out[1] = F.rho_u; out[2] = F.rho_v; out[3] = F.E;
+}
 void orc_euler_run(void* ep, int n, double* hist) {
     auto* e = static_cast<orc::Euler*>(ep);
     for (int s = 0; s < n; ++s) {

@@ -37,6 +37,7 @@ def lib():
         L.orc_euler_create.restype = C.c_void_p
         L.orc_euler_create.argtypes = [C.c_void_p, _I, _D, _D, _I, _D]
         L.orc_euler_free.argtypes = [C.c_void_p]
+        L.orc_flux.argtypes = [C.c_int, _D, _D, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _D]
         L.orc_euler_run.argtypes = [C.c_void_p, C.c_int, _D]
         L.orc_euler_field.argtypes = [C.c_void_p, _D]
         L.orc_euler_set_field.argtypes = [C.c_void_p, _D]
@@ -56,6 +57,17 @@ def lib():
 
 def _d(a):
     return np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(_D)
+
+
+def flux(kind: int, UL, UR, nx: float, ny: float, gamma: float = 1.4, tol: float = 1e-6, maxit: int = 20):
+    """One numerical flux of the oracle (0 Rusanov, 1 HLLC, 2 exact Riemann,
+    3 the physical flux of UL) through the unit normal (nx, ny)."""
+    out = np.zeros(4)
+    ul = np.ascontiguousarray(UL, dtype=np.float64)
+    ur = np.ascontiguousarray(UR, dtype=np.float64)
+    lib().orc_flux(int(kind), ul.ctypes.data_as(_D), ur.ctypes.data_as(_D), nx, ny, gamma, tol, int(maxit),
+                   out.ctypes.data_as(_D))
+    return out
 
 
 class OracleMesh:
