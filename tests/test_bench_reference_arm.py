@@ -1,0 +1,50 @@
+"""bench.py --impl reference: the line the reference arm prints (CPU).
+
+The reference arm times the CPU restatement of the reference's loop on the
+host cores and prints one JSON line with the same metric, unit and config
+as the GPU arm plus "impl": "reference", a cpu_baseline block and an e2e
+block with no host-device traffic.  Run here on a small mesh (the full
+1M-cell mesh is swapped for a 2k-cell one) so it finishes in seconds.
+"""
+import argparse
+import io
+import json
+import os
+import sys
+from contextlib import redirect_stdout
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_one_contract_line(monkeypatch):
+    sys.path.insert(0, ROOT)
+    import bench
+    from finitevolume_gb300 import meshgen
+
+    monkeypatch.setattr(bench, "load_mesh", lambda: meshgen.naca_mixed(32, 16, seed=0))
+    monkeypatch.setenv("FV_REF_SECONDS", "2")
+    args = argparse.Namespace(gpus=1, steps=3, warmup=1)
+    buf = io.StringIO()
+    with redirect_stdout(buf):
+        bench.run_reference(args, 0)
+    lines = [ln for ln in buf.getvalue().splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"] == bench.METRIC and d["unit"] == "Mcell-iters/s"
+    assert d["higher_is_better"] is True and d["n_gpus"] == 1
+    assert d["value"] > 0 and 1 <= d["steps"] <= 3
+    assert d["config"]["workload"] == "naca0012_mixed_1M_o2_hllc_lsq_venkat_rk3"
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "Mcell-iters/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_print_nothing():
+    sys.path.insert(0, ROOT)
+    import bench
+    buf = io.StringIO()
+    with redirect_stdout(buf):
+        bench.run_reference(argparse.Namespace(gpus=2, steps=3, warmup=1), 1)
+    assert buf.getvalue() == ""
