@@ -692,6 +692,25 @@ def cpu_port_rate(poly, U0, max_seconds: float, threads: int = 0):
     return om.n_cells * n / dt / 1e6, n, dt, port.num_threads()
 
 
+def cpu_baseline_block(poly, U0, seconds: float, seconds_1t: float) -> dict:
+    """The bench line's cpu_baseline: the oracle port on all host threads,
+    plus a single-thread sample of the same scheme on the same mesh."""
+    from oracle import port
+    all_threads = port.num_threads()
+    v, n, dt, cores = cpu_port_rate(poly, U0, seconds)
+    out = {"value": round(v, 3), "unit": "Mcell-iters/s", "cores": cores, "kind": "port",
+           "sample": f"{n} SSP-RK3 iterations of the same 2nd-order HLLC scheme on the full mesh, "
+                     f"OpenMP over {cores} threads ({dt:.1f} s)"}
+    if seconds_1t > 0:
+        try:
+            v1, n1, dt1, _ = cpu_port_rate(poly, U0, seconds_1t, threads=1)
+        finally:
+            port.set_threads(all_threads)
+        out["single_thread"] = {"value": round(v1, 3), "unit": "Mcell-iters/s", "cores": 1,
+                                "sample": f"{n1} iterations on one thread ({dt1:.1f} s)"}
+    return out
+
+
 def run_reference(args, rank):
     """--impl reference: the CPU restatement of the reference's loop."""
     if rank != 0:
@@ -790,11 +809,8 @@ def main():
     poly = load_mesh()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, n, dt, cores = cpu_port_rate(poly, initial_state(poly),
-                                        float(os.environ.get("FV_CPU_SECONDS", "15")))
-        cpu = {"value": round(v, 3), "unit": "Mcell-iters/s", "cores": cores, "kind": "port",
-               "sample": f"{n} SSP-RK3 iterations of the same 2nd-order HLLC scheme on the full mesh, "
-                         f"OpenMP over {cores} threads ({dt:.1f} s)"}
+        cpu = cpu_baseline_block(poly, initial_state(poly), float(os.environ.get("FV_CPU_SECONDS", "15")),
+                                 float(os.environ.get("FV_CPU_1T_SECONDS", "5")))
 
     solver, mesh = make_solver(poly)
     n_cells, n_faces, n_bf = mesh.n_cells, mesh.n_faces, mesh.n_bfaces

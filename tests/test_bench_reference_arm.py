@@ -48,3 +48,19 @@ def test_reference_arm_other_ranks_print_nothing():
     with redirect_stdout(buf):
         bench.run_reference(argparse.Namespace(gpus=2, steps=3, warmup=1), 1)
     assert buf.getvalue() == ""
+
+
+def test_cpu_baseline_block_has_all_threads_and_single_thread_samples():
+    sys.path.insert(0, ROOT)
+    import bench
+    from finitevolume_gb300 import meshgen
+    from oracle import port
+
+    poly = meshgen.naca_mixed(32, 16, seed=0)
+    before = port.num_threads()
+    cb = bench.cpu_baseline_block(poly, bench.initial_state(poly), 0.5, 0.5)
+    assert cb["kind"] == "port" and cb["unit"] == "Mcell-iters/s" and cb["value"] > 0
+    assert cb["cores"] == before
+    st = cb["single_thread"]
+    assert st["cores"] == 1 and st["value"] > 0 and st["unit"] == "Mcell-iters/s"
+    assert port.num_threads() == before  # thread count restored
