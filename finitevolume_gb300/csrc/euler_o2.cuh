@@ -498,7 +498,8 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
                     // past the largest binade as 2y would be; a subnormal
                     // y gives a value below twice the smallest normal, as
                     // 2y is, which only scales an already negligible 2y^2)
-                    const T y2 = OK::from_bits(yb + OK::one_exp());
+                    using U = typename std::make_unsigned<I>::type;  // wraps, never overflows
+                    const T y2 = OK::from_bits((I)((U)yb + (U)OK::one_exp()));
                     den = y2 * y + (q + p);
                 }
                 if (num * dmn < nmin * den) { nmin = num; dmn = den; lim = true; }
