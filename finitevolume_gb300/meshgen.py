@@ -7,7 +7,8 @@ counter-clockwise cells and tagged boundary edges, ready for
 * :func:`naca_ogrid`     NACA 4-digit O-grid (closed trailing edge, geometric
                          wall-normal stretching, circular farfield)
 * :func:`naca_mixed`     O-grid core + a Lloyd-relaxed polygonal outer region
-                         (dual of a Delaunay triangulation, 3-9 sided cells)
+                         (dual of a Delaunay triangulation; cells of 3-11
+                         sides, more than 99.9% of them 4-9)
 * :func:`sod_strip`      randomly perturbed triangle strip (shock tube)
 * :func:`wavy_quads`     non-affine ("wavy") structured quads, for gradient
                          exactness checks
@@ -226,7 +227,8 @@ def naca_mixed(ni: int = 1024, nj: int = 512, first: float = 1e-3, r_core: float
     (Voronoi-centroid moves, periodic in eta), then triangulated; each point
     becomes one polygonal cell whose vertices are the centroids of its
     Delaunay triangles (the centroid dual: always a simple, star-shaped
-    polygon, 3-9 sided after relaxation).  The core's outer ring nodes are
+    polygon; after relaxation more than 99.9% of them have 4-9 sides, a
+    few 10 or 11).  The core's outer ring nodes are
     the dual's inner boundary vertices: their cells close on the ring edge
     midpoints, which also become the fifth vertex of the core's outermost
     quads, so the two regions share faces exactly.
