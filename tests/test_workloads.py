@@ -99,6 +99,11 @@ def test_naca4412_hybrid_structure():
     assert abs(m.nodes[wall][:, 1].max() + m.nodes[wall][:, 1].min()) > 0.02
     sp = _first_spacing(m, wall)
     assert abs(np.median(sp) - 4.5e-6) < 0.1 * 4.5e-6
+    # y+ of the first cell at Re 6e6 from the flat-plate skin friction
+    # Cf = 0.026 Re^(-1/7): about 1
+    re = 6e6
+    yplus = np.median(sp) * re * np.sqrt(0.5 * 0.026 * re ** (-1.0 / 7.0))
+    assert 0.7 < yplus < 1.4
 
 
 def test_batch_family_ranges():
