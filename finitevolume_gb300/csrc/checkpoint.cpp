@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <string>
 
 #include "../../include/fv_gb300.h"
@@ -48,6 +49,9 @@ int guard(Fn&& fn) {
     } catch (const fvgb::Error& e) {
         fvgb::set_last_error(e.msg);
         return e.code;
+    } catch (const std::exception& e) {  // no exception crosses the C ABI
+        fvgb::set_last_error(e.what());
+        return FV_ERR_BAD_ARG;
     }
 }
 

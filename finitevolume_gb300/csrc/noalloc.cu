@@ -21,6 +21,7 @@
 // therefore race on the scratch and must be serialised by the caller.
 #include <cfloat>
 #include <cstring>
+#include <exception>
 #include <mutex>
 
 #include "../../include/fv_gb300.h"
@@ -150,5 +151,8 @@ extern "C" int fv_step_noalloc(const fv_noalloc_mesh_t* mesh, const fv_bc_t* bcs
     } catch (const Error& e) {
         set_last_error(e.msg);
         return e.code;
+    } catch (const std::exception& e) {  // no exception crosses the C ABI
+        set_last_error(e.what());
+        return FV_ERR_BAD_ARG;
     }
 }
