@@ -66,6 +66,17 @@ def test_driver_compiles_against_stand_in_declarations(tmp_path):
     assert os.path.exists(compile_driver(str(tmp_path), os.path.join(SHIM, "ref_decls")))
 
 
+@pytest.mark.parametrize("which", ["reference", "stand-in"])
+def test_class_surface_compiles(which):
+    """Every member of the reference's solver classes, called with the
+    reference's argument types, compiles against the drop-in headers."""
+    inc = REF_INCLUDE if which == "reference" and os.path.isdir(REF_INCLUDE) else os.path.join(SHIM, "ref_decls")
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include", "fvgb300"),
+           "-I", os.path.join(ROOT, "include"), "-I", inc, os.path.join(SHIM, "api_surface.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
 def _run(exe, mesh_txt, case, out):
     with open(out + ".case", "w") as f:
         f.write("\n".join(f"{k} {float(v)!r}" for k, v in case.items()) + "\n")
