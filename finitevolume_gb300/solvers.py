@@ -21,7 +21,7 @@ from __future__ import annotations
 import ctypes as C
 import dataclasses
 import enum
-from typing import List, Optional, Sequence
+from typing import Optional, Sequence
 
 import numpy as np
 

@@ -9,7 +9,7 @@ sums are reductions in a different order).
 import numpy as np
 import pytest
 
-from finitevolume_gb300 import capi, meshgen, solvers
+from finitevolume_gb300 import capi, meshgen
 from helpers import (GAMMA, case_of, cons, gpu_solver, load_golden, parse_bcs, parse_ic, poly_of, rel_err)
 from oracle import port
 
