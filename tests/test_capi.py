@@ -33,6 +33,26 @@ def test_library_exports_every_declared_symbol():
     assert set(capi.SIGNATURES) >= names
 
 
+def declared_arity():
+    """Parameter count of every prototype in include/fv_gb300.h."""
+    txt = open(os.path.join(ROOT, "include", "fv_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\b(fv_[a-z0-9_]+)\s*\(([^;{)]*)\)\s*;", txt):
+        params = params.strip()
+        out[name] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_bindings_match_the_declared_arity():
+    """capi.py declares each entry point with as many arguments as the
+    header's prototype (a drifted binding would pass garbage silently)."""
+    arity = declared_arity()
+    assert len(arity) >= 50
+    for name, n in sorted(arity.items()):
+        assert len(capi.SIGNATURES[name][1]) == n, (name, n, capi.SIGNATURES[name])
+
+
 def test_abi_version_and_device_count():
     L = capi.lib()
     assert L.fv_abi_version() >= 100
