@@ -126,3 +126,40 @@ def test_batch_family_ranges():
     # seeded: the same family every time
     again = meshgen.batch_cases(256, seed=0)
     assert all(a == b for a, b in zip(cases, again))
+
+
+def test_surface_displacement_directions():
+    """The shape-gradient check's directions: seeded white noise on the
+    wall nodes smoothed by a Gaussian over 20 nodes, along the unit wall
+    normal, zero elsewhere, scaled to a maximum of 1."""
+    poly = meshgen.naca_ogrid(128, 32)
+    dirs = meshgen.wall_normal_directions(poly, 16, seed=0, width=20)
+    assert len(dirs) == 16
+    _, wall, _ = _wall_and_far(poly)
+    off_wall = np.setdiff1d(np.arange(poly.nodes.shape[0]), wall)
+    for d in dirs:
+        assert d.shape == poly.nodes.shape
+        assert not d[off_wall].any()
+        mag = np.hypot(d[wall, 0], d[wall, 1])
+        np.testing.assert_allclose(mag.max(), 1.0, rtol=1e-12)
+    # normal to the wall: orthogonal to the local tangent (central difference
+    # along the wall loop)
+    e = poly.bedges[poly.bpatch == list(poly.patch_names).index("airfoil")]
+    nxt = {int(a): int(b) for a, b in e}
+    order = [int(e[0, 0])]
+    while nxt[order[-1]] != order[0]:
+        order.append(nxt[order[-1]])
+    P = poly.nodes[order]
+    tang = np.roll(P, -1, axis=0) - np.roll(P, 1, axis=0)
+    for d in dirs:
+        dd = d[order]
+        assert np.abs(np.sum(dd * tang, axis=1)).max() <= 1e-12 * np.abs(tang).max()
+    # smooth: neighbouring wall nodes move alike (white noise would not)
+    a = np.array([np.sum(d[order] * np.stack([tang[:, 1], -tang[:, 0]], 1), axis=1) for d in dirs])
+    a /= np.abs(a).max(axis=1, keepdims=True)
+    jumps = np.abs(np.diff(a, axis=1)).max()
+    assert jumps < 0.3
+    # seeded
+    again = meshgen.wall_normal_directions(poly, 16, seed=0, width=20)
+    assert all(np.array_equal(x, y) for x, y in zip(dirs, again))
+    assert not np.array_equal(dirs[0], meshgen.wall_normal_directions(poly, 1, seed=1, width=20)[0])
