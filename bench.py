@@ -617,11 +617,42 @@ def config1_rate(steps: int = 3000):
     h = s.run(steps, history=True)
     t = time.perf_counter() - t0
     f = s.wall_forces(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0)
-    return {"workload": "naca0012 O-grid 256x128, 1st-order Rusanov, forward Euler, local dt, CFL 0.5, M 0.5, AoA 2",
-            "cells": mesh.n_cells, "steps": steps, "seconds": round(t, 4),
-            "value": round(mesh.n_cells * steps / t / 1e6, 3), "unit": "Mcell-iters/s (wall clock, graph path)",
-            "cl": f["cl"], "cd": f["cd_total"], "residual_rho_first": float(h[0, 0]),
-            "residual_rho_last": float(h[-1, 0])}
+    out = {"workload": "naca0012 O-grid 256x128, 1st-order Rusanov, forward Euler, local dt, CFL 0.5, M 0.5, AoA 2",
+           "cells": mesh.n_cells, "steps": steps, "seconds": round(t, 4),
+           "value": round(mesh.n_cells * steps / t / 1e6, 3), "unit": "Mcell-iters/s (wall clock, graph path)",
+           "cl": f["cl"], "cd": f["cd_total"], "residual_rho_first": float(h[0, 0]),
+           "residual_rho_last": float(h[-1, 0])}
+    try:
+        out["cpu_baseline"] = config1_cpu_rate(steps)
+    except Exception as e:  # an auxiliary figure never breaks the bench line
+        out["cpu_baseline"] = {"error": str(e)[:200]}
+    return out
+
+
+def config1_cpu_rate(steps: int = 3000, seconds: float = 3.0) -> dict:
+    """The same first-order case on the host cores: the oracle port (the
+    reference's first-order loop, here with local time stepping and the
+    characteristic farfield), OpenMP over all threads, a bounded sample of
+    the iterations."""
+    from finitevolume_gb300 import meshgen
+    from oracle import port
+    M, aoa = 0.5, 2.0
+    a = np.radians(aoa)
+    r, u, v, p = 1.0, M * np.cos(a), M * np.sin(a), 1.0 / GAMMA
+    st = [r, r * u, r * v, p / (GAMMA - 1.0) + 0.5 * r * (u * u + v * v)]
+    om = port.OracleMesh(meshgen.naca_ogrid(256, 128))
+    e = port.OracleEuler(om, [(0, [0.0] * 4), (3, st)], gamma=GAMMA, cfl=0.5,
+                         ic={"mode": "free", "rho": r, "u": u, "v": v, "p": p}, flux=0, order=1, rk=1,
+                         local_dt=True)
+    t0 = time.perf_counter()
+    e.run(10)
+    per = (time.perf_counter() - t0) / 10
+    n = max(10, min(steps, int(seconds / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    e.run(n)
+    dt = time.perf_counter() - t0
+    return {"value": round(om.n_cells * n / dt / 1e6, 3), "unit": "Mcell-iters/s", "cores": port.num_threads(),
+            "kind": "port", "sample": f"{n} of the {steps} iterations after 10 warm-up ({dt:.2f} s)"}
 
 
 def profile_target(target: str, steps: int) -> dict:

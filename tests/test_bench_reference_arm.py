@@ -64,3 +64,11 @@ def test_cpu_baseline_block_has_all_threads_and_single_thread_samples():
     st = cb["single_thread"]
     assert st["cores"] == 1 and st["value"] > 0 and st["unit"] == "Mcell-iters/s"
     assert port.num_threads() == before  # thread count restored
+
+
+def test_config1_cpu_baseline():
+    sys.path.insert(0, ROOT)
+    import bench
+    cb = bench.config1_cpu_rate(steps=50, seconds=0.2)
+    assert cb["kind"] == "port" and cb["value"] > 0 and cb["cores"] >= 1
+    assert cb["unit"] == "Mcell-iters/s" and "of the 50 iterations" in cb["sample"]
