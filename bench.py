@@ -36,6 +36,7 @@ GAMMA = 1.4
 MACH, AOA_DEG, CFL, VENKAT_K = 0.8, 1.25, 1.2, 5.0
 MESH_KW = dict(ni=1024, nj=512, first=1e-3, r_core=2.0, r_far=20.0, code="0012", lloyd_iters=4, seed=0)
 METRIC = "Mcell-iters/s, 2nd-order HLLC Euler at 1M cells; batched/FP32/adjoint vs plain"
+DATA = "synthetic (seeded NACA0012 mixed mesh; freestream + seeded smooth 1% perturbation start)"
 # FP64-pipe thread instructions per second of one GB300 (152 SMs at 2070 MHz,
 # a dependent-chain-free DFMA loop timed with CUDA events: 1.02 TFLOP/s).
 FP64_PIPE_GINST_S = 510.0
@@ -87,6 +88,28 @@ def initial_state(poly):
     pp = p * (1.0 + 0.01 * fields[3])
     return np.ascontiguousarray(np.stack([rho, rho * uu, rho * vv, pp / (GAMMA - 1.0) + 0.5 * rho * (uu * uu + vv * vv)],
                                          1))
+
+
+def port_solver(poly):
+    """The oracle port (CPU FP64 restatement of the reference's loop, with
+    this build's second-order extensions) configured for the headline
+    scheme, starting from the benchmark's initial state."""
+    from oracle import port
+    r, u, v, p = freestream()
+    st = [r, r * u, r * v, p / (GAMMA - 1.0) + 0.5 * r * (u * u + v * v)]
+    e = port.OracleEuler(port.OracleMesh(poly), [(0, [0.0] * 4), (3, st)], gamma=GAMMA, cfl=CFL,
+                         ic={"mode": "free", "rho": r, "u": u, "v": v, "p": p}, flux=1, order=2, rk=3, local_dt=True,
+                         gradient=0, limiter=2, venkat_k=VENKAT_K)
+    e.set_field(initial_state(poly))
+    return e
+
+
+def headline_config(n_cells: int, n_faces: int, world: int) -> dict:
+    """The ``config`` block of the headline line, the same on both arms."""
+    return {"workload": "naca0012_mixed_1M_o2_hllc_lsq_venkat_rk3", "cells": n_cells, "faces": n_faces,
+            "mach": MACH, "aoa_deg": AOA_DEG, "cfl": CFL,
+            "l2": "inputs larger than L2 (working set > 400 MB), no flush",
+            "parallelism": f"replicas{world}" if world > 1 else "single"}
 
 
 def force_ref():
@@ -701,18 +724,14 @@ def run_batched(args):
 
 
 # --------------------------------------------------------------------------
-def cpu_port_rate(poly, U0, max_seconds: float, threads: int = 0):
-    """Time the oracle port (CPU restatement, OpenMP) on the same workload."""
+def cpu_port_rate(poly, max_seconds: float, threads: int = 0, keep: dict = None):
+    """Time the oracle port (CPU restatement, OpenMP) on the same workload,
+    from the benchmark's start state.  ``keep`` (a dict) receives the
+    port's field and the number of iterations it took."""
     from oracle import port
     if threads:
         port.set_threads(threads)
-    r, u, v, p = freestream()
-    om = port.OracleMesh(poly)
-    st = [r, r * u, r * v, p / (GAMMA - 1.0) + 0.5 * r * (u * u + v * v)]
-    e = port.OracleEuler(om, [(0, [0.0] * 4), (3, st)], gamma=GAMMA, cfl=CFL,
-                         ic={"mode": "free", "rho": r, "u": u, "v": v, "p": p}, flux=1, order=2, rk=3, local_dt=True,
-                         gradient=0, limiter=2, venkat_k=VENKAT_K)
-    e.set_field(U0)
+    e = port_solver(poly)
     t0 = time.perf_counter()
     e.run(1)  # warm-up iteration (page faults, thread start-up)
     first = time.perf_counter() - t0
@@ -720,21 +739,23 @@ def cpu_port_rate(poly, U0, max_seconds: float, threads: int = 0):
     t0 = time.perf_counter()
     e.run(n)
     dt = time.perf_counter() - t0
-    return om.n_cells * n / dt / 1e6, n, dt, port.num_threads()
+    if keep is not None:
+        keep["field"], keep["iterations"] = e.field(), n + 1
+    return e.n_cells * n / dt / 1e6, n, dt, port.num_threads()
 
 
-def cpu_baseline_block(poly, U0, seconds: float, seconds_1t: float) -> dict:
+def cpu_baseline_block(poly, seconds: float, seconds_1t: float, keep: dict = None) -> dict:
     """The bench line's cpu_baseline: the oracle port on all host threads,
     plus a single-thread sample of the same scheme on the same mesh."""
     from oracle import port
     all_threads = port.num_threads()
-    v, n, dt, cores = cpu_port_rate(poly, U0, seconds)
+    v, n, dt, cores = cpu_port_rate(poly, seconds, keep=keep)
     out = {"value": round(v, 3), "unit": "Mcell-iters/s", "cores": cores, "kind": "port",
            "sample": f"{n} SSP-RK3 iterations of the same 2nd-order HLLC scheme on the full mesh, "
                      f"OpenMP over {cores} threads ({dt:.1f} s)"}
     if seconds_1t > 0:
         try:
-            v1, n1, dt1, _ = cpu_port_rate(poly, U0, seconds_1t, threads=1)
+            v1, n1, dt1, _ = cpu_port_rate(poly, seconds_1t, threads=1)
         finally:
             port.set_threads(all_threads)
         out["single_thread"] = {"value": round(v1, 3), "unit": "Mcell-iters/s", "cores": 1,
@@ -743,34 +764,33 @@ def cpu_baseline_block(poly, U0, seconds: float, seconds_1t: float) -> dict:
 
 
 def run_reference(args, rank):
-    """--impl reference: the CPU restatement of the reference's loop."""
+    """--impl reference: the CPU restatement of the reference's loop (the
+    oracle port, OpenMP over all host threads) on the same workload, with the
+    same config block, warm-up and step count as this build's arm where the
+    time budget allows (each step is one full SSP-RK3 iteration)."""
     if rank != 0:
         return
     poly = load_mesh()
     budget = float(os.environ.get("FV_REF_SECONDS", "60"))
     from oracle import port
-    r, u, v, p = freestream()
-    om = port.OracleMesh(poly)
-    st = [r, r * u, r * v, p / (GAMMA - 1.0) + 0.5 * r * (u * u + v * v)]
-    e = port.OracleEuler(om, [(0, [0.0] * 4), (3, st)], gamma=GAMMA, cfl=CFL,
-                         ic={"mode": "free", "rho": r, "u": u, "v": v, "p": p}, flux=1, order=2, rk=3, local_dt=True,
-                         gradient=0, limiter=2, venkat_k=VENKAT_K)
-    e.set_field(initial_state(poly))
+    e = port_solver(poly)
+    w = max(args.warmup, 3)
     t0 = time.perf_counter()
-    e.run(min(args.warmup, 1))
-    per = (time.perf_counter() - t0) / max(min(args.warmup, 1), 1)
+    e.run(1)
+    per = time.perf_counter() - t0
+    if w > 1:
+        e.run(w - 1)
     k = max(1, min(args.steps, int(budget / max(per, 1e-3))))
     t0 = time.perf_counter()
     e.run(k)
     dt = time.perf_counter() - t0
-    value = om.n_cells * k / dt / 1e6
-    sample = f"{k} of the requested {args.steps} iterations on the full {om.n_cells}-cell mesh"
+    value = e.n_cells * k / dt / 1e6
+    sample = f"{k} of the requested {args.steps} iterations on the full {e.n_cells}-cell mesh after {w} warm-up"
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": args.gpus,
-            "steps": k, "warmup": min(args.warmup, 1), "ms_per_step": round(dt / k * 1e3, 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "steps": k, "warmup": w, "ms_per_step": round(dt / k * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
             "impl": "reference",
-            "config": {"workload": "naca0012_mixed_1M_o2_hllc_lsq_venkat_rk3", "cells": om.n_cells,
-                       "faces": om.n_faces},
+            "config": headline_config(e.n_cells, e.mesh.n_faces, args.gpus),
             "cpu_baseline": {"value": round(value, 3), "unit": "Mcell-iters/s", "cores": port.num_threads(),
                              "kind": "port", "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "Mcell-iters/s", "h2d_bytes_per_step": 0,
@@ -839,9 +859,10 @@ def main():
     # threads only, no fork).
     poly = load_mesh()
     cpu = None
+    port_run = {}
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_block(poly, initial_state(poly), float(os.environ.get("FV_CPU_SECONDS", "15")),
-                                 float(os.environ.get("FV_CPU_1T_SECONDS", "5")))
+        cpu = cpu_baseline_block(poly, float(os.environ.get("FV_CPU_SECONDS", "15")),
+                                 float(os.environ.get("FV_CPU_1T_SECONDS", "5")), keep=port_run)
 
     solver, mesh = make_solver(poly)
     n_cells, n_faces, n_bf = mesh.n_cells, mesh.n_faces, mesh.n_bfaces
@@ -913,6 +934,18 @@ def main():
            "h2d_bytes_per_step": 32 * n_cells, "d2h_bytes_per_step": 32 * n_cells + 32,
            "steps": e2e_steps, "api": "fv_set_field + fv_step(1) + fv_get_residual + fv_get_field"}
 
+    # Parity of the headline itself: the GPU solver run from the same start
+    # state for as many iterations as the CPU baseline's port run took.
+    parity = None
+    if port_run:
+        ps, _ = make_solver(poly)
+        ps.run(port_run["iterations"])
+        Ug, Uc = ps.field(), port_run["field"]
+        parity = {"against": "oracle port (CPU FP64, oracle/fv_oracle.cpp), same start state",
+                  "iterations": port_run["iterations"], "tolerance": 1e-10,
+                  "max_rel_field_err": float(np.max(np.abs(Ug - Uc)) / np.max(np.abs(Uc)))}
+        del ps
+
     variants = {}
     if not args.no_variants:
         # FP32 flux/gradient arithmetic, FP64 accumulation/update/norms.
@@ -963,13 +996,9 @@ def main():
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mcell-iters/s", "n_gpus": world,
                 "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(elapsed_ms / args.steps, 4),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (seeded NACA0012 mixed mesh; freestream + seeded smooth 1% perturbation start)",
-                "config": {"workload": "naca0012_mixed_1M_o2_hllc_lsq_venkat_rk3", "cells": n_cells,
-                           "faces": n_faces, "mach": MACH, "aoa_deg": AOA_DEG, "cfl": CFL,
-                           "l2": "inputs larger than L2 (working set > 400 MB), no flush",
-                           "launch_threads_per_block": {k: launch[k] for k in ("gradients", "faces", "cells")},
-                           "parallelism": f"replicas{world}" if world > 1 else "single"},
-                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "data": DATA, "config": headline_config(n_cells, n_faces, world),
+                "launch_threads_per_block": {k: launch[k] for k in ("gradients", "faces", "cells")},
+                "roofline": roof, "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": int(np.sum(launches)), "variants": variants}
         print(json.dumps(line), flush=True)
     if world > 1:

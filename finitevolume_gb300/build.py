@@ -67,6 +67,13 @@ def _sources():
     return cu, cpp, hdr
 
 
+def reference_dir() -> str:
+    """The reference checkout: $FV_REFERENCE, else the directory named
+    ``reference`` beside this repository (used only to build the oracle's
+    reference binaries and the fixtures; absent on machines without it)."""
+    return os.environ.get("FV_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
 def build_library(force: bool = False, verbose: bool = False, jobs: int = 0) -> str:
     cu, cpp, hdr = _sources()
     allsrc = [os.path.join(CSRC, f) for f in cu + cpp + hdr] + [os.path.join(ROOT, "include", "fv_gb300.h")]
@@ -117,7 +124,7 @@ def build_oracle(force: bool = False, reference: str = None) -> str:
         os.replace(tmp, ORACLE_LIB)
         with open(stamp_file, "w") as f:
             f.write(stamp)
-    ref = reference or os.environ.get("FV_REFERENCE", "/root/reference")
+    ref = reference or reference_dir()
     if os.path.isdir(os.path.join(ref, "src")) and shutil.which("make"):
         _run(["make", "-s", "-C", ORACLE_DIR, "ref", "REF=" + ref])
     return ORACLE_LIB

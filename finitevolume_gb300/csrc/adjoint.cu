@@ -1505,7 +1505,7 @@ int fv_adjoint_create(fv_solver_t solver, int32_t limiter_mode, fv_adjoint_t* ou
                     if (twin[e] < 0) fvgb::raise(FV_ERR_BAD_MESH, "adjoint: face without a twin entry");
                 }
             int* d_twin = A->alloc<int>(E);
-            FV_CUDA(cudaMemcpy(d_twin, twin.data(), sizeof(int) * E, cudaMemcpyHostToDevice));
+            fvgb::h2d_sync(d_twin, twin.data(), sizeof(int) * E, s.stream);
             a.twin = d_twin;
         }
         *out = A.release();

@@ -141,7 +141,7 @@ struct DiffSolver {
         void* p = nullptr;
         FV_CUDA(cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(T)));
         owned.push_back(p);
-        if (!v.empty()) FV_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (!v.empty()) h2d_sync(p, v.data(), v.size() * sizeof(T));
         return static_cast<T*>(p);
     }
     template <typename T>
@@ -239,7 +239,7 @@ int fv_diffusion_create(fv_mesh_t mesh, double alpha, double dt, double initial_
         a.hist_cap = 1 << 16;
         a.hist = s.alloc<double>(a.hist_cap);
         a.ctl = s.alloc<fvgb::StepCtl>(1);
-        FV_CUDA(cudaMemset(a.ctl, 0, sizeof(fvgb::StepCtl)));
+        FV_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(fvgb::StepCtl), s.stream));
         a.alpha = alpha;
         a.dt = dt;
         for (int p = 0; p < h.n_patches; ++p) {
@@ -254,7 +254,7 @@ int fv_diffusion_create(fv_mesh_t mesh, double alpha, double dt, double initial_
         std::vector<double> phi0(s.N, 0.0);
         for (int c = 0; c < s.N; ++c)
             if (std::sqrt(h.cx[c] * h.cx[c] + h.cy[c] * h.cy[c]) < initial_radius) phi0[c] = initial_value;
-        FV_CUDA(cudaMemcpy(s.staging, phi0.data(), sizeof(double) * s.N, cudaMemcpyHostToDevice));
+        fvgb::h2d_sync(s.staging, phi0.data(), sizeof(double) * s.N, s.stream);
         fvgb::k_diff_gather<<<(s.N + 255) / 256, 256, 0, s.stream>>>(s.staging, a.phi, s.d_perm, s.N);
         FV_CUDA(cudaStreamSynchronize(s.stream));
         *out = d.release();

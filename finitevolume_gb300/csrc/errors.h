@@ -22,3 +22,18 @@ const char* last_error();
         if (e_ != cudaSuccess)                                                               \
             ::fvgb::raise(2, std::string(#call) + ": " + cudaGetErrorString(e_));          \
     } while (0)
+
+#ifdef __CUDACC__
+namespace fvgb {
+// Host -> device upload that has landed when it returns.  A plain
+// cudaMemcpy from pageable memory may return once the bytes are staged,
+// before the DMA reaches the device, and kernels on a non-blocking stream
+// are not ordered after the legacy stream; copying on `s` and waiting for
+// `s` closes that gap whatever stream later reads the data.
+inline void h2d_sync(void* dst, const void* src, size_t bytes, cudaStream_t s = cudaStreamLegacy) {
+    if (!bytes) return;
+    FV_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    FV_CUDA(cudaStreamSynchronize(s));
+}
+}  // namespace fvgb
+#endif

@@ -249,7 +249,7 @@ extern "C" int fv_solver_update_nodes(fv_solver_t solver, fv_mesh_t mesh, const 
             void* d = nullptr;
             FV_CUDA(cudaMalloc(&d, bytes ? bytes : 1));
             tmp.push_back(d);
-            if (bytes) FV_CUDA(cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice));
+            if (bytes) fvgb::h2d_sync(d, src, bytes, s.stream);
             return d;
         };
         struct Free {

@@ -71,7 +71,7 @@ struct GradApi {
         void* p = nullptr;
         FV_CUDA(cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(T)));
         owned.push_back(p);
-        if (!v.empty()) FV_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (!v.empty()) h2d_sync(p, v.data(), v.size() * sizeof(T));
         return static_cast<T*>(p);
     }
     template <typename T>
@@ -159,8 +159,8 @@ int fv_gradient_compute(fv_gradient_t h, const double* phi, const double* bounda
         if (!h || !phi || !boundary_phi || !grad) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
         fvgb::GradApi& a = h->a;
         const int N = a.N, F = a.F;
-        FV_CUDA(cudaMemcpy(a.phi_ref, phi, sizeof(double) * N, cudaMemcpyHostToDevice));
-        FV_CUDA(cudaMemcpy(a.bphi_ref, boundary_phi, sizeof(double) * F, cudaMemcpyHostToDevice));
+        fvgb::h2d_sync(a.phi_ref, phi, sizeof(double) * N);
+        fvgb::h2d_sync(a.bphi_ref, boundary_phi, sizeof(double) * F);
         fvgb::k_perm_gather<<<(N + 255) / 256, 256>>>(a.phi_ref, a.phi, a.perm, N);
         fvgb::k_perm_gather<<<(F + 255) / 256, 256>>>(a.bphi_ref, a.bphi, a.fperm, F);
         fvgb::k_api_grad<<<(N + 255) / 256, 256>>>(a.g, a.phi, a.bphi, a.grad);

@@ -19,10 +19,10 @@
 // other regions are fully overwritten before they are read.  Calls whose
 // GPU work overlaps (on different streams, or from different threads)
 // therefore race on the scratch and must be serialised by the caller.
+#include <algorithm>
 #include <cfloat>
 #include <cstring>
 #include <exception>
-#include <mutex>
 
 #include "../../include/fv_gb300.h"
 #include "errors.h"
@@ -39,37 +39,61 @@ constexpr size_t kPartBytes = sizeof(double) * 4 * (size_t)kMaxBlocks;
 constexpr size_t kHistOff = kPartOff + kPartBytes;
 constexpr size_t kHistBytes = 256;
 constexpr size_t kCtlOff = kHistOff + kHistBytes;
-constexpr size_t kScratchBytes = kCtlOff + 256;
+constexpr size_t kCheckOff = kCtlOff + 256;
+constexpr size_t kScratchBytes = kCheckOff + 256;
 static_assert(sizeof(StepCtl) <= 256, "control block must fit its slot");
 
 // The fixed scratch.  In host code the name is only a stand-in for the
 // device symbol: its device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
-
-// Device address of the scratch on the current device; resolved once per
-// device (module load happens here on the first call, so that first call
-// belongs before any stream capture).
-unsigned char* scratch_on_current_device() {
-    int dev = -1;
-    FV_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) raise(FV_ERR_UNSUPPORTED, "device ordinal beyond 63");
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (rc != cudaSuccess || !p)
-            raise(FV_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(rc));
-        g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-    }
-    return g_scratch_addr[dev];
+// Device address of the scratch in the current context.  It is resolved on
+// every call (cudaGetSymbolAddress allocates nothing), so it stays right
+// after a cudaDeviceReset or under a context the caller made current
+// itself.  The first call in a context may load the module: make it
+// before any stream capture.
+unsigned char* scratch_in_current_context() {
+    void* p = nullptr;
+    cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (rc != cudaSuccess || !p)
+        raise(FV_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(rc));
+    return static_cast<unsigned char*>(p);
 }
 
-__global__ void k_noalloc_arm(StepCtl* ctl, double cfl) {
+// Checks the caller's device mesh before any step kernel reads it: every
+// face's cells in range (right = -1 only with a patch), every boundary
+// face's patch in [0, n_bcs), the CSR offsets non-decreasing from 0 and
+// every entry naming a face.  Bits of *bad: 1 patch, 2 cell index, 4 CSR.
+__global__ void k_noalloc_check(const fv_noalloc_mesh_t m, int n_bcs, int* bad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = 0;
+    if (i < m.n_faces) {
+        const int L = m.face_left[i], R = m.face_right[i];
+        if (L < 0 || L >= m.n_cells || R < -1 || R >= m.n_cells) b |= 2;
+        if (R < 0) {
+            const int p = m.face_patch[i];
+            if (p < 0 || p >= n_bcs) b |= 1;
+        }
+    }
+    if (i < m.n_cells) {
+        const int e0 = m.cell_face_off[i], e1 = m.cell_face_off[i + 1];
+        if (e1 < e0 || (i == 0 && e0 != 0)) b |= 4;
+    }
+    if (i == 0) {
+        const int e1 = m.cell_face_off[m.n_cells];
+        if (e1 < 0) b |= 4;
+    }
+    if (b) atomicOr(bad, b);
+}
+
+__global__ void k_noalloc_check_entries(const fv_noalloc_mesh_t m, int* bad) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < m.cell_face_off[m.n_cells] && (unsigned)(m.cell_faces[e] >> 1) >= (unsigned)m.n_faces) atomicOr(bad, 4);
+}
+
+__global__ void k_noalloc_arm(StepCtl* ctl, double cfl, int* bad) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *bad = 0;
         ctl->dt_bits = (unsigned long long)__double_as_longlong(DBL_MAX);
         ctl->done_blocks = 0u;
         ctl->step = 0;
@@ -102,7 +126,7 @@ extern "C" int fv_step_noalloc(const fv_noalloc_mesh_t* mesh, const fv_bc_t* bcs
         if (flux < FV_FLUX_RUSANOV || flux > FV_FLUX_EXACT) raise(FV_ERR_BAD_ARG, "fv_step_noalloc: unknown flux");
         if (!(gamma > 1.0) || !(cfl > 0.0)) raise(FV_ERR_BAD_ARG, "fv_step_noalloc: gamma must be > 1, cfl > 0");
 
-        unsigned char* base = scratch_on_current_device();
+        unsigned char* base = scratch_in_current_context();
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         O1Args a;
         std::memset(&a, 0, sizeof(a));
@@ -137,8 +161,29 @@ extern "C" int fv_step_noalloc(const fv_noalloc_mesh_t* mesh, const fv_bc_t* bcs
         a.flux = flux;
         a.local_dt = 0;
 
-        k_noalloc_arm<<<1, 32, 0, s>>>(a.ctl, cfl);
+        int* bad = reinterpret_cast<int*>(base + kCheckOff);
+        k_noalloc_arm<<<1, 32, 0, s>>>(a.ctl, cfl, bad);
+        const int n_chk = std::max(mesh->n_faces, mesh->n_cells);
+        k_noalloc_check<<<(n_chk + 255) / 256, 256, 0, s>>>(*mesh, n_bcs, bad);
         FV_CUDA(cudaGetLastError());
+        int bad_h = 0;
+        FV_CUDA(cudaMemcpyAsync(&bad_h, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FV_CUDA(cudaStreamSynchronize(s));
+        if (!(bad_h & 4)) {
+            // the entries are only walked once the offsets are known sane
+            int n_ent = 0;
+            FV_CUDA(cudaMemcpyAsync(&n_ent, mesh->cell_face_off + mesh->n_cells, sizeof(int), cudaMemcpyDeviceToHost, s));
+            FV_CUDA(cudaStreamSynchronize(s));
+            if (n_ent > 0) {
+                k_noalloc_check_entries<<<(n_ent + 255) / 256, 256, 0, s>>>(*mesh, bad);
+                FV_CUDA(cudaGetLastError());
+                FV_CUDA(cudaMemcpyAsync(&bad_h, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+                FV_CUDA(cudaStreamSynchronize(s));
+            }
+        }
+        if (bad_h & 1) raise(FV_ERR_BAD_ARG, "fv_step_noalloc: a boundary face's patch is outside [0, n_bcs)");
+        if (bad_h & 2) raise(FV_ERR_BAD_ARG, "fv_step_noalloc: a face's cell index is out of range");
+        if (bad_h & 4) raise(FV_ERR_BAD_ARG, "fv_step_noalloc: cell_face_off / cell_faces are not a valid CSR");
         fast::launch_o1_part(a, 0, s);
         fast::launch_o1_part(a, 1, s);
         FV_CUDA(cudaGetLastError());

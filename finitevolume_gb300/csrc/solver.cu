@@ -49,7 +49,7 @@ static std::vector<float> to_float(const std::vector<double>& v) {
 template <typename T>
 static T* dupload(const std::vector<T>& v, std::vector<void*>& owned) {
     T* p = dalloc<T>(v.size(), owned);
-    if (!v.empty()) FV_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    if (!v.empty()) h2d_sync(p, v.data(), v.size() * sizeof(T));
     return p;
 }
 
@@ -169,7 +169,7 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     c0.cfl = cfl0;
     double dmax = DBL_MAX;
     std::memcpy(&c0.dt_bits, &dmax, sizeof(dmax));
-    FV_CUDA(cudaMemcpy(ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice));
+    h2d_sync(ctl, &c0, sizeof(c0));
     ensure_history(64);
 
     if (general) {
@@ -298,8 +298,7 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         }
         if (seg.empty()) {
             // no wall: infinite distance, as compute_wall_distance
-            FV_CUDA(cudaMemcpy(r.walld, std::vector<double>(N, INFINITY).data(), sizeof(double) * N,
-                               cudaMemcpyHostToDevice));
+            h2d_sync(r.walld, std::vector<double>(N, INFINITY).data(), sizeof(double) * N);
         } else {
             double4_32a* d_seg = dupload(seg, owned);
             RansArgs tmp = rans_args();
@@ -335,21 +334,34 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
 
 void Solver::ensure_history(int n) {
     if (hist && hist_cap >= n) return;
-    int cap = std::max(64, n);
-    double* h = nullptr;
-    FV_CUDA(cudaMalloc(&h, sizeof(double) * 4 * (size_t)cap));
-    FV_CUDA(cudaMemsetAsync(h, 0, sizeof(double) * 4 * (size_t)cap, stream));
-    FV_CUDA(cudaStreamSynchronize(stream));
-    if (hist) cudaFree(hist);
-    hist = h;
-    hist_cap = cap;
-    if (rans) {
-        double* nh = nullptr;
-        FV_CUDA(cudaMalloc(&nh, sizeof(double) * (size_t)cap));
-        FV_CUDA(cudaMemset(nh, 0, sizeof(double) * (size_t)cap));
-        if (nut_hist) cudaFree(nut_hist);
-        nut_hist = nh;
+    const int cap = std::max(64, n);
+    // Rows already recorded move to their slots in the larger ring (row =
+    // step % capacity), so a later history() still returns them.
+    int step = 0;
+    if (hist) {
+        FV_CUDA(cudaMemcpyAsync(&step, reinterpret_cast<const char*>(ctl) + offsetof(StepCtl, step), sizeof(int),
+                                cudaMemcpyDeviceToHost, stream));
+        FV_CUDA(cudaStreamSynchronize(stream));
     }
+    auto regrow = [&](double*& ring, int width) {
+        std::vector<double> next((size_t)width * cap, 0.0);
+        if (ring) {
+            std::vector<double> prev((size_t)width * hist_cap);
+            FV_CUDA(cudaMemcpyAsync(prev.data(), ring, prev.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            FV_CUDA(cudaStreamSynchronize(stream));
+            for (int s = std::max(0, step - hist_cap); s < step; ++s)
+                std::memcpy(&next[(size_t)width * (s % cap)], &prev[(size_t)width * (s % hist_cap)],
+                            sizeof(double) * width);
+        }
+        double* h = nullptr;
+        FV_CUDA(cudaMalloc(&h, sizeof(double) * next.size()));
+        h2d_sync(h, next.data(), sizeof(double) * next.size(), stream);
+        if (ring) cudaFree(ring);
+        ring = h;
+    };
+    regrow(hist, 4);
+    if (rans) regrow(nut_hist, 1);
+    hist_cap = cap;
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
 }
@@ -645,8 +657,8 @@ void Solver::limiter_values(double* out_ref, const double* in_ref) {
                 if (cfg.fp32) f[4 * (size_t)i + k] = (float)v;
                 else d[4 * (size_t)i + k] = v;
             }
-        FV_CUDA(cudaMemcpy(psi_buf, cfg.fp32 ? static_cast<const void*>(f.data()) : static_cast<const void*>(d.data()),
-                           4 * (size_t)N * esz, cudaMemcpyHostToDevice));
+        h2d_sync(psi_buf, cfg.fp32 ? static_cast<const void*>(f.data()) : static_cast<const void*>(d.data()),
+                 4 * (size_t)N * esz, stream);
         psi_mode = 2;
     }
     if (out_ref) {
@@ -1074,9 +1086,9 @@ int fv_set_nut(fv_solver_t s, const double* nut) {
         std::vector<double> d(v.N);
         for (int i = 0; i < v.N; ++i) d[i] = nut[v.perm[i]];
         FV_CUDA(cudaStreamSynchronize(v.stream));
-        FV_CUDA(cudaMemcpy(v.rs.nut, d.data(), sizeof(double) * v.N, cudaMemcpyHostToDevice));
+        fvgb::h2d_sync(v.rs.nut, d.data(), sizeof(double) * v.N, v.stream);
         const double z = 0.0;
-        FV_CUDA(cudaMemcpy(v.rs.nut_norm, &z, sizeof(z), cudaMemcpyHostToDevice));
+        fvgb::h2d_sync(v.rs.nut_norm, &z, sizeof(z), v.stream);
     });
 }
 

@@ -160,7 +160,7 @@ struct Solver {
     template <typename T>
     T* upload_owned(const std::vector<T>& v) {
         T* p = dalloc_owned<T>(v.size());
-        if (!v.empty()) FV_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (!v.empty()) h2d_sync(p, v.data(), v.size() * sizeof(T), stream);
         return p;
     }
     void eval_residual(St* out);

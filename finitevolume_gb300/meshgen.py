@@ -227,8 +227,10 @@ def naca_mixed(ni: int = 1024, nj: int = 512, first: float = 1e-3, r_core: float
     (Voronoi-centroid moves, periodic in eta), then triangulated; each point
     becomes one polygonal cell whose vertices are the centroids of its
     Delaunay triangles (the centroid dual: always a simple, star-shaped
-    polygon; after relaxation more than 99.9% of them have 4-9 sides, a
-    few 10 or 11).  The core's outer ring nodes are
+    polygon; after relaxation more than 99.9% of them have 4-9 sides).  The
+    few with 10 or more sides are split in two along a chord between two of
+    their vertices, so every outer cell has 3-9 sides.  The core's outer
+    ring nodes are
     the dual's inner boundary vertices: their cells close on the ring edge
     midpoints, which also become the fifth vertex of the core's outermost
     quads, so the two regions share faces exactly.
@@ -341,6 +343,8 @@ def naca_mixed(ni: int = 1024, nj: int = 512, first: float = 1e-3, r_core: float
         fan = off_tri + fan_t[np.argsort(ang)]
         cells.append([off_out + k, off_mid_out + (k - 1) % n_far] + fan.tolist() + [off_mid_out + k])
 
+    cells = _split_polygons(nodes, cells, max_sides=9)
+
     wall = np.stack([np.arange(ni), (np.arange(ni) + 1) % ni], 1)
     kk = np.arange(n_far)
     far = np.concatenate([np.stack([off_out + kk, off_mid_out + kk], 1),
@@ -350,6 +354,44 @@ def naca_mixed(ni: int = 1024, nj: int = 512, first: float = 1e-3, r_core: float
     _orient(mesh)
     mesh.validate_ccw()
     return mesh
+
+
+def _split_polygons(nodes, cells, max_sides: int = 9):
+    """Split every cell with more than ``max_sides`` vertices in two along a
+    chord between two of its vertices about half-way round (n vertices give
+    halves of n//2 + 1 and n - n//2 + 1).  No vertex is added, so the
+    neighbouring cells keep their faces.  Of the n candidate chords the one
+    whose halves are both convex and have the largest smaller area is
+    taken (failing convexity: the largest smaller signed area).  Cells keep
+    their vertex orientation."""
+    def signed_area(p):
+        x, y = p[:, 0], p[:, 1]
+        return 0.5 * float(np.sum(x * np.roll(y, -1) - np.roll(x, -1) * y))
+
+    def convex(p, sgn):
+        d1 = np.roll(p, -1, axis=0) - p
+        d2 = np.roll(d1, -1, axis=0)
+        return bool((sgn * (d1[:, 0] * d2[:, 1] - d1[:, 1] * d2[:, 0]) > 0).all())
+
+    out = []
+    for c in cells:
+        n = len(c)
+        if n <= max_sides:
+            out.append(c)
+            continue
+        pts = nodes[np.asarray(c)]
+        sgn = 1.0 if signed_area(pts) > 0 else -1.0
+        best, best_key = None, None
+        for i in range(n):
+            j = (i + n // 2) % n
+            a = [c[(i + k) % n] for k in range((j - i) % n + 1)]
+            b = [c[(j + k) % n] for k in range((i - j) % n + 1)]
+            pa, pb = nodes[np.asarray(a)], nodes[np.asarray(b)]
+            key = (convex(pa, sgn) and convex(pb, sgn), min(sgn * signed_area(pa), sgn * signed_area(pb)))
+            if best_key is None or key > best_key:
+                best, best_key = (a, b), key
+        out.extend(_split_polygons(nodes, list(best), max_sides))
+    return out
 
 
 def naca_hybrid(ni: int = 1024, n_layers: int = 40, first: float = 4.5e-6, growth: float = 1.15,
@@ -480,11 +522,15 @@ def wall_normal_directions(poly: PolyMesh, n_dirs: int, seed: int = 0, width: in
     return out
 
 
+CACHE_VERSION = 2  # 2: naca_mixed splits cells of more than 9 sides
+
+
 def cached(name: str, **kw) -> PolyMesh:
     """Generate ``name(**kw)`` once and keep it as .npz in a cache folder.
 
     The folder is ``$FV_MESH_CACHE`` or ``~/.cache/finitevolume_gb300``; the
-    key is the generator name and its keyword arguments.
+    key is the generator name, its keyword arguments and ``CACHE_VERSION``
+    (raised whenever a generator's output changes).
     """
     import hashlib
     import json
@@ -493,7 +539,7 @@ def cached(name: str, **kw) -> PolyMesh:
     from .fvmesh import PolyMesh as _PM
 
     root = os.environ.get("FV_MESH_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "finitevolume_gb300"))
-    key = hashlib.sha256(json.dumps([name, sorted(kw.items())], default=str).encode()).hexdigest()[:16]
+    key = hashlib.sha256(json.dumps([name, sorted(kw.items()), CACHE_VERSION], default=str).encode()).hexdigest()[:16]
     path = os.path.join(root, f"{name}_{key}.npz")
     if os.path.exists(path):
         z = np.load(path, allow_pickle=False)

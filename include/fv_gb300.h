@@ -465,14 +465,19 @@ int fv_checkpoint_read(const char* path, int32_t expected_equation, int64_t expe
  *
  * Its work arrays live in one fixed, file-scope device array of about
  * 4 MiB, held by every GPU that loads the library until the process exits;
- * hence the limits below (larger meshes fail with FV_ERR_BAD_ARG).  The
- * first call on each device resolves that array's device address (and may
- * load the module): make the first call before any stream capture.  All
- * calls share the array; calls whose GPU work overlaps race on it and must
- * be serialised by the caller.  The call synchronises `stream`.
+ * hence the limits below (larger meshes fail with FV_ERR_BAD_ARG).  Every
+ * call resolves that array's device address in the current context; the
+ * first call in a context may load the module, so make it before any
+ * stream capture.  All calls share the array; calls whose GPU work overlaps
+ * race on it and must be serialised by the caller.  The call synchronises
+ * `stream`.  Before stepping, a device-side check rejects (FV_ERR_BAD_ARG)
+ * a boundary face whose patch is outside [0, n_bcs), a face cell index out
+ * of range, and CSR offsets or entries that are not a valid cell-to-face
+ * map.
  *
  * Mesh arrays are device pointers in the caller's cell/face numbering:
- *   face_left/face_right [F] (right = -1 on boundary faces), face_patch [F],
+ *   face_left/face_right [F] (right = -1 on boundary faces), face_patch [F]
+ *   (0 <= patch < n_bcs on boundary faces),
  *   face_geom [4F] = nx, ny, length, CFL length (min(V_L, V_R)/length, or
  *   V_L/length on boundary faces), 32-byte aligned,
  *   cell_face_off [N+1], cell_faces [E] = face << 1 | (cell owns the face),

@@ -158,6 +158,43 @@ int run_euler(const UnstructuredMesh& m, const std::string& out) {
     std::vector<double> field;
     for (const EulerState& s : solver.field()) field.insert(field.end(), {s.rho, s.rho_u, s.rho_v, s.E});
     dump(out + "/field.f64", field);
+    if (!arg("ref_rho").empty()) {
+        // Inviscid wall forces: compute_wall_traction over every slip-wall
+        // face with zero viscosity and zero gradients (the traction is then
+        // the owner cell's pressure alone), then compute_wall_forces.
+        const size_t N = m.cells.size();
+        std::vector<double> u(N), v(N), p(N), rho(N), mu0(N, 0.0);
+        std::vector<Gradient2> g0(N);
+        for (size_t c = 0; c < N; ++c) {
+            const EulerState& s = solver.field()[c];
+            rho[c] = s.rho;
+            u[c] = s.rho_u / s.rho;
+            v[c] = s.rho_v / s.rho;
+            p[c] = pressure(s, gamma);
+        }
+        std::vector<int> wall_faces;
+        for (size_t f = 0; f < m.faces.size(); ++f)
+            if (m.faces[f].cell_right == -1 && bcs[m.faces[f].patch_id].type == EulerBoundaryType::Wall)
+                wall_faces.push_back((int)f);
+        UnstructuredMesh mg = m;
+        mg.compute_geometry();
+        std::vector<double> bz(m.faces.size(), 0.0);
+        std::vector<WallFaceSample> samples =
+            compute_wall_traction(mg, wall_faces, u, v, p, rho, mu0, bz, bz, g0, g0);
+        WallReferenceQuantities ref;
+        ref.rho_ref = argd("ref_rho", 1.0);
+        ref.velocity_x_ref = argd("ref_u", 1.0);
+        ref.velocity_y_ref = argd("ref_v", 0.0);
+        ref.p_ref = argd("ref_p", 0.0);
+        ref.length_ref = argd("ref_len", 1.0);
+        ref.moment_reference_x = argd("ref_mx", 0.25);
+        ref.moment_reference_y = argd("ref_my", 0.0);
+        std::vector<double> forces;
+        for (const WallForceReport& r : compute_wall_forces(mg, samples, ref))
+            forces.insert(forces.end(), {(double)r.patch_id, r.friction_drag, r.pressure_drag, r.total_drag, r.lift,
+                                         r.moment, r.cd_friction, r.cd_pressure, r.cd_total, r.cl, r.cm});
+        dump(out + "/forces.f64", forces);
+    }
     dump_history(out, hist, secs, steps, m.cells.size());
     return 0;
 }

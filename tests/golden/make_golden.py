@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from finitevolume_gb300 import fvmesh, meshgen  # noqa: E402
+from finitevolume_gb300 import build, fvmesh, meshgen  # noqa: E402
 
 GAMMA = 1.4
 
@@ -162,10 +162,50 @@ def cfl_ramp_fixture(tmp):
                         out=np.fromfile(out))
 
 
+def mesh_sha256(m) -> str:
+    """Digest of a mesh's arrays: pins a generator's output without storing it."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in (m.nodes, m.cell_off, m.cell_nodes, m.bedges, m.bpatch):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def config1_fixture(tmp, steps=3000):
+    """The small plain-method configuration at its own size, in the
+    reference's mode: NACA0012 O-grid 256 x 128 (32,768 cells), first-order
+    Rusanov, forward Euler with the global CFL time step at CFL 0.5, slip
+    wall and fixed-state farfield, M 0.5, AoA 2 deg, 3,000 iterations.  The
+    mesh is regenerated by the tests (its digest is stored); the field, the
+    residual history and the inviscid wall forces (compute_wall_forces) are
+    the reference's."""
+    M, aoa = 0.5, np.radians(2.0)
+    u, v, p = M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA
+    og = meshgen.naca_ogrid(256, 128)
+    path = os.path.join(tmp, "og256.fvmesh")
+    fvmesh.write_fvmesh(og, path)
+    out = os.path.join(tmp, "og256")
+    os.makedirs(out, exist_ok=True)
+    case = {"flux": "rusanov", "cfl": 0.5, "ic": "free:" + prim_str(1.0, u, v, p),
+            "bc": ["airfoil:wall", "farfield:farfield:" + prim_str(1.0, u, v, p)], "mach": M, "aoa_deg": 2.0,
+            "ref": [1.0, float(u), float(v), float(p), 1.0, 0.25, 0.0], "steps": steps, "mesh": "naca_ogrid(256, 128)"}
+    ref = case["ref"]
+    info = fvref("euler", path, out, flux="rusanov", cfl=case["cfl"], ic=case["ic"], bc=case["bc"], steps=steps,
+                 gamma=GAMMA, ref_rho=ref[0], ref_u=ref[1], ref_v=ref[2], ref_p=ref[3], ref_len=ref[4],
+                 ref_mx=ref[5], ref_my=ref[6])
+    np.savez_compressed(os.path.join(HERE, "config1_og256_ref.npz"), mesh_sha256=np.array(mesh_sha256(og)),
+                        field=np.fromfile(os.path.join(out, "field.f64")).reshape(-1, 4),
+                        hist=np.fromfile(os.path.join(out, "resid.f64")).reshape(-1, 4),
+                        forces=np.fromfile(os.path.join(out, "forces.f64")).reshape(-1, 11),
+                        case=np.array(json.dumps(case)))
+    return info
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["rans", "cfl"], default=None, help="regenerate one group of fixtures")
+    ap.add_argument("--ref", default=build.reference_dir())
+    ap.add_argument("--only", choices=["rans", "cfl", "config1"], default=None,
+                    help="regenerate one group of fixtures")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
     if a.only == "cfl":
@@ -176,9 +216,14 @@ def main():
         with tempfile.TemporaryDirectory() as tmp:
             rans_fixtures(tmp)
         return
+    if a.only == "config1":
+        with tempfile.TemporaryDirectory() as tmp:
+            print(config1_fixture(tmp))
+        return
     with tempfile.TemporaryDirectory() as tmp:
         rans_fixtures(tmp)
         cfl_ramp_fixture(tmp)
+        config1_fixture(tmp)
         # NACA0012 O-grid, M=0.5, AoA=2 deg, slip wall + fixed farfield.
         M, aoa = 0.5, np.radians(2.0)
         u, v, p = M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA

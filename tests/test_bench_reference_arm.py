@@ -33,7 +33,9 @@ def test_reference_arm_prints_one_contract_line(monkeypatch):
     assert d["impl"] == "reference"
     assert d["metric"] == bench.METRIC and d["unit"] == "Mcell-iters/s"
     assert d["higher_is_better"] is True and d["n_gpus"] == 1
-    assert d["value"] > 0 and 1 <= d["steps"] <= 3
+    assert d["value"] > 0 and 1 <= d["steps"] <= 3 and d["warmup"] == 3
+    # the same config block as the GPU arm prints
+    assert d["config"] == bench.headline_config(d["config"]["cells"], d["config"]["faces"], 1)
     assert d["config"]["workload"] == "naca0012_mixed_1M_o2_hllc_lsq_venkat_rk3"
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
@@ -58,8 +60,11 @@ def test_cpu_baseline_block_has_all_threads_and_single_thread_samples():
 
     poly = meshgen.naca_mixed(32, 16, seed=0)
     before = port.num_threads()
-    cb = bench.cpu_baseline_block(poly, bench.initial_state(poly), 0.5, 0.5)
+    keep = {}
+    cb = bench.cpu_baseline_block(poly, 0.5, 0.5, keep=keep)
     assert cb["kind"] == "port" and cb["unit"] == "Mcell-iters/s" and cb["value"] > 0
+    # the port's field is kept for the headline parity check
+    assert keep["field"].shape == (poly.n_cells, 4) and keep["iterations"] >= 2
     assert cb["cores"] == before
     st = cb["single_thread"]
     assert st["cores"] == 1 and st["value"] > 0 and st["unit"] == "Mcell-iters/s"

@@ -19,7 +19,7 @@ from helpers import case_of, load_golden, parse_ic, poly_of, rel_err
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SHIM = os.path.join(ROOT, "tests", "shim")
-REF_INCLUDE = os.path.join(os.environ.get("FV_REFERENCE", "/root/reference"), "include")
+REF_INCLUDE = os.path.join(build.reference_dir(), "include")
 
 
 def compile_driver(out_dir, ref_include):

@@ -73,6 +73,36 @@ def test_noalloc_step_matches_solver_twice(gpu, flux):
         want = ref.field()
         assert np.max(np.abs(got - want)) <= TOL * np.max(np.abs(want))
         np.testing.assert_allclose(norms, ref.residual().as_array(), rtol=TOL)
+
+    # The promise itself: once the first call has loaded the module, further
+    # calls take no device memory (free bytes of the device unchanged).
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        capi.check(L.fv_step_noalloc(C.byref(desc), bc_arr, 2, GAMMA, 0.5, int(flux), C.c_void_p(U.data_ptr()),
+                                     capi.dptr(norms), None))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    del keep
+
+
+def test_noalloc_rejects_patches_outside_the_bc_table(gpu):
+    """A boundary face whose patch has no boundary condition is an error
+    found on the device before any step kernel runs; the state is left
+    untouched."""
+    torch = pytest.importorskip("torch")
+    mesh = S.Mesh(meshgen.naca_ogrid(32, 16))
+    desc, keep = _caller_mesh(mesh, torch)
+    U0 = np.tile(np.array([1.0, 0.5, 0.0, 2.5]), (mesh.n_cells, 1))
+    U = torch.from_numpy(U0.copy()).cuda()
+    bc_arr = (capi.BC * 1)()  # the farfield patch (1) has no entry
+    norms = np.zeros(4)
+    rc = capi.lib().fv_step_noalloc(C.byref(desc), bc_arr, 1, GAMMA, 0.5, 0, C.c_void_p(U.data_ptr()),
+                                    capi.dptr(norms), None)
+    assert rc == capi.FV_ERR_BAD_ARG
+    assert b"patch" in capi.lib().fv_last_error()
+    assert np.array_equal(U.cpu().numpy(), U0)
     del keep
 
 
