@@ -30,6 +30,13 @@ class FVError(RuntimeError):
         self.status = status
 
 
+class NewtonOpts(C.Structure):
+    _fields_ = [("limiter_mode", C.c_int32), ("max_newton", C.c_int32), ("tol", C.c_double), ("cfl0", C.c_double),
+                ("cfl_max", C.c_double), ("cfl_growth", C.c_double), ("krylov_dim", C.c_int32),
+                ("krylov_rtol", C.c_double), ("precond_sweeps", C.c_int32), ("precond_kind", C.c_int32),
+                ("max_rel_change", C.c_double)]
+
+
 class BC(C.Structure):
     _fields_ = [("type", C.c_int32), ("isothermal", C.c_int32), ("state", C.c_double * 4),
                 ("wall_u", C.c_double), ("wall_v", C.c_double), ("wall_T", C.c_double), ("nut", C.c_double)]
@@ -100,6 +107,11 @@ SIGNATURES = {
     "fv_get_wall_distance": (C.c_int, [_P, _D]),
     "fv_solver_set_launch": (C.c_int, [_P, _I32]),
     "fv_solver_freeze_limiter": (C.c_int, [_P, C.c_int32]),
+    "fv_solver_set_persistent": (C.c_int, [_P, C.c_int32]),
+    "fv_solver_persistent": (C.c_int, [_P, _I32, _I32]),
+    "fv_solver_set_wait_limit": (C.c_int, [_P, C.c_int64, C.c_int32]),
+    "fv_newton_default": (None, [C.POINTER(NewtonOpts)]),
+    "fv_steady_newton": (C.c_int, [_P, C.POINTER(NewtonOpts), _D, _I32]),
     "fv_solver_limiter_values": (C.c_int, [_P, _D, _D]),
     "fv_solver_update_nodes": (C.c_int, [_P, _P, _D]),
     "fv_solver_multigrid": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_double]),

@@ -41,6 +41,7 @@
 #include <vector>
 
 #include "capi_internal.h"
+#include "adjoint_internal.h"
 
 namespace adjk {
 
@@ -137,54 +138,7 @@ template <> __device__ __forceinline__ D4 tpow<D4>(D4 a, D4 b) {
 }
 
 // ---------------------------------------------------------------------------
-struct AdjArgs {
-    int n_cells, n_faces, n_int_faces, order, flux;
-    const int* fl;
-    const int* fr;
-    const int* fpatch;
-    const double4_32a* fgeom;
-    const int* cf_off;
-    const int* cf;
-    const int* cnb;
-    const double2* lsq;
-    const double2* lsq_sum;
-    const double4_32a* frf;
-    const int* twin;
-    BCTable bc;
-    double gamma, igm1, cfl;
-    // linearisation state
-    const St* W;         // [N] primitives
-    const double2* Gu;   // [4N] unlimited gradients
-    const double* psi;   // [4N] limiter values
-    double* JL;          // [16F] dF/dw_L (boundary: through the ghost state)
-    double* JR;          // [16F] dF/dw_R (boundary: dF/d fs)
-    double* Gb;          // [32 Fb] 0.5 (I + dghost/dw) | 0.5 dghost/dfs of the gradient's boundary value
-    unsigned char* fb;   // [F] bit 0 owner side fell back to the cell value, bit 1 neighbour side
-    St* F;               // [F] flux times length
-    double* D;           // [N] local dt / V
-    // work arrays
-    double* wbar;        // [8F]
-    St* Wbar;            // [N]
-    double2* Gub;        // [4N]
-    double* fsb;         // [4 Fb]
-    St* dW;              // [N]
-    double2* dG;         // [4N]
-    St* dF;              // [F]
-    const double* dfs;   // [4 * kMaxPatches] primitive freestream tangents
-    // full-limiter linearisation (limiter != 0 and full == 1): per cell and
-    // variable the active side (0 none, +1 dmax side, -1 dmin side), the
-    // entry of the extreme neighbour value (-1: the cell itself), the entry
-    // of the extreme face extrapolation, and dpsi/d(d1), dpsi/dy
-    int full, limiter;
-    const double2* erf;  // [E] face midpoint - centroid
-    const double* eps2;  // [N] Venkatakrishnan eps^2
-    signed char* lside;  // [4N]
-    int* led;            // [4N]
-    int* ler;            // [4N]
-    double2* lpd;        // [4N] (dpsi/dd1, dpsi/dy)
-    double* lpe;         // [4N] dpsi/d eps^2 (Venkatakrishnan; 0 otherwise)
-    double* ldb;         // [4N] cotangent of d1 passed to the extreme neighbour
-};
+
 
 __device__ __forceinline__ V4<double> ldW(const St* W, int i) {
     const St s = ld_state(W, i);
@@ -1056,39 +1010,7 @@ namespace fvgb {
 const HostMesh& host_mesh_of(const fv_mesh_s* m);
 }
 
-struct fv_adjoint_s {
-    fv_solver_s* solver = nullptr;
-    AdjArgs a{};
-    int N = 0, F = 0, Fb = 0, P = 0;
-    std::vector<void*> owned;
-    St *U = nullptr, *W = nullptr, *stage_ref = nullptr, *stage_dev = nullptr, *lam = nullptr, *lam0 = nullptr,
-       *rhs = nullptr, *Rdev = nullptr;
-    double2 *Gu = nullptr, *G = nullptr;
-    double *psi = nullptr, *cs = nullptr, *partials = nullptr, *hist = nullptr, *dfs_dev = nullptr;
-    int* counter = nullptr;
-    // GMRES work arrays (allocated on first use): restart + 1 basis vectors,
-    // the affine part c, the work vector, the iterate, reduction partials
-    // and device scalars
-    double *kV = nullptr, *kc = nullptr, *kw = nullptr, *kx = nullptr, *kpart = nullptr, *kh = nullptr;
-    int k_restart = 0;
-    // shape-gradient work arrays (allocated on first use)
-    double *geo_face = nullptr, *geo_ab = nullptr, *geo_sb = nullptr, *geo_nbg = nullptr, *geo_er = nullptr,
-           *geo_ep = nullptr;
-    int hist_cap = 0;
-    bool linearised = false;
-    bool solved = false;
-    ~fv_adjoint_s() {
-        for (void* p : owned) cudaFree(p);
-        if (hist) cudaFree(hist);
-    }
-    template <typename T>
-    T* alloc(size_t n) {
-        void* p = nullptr;
-        FV_CUDA(cudaMalloc(&p, sizeof(T) * (n ? n : 1)));
-        owned.push_back(p);
-        return static_cast<T*>(p);
-    }
-};
+
 
 namespace {
 
@@ -1400,6 +1322,35 @@ void kdot(fv_adjoint_s* A, const double* x, const double* y, double* out, bool s
 }
 
 }  // namespace
+
+namespace adjh {
+void linearise(fv_adjoint_s* A) { ::linearise(A); }
+void lin_dt(fv_adjoint_s* A, double cfl) {
+    fvgb::Solver& s = A->solver->s;
+    A->a.cfl = cfl;
+    adjk::k_lin_dt<<<blocks(A->N), kB, 0, s.stream>>>(A->a);
+    check_launch();
+}
+void residual_dev(fv_adjoint_s* A, St* R) {
+    fvgb::Solver& s = A->solver->s;
+    adjk::k_res_cell<<<blocks(A->N), kB, 0, s.stream>>>(A->a, R);
+    check_launch();
+}
+void jvp_dev(fv_adjoint_s* A, const St* dU, St* dR) {
+    fvgb::Solver& s = A->solver->s;
+    FV_CUDA(cudaMemsetAsync(A->dfs_dev, 0, sizeof(double) * 4 * fvgb::kMaxPatches, s.stream));
+    adjk::k_fwd_cell1<<<blocks(A->N), kB, 0, s.stream>>>(A->a, dU);
+    check_launch();
+    if (A->a.order == 2) {
+        adjk::k_fwd_cell2<<<blocks(A->N), kB, 0, s.stream>>>(A->a);
+        check_launch();
+    }
+    adjk::k_fwd_face<<<blocks(A->F), kB, 0, s.stream>>>(A->a);
+    check_launch();
+    adjk::k_fwd_cell3<<<blocks(A->N), kB, 0, s.stream>>>(A->a, dR);
+    check_launch();
+}
+}  // namespace adjh
 
 extern "C" {
 

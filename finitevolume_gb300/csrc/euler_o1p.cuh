@@ -1,0 +1,373 @@
+// First-order explicit steps as one persistent, cooperative launch.
+//
+// The reference's step (src/EulerFVMSolver.cpp:58-112) needs every face flux
+// before any cell update and, in its global-dt mode, the minimum over all
+// faces of the CFL step (compute_dt, :133-162) before the first update.  The
+// two-kernel path (euler_o1.cuh) makes those dependencies kernel boundaries,
+// which on a 32k-cell mesh costs more than the arithmetic.  Here one launch
+// of co-resident blocks (a cooperative launch) runs K steps and
+// meets each dependency at a grid barrier:
+//
+//   prologue   per-cell primitives P = (u, v, p, c) of the current state
+//   per step   face phase: fluxes (and the CFL candidate or lambda*A),
+//                 block 0 also folds the previous step's norm partials
+//              barrier
+//              cell phase: signed gather, U += dt/V R, the new P, and one
+//                 norm partial per 256-cell tile
+//              barrier
+//   epilogue   block 0 folds the last step's partials
+//
+// P is the reference's own per-side quantities (u = rho_u/rho, v, the
+// pressure and sound speed expressions of EulerState.h:58-82), formed once
+// per cell instead of once per face side; the fluxes read them instead of
+// recomputing them.  Every value is the same IEEE result as before, so the
+// strict build (--fmad=false) stays bit-identical to the reference, and the
+// norm partials are formed over the same 256-cell tiles and folded in the
+// same order as k_cell_o1's, so the residual history is bit-identical to
+// the two-kernel path too.
+//
+// The grid barrier is a counter plus a generation word.  Every wait is
+// bounded (PersistCtl::limit, in SM clock cycles): a block that gives up
+// sets PersistCtl::err and leaves, so the others give up at their next
+// barrier too and the launch always ends; the host reports FV_ERR_TIMEOUT.
+//
+// Included by kernels_fast.cu and kernels_strict.cu with FV_KNS defined,
+// after euler_o1.cuh.
+#pragma once
+
+#include "euler_o1.cuh"
+
+namespace FV_KNS {
+
+using fvgb::PersistCtl;
+
+struct Prim {
+    double u, v, p, c;
+};
+
+__device__ __forceinline__ Prim prim_of(const St& s, double g) {
+    Prim q;
+    q.u = s.ru / s.r;
+    q.v = s.rv / s.r;
+    q.p = pressure(s, g);
+    q.c = sqrt(g * q.p / s.r);  // sound_speed: sqrt(g * pressure / rho)
+    return q;
+}
+// Loads of arrays this kernel itself writes (state, primitives, fluxes,
+// wave-speed sums) bypass L1 (ld.global.cg): another block may have
+// written them since this SM last cached the line, and only L2 is
+// coherent across SMs.  The read-only path (__ldg) would be wrong here.
+__device__ __forceinline__ St ld_state_cg(const St* U, int i) {
+    const double2* p = reinterpret_cast<const double2*>(U + i);
+    const double2 a = __ldcg(p), b = __ldcg(p + 1);
+    return st_make(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ Prim ld_prim(const double4_32a* P, int i) {
+    const double2* p = reinterpret_cast<const double2*>(P + i);
+    const double2 a = __ldcg(p), b = __ldcg(p + 1);
+    Prim o;
+    o.u = a.x; o.v = a.y; o.p = b.x; o.c = b.y;
+    return o;
+}
+__device__ __forceinline__ void st_prim(double4_32a* P, int i, const Prim& q) {
+    double4_32a o;
+    o.x = q.u; o.y = q.v; o.z = q.p; o.w = q.c;
+    P[i] = o;
+}
+
+// phys_flux (EulerState.h:89-101) with u, v, p taken from P.
+__device__ __forceinline__ St phys_flux_p(const St& s, const Prim& q, double nx, double ny) {
+    const double Vn = q.u * nx + q.v * ny;
+    St f;
+    f.r = s.r * Vn;
+    f.ru = s.ru * Vn + q.p * nx;
+    f.rv = s.rv * Vn + q.p * ny;
+    f.E = (s.E + q.p) * Vn;
+    return f;
+}
+
+// rusanov (RusanovFlux.h:33-43) with the per-side primitives from P.
+__device__ __forceinline__ St rusanov_p(const St& L, const Prim& PL, const St& R, const Prim& PR, double nx,
+                                        double ny) {
+    const double VnL = (L.ru * nx + L.rv * ny) / L.r;
+    const double VnR = (R.ru * nx + R.rv * ny) / R.r;
+    const double Smax = rmax(fabs(VnL) + PL.c, fabs(VnR) + PR.c);
+    const St FL = phys_flux_p(L, PL, nx, ny);
+    const St FR = phys_flux_p(R, PR, nx, ny);
+    return 0.5 * (FL + FR) - 0.5 * Smax * (R - L);
+}
+
+// hllc (HllcFlux.h:35-76) with the per-side primitives from P.
+__device__ __forceinline__ St hllc_p1(const St& UL, const Prim& PL, const St& UR, const Prim& PR, double nx,
+                                      double ny) {
+    const double tx = -ny, ty = nx;
+    const double rL = UL.r, rR = UR.r;
+    const double VnL = PL.u * nx + PL.v * ny, VnR = PR.u * nx + PR.v * ny;
+    const double VtL = PL.u * tx + PL.v * ty, VtR = PR.u * tx + PR.v * ty;
+    const double pL = PL.p, pR = PR.p, cL = PL.c, cR = PR.c;
+    const double SL = rmin(VnL - cL, VnR - cR);
+    const double SR = rmax(VnL + cL, VnR + cR);
+    if (SL >= 0.0) return phys_flux_p(UL, PL, nx, ny);
+    if (SR <= 0.0) return phys_flux_p(UR, PR, nx, ny);
+    const double Ss = (pR - pL + rL * VnL * (SL - VnL) - rR * VnR * (SR - VnR)) / (rL * (SL - VnL) - rR * (SR - VnR));
+    const bool left = (Ss >= 0.0);
+    const double SK = left ? SL : SR;
+    const double rK = left ? rL : rR;
+    const double VnK = left ? VnL : VnR;
+    const double VtK = left ? VtL : VtR;
+    const double pK = left ? pL : pR;
+    const St& UK = left ? UL : UR;
+    const Prim& PK = left ? PL : PR;
+    const double factor = rK * (SK - VnK) / (SK - Ss);
+    const double mn = factor * Ss;
+    const double mt = factor * VtK;
+    const double Es = factor * (UK.E / rK + (Ss - VnK) * (Ss + pK / (rK * (SK - VnK))));
+    St Us;
+    Us.r = factor;
+    Us.ru = mn * nx - mt * ny;
+    Us.rv = mn * ny + mt * nx;
+    Us.E = Es;
+    return phys_flux_p(UK, PK, nx, ny) + SK * (Us - UK);
+}
+
+template <int FLUX>
+__device__ __forceinline__ St num_flux_p(const St& L, const Prim& PL, const St& R, const Prim& PR, double nx,
+                                         double ny, double g, double tol, int maxit) {
+    if constexpr (FLUX == FLUX_HLLC) return hllc_p1(L, PL, R, PR, nx, ny);
+    else if constexpr (FLUX == FLUX_EXACT) return exact_riemann(L, R, nx, ny, g, tol, maxit);
+    else return rusanov_p(L, PL, R, PR, nx, ny);
+}
+
+// face_smax (compute_dt's per-face max(|Vn| + c)) with P.
+__device__ __forceinline__ double face_smax_p(const Prim& PL, const Prim& PR, bool interior, double nx, double ny) {
+    double Smax = fabs(PL.u * nx + PL.v * ny) + PL.c;
+    if (interior) Smax = rmax(Smax, fabs(PR.u * nx + PR.v * ny) + PR.c);
+    return Smax;
+}
+
+// Grid barrier with a bounded wait.  Returns false (in every thread of the
+// block) once any block has given up; the caller then returns.
+__device__ __forceinline__ bool grid_barrier(PersistCtl* pc, unsigned int expected) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = &pc->gen;
+        volatile int* verr = &pc->err;
+        const unsigned int g0 = *vgen;  // read before arriving: gen cannot move until this block arrives
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&pc->count, 1u);
+        int good = 1;
+        if (arrived == expected - 1) {
+            atomicExch(&pc->count, 0u);
+            __threadfence();
+            atomicAdd(&pc->gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*vgen == g0) {
+                if (*verr || clock64() - t0 > pc->limit) {
+                    atomicExch(&pc->err, 1);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = good && !*verr;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Block 0 folds one step's tile partials exactly as finish_norms' last
+// block does (tiles strided over the block's threads, transposed warp sums,
+// warps in order), records the history row and advances the step counter.
+__device__ __forceinline__ void fold_step_norms(StepCtl* ctl, const double* partials, int n_tiles, double* hist,
+                                                int hist_cap) {
+    __shared__ double red[fvgb::kCellBlock / 32][4];
+    constexpr int nw = fvgb::kCellBlock / 32;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < n_tiles; b += fvgb::kCellBlock) {
+        const volatile double* p = partials + 4 * b;
+        t[0] += p[0]; t[1] += p[1]; t[2] += p[2]; t[3] += p[3];
+    }
+    const double ts = warp_sum4(t[0], t[1], t[2], t[3]);
+    __syncthreads();
+    if ((lane & 7) == 0) red[w][lane >> 3] = ts;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double n[4];
+        int bad = 0;
+        for (int k = 0; k < 4; ++k) {
+            double v = 0.0;
+            for (int i = 0; i < nw; ++i) v += red[i][k];
+            n[k] = sqrt(v);
+            if (!isfinite(n[k])) bad = 1;
+            ctl->norms[k] = n[k];
+        }
+        const int row = ctl->step % hist_cap;
+        for (int k = 0; k < 4; ++k) hist[row * 4 + k] = n[k];
+        if (bad) ctl->nonfinite = 1;
+        ctl->step += 1;
+    }
+    __syncthreads();
+}
+
+template <int FLUX, bool LOCAL>
+__global__ void __launch_bounds__(fvgb::kCellBlock) k_o1_persistent(const O1Args a, double4_32a* __restrict__ P,
+                                                                     PersistCtl* __restrict__ pc, int nsteps) {
+    const double g = a.gamma;
+    const int nb = gridDim.x;
+    const unsigned int expected = (unsigned int)nb + (unsigned int)pc->phantom;
+    const int n_tiles = (a.m.n_cells + fvgb::kCellBlock - 1) / fvgb::kCellBlock;
+    const int F = a.m.n_faces, N = a.m.n_cells;
+
+    // prologue: primitives of the current state; both dt slots armed
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += nb * blockDim.x)
+        st_prim(P, c, prim_of(ld_state_cg(a.U, c), g));
+    if (blockIdx.x == 0 && threadIdx.x < 2)
+        pc->dt_slot[threadIdx.x] = (unsigned long long)__double_as_longlong(DBL_MAX);
+    if (!grid_barrier(pc, expected)) return;
+
+    for (int s = 0; s < nsteps; ++s) {
+        const int slot = s & 1;
+        if (blockIdx.x == 0 && s > 0) {
+            fold_step_norms(a.ctl, a.partials, n_tiles, a.hist, a.hist_cap);
+            if (threadIdx.x == 0) pc->dt_slot[slot ^ 1] = (unsigned long long)__double_as_longlong(DBL_MAX);
+        }
+        // face phase
+        const double cfl = a.ctl->cfl;
+        double cand = DBL_MAX;
+        for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += nb * blockDim.x) {
+            const int L = a.m.fl[f], R = a.m.fr[f];
+            const double4_32a geo = a.m.fgeom[f];
+            const St UL = ld_state_cg(a.U, L);
+            const Prim PL = ld_prim(P, L);
+            St UR;
+            Prim PR;
+            if (R >= 0) {
+                UR = ld_state_cg(a.U, R);
+                PR = ld_prim(P, R);
+            } else {
+                UR = ghost_state(a.bc, a.m.fpatch[f], UL, geo.x, geo.y, g);
+                PR = prim_of(UR, g);
+            }
+            const St Fl = num_flux_p<FLUX>(UL, PL, UR, PR, geo.x, geo.y, g, a.exact_tol, a.exact_max_iter);
+            st_state(a.ff, f, geo.z * Fl);
+            const double Smax = face_smax_p(PL, PR, R >= 0, geo.x, geo.y);
+            if (LOCAL) a.dtf[f] = Smax * geo.z;
+            else cand = fmin(cand, cfl * geo.w / Smax);
+        }
+        if (!LOCAL) {
+            __shared__ double smin[fvgb::kCellBlock / 32];
+            cand = warp_min(cand);
+            if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = cand;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double v = smin[0];
+                for (int w = 1; w < fvgb::kCellBlock / 32; ++w) v = fmin(v, smin[w]);
+                atomicMin(&pc->dt_slot[slot], (unsigned long long)__double_as_longlong(v));
+            }
+        }
+        if (!grid_barrier(pc, expected)) return;
+
+        // cell phase, one 256-cell tile at a time (the tiles of k_cell_o1)
+        const double dt_g = LOCAL ? 0.0 : __longlong_as_double((long long)*(volatile unsigned long long*)&pc->dt_slot[slot]);
+        for (int tile = blockIdx.x; tile < n_tiles; tile += nb) {
+            const int c = tile * fvgb::kCellBlock + threadIdx.x;
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            if (c < N) {
+                double dt = dt_g;
+                St Rs = st_make(0.0, 0.0, 0.0, 0.0);
+                const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
+                double lam = 0.0;
+                for (int e = e0; e < e1; ++e) {
+                    const int ent = a.m.cf[e];
+                    const int f = ent >> 1;
+                    Rs += flip_if(ld_state_cg(a.ff, f), ent);
+                    if (LOCAL) lam += __ldcg(a.dtf + f);
+                }
+                if (LOCAL) dt = cfl * a.m.vol[c] / lam;
+                s0 = Rs.r * Rs.r; s1 = Rs.ru * Rs.ru; s2 = Rs.rv * Rs.rv; s3 = Rs.E * Rs.E;
+                const St u = ld_state_cg(a.U, c);
+                const St un = u + (dt / a.m.vol[c]) * Rs;
+                st_state(a.U, c, un);
+                st_prim(P, c, prim_of(un, g));
+            }
+            // the tile's partial: finish_norms' block reduction
+            __shared__ double red[fvgb::kCellBlock / 32][4];
+            const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            const double ws = warp_sum4(s0, s1, s2, s3);
+            if ((lane & 7) == 0) red[w][lane >> 3] = ws;
+            __syncthreads();
+            if (threadIdx.x < 4) {
+                double v = 0.0;
+                for (int i = 0; i < fvgb::kCellBlock / 32; ++i) v += red[i][threadIdx.x];
+                a.partials[tile * 4 + threadIdx.x] = v;
+            }
+            __syncthreads();
+        }
+        if (!grid_barrier(pc, expected)) return;
+    }
+    if (blockIdx.x == 0 && nsteps > 0) fold_step_norms(a.ctl, a.partials, n_tiles, a.hist, a.hist_cap);
+}
+
+template <int FLUX, bool LOCAL>
+static int o1p_blocks_per_sm() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_o1_persistent<FLUX, LOCAL>, fvgb::kCellBlock, 0) !=
+        cudaSuccess)
+        return 0;
+    return nb;
+}
+
+template <int FLUX, bool LOCAL>
+static cudaError_t launch_o1p(const O1Args& a, double4_32a* P, PersistCtl* pc, int nsteps, int grid,
+                              cudaStream_t s) {
+    // cudaLaunchKernelEx with the cooperative attribute: co-residency of all
+    // blocks is guaranteed (or the launch fails), and the launch can be
+    // captured into a CUDA graph.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(fvgb::kCellBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_o1_persistent<FLUX, LOCAL>, a, P, pc, nsteps);
+}
+
+}  // namespace FV_KNS
+
+#ifdef FV_DEFINE_O1_LAUNCH
+namespace fvgb {
+namespace FV_KNS {
+// Largest co-resident grid of the persistent kernel for this flux/dt mode.
+int o1p_max_blocks_per_sm(int flux, int local) {
+    switch (flux * 2 + (local ? 1 : 0)) {
+        case 0: return ::FV_KNS::o1p_blocks_per_sm<0, false>();
+        case 1: return ::FV_KNS::o1p_blocks_per_sm<0, true>();
+        case 2: return ::FV_KNS::o1p_blocks_per_sm<1, false>();
+        case 3: return ::FV_KNS::o1p_blocks_per_sm<1, true>();
+        case 4: return ::FV_KNS::o1p_blocks_per_sm<2, false>();
+        default: return ::FV_KNS::o1p_blocks_per_sm<2, true>();
+    }
+}
+cudaError_t launch_o1_persistent(const O1Args& a, double4_32a* P, PersistCtl* pc, int nsteps, int grid,
+                                 cudaStream_t s) {
+    switch (a.flux * 2 + (a.local_dt ? 1 : 0)) {
+        case 0: return ::FV_KNS::launch_o1p<0, false>(a, P, pc, nsteps, grid, s);
+        case 1: return ::FV_KNS::launch_o1p<0, true>(a, P, pc, nsteps, grid, s);
+        case 2: return ::FV_KNS::launch_o1p<1, false>(a, P, pc, nsteps, grid, s);
+        case 3: return ::FV_KNS::launch_o1p<1, true>(a, P, pc, nsteps, grid, s);
+        case 4: return ::FV_KNS::launch_o1p<2, false>(a, P, pc, nsteps, grid, s);
+        default: return ::FV_KNS::launch_o1p<2, true>(a, P, pc, nsteps, grid, s);
+    }
+}
+}  // namespace FV_KNS
+}  // namespace fvgb
+#endif  // FV_DEFINE_O1_LAUNCH

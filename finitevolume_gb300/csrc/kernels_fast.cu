@@ -2,3 +2,4 @@
 #define FV_KNS fast
 #define FV_DEFINE_O1_LAUNCH
 #include "euler_o1.cuh"
+#include "euler_o1p.cuh"

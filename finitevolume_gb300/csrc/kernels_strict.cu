@@ -4,3 +4,4 @@
 #define FV_KNS strict
 #define FV_DEFINE_O1_LAUNCH
 #include "euler_o1.cuh"
+#include "euler_o1p.cuh"

@@ -11,13 +11,21 @@
 //               Jasak-corrected face gradients, Newtonian stress and Fourier
 //               heat flux; face_flux = length * (inviscid - viscous)
 //   cell pass   the Euler cell pass (gather, norms, U += dt/V R)
-// Built without FMA contraction, in the reference's evaluation order.
+// Built twice: without FMA contraction, in the reference's evaluation order
+// (this file), and with contraction (ns_fast.cu defines FV_NS_FAST and
+// includes it; kernel namespace nsk_fast, launchers suffixed _fast).
+#ifdef FV_NS_FAST
+#define FV_KNS nsk_fast
+#define FV_NS_FN(name) name##_fast
+#else
 #define FV_KNS nsk
+#define FV_NS_FN(name) name
+#endif
 #include "euler_o1.cuh"
 #include "gradients.cuh"
 #include "ns.h"
 
-namespace nsk {
+namespace FV_KNS {
 
 using fvgb::NSArgs;
 
@@ -171,28 +179,28 @@ __global__ void k_ns_wall(const NSArgs a, const int* __restrict__ faces, int n, 
     out[i] = make_double2(-(traction_x * tx + traction_y * ty), pressure(s, a.gamma));
 }
 
-}  // namespace nsk
+}  // namespace FV_KNS
 
 namespace fvgb {
 
-void ns_launch_step(const NSArgs& a, const O1Args& cell, cudaStream_t s) {
+void FV_NS_FN(ns_launch_step)(const NSArgs& a, const O1Args& cell, cudaStream_t s) {
     const int cb = (a.g.n_cells + kCellBlock - 1) / kCellBlock;
     const int fb = (a.g.n_faces + kFaceBlock - 1) / kFaceBlock;
-    nsk::k_ns_prim<<<cb, kCellBlock, 0, s>>>(a);
-    nsk::k_ns_grad<<<cb, kCellBlock, 0, s>>>(a);
+    FV_KNS::k_ns_prim<<<cb, kCellBlock, 0, s>>>(a);
+    FV_KNS::k_ns_grad<<<cb, kCellBlock, 0, s>>>(a);
     switch (a.flux) {
-        case 1: nsk::k_ns_face<1><<<fb, kFaceBlock, 0, s>>>(a); break;
-        case 2: nsk::k_ns_face<2><<<fb, kFaceBlock, 0, s>>>(a); break;
-        default: nsk::k_ns_face<0><<<fb, kFaceBlock, 0, s>>>(a); break;
+        case 1: FV_KNS::k_ns_face<1><<<fb, kFaceBlock, 0, s>>>(a); break;
+        case 2: FV_KNS::k_ns_face<2><<<fb, kFaceBlock, 0, s>>>(a); break;
+        default: FV_KNS::k_ns_face<0><<<fb, kFaceBlock, 0, s>>>(a); break;
     }
-    nsk::k_cell_o1<false><<<cb, kCellBlock, 0, s>>>(cell);
+    FV_KNS::k_cell_o1<false><<<cb, kCellBlock, 0, s>>>(cell);
 }
 
-void ns_launch_wall(const NSArgs& a, const int* faces, int n, double2* out, cudaStream_t s) {
+void FV_NS_FN(ns_launch_wall)(const NSArgs& a, const int* faces, int n, double2* out, cudaStream_t s) {
     const int cb = (a.g.n_cells + kCellBlock - 1) / kCellBlock;
-    nsk::k_ns_prim<<<cb, kCellBlock, 0, s>>>(a);
-    nsk::k_ns_grad<<<cb, kCellBlock, 0, s>>>(a);
-    if (n > 0) nsk::k_ns_wall<<<(n + 127) / 128, 128, 0, s>>>(a, faces, n, out);
+    FV_KNS::k_ns_prim<<<cb, kCellBlock, 0, s>>>(a);
+    FV_KNS::k_ns_grad<<<cb, kCellBlock, 0, s>>>(a);
+    if (n > 0) FV_KNS::k_ns_wall<<<(n + 127) / 128, 128, 0, s>>>(a, faces, n, out);
 }
 
 }  // namespace fvgb

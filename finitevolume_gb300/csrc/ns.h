@@ -21,7 +21,11 @@ struct NSArgs {
     int exact_max_iter, flux;
 };
 
+// Strict (no FMA contraction, reference evaluation order) and _fast
+// (contracted) builds of the same kernels.
 void ns_launch_step(const NSArgs& a, const O1Args& cell, cudaStream_t s);
 void ns_launch_wall(const NSArgs& a, const int* faces, int n, double2* out, cudaStream_t s);
+void ns_launch_step_fast(const NSArgs& a, const O1Args& cell, cudaStream_t s);
+void ns_launch_wall_fast(const NSArgs& a, const int* faces, int n, double2* out, cudaStream_t s);
 
 }  // namespace fvgb

@@ -16,13 +16,21 @@
 //                       nu-tilde diffusion (nu + nu_t) / sigma
 //   k_sa_cell           gather of both fluxes, volume x (production -
 //                       destruction + cross diffusion), five norms, update
-// Built without FMA contraction, in the reference's evaluation order.
+// Built twice: without FMA contraction, in the reference's evaluation order
+// (this file), and with contraction (rans_fast.cu defines FV_NS_FAST and
+// includes it; kernel namespace ransk_fast, launchers suffixed _fast).
+#ifdef FV_NS_FAST
+#define FV_KNS ransk_fast
+#define FV_NS_FN(name) name##_fast
+#else
 #define FV_KNS ransk
+#define FV_NS_FN(name) name
+#endif
 #include "euler_o1.cuh"
 #include "gradients.cuh"
 #include "rans.h"
 
-namespace ransk {
+namespace FV_KNS {
 
 using fvgb::RansArgs;
 
@@ -350,33 +358,35 @@ __global__ void k_sa_wall(const RansArgs a, const int* __restrict__ faces, int n
     out[i] = make_double2(-(traction_x * tx + traction_y * ty), pressure(s, a.ns.gamma));
 }
 
-}  // namespace ransk
+}  // namespace FV_KNS
 
 namespace fvgb {
 
+#ifndef FV_NS_FAST  // the wall distance is built once, in the strict unit
 void rans_wall_distance(const RansArgs& a, const double4_32a* seg, int n_seg, cudaStream_t s) {
     const int cb = (a.ns.g.n_cells + kCellBlock - 1) / kCellBlock;
-    ransk::k_sa_wall_distance<<<cb, kCellBlock, 0, s>>>(a, seg, n_seg);
+    FV_KNS::k_sa_wall_distance<<<cb, kCellBlock, 0, s>>>(a, seg, n_seg);
 }
+#endif
 
-void rans_launch_step(const RansArgs& a, cudaStream_t s) {
+void FV_NS_FN(rans_launch_step)(const RansArgs& a, cudaStream_t s) {
     const int cb = (a.ns.g.n_cells + kCellBlock - 1) / kCellBlock;
     const int fb = (a.ns.g.n_faces + kFaceBlock - 1) / kFaceBlock;
-    ransk::k_sa_prim<<<cb, kCellBlock, 0, s>>>(a);
-    ransk::k_sa_grad<<<cb, kCellBlock, 0, s>>>(a);
+    FV_KNS::k_sa_prim<<<cb, kCellBlock, 0, s>>>(a);
+    FV_KNS::k_sa_grad<<<cb, kCellBlock, 0, s>>>(a);
     switch (a.ns.flux) {
-        case 1: ransk::k_sa_face<1><<<fb, kFaceBlock, 0, s>>>(a); break;
-        case 2: ransk::k_sa_face<2><<<fb, kFaceBlock, 0, s>>>(a); break;
-        default: ransk::k_sa_face<0><<<fb, kFaceBlock, 0, s>>>(a); break;
+        case 1: FV_KNS::k_sa_face<1><<<fb, kFaceBlock, 0, s>>>(a); break;
+        case 2: FV_KNS::k_sa_face<2><<<fb, kFaceBlock, 0, s>>>(a); break;
+        default: FV_KNS::k_sa_face<0><<<fb, kFaceBlock, 0, s>>>(a); break;
     }
-    ransk::k_sa_cell<<<cb, kCellBlock, 0, s>>>(a);
+    FV_KNS::k_sa_cell<<<cb, kCellBlock, 0, s>>>(a);
 }
 
-void rans_launch_wall(const RansArgs& a, const int* faces, int n, double2* out, cudaStream_t s) {
+void FV_NS_FN(rans_launch_wall)(const RansArgs& a, const int* faces, int n, double2* out, cudaStream_t s) {
     const int cb = (a.ns.g.n_cells + kCellBlock - 1) / kCellBlock;
-    ransk::k_sa_prim<<<cb, kCellBlock, 0, s>>>(a);
-    ransk::k_sa_grad<<<cb, kCellBlock, 0, s>>>(a);
-    if (n > 0) ransk::k_sa_wall<<<(n + 127) / 128, 128, 0, s>>>(a, faces, n, out);
+    FV_KNS::k_sa_prim<<<cb, kCellBlock, 0, s>>>(a);
+    FV_KNS::k_sa_grad<<<cb, kCellBlock, 0, s>>>(a);
+    if (n > 0) FV_KNS::k_sa_wall<<<(n + 127) / 128, 128, 0, s>>>(a, faces, n, out);
 }
 
 }  // namespace fvgb

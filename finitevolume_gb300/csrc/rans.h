@@ -29,7 +29,10 @@ struct RansArgs {
 };
 
 void rans_wall_distance(const RansArgs& a, const double4_32a* seg, int n_seg, cudaStream_t s);
+// Strict and _fast (FMA-contracted) builds, as for the NS kernels.
 void rans_launch_step(const RansArgs& a, cudaStream_t s);
 void rans_launch_wall(const RansArgs& a, const int* faces, int n, double2* out, cudaStream_t s);
+void rans_launch_step_fast(const RansArgs& a, cudaStream_t s);
+void rans_launch_wall_fast(const RansArgs& a, const int* faces, int n, double2* out, cudaStream_t s);
 
 }  // namespace fvgb

@@ -172,6 +172,29 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     h2d_sync(ctl, &c0, sizeof(c0));
     ensure_history(64);
 
+    if (!general && !viscous) {
+        // Persistent first-order path: co-resident grid sized to the larger
+        // of the face tiles and the 256-cell tiles, capped at what fits.
+        int dev = 0, coop = 0, sms = 0;
+        FV_CUDA(cudaGetDevice(&dev));
+        FV_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        FV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int per_sm = opt.strict ? strict::o1p_max_blocks_per_sm(opt.flux, opt.dt_mode == FV_DT_LOCAL)
+                                      : fast::o1p_max_blocks_per_sm(opt.flux, opt.dt_mode == FV_DT_LOCAL);
+        const int want = std::max((F + kCellBlock - 1) / kCellBlock, (N + kCellBlock - 1) / kCellBlock);
+        p_grid = std::min(want, per_sm * sms);
+        persistent_ok = coop != 0 && p_grid > 0;
+        if (persistent_ok) {
+            Pc = dalloc<double4_32a>(N, owned);
+            pctl = dalloc<PersistCtl>(1, owned);
+            PersistCtl p0;
+            std::memset(&p0, 0, sizeof(p0));
+            p0.limit = kDefaultWaitCycles;
+            h2d_sync(pctl, &p0, sizeof(p0), stream);
+            persistent = true;
+        }
+    }
+
     if (general) {
         HostMesh h2 = hm;  // the per-entry geometry is derived on a copy
         h2.build_o2_geometry();
@@ -454,13 +477,15 @@ void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* ev
         if (events) FV_CUDA(cudaEventRecord((*events)[++*ev_pos], stream));
     };
     if (rans) {
-        rans_launch_step(rans_args(), stream);
+        if (opt.strict) rans_launch_step(rans_args(), stream);
+        else rans_launch_step_fast(rans_args(), stream);
         mark(1);
         return;
     }
     if (viscous) {
         // NS step: prim + gradients + face fluxes + cell pass, timed as one.
-        ns_launch_step(ns, o1_args(), stream);
+        if (opt.strict) ns_launch_step(ns, o1_args(), stream);
+        else ns_launch_step_fast(ns, o1_args(), stream);
         mark(1);
         return;
     }
@@ -487,11 +512,53 @@ void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* ev
     }
 }
 
+void Solver::launch_steps(int k, std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos) {
+    if (!persistent) {
+        for (int i = 0; i < k; ++i) launch_step(classes, events, ev_pos);
+        return;
+    }
+    // re-arm the barrier (arrival counter, error flag), then one launch
+    FV_CUDA(cudaMemsetAsync(pctl, 0, 2 * sizeof(int), stream));
+    const O1Args a = o1_args();
+    const cudaError_t rc = opt.strict ? strict::launch_o1_persistent(a, Pc, pctl, k, p_grid, stream)
+                                      : fast::launch_o1_persistent(a, Pc, pctl, k, p_grid, stream);
+    FV_CUDA(rc);
+    if (classes) classes->push_back(1);
+    if (events) FV_CUDA(cudaEventRecord((*events)[++*ev_pos], stream));
+}
+
+void Solver::set_persistent(bool on) {
+    if (on && !persistent_ok)
+        raise(FV_ERR_UNSUPPORTED, "the persistent kernel covers the first-order forward-Euler FP64 Euler path on a "
+                                  "device with cooperative launch");
+    FV_CUDA(cudaStreamSynchronize(stream));
+    persistent = on;
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+}
+
+void Solver::set_wait_limit(long long cycles, int phantom) {
+    if (!persistent_ok) raise(FV_ERR_UNSUPPORTED, "no persistent kernel on this solver");
+    if (cycles <= 0 || phantom < 0) raise(FV_ERR_BAD_ARG, "wait limit must be > 0 cycles, phantom arrivals >= 0");
+    FV_CUDA(cudaStreamSynchronize(stream));
+    h2d_sync(reinterpret_cast<char*>(pctl) + offsetof(PersistCtl, phantom), &phantom, sizeof(int), stream);
+    h2d_sync(reinterpret_cast<char*>(pctl) + offsetof(PersistCtl, limit), &cycles, sizeof(long long), stream);
+}
+
+void Solver::check_persistent() {
+    if (!persistent_ok) return;
+    int err = 0;
+    FV_CUDA(cudaMemcpyAsync(&err, reinterpret_cast<const char*>(pctl) + offsetof(PersistCtl, err), sizeof(int),
+                            cudaMemcpyDeviceToHost, stream));
+    FV_CUDA(cudaStreamSynchronize(stream));
+    if (err) raise(FV_ERR_TIMEOUT, "a grid barrier of the persistent kernel gave up waiting (the state is unspecified)");
+}
+
 void Solver::step_timed(int n, double ms[3], int launches[3]) {
     if (n <= 0) raise(FV_ERR_BAD_ARG, "step_timed needs n > 0");
     ensure_history(n);
     const int per_step = viscous ? 1 : (general ? cfg.stages * (cfg.order == 2 ? 3 : 2) + (batch ? 1 : 0) : 2);
-    const size_t need = (size_t)n * per_step + 1;
+    const size_t need = persistent ? 2 : (size_t)n * per_step + 1;
     while (events.size() < need) {
         cudaEvent_t e;
         FV_CUDA(cudaEventCreate(&e));
@@ -501,7 +568,7 @@ void Solver::step_timed(int n, double ms[3], int launches[3]) {
     classes.reserve(need);
     size_t pos = 0;
     FV_CUDA(cudaEventRecord(events[0], stream));
-    for (int i = 0; i < n; ++i) launch_step(&classes, &events, &pos);
+    launch_steps(n, &classes, &events, &pos);
     FV_CUDA(cudaGetLastError());
     FV_CUDA(cudaEventSynchronize(events[pos]));
     for (int k = 0; k < 3; ++k) { ms[k] = 0.0; launches[k] = 0; }
@@ -519,7 +586,7 @@ cudaGraphExec_t Solver::graph_for(int k) {
     if (it != graphs.end()) return it->second;
     cudaGraph_t g = nullptr;
     FV_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < k; ++i) launch_step(nullptr, nullptr, nullptr);
+    launch_steps(k, nullptr, nullptr, nullptr);
     FV_CUDA(cudaStreamEndCapture(stream, &g));
     cudaGraphExec_t ge = nullptr;
     FV_CUDA(cudaGraphInstantiate(&ge, g, 0));
@@ -542,7 +609,7 @@ void Solver::step_async(int n) {
         steps_taken += n;
         return;
     }
-    const int chunk = kGraphChunk;
+    const int chunk = persistent ? kPersistChunk : kGraphChunk;
     int q = n / chunk, r = n % chunk;
     if (q) {
         cudaGraphExec_t ge = graph_for(chunk);
@@ -751,8 +818,13 @@ void Solver::wall_forces(const double ref[7], double out[11], int instance) {
     std::vector<double> tau(nw, 0.0), pw(nw, 0.0);
     if (viscous) {
         std::vector<double2> tp(nw);
-        if (rans) rans_launch_wall(rans_args(), ns_wall_faces, (int)nw, ns_wall_out, stream);
-        else ns_launch_wall(ns, ns_wall_faces, (int)nw, ns_wall_out, stream);
+        if (rans) {
+            if (opt.strict) rans_launch_wall(rans_args(), ns_wall_faces, (int)nw, ns_wall_out, stream);
+            else rans_launch_wall_fast(rans_args(), ns_wall_faces, (int)nw, ns_wall_out, stream);
+        } else {
+            if (opt.strict) ns_launch_wall(ns, ns_wall_faces, (int)nw, ns_wall_out, stream);
+            else ns_launch_wall_fast(ns, ns_wall_faces, (int)nw, ns_wall_out, stream);
+        }
         FV_CUDA(cudaGetLastError());
         if (nw) FV_CUDA(cudaMemcpyAsync(tp.data(), ns_wall_out, sizeof(double2) * nw, cudaMemcpyDeviceToHost, stream));
         FV_CUDA(cudaStreamSynchronize(stream));
@@ -984,6 +1056,7 @@ int fv_step(fv_solver_t s, int32_t n, double* history) {
         s->s.step_async(n);
         fvgb::StepCtl c;
         s->s.read_ctl(c);
+        s->s.check_persistent();
         if (history && n > 0) s->s.history(n, history);
         if (c.nonfinite) fvgb::raise(FV_ERR_NONFINITE, "non-finite residual norm");
     });
@@ -998,6 +1071,7 @@ int fv_step_timed(fv_solver_t s, int32_t n, double kernel_ms[3], int32_t launche
         for (int k = 0; k < 3; ++k) launches[k] = l[k];
         fvgb::StepCtl c;
         s->s.read_ctl(c);
+        s->s.check_persistent();
         if (c.nonfinite) fvgb::raise(FV_ERR_NONFINITE, "non-finite residual norm");
     });
 }
@@ -1036,6 +1110,28 @@ int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]) {
     return guarded([&] {
         if (!s || !blocks) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
         s->s.set_launch(blocks[0], blocks[1], blocks[2]);
+    });
+}
+
+int fv_solver_set_persistent(fv_solver_t s, int32_t on) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        s->s.set_persistent(on != 0);
+    });
+}
+
+int fv_solver_persistent(fv_solver_t s, int32_t* on, int32_t* grid) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        if (on) *on = s->s.persistent ? 1 : 0;
+        if (grid) *grid = s->s.p_grid;
+    });
+}
+
+int fv_solver_set_wait_limit(fv_solver_t s, int64_t cycles, int32_t phantom_arrivals) {
+    return guarded([&] {
+        if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
+        s->s.set_wait_limit(cycles, phantom_arrivals);
     });
 }
 

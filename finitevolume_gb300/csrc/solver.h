@@ -106,6 +106,16 @@ struct Solver {
     void* psi_buf = nullptr;        // frozen limiter values [4N], flux precision
     int psi_mode = 0;               // 0 evaluated, 2 frozen (see O2Args)
 
+    // Persistent first-order path (order 1, forward Euler, FP64 Euler): one
+    // cooperative launch runs a chunk of steps (euler_o1p.cuh).
+    bool persistent = false;        // in use
+    bool persistent_ok = false;     // available (device and scheme)
+    int p_grid = 0;                 // co-resident blocks of the launch
+    PersistCtl* pctl = nullptr;
+    double4_32a* Pc = nullptr;      // per-cell primitives u, v, p, c
+    static constexpr int kPersistChunk = 256;
+    static constexpr long long kDefaultWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
+
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::map<int, cudaGraphExec_t> graphs;
@@ -120,6 +130,12 @@ struct Solver {
     O2Args o2_args() const;
     void refresh_primitives();
     void launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos);
+    // k steps: one persistent launch, or k x launch_step
+    void launch_steps(int k, std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos);
+    void set_persistent(bool on);
+    void set_wait_limit(long long cycles, int phantom);
+    // FV_ERR_TIMEOUT if a persistent launch gave up at a grid barrier
+    void check_persistent();
     void step_timed(int n, double ms[3], int launches[3]);
     cudaGraphExec_t graph_for(int k);
     void step_async(int n);

@@ -50,6 +50,20 @@ struct StepCtl {
     int pad;
 };
 
+// Control block of the persistent first-order kernel: its grid barrier
+// (arrival counter, generation, error flag), the bound on every wait in SM
+// clock cycles, and the two global-dt min slots (alternating by step).
+// `phantom` extra arrivals are waited for at every barrier; nothing ever
+// makes them, so a positive value exercises the timeout path.
+struct PersistCtl {
+    unsigned int count;
+    int err;
+    unsigned int gen;
+    int phantom;
+    long long limit;
+    unsigned long long dt_slot[2];
+};
+
 struct O1Args {
     DevMesh m;
     St* U;
@@ -154,5 +168,18 @@ void launch_batch_norms(const O2Args& a, int n_inst, const int* inst_off, double
 // part 0: face pass, 1: cell pass.
 namespace fast { void launch_o1_part(const O1Args& a, int part, cudaStream_t s); }
 namespace strict { void launch_o1_part(const O1Args& a, int part, cudaStream_t s); }
+// The persistent first-order kernel (cooperative launch of `grid` blocks of
+// kCellBlock threads running nsteps steps) and its co-resident block count
+// per SM; P holds the per-cell primitives.
+namespace fast {
+int o1p_max_blocks_per_sm(int flux, int local);
+cudaError_t launch_o1_persistent(const O1Args& a, double4_32a* P, PersistCtl* pc, int nsteps, int grid,
+                                 cudaStream_t s);
+}  // namespace fast
+namespace strict {
+int o1p_max_blocks_per_sm(int flux, int local);
+cudaError_t launch_o1_persistent(const O1Args& a, double4_32a* P, PersistCtl* pc, int nsteps, int grid,
+                                 cudaStream_t s);
+}  // namespace strict
 
 }  // namespace fvgb

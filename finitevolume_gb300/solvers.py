@@ -319,6 +319,45 @@ class EulerFVMSolver:
         step becomes one smoothing iteration plus one V-cycle."""
         capi.check(capi.lib().fv_solver_multigrid(self._h, self.mesh.handle, int(levels), int(smooth), float(relax)))
 
+    def newton(self, max_newton: int = 200, tol: float = 1e-11, limiter_mode: int = 0, **kw):
+        """Newton-Krylov steady solve from the current state (pseudo-transient
+        continuation, exact Jacobian-vector products, block-Jacobi
+        preconditioned GMRES).  ``limiter_mode`` 0 frozen / 1 full limiter
+        Jacobian; other keywords: cfl0, cfl_max, cfl_growth, krylov_dim,
+        krylov_rtol, precond_sweeps, precond_kind (1 multicolour symmetric
+        Gauss-Seidel, 0 block Jacobi), max_rel_change.  Returns (history
+        [(steps + 1) x 8]: four residual norms, CFL, GMRES iterations, GMRES
+        relative residual, step length; Newton steps taken)."""
+        o = capi.NewtonOpts()
+        capi.lib().fv_newton_default(C.byref(o))
+        o.max_newton, o.tol, o.limiter_mode = int(max_newton), float(tol), int(limiter_mode)
+        for k, v in kw.items():
+            if not hasattr(o, k):
+                raise TypeError(f"unknown Newton option {k}")
+            setattr(o, k, type(getattr(o, k))(v))
+        hist = np.zeros((int(max_newton) + 1, 8))
+        it = C.c_int32()
+        capi.check(capi.lib().fv_steady_newton(self._h, C.byref(o), capi.dptr(hist), C.byref(it)))
+        return hist[:it.value + 1], it.value
+
+    def set_persistent(self, on: bool = True) -> None:
+        """First-order forward-Euler FP64 path: one persistent cooperative
+        launch per chunk of steps (on, the default where supported) or two
+        kernels per step (off)."""
+        capi.check(capi.lib().fv_solver_set_persistent(self._h, 1 if on else 0))
+
+    def persistent(self):
+        """(in use, grid size in blocks) of the persistent kernel."""
+        on, grid = C.c_int32(), C.c_int32()
+        capi.check(capi.lib().fv_solver_persistent(self._h, C.byref(on), C.byref(grid)))
+        return bool(on.value), int(grid.value)
+
+    def set_wait_limit(self, cycles: int, phantom_arrivals: int = 0) -> None:
+        """Bound (SM clock cycles) on each grid-barrier wait of the persistent
+        kernel; phantom_arrivals > 0 makes every barrier wait for arrivals
+        that never come (checks the FV_ERR_TIMEOUT path)."""
+        capi.check(capi.lib().fv_solver_set_wait_limit(self._h, int(cycles), int(phantom_arrivals)))
+
     def freeze_limiter(self, on: bool = True) -> None:
         """Capture the limiter values at the current state and reuse them in
         every later step (on=False: evaluate the limiter again)."""
@@ -748,14 +787,16 @@ _NS_TO_ABI = {NSBoundaryType.NoSlipWall: 4, NSBoundaryType.Farfield: 1, NSBounda
 class NavierStokesFVMSolver(EulerFVMSolver):
     """GPU Navier-Stokes solver with the reference's constructor and methods
     (include/NavierStokesFVMSolver.h:118-218): the reference's first-order
-    scheme with the Jasak-corrected viscous flux."""
+    scheme with the Jasak-corrected viscous flux.  ``strict`` selects the
+    kernels built without FMA contraction in the reference's evaluation
+    order; the default build contracts multiply-adds."""
 
     def __init__(self, input_mesh: Mesh, boundary_conditions: Sequence[NSBoundaryCondition], gamma: float,
                  gas_constant: float, mu: float, prandtl: float, cfl: float,
                  initial_condition: EulerInitialCondition,
                  flux_scheme: NumericalFluxScheme = NumericalFluxScheme.Rusanov,
                  gradient_scheme: GradientScheme = GradientScheme.LeastSquares, exact_riemann_tol: float = 1e-6,
-                 exact_riemann_max_iter: int = 20):
+                 exact_riemann_max_iter: int = 20, strict: bool = False):
         arr = (capi.BC * max(1, len(boundary_conditions)))()
         for i, b in enumerate(boundary_conditions):
             arr[i].type = _NS_TO_ABI[NSBoundaryType(b.type)]
@@ -764,7 +805,8 @@ class NavierStokesFVMSolver(EulerFVMSolver):
             for k in range(4):
                 arr[i].state[k] = float(b.farfield_state[k])
         super().__init__(input_mesh, arr, gamma, cfl, initial_condition, flux_scheme, exact_riemann_tol,
-                         exact_riemann_max_iter, gradient=gradient_scheme, _viscous=(gas_constant, mu, prandtl))
+                         exact_riemann_max_iter, gradient=gradient_scheme, strict=strict,
+                         _viscous=(gas_constant, mu, prandtl))
 
 
 @dataclasses.dataclass
@@ -802,7 +844,7 @@ class RANSTurbulenceSASolver(EulerFVMSolver):
                  initial_condition: EulerInitialCondition, initial_nut: float,
                  flux_scheme: NumericalFluxScheme = NumericalFluxScheme.Rusanov,
                  gradient_scheme: GradientScheme = GradientScheme.LeastSquares, exact_riemann_tol: float = 1e-6,
-                 exact_riemann_max_iter: int = 20, sa_constants: SAModelConstants = None):
+                 exact_riemann_max_iter: int = 20, sa_constants: SAModelConstants = None, strict: bool = False):
         arr = (capi.BC * max(1, len(boundary_conditions)))()
         for i, rb in enumerate(boundary_conditions):
             b = rb.ns
@@ -814,7 +856,8 @@ class RANSTurbulenceSASolver(EulerFVMSolver):
             arr[i].nut = float(rb.farfield_nut)
         sa = (sa_constants or SAModelConstants()).as_list()
         super().__init__(input_mesh, arr, gamma, cfl, initial_condition, flux_scheme, exact_riemann_tol,
-                         exact_riemann_max_iter, gradient=gradient_scheme, _viscous=(gas_constant, mu, prandtl),
+                         exact_riemann_max_iter, gradient=gradient_scheme, strict=strict,
+                         _viscous=(gas_constant, mu, prandtl),
                          _rans={"prandtl_t": prandtl_t, "initial_nut": initial_nut, "sa": sa})
 
     def nut_field(self) -> np.ndarray:

@@ -219,6 +219,25 @@ int fv_get_history(fv_solver_t s, int32_t n, double* history);
  * restored afterwards.  No reference counterpart (the reference's loops are
  * OpenMP). */
 int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]);
+/* Persistent kernel of the first-order forward-Euler FP64 Euler path (the
+ * reference's own scheme, EulerFVMSolver::step / compute_dt,
+ * src/EulerFVMSolver.cpp:58-162): one cooperative launch runs a chunk of
+ * steps, meeting the flux -> update and global-dt dependencies at grid
+ * barriers instead of kernel boundaries; same results as the two-kernel
+ * path (bit for bit in strict mode).  On by default where the device
+ * supports cooperative launch; on = 0 selects the two-kernel path.
+ * fv_solver_persistent reports whether it is in use and its grid size
+ * (either pointer may be NULL).  No reference counterpart (the reference's
+ * loops are OpenMP). */
+int fv_solver_set_persistent(fv_solver_t s, int32_t on);
+int fv_solver_persistent(fv_solver_t s, int32_t* on, int32_t* grid);
+/* Bound on every grid-barrier wait of the persistent kernel, in SM clock
+ * cycles (default 2e9, about one second).  A wait that runs out makes the
+ * launch end early and fv_step / fv_step_timed return FV_ERR_TIMEOUT (the
+ * state is then unspecified).  phantom_arrivals > 0 makes every barrier wait
+ * for that many arrivals that never come: a check of the timeout path that
+ * faults and hangs nothing; set it back to 0 afterwards. */
+int fv_solver_set_wait_limit(fv_solver_t s, int64_t cycles, int32_t phantom_arrivals);
 /* Limiter freezing (second order with a limiter; a no-op otherwise): on=1
  * evaluates the limiter once at the current state and reuses those values
  * in every later step (the scheme becomes smooth, so steady solves that
@@ -370,6 +389,47 @@ int fv_adjoint_shape_gradient(fv_adjoint_t a, fv_mesh_t mesh, int32_t objective,
  * linearisation state (the residual's node sensitivities alone; the same
  * map the shape gradient applies to lambda). */
 int fv_residual_shape_vjp(fv_adjoint_t a, fv_mesh_t mesh, const double* Rbar, double* Xbar);
+/* ------------------------------------------------------------------------
+ * Newton-Krylov steady solves (no reference counterpart: the reference
+ * reaches steady states with its explicit loop only).  Drives the same
+ * discrete residual R(U) that EulerFVMSolver::step advances
+ * (src/EulerFVMSolver.cpp:58-112, with this library's MUSCL / limiter /
+ * characteristic-farfield extensions) to zero by pseudo-transient
+ * continuation: each step solves (V/dt - dR/dU) dU = R by GMRES with the
+ * adjoint's exact Jacobian-vector products, preconditioned on the
+ * first-order Jacobian (multicolour symmetric block Gauss-Seidel, or block
+ * Jacobi), then U += alpha dU with alpha <= 1 bounding the relative change
+ * of every cell's density and pressure.  The CFL number of V/dt starts at
+ * cfl0, grows by cfl_growth after each step that lowers the density
+ * residual (up to cfl_max), holds after a rise below 2x, halves after a
+ * larger one; a step that raises it more than 10x is undone and retried at
+ * a quarter of its CFL number.  FP64 Euler solvers with the Rusanov or HLLC
+ * flux (least-squares gradients at second order); not batched.
+ * --------------------------------------------------------------------- */
+typedef struct {
+    int32_t limiter_mode;   /* FV_ADJ_FROZEN_LIMITER or FV_ADJ_FULL_LIMITER: the limiter's
+                               treatment in the Jacobian (freeze the solver's limiter,
+                               fv_solver_freeze_limiter, for an exact Newton method)     */
+    int32_t max_newton;     /* Newton steps                                               */
+    double tol;             /* stop when the density residual L2 norm is below tol       */
+    double cfl0, cfl_max, cfl_growth;
+    int32_t krylov_dim;     /* GMRES(m), one cycle per Newton step (1..200)               */
+    double krylov_rtol;     /* relative GMRES tolerance                                   */
+    int32_t precond_sweeps; /* preconditioner sweeps                                      */
+    int32_t precond_kind;   /* 1 multicolour symmetric block Gauss-Seidel, 0 block Jacobi  */
+    double max_rel_change;  /* bound on the relative density / pressure change per step   */
+} fv_newton_t;
+/* Defaults: frozen-limiter Jacobian, 200 steps, tol 1e-11, CFL 10 growing
+ * x1.5 up to 1e6, GMRES(40) to 1e-2, 2 symmetric Gauss-Seidel sweeps, 20%
+ * change. */
+void fv_newton_default(fv_newton_t* opt);
+/* Runs from the solver's current state and leaves the result there.
+ * history (may be NULL) receives one row of 8 per evaluated state
+ * [iterations + 1 rows]: the four residual norms, then the CFL number, the
+ * GMRES iterations, its relative residual and the step length alpha of the
+ * step that produced it (zeros in row 0). */
+int fv_steady_newton(fv_solver_t s, const fv_newton_t* opt, double* history, int32_t* iterations);
+
 /* Wall-force coefficient J (objective 0 drag, 1 lift, 2 moment; pressure
  * part with the owner-cell pressure, ref as fv_wall_forces) at the
  * solver's current state, and dJ/dU (may be NULL). */

@@ -162,23 +162,15 @@ def cfl_ramp_fixture(tmp):
                         out=np.fromfile(out))
 
 
-def mesh_sha256(m) -> str:
-    """Digest of a mesh's arrays: pins a generator's output without storing it."""
-    import hashlib
-    h = hashlib.sha256()
-    for a in (m.nodes, m.cell_off, m.cell_nodes, m.bedges, m.bpatch):
-        h.update(np.ascontiguousarray(a).tobytes())
-    return h.hexdigest()
-
-
 def config1_fixture(tmp, steps=3000):
     """The small plain-method configuration at its own size, in the
     reference's mode: NACA0012 O-grid 256 x 128 (32,768 cells), first-order
     Rusanov, forward Euler with the global CFL time step at CFL 0.5, slip
     wall and fixed-state farfield, M 0.5, AoA 2 deg, 3,000 iterations.  The
-    mesh is regenerated by the tests (its digest is stored); the field, the
-    residual history and the inviscid wall forces (compute_wall_forces) are
-    the reference's."""
+    field, the residual history and the inviscid wall forces
+    (compute_wall_forces) are the reference's; the mesh arrays are stored
+    with them, since the generator's trigonometry differs in the last bits
+    between host maths libraries."""
     M, aoa = 0.5, np.radians(2.0)
     u, v, p = M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA
     og = meshgen.naca_ogrid(256, 128)
@@ -193,7 +185,7 @@ def config1_fixture(tmp, steps=3000):
     info = fvref("euler", path, out, flux="rusanov", cfl=case["cfl"], ic=case["ic"], bc=case["bc"], steps=steps,
                  gamma=GAMMA, ref_rho=ref[0], ref_u=ref[1], ref_v=ref[2], ref_p=ref[3], ref_len=ref[4],
                  ref_mx=ref[5], ref_my=ref[6])
-    np.savez_compressed(os.path.join(HERE, "config1_og256_ref.npz"), mesh_sha256=np.array(mesh_sha256(og)),
+    np.savez_compressed(os.path.join(HERE, "config1_og256_ref.npz"), **mesh_arrays(og),
                         field=np.fromfile(os.path.join(out, "field.f64")).reshape(-1, 4),
                         hist=np.fromfile(os.path.join(out, "resid.f64")).reshape(-1, 4),
                         forces=np.fromfile(os.path.join(out, "forces.f64")).reshape(-1, 11),
@@ -201,10 +193,51 @@ def config1_fixture(tmp, steps=3000):
     return info
 
 
+def adjoint_fd_fixture(tmp, steps=80000, h_mach=1e-4, h_aoa_deg=1e-3):
+    """Drag and lift of the reference's own EulerFVMSolver converged to its
+    round-off floor at a freestream and at the four central-difference
+    neighbours in Mach number and angle of attack: NACA0012 O-grid 64 x 32
+    (first spacing 1e-2, farfield at 10 chords), first order, forward Euler,
+    global dt at CFL 0.9, slip wall and fixed-state farfield, M 0.5, AoA 2
+    deg, Rusanov and HLLC, 80,000 iterations each.  Forces by
+    compute_wall_forces with zero viscosity, the freestream as the force
+    reference.  The central differences of these drags are the
+    reference-solver derivatives the discrete adjoint is checked against."""
+    og = meshgen.naca_ogrid(64, 32, first=1e-2, r_far=10.0)
+    path = os.path.join(tmp, "og64c.fvmesh")
+    fvmesh.write_fvmesh(og, path)
+    M0, a0 = 0.5, 2.0
+    points = [(M0, a0), (M0 + h_mach, a0), (M0 - h_mach, a0), (M0, a0 + h_aoa_deg), (M0, a0 - h_aoa_deg)]
+    res = {}
+    for flux in ("rusanov", "hllc"):
+        rows, last = [], []
+        for (M, ad) in points:
+            a = np.radians(ad)
+            u, v, p = M * np.cos(a), M * np.sin(a), 1.0 / GAMMA
+            out = os.path.join(tmp, f"adj_{flux}_{M}_{ad}")
+            os.makedirs(out, exist_ok=True)
+            fvref("euler", path, out, flux=flux, cfl=0.9, ic="free:" + prim_str(1.0, u, v, p),
+                  bc=["airfoil:wall", "farfield:farfield:" + prim_str(1.0, u, v, p)], steps=steps, gamma=GAMMA,
+                  ref_rho=1.0, ref_u=u, ref_v=v, ref_p=p, ref_len=1.0, ref_mx=0.25, ref_my=0.0)
+            f = np.fromfile(os.path.join(out, "forces.f64")).reshape(-1, 11)
+            tot = f[f[:, 0] == -1][0]
+            rows.append([M, ad, tot[8], tot[9]])  # cd_total, cl
+            last.append(np.fromfile(os.path.join(out, "resid.f64")).reshape(-1, 4)[-1])
+            if M == M0 and ad == a0:
+                res[f"field_{flux}"] = np.fromfile(os.path.join(out, "field.f64")).reshape(-1, 4)
+        res[f"points_{flux}"] = np.array(rows)
+        res[f"final_resid_{flux}"] = np.array(last)
+    case = {"mach": M0, "aoa_deg": a0, "h_mach": h_mach, "h_aoa_deg": h_aoa_deg, "cfl": 0.9, "steps": steps,
+            "mesh": "naca_ogrid(64, 32, first=1e-2, r_far=10)", "bc": ["airfoil:wall", "farfield:farfield"],
+            "columns": ["mach", "aoa_deg", "cd_total", "cl"]}
+    np.savez_compressed(os.path.join(HERE, "adjoint_fd_ref.npz"), **mesh_arrays(og), **res,
+                        case=np.array(json.dumps(case)))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=build.reference_dir())
-    ap.add_argument("--only", choices=["rans", "cfl", "config1"], default=None,
+    ap.add_argument("--only", choices=["rans", "cfl", "config1", "adjoint"], default=None,
                     help="regenerate one group of fixtures")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
@@ -220,10 +253,15 @@ def main():
         with tempfile.TemporaryDirectory() as tmp:
             print(config1_fixture(tmp))
         return
+    if a.only == "adjoint":
+        with tempfile.TemporaryDirectory() as tmp:
+            adjoint_fd_fixture(tmp)
+        return
     with tempfile.TemporaryDirectory() as tmp:
         rans_fixtures(tmp)
         cfl_ramp_fixture(tmp)
         config1_fixture(tmp)
+        adjoint_fd_fixture(tmp)
         # NACA0012 O-grid, M=0.5, AoA=2 deg, slip wall + fixed farfield.
         M, aoa = 0.5, np.radians(2.0)
         u, v, p = M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA

@@ -7,26 +7,20 @@ NACA0012 O-grid of 256 x 128 quads (32,768 cells), first-order Rusanov,
 forward Euler with the global CFL time step at CFL 0.5, slip wall and
 fixed-state farfield, M 0.5, AoA 2 deg, after 3,000 iterations: the field,
 the 3,000 x 4 residual history and the inviscid wall forces of
-compute_wall_forces (src/WallTraction.cpp:163-217).  The mesh itself is not
-stored: the generator's output is pinned by its digest.
+compute_wall_forces (src/WallTraction.cpp:163-217).  The fixture carries the
+mesh it was made on (meshgen.naca_ogrid(256, 128) on the host that made it).
 """
-import hashlib
-
 import numpy as np
 
-from finitevolume_gb300 import meshgen
-from helpers import case_of, load_golden, parse_bcs, parse_ic, FLUX_ID, GAMMA
+from helpers import case_of, load_golden, parse_bcs, parse_ic, poly_of, FLUX_ID, GAMMA
 from oracle import port
 
 TOL = 1e-10
 
 
 def config1_mesh(g):
-    poly = meshgen.naca_ogrid(256, 128)
-    h = hashlib.sha256()
-    for a in (poly.nodes, poly.cell_off, poly.cell_nodes, poly.bedges, poly.bpatch):
-        h.update(np.ascontiguousarray(a).tobytes())
-    assert h.hexdigest() == str(g["mesh_sha256"]), "the O-grid generator no longer makes the fixture's mesh"
+    poly = poly_of(g)
+    assert poly.n_cells == 256 * 128
     return poly
 
 

@@ -3,8 +3,9 @@
 The fixtures hold the reference's fields, residual histories and wall
 forces for a no-slip NACA0012 O-grid and a channel with an isothermal
 moving wall, for Rusanov/HLLC fluxes and LSQ/Green-Gauss viscous gradients.
-The NS kernels keep the reference's evaluation order without FMA
-contraction; fields, norms and forces agree within 1e-10 relative.
+Both builds of the NS kernels are checked: the strict one (the reference's
+evaluation order without FMA contraction) and the default FMA-contracted
+one; fields, norms and forces agree within 1e-10 relative.
 """
 import numpy as np
 import pytest
@@ -48,14 +49,15 @@ CASES = [("ns_naca_og64", "rusanov", "lsq"), ("ns_naca_og64", "rusanov", "gg"), 
          ("ns_naca_og64", "hllc", "gg"), ("ns_channel_tri", "rusanov", "lsq"), ("ns_channel_tri", "rusanov", "gg")]
 
 
+@pytest.mark.parametrize("strict", [True, False])
 @pytest.mark.parametrize("name,flux,grad", CASES)
-def test_ns_vs_reference(gpu, name, flux, grad):
+def test_ns_vs_reference(gpu, name, flux, grad, strict):
     g = load_golden(name)
     case = case_of(g)
     poly = poly_of(g)
     tag = f"{flux}_{grad}"
     s = S.NavierStokesFVMSolver(S.Mesh(poly), _bcs(case["bc"], poly.patch_names), GAMMA, case["R"], case["mu"],
-                                case["Pr"], case["cfl"], _ic(case["ic"]), FLUX[flux], GRAD[grad])
+                                case["Pr"], case["cfl"], _ic(case["ic"]), FLUX[flux], GRAD[grad], strict=strict)
     hist = s.run(case["steps"], history=True)
     U = s.field()
     # Within 1e-10 relative: the face geometry of the viscous flux goes through

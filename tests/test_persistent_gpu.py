@@ -1,0 +1,76 @@
+"""The persistent first-order kernel (one cooperative launch per chunk of
+steps, grid barriers between the face and cell phases) against the
+two-kernel path, and its bounded barrier waits.
+
+- Same fields and residual histories bit for bit as the two-kernel path in
+  strict mode (Rusanov and HLLC, global dt with the fixed farfield, local dt
+  with the characteristic farfield), and within 1e-12 in the default build.
+- A barrier that waits for an arrival that never comes gives up after its
+  cycle limit: fv_step returns FV_ERR_TIMEOUT, nothing hangs, the state is
+  untouched (the first barrier precedes every update) and the solver steps
+  normally once the limit is restored.
+
+Reference: src/EulerFVMSolver.cpp:58-162 (step, compute_dt).
+"""
+import numpy as np
+import pytest
+
+from finitevolume_gb300 import capi, meshgen, solvers as S
+from helpers import gpu_solver, rel_err, GAMMA
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(local):
+    M, aoa = 0.5, np.radians(2.0)
+    r, u, v, p = 1.0, M * np.cos(aoa), M * np.sin(aoa), 1.0 / GAMMA
+    st = list(S.from_primitive(r, u, v, p, GAMMA))
+    bcs = [(0, [0.0] * 4), (3 if local else 1, st)]
+    return bcs, {"mode": "free", "rho": r, "u": u, "v": v, "p": p}
+
+
+@pytest.mark.parametrize("flux", ["rusanov", "hllc"])
+@pytest.mark.parametrize("local", [False, True])
+@pytest.mark.parametrize("strict", [True, False])
+def test_persistent_matches_two_kernel_path(gpu, flux, local, strict):
+    poly = meshgen.naca_ogrid(128, 64)
+    bcs, ic = _case(local)
+    a = gpu_solver(poly, bcs, ic, flux, cfl=0.5, local_dt=local, strict=strict)
+    b = gpu_solver(poly, bcs, ic, flux, cfl=0.5, local_dt=local, strict=strict)
+    on, grid = a.persistent()
+    assert on and grid > 0
+    b.set_persistent(False)
+    assert not b.persistent()[0]
+    ha = a.run(300, history=True)
+    hb = b.run(300, history=True)
+    if strict:
+        assert np.array_equal(a.field(), b.field())
+        assert np.array_equal(ha, hb)
+    else:
+        assert rel_err(a.field(), b.field()) <= 1e-12
+        np.testing.assert_allclose(ha, hb, rtol=1e-12, atol=0)
+    # chunk boundaries (256 steps per launch) are invisible: 300 = 256 + 44
+    c = gpu_solver(poly, bcs, ic, flux, cfl=0.5, local_dt=local, strict=strict)
+    for _ in range(3):
+        c.run(100)
+    assert np.array_equal(c.field(), a.field())
+
+
+def test_barrier_wait_runs_out_and_reports_timeout(gpu):
+    poly = meshgen.naca_ogrid(64, 32)
+    bcs, ic = _case(False)
+    s = gpu_solver(poly, bcs, ic, "rusanov", cfl=0.5)
+    s.run(5)
+    before = s.field()
+    # every barrier now waits for one more block than the grid has
+    s.set_wait_limit(2_000_000, phantom_arrivals=1)
+    with pytest.raises(capi.FVError) as ei:
+        s.run(1)
+    assert ei.value.status == capi.FV_ERR_TIMEOUT
+    assert np.array_equal(s.field(), before)
+    # restored: steps again, same as a solver that never timed out
+    s.set_wait_limit(2_000_000_000, phantom_arrivals=0)
+    s.run(3)
+    ref = gpu_solver(poly, bcs, ic, "rusanov", cfl=0.5)
+    ref.run(8)
+    assert np.array_equal(s.field(), ref.field())

@@ -52,12 +52,12 @@ def _ic(spec):
     return S.EulerInitialCondition(S.EulerICMode.Freestream, rho=r, u=u, v=v, p=p)
 
 
-def _solver(g, flux, grad):
+def _solver(g, flux, grad, strict=False):
     case = case_of(g)
     poly = poly_of(g)
     return S.RANSTurbulenceSASolver(S.Mesh(poly), _bcs(case["bc"], poly.patch_names), GAMMA, case["R"], case["mu"],
                                     case["Pr"], case["Prt"], case["cfl"], _ic(case["ic"]), case["nut0"], FLUX[flux],
-                                    GRAD[grad]), case
+                                    GRAD[grad], strict=strict), case
 
 
 CASES = [("rans_naca_og64", "rusanov", "lsq"), ("rans_naca_og64", "rusanov", "gg"),
@@ -65,10 +65,13 @@ CASES = [("rans_naca_og64", "rusanov", "lsq"), ("rans_naca_og64", "rusanov", "gg
          ("rans_channel_tri", "rusanov", "lsq"), ("rans_channel_tri", "rusanov", "gg")]
 
 
+@pytest.mark.parametrize("strict", [True, False])
 @pytest.mark.parametrize("name,flux,grad", CASES)
-def test_rans_sa_vs_reference(gpu, name, flux, grad):
+def test_rans_sa_vs_reference(gpu, name, flux, grad, strict):
+    """Strict (reference evaluation order, no FMA) and default (contracted)
+    kernel builds."""
     g = load_golden(name)
-    s, case = _solver(g, flux, grad)
+    s, case = _solver(g, flux, grad, strict)
     tag = f"{flux}_{grad}"
     assert np.array_equal(s.wall_distance(), g["walld"])
     nut_hist = []
