@@ -926,6 +926,7 @@ def main():
         ach_inst = inst * n_cells / (per_launch_ms / 1e3) / 1e9
         roof["fp64_pipe"] = {"inst_per_cell_ncu": inst, "achieved_ginst_s": round(ach_inst, 1),
                              "peak_ginst_s": FP64_PIPE_GINST_S, "frac": round(ach_inst / FP64_PIPE_GINST_S, 4)}
+        roof["fp64_pipe_frac"] = roof["fp64_pipe"]["frac"]
 
     # End to end through the public API with host buffers: every step
     # uploads the state from pinned host memory (set_field), advances one

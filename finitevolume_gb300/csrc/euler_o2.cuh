@@ -484,6 +484,16 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
                 if (yb <= 0) continue;                       // no face with D2 of this sign
                 const T y = OK::from_bits(yb);               // |D2| extreme, > 0
                 const T d1 = side == 0 ? dmax[k] : -dmin[k];  // |D1| >= 0
+                // phi(d1, y) < 1 only where d1 < 2y (Venkatakrishnan: the
+                // eps^2 terms cancel in num < den) or d1 < y (Barth-
+                // Jespersen); for d1 >= 0 and y > 0 that compare is an
+                // integer compare of the bit patterns, so a side that cannot
+                // limit costs no FP64 instruction.
+                {
+                    using U = typename std::make_unsigned<I>::type;
+                    const I bound = LIM == 1 ? yb : (I)((U)yb + (U)OK::one_exp());
+                    if (!(OK::bits(d1) < bound)) continue;
+                }
                 T num, den;
                 if (LIM == 1) {
                     num = d1;

@@ -4,7 +4,8 @@ two-kernel path, and its bounded barrier waits.
 
 - Same fields and residual histories bit for bit as the two-kernel path in
   strict mode (Rusanov and HLLC, global dt with the fixed farfield, local dt
-  with the characteristic farfield), and within 1e-12 in the default build.
+  with the characteristic farfield), and within 1e-10 in the default build
+  (which forms 1/rho and the local-dt factor with fewer FP64 instructions).
 - A barrier that waits for an arrival that never comes gives up after its
   cycle limit: fv_step returns FV_ERR_TIMEOUT, nothing hangs, the state is
   untouched (the first barrier precedes every update) and the solver steps
@@ -47,8 +48,8 @@ def test_persistent_matches_two_kernel_path(gpu, flux, local, strict):
         assert np.array_equal(a.field(), b.field())
         assert np.array_equal(ha, hb)
     else:
-        assert rel_err(a.field(), b.field()) <= 1e-12
-        np.testing.assert_allclose(ha, hb, rtol=1e-12, atol=0)
+        assert rel_err(a.field(), b.field()) <= 1e-10
+        np.testing.assert_allclose(ha, hb, rtol=1e-10, atol=0)
     # chunk boundaries (256 steps per launch) are invisible: 300 = 256 + 44
     c = gpu_solver(poly, bcs, ic, flux, cfl=0.5, local_dt=local, strict=strict)
     for _ in range(3):
