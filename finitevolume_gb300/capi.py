@@ -111,7 +111,9 @@ SIGNATURES = {
     "fv_solver_persistent": (C.c_int, [_P, _I32, _I32]),
     "fv_solver_set_wait_limit": (C.c_int, [_P, C.c_int64, C.c_int32]),
     "fv_newton_default": (None, [C.POINTER(NewtonOpts)]),
-    "fv_steady_newton": (C.c_int, [_P, C.POINTER(NewtonOpts), _D, _I32]),
+    "fv_steady_newton": (C.c_int, [_P, C.POINTER(NewtonOpts), _D, _I32, _I32]),
+    "fv_adjoint_solve_krylov": (C.c_int, [_P, _D, C.c_double, C.c_int32, C.c_int32, C.c_double, C.c_int32, _D, _D,
+                                          _D, _I32, _D]),
     "fv_solver_limiter_values": (C.c_int, [_P, _D, _D]),
     "fv_solver_update_nodes": (C.c_int, [_P, _P, _D]),
     "fv_solver_multigrid": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_double]),

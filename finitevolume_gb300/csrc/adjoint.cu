@@ -145,6 +145,11 @@ __device__ __forceinline__ V4<double> ldW(const St* W, int i) {
     return {s.r, s.ru, s.rv, s.E};
 }
 __device__ __forceinline__ double vget(const V4<double>& w, int k) { return (&w.r)[k]; }
+// Conserved freestream of boundary face f's farfield: the patch's, or (batched
+// solvers) the owner cell's instance's.
+__device__ __forceinline__ const double* fs_of(const AdjArgs& a, int patch, int f) {
+    return a.inst_fs ? a.inst_fs + 4 * a.cell_inst[a.fl[f]] : a.bc.st[patch];
+}
 template <int N> __device__ __forceinline__ Dual<N> dget(const V4<Dual<N>>& w, int k) { return (&w.r)[k]; }
 
 template <typename T>
@@ -228,7 +233,7 @@ __global__ void k_lin_face(const AdjArgs a) {
         const int patch = a.fpatch[f];
         const int t = a.bc.type[patch];
         V4<double> fsp = {0, 0, 0, 0};
-        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(fs_of(a, patch, f), g);
         const D4 wu(t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0), wv(t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0);
         const V4<D4> wlD = seed(wl);
         F1 = flux_of<D4>(a.flux, wlD, ghost_core<D4>(t, wlD, nxD, nyD, gD, cst(fsp), wu, wv), nxD, nyD, gD, iD);
@@ -279,7 +284,7 @@ __global__ void k_lin_lim(const AdjArgs a) {
                 const int patch = a.fpatch[f];
                 const int t = a.bc.type[patch];
                 V4<double> fsp = {0, 0, 0, 0};
-                if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+                if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(fs_of(a, patch, f), g);
                 const double wu = t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0;
                 const double wv = t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0;
                 const V4<double> gh = ghost_core<double>(t, wc, geo.x, geo.y, g, fsp, wu, wv);
@@ -760,7 +765,7 @@ __global__ void k_geo_face(const AdjArgs a, const St* __restrict__ lam, double* 
         const int patch = a.fpatch[f];
         const int t = a.bc.type[patch];
         V4<double> fsp = {0, 0, 0, 0};
-        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(fs_of(a, patch, f), g);
         const D4 wu(t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0), wv(t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0);
         Fl = flux_of<D4>(a.flux, cst(wl), ghost_core<D4>(t, cst(wl), nxD, nyD, gD, cst(fsp), wu, wv), nxD, nyD, gD,
                          iD);
@@ -828,7 +833,7 @@ __global__ void k_geo_cell(const AdjArgs a, double* __restrict__ abar, double* _
             const int patch = a.fpatch[f];
             const int t = a.bc.type[patch];
             V4<double> fsp = {0, 0, 0, 0};
-            if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+            if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(fs_of(a, patch, f), g);
             const D4 wu(t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0), wv(t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0);
             D4 nxD(geo.x), nyD(geo.y);
             nxD.d[0] = 1.0;
@@ -903,7 +908,7 @@ __global__ void k_geo_lim(const AdjArgs a, double* __restrict__ erb, double* __r
         const int patch = a.fpatch[f];
         const int t = a.bc.type[patch];
         V4<double> fsp = {0, 0, 0, 0};
-        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(a.bc.st[patch], g);
+        if (t == BC_FARFIELD || t == BC_CHAR) fsp = fs_prim<double>(fs_of(a, patch, f), g);
         const D4 wu(t == BC_NOSLIP ? a.bc.wall_u[patch] : 0.0), wv(t == BC_NOSLIP ? a.bc.wall_v[patch] : 0.0);
         D4 nxD(geo.x), nyD(geo.y);
         nxD.d[0] = 1.0;
@@ -1350,17 +1355,20 @@ void jvp_dev(fv_adjoint_s* A, const St* dU, St* dR) {
     adjk::k_fwd_cell3<<<blocks(A->N), kB, 0, s.stream>>>(A->a, dR);
     check_launch();
 }
+void vjp_dev(fv_adjoint_s* A, const St* lam, St* out) { backward(A, lam, 0, out); }
+void upload(fv_adjoint_s* A, const double* host_ref, St* dev) { upload_ref(A, host_ref, dev); }
+void download(fv_adjoint_s* A, const St* dev, double* host_ref) { download_ref(A, dev, host_ref); }
+void fsbar(fv_adjoint_s* A, double* out) { reduce_fsbar(A, out); }
 }  // namespace adjh
 
-extern "C" {
-
-int fv_adjoint_create(fv_solver_t solver, int32_t limiter_mode, fv_adjoint_t* out) {
-    return fvgb::guarded([&] {
+void adjh::create(fv_solver_t solver, int limiter_mode, bool allow_batch, fv_adjoint_t* out) {
+    {
         if (!solver || !out) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
         if (limiter_mode != FV_ADJ_FROZEN_LIMITER && limiter_mode != FV_ADJ_FULL_LIMITER)
             fvgb::raise(FV_ERR_BAD_ARG, "limiter_mode: FV_ADJ_FROZEN_LIMITER or FV_ADJ_FULL_LIMITER");
         fvgb::Solver& s = solver->s;
-        if (s.viscous || s.batch) fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: Euler solvers only (not NS, not batched)");
+        if (s.viscous || (s.batch && !allow_batch))
+            fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: Euler solvers only (not NS, not batched)");
         if (s.opt.precision != FV_PREC_FP64) fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: FP64 solvers only");
         if (s.opt.flux != FV_FLUX_RUSANOV && s.opt.flux != FV_FLUX_HLLC)
             fvgb::raise(FV_ERR_UNSUPPORTED, "adjoint: Rusanov or HLLC flux");
@@ -1459,8 +1467,18 @@ int fv_adjoint_create(fv_solver_t solver, int32_t limiter_mode, fv_adjoint_t* ou
             fvgb::h2d_sync(d_twin, twin.data(), sizeof(int) * E, s.stream);
             a.twin = d_twin;
         }
+        if (s.batch) {
+            a.cell_inst = s.cell_inst;
+            a.inst_fs = s.inst_fs;
+        }
         *out = A.release();
-    });
+    }
+}
+
+extern "C" {
+
+int fv_adjoint_create(fv_solver_t solver, int32_t limiter_mode, fv_adjoint_t* out) {
+    return fvgb::guarded([&] { adjh::create(solver, limiter_mode, false, out); });
 }
 
 int fv_adjoint_destroy(fv_adjoint_t adj) {

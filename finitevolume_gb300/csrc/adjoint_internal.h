@@ -61,6 +61,10 @@ struct AdjArgs {
     double2* lpd;        // [4N] (dpsi/dd1, dpsi/dy)
     double* lpe;         // [4N] dpsi/d eps^2 (Venkatakrishnan; 0 otherwise)
     double* ldb;         // [4N] cotangent of d1 passed to the extreme neighbour
+    // batched solvers (Newton only; null otherwise): instance of each cell
+    // and each instance's conserved freestream, used by the farfield ghosts
+    const int* cell_inst;
+    const double* inst_fs;
 };
 
 }  // namespace adjk
@@ -100,6 +104,10 @@ struct fv_adjoint_s {
 };
 
 namespace adjh {
+// fv_adjoint_create, also for batched solvers when allow_batch (the
+// farfield ghosts then take each instance's own freestream; the freestream
+// tangents and cotangents of the adjoint pair are not defined there).
+void create(fv_solver_t solver, int limiter_mode, bool allow_batch, fv_adjoint_t* out);
 // Linearise at A->U (flux Jacobians, limiter values, residual fluxes and
 // the local dt at the solver's CFL number).
 void linearise(fv_adjoint_s* A);
@@ -110,4 +118,12 @@ void residual_dev(fv_adjoint_s* A, fvgb::St* R);
 // dR = (dR/dU) dU at the linearisation state (freestream held fixed),
 // device order in and out.
 void jvp_dev(fv_adjoint_s* A, const fvgb::St* dU, fvgb::St* dR);
+// out = (dR/dU)^T lam at the linearisation state, device order; also
+// leaves the per-boundary-face freestream cotangents for fsbar().
+void vjp_dev(fv_adjoint_s* A, const fvgb::St* lam, fvgb::St* out);
+// reference-order host array <-> device-order state
+void upload(fv_adjoint_s* A, const double* host_ref, fvgb::St* dev);
+void download(fv_adjoint_s* A, const fvgb::St* dev, double* host_ref);
+// (dR/dfs)^T lam per patch [4 n_patches] after vjp_dev(lam)
+void fsbar(fv_adjoint_s* A, double* out);
 }  // namespace adjh

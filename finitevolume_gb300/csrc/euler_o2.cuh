@@ -359,9 +359,9 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
     // Batched solves: converged instances are frozen; each instance has
     // its own freestream.
     const double* fs = nullptr;
-    if (a.active) {
+    if (a.cell_inst) {
         const int inst = a.cell_inst[c];
-        if (!a.active[inst]) return;
+        if (a.active && !a.active[inst]) return;
         fs = a.inst_fs + 4 * inst;
     }
     const WT* W = static_cast<const WT*>(a.W);
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_face(const O2Args a) {
         const WT* W = static_cast<const WT*>(a.W);
         const T g = pick<T>(a.gamma, a.gamma32), igm1 = pick<T>(a.igm1, a.igm1_32);
         const int L = a.m.fl[f], R = a.m.fr[f];
-        const double* fs = a.active ? a.inst_fs + 4 * a.cell_inst[L] : nullptr;
+        const double* fs = a.cell_inst ? a.inst_fs + 4 * a.cell_inst[L] : nullptr;
         T nx, ny, ar, len;
         face_geom<T>(a, f, nx, ny, ar, len);
         V4<T> wl = WS::ld(W, L), wr;

@@ -30,6 +30,11 @@
 // A step whose residual comes out more than ten times larger than the one
 // before is undone and retried with the CFL number divided by four.
 //
+// Batched solvers are solved as one block-diagonal system: every instance
+// (a contiguous cell range) has its own residual norms, CFL number, step
+// length and accept / undo decision, and leaves the iteration once its
+// density residual is below the tolerance; a single solver is one instance.
+//
 // Every reduction is a fixed-grid block sum folded in block order, so runs
 // are bit reproducible.
 #include <algorithm>
@@ -213,6 +218,65 @@ __global__ void k_gs_colour(const adjk::AdjArgs a, const double* __restrict__ Di
     st_state(z, c, st_make(o[0], o[1], o[2], o[3]));
 }
 
+// One colour of a block Gauss-Seidel sweep of the transposed matrix, in
+// place: z_c = Dinv_c^T (r_c - sum_nb (P^T)_c,nb z_nb) with
+// (P^T)_c,nb = P_nb,c^T = -M_c^T J_L^T (c owns the face) or M_c^T J_R^T (c
+// is its neighbour).
+__global__ void k_gs_colour_t(const adjk::AdjArgs a, const double* __restrict__ Dinv, const St* __restrict__ r,
+                              St* __restrict__ z, const int* __restrict__ cells, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cells[i];
+    double q[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int ent = a.cf[e];
+        const int f = ent >> 1;
+        const int L = a.fl[f], R = a.fr[f];
+        if (R < 0) continue;
+        const bool own = ent & 1;
+        const int nb = own ? R : L;
+        const double* J = own ? a.JL + 16 * (size_t)f : a.JR + 16 * (size_t)f;
+        const double sg = own ? 1.0 : -1.0;
+        const St zz = ld_state(z, nb);
+        const double x[4] = {zz.r, zz.ru, zz.rv, zz.E};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) q[k] += sg * (J[k] * x[0] + J[4 + k] * x[1] + J[8 + k] * x[2] + J[12 + k] * x[3]);
+    }
+    double M[16];
+    prim_jac(ld_state(a.W, c), a.gamma, M);
+    const St rc = ld_state(r, c);
+    double t[4] = {rc.r, rc.ru, rc.rv, rc.E};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) t[k] += M[k] * q[0] + M[4 + k] * q[1] + M[8 + k] * q[2] + M[12 + k] * q[3];
+    const double* X = Dinv + 16 * (size_t)c;
+    double o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[k] = X[k] * t[0] + X[4 + k] * t[1] + X[8 + k] * t[2] + X[12 + k] * t[3];
+    st_state(z, c, st_make(o[0], o[1], o[2], o[3]));
+}
+
+// out = -x
+__global__ void k_neg(St* __restrict__ out, const St* __restrict__ x, int n) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const St a = ld_state(x, c);
+    st_state(out, c, st_make(-a.r, -a.ru, -a.rv, -a.E));
+}
+
+// x += y
+__global__ void k_axpy_state(St* __restrict__ x, const St* __restrict__ y, int n) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    st_state(x, c, ld_state(x, c) + ld_state(y, c));
+}
+
+// out = a - b
+__global__ void k_sub_state(St* __restrict__ out, const St* __restrict__ a, const St* __restrict__ b, int n) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    st_state(out, c, ld_state(a, c) - ld_state(b, c));
+}
+
 // w = x / D - Jx  (the PTC operator applied to x; D = dt / V)
 __global__ void k_ptc(const double* __restrict__ D, const St* __restrict__ x, const St* __restrict__ Jx,
                       St* __restrict__ w, int n) {
@@ -287,25 +351,44 @@ __global__ void k_combine(double* __restrict__ out, const double* __restrict__ V
     out[k] = t;
 }
 
-// Per block: the four squared residual sums; one fold per component.
-__global__ void __launch_bounds__(kB) k_norm4(const St* __restrict__ R, int n, double* __restrict__ partials) {
+// Per instance (one block per instance; instances are contiguous cell
+// ranges, a single solver is one instance): the four residual L2 norms.
+__global__ void __launch_bounds__(kB) k_inst_norm4(const St* __restrict__ R, const int* __restrict__ off,
+                                                  double* __restrict__ out) {
+    const int i = blockIdx.x;
     double t[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int c = blockIdx.x * kB + threadIdx.x; c < n; c += gridDim.x * kB) {
+    for (int c = off[i] + threadIdx.x; c < off[i + 1]; c += kB) {
         const St r = ld_state(R, c);
         t[0] += r.r * r.r; t[1] += r.ru * r.ru; t[2] += r.rv * r.rv; t[3] += r.E * r.E;
     }
     for (int k = 0; k < 4; ++k) {
-        const double s = block_sum(t[k]);
-        if (threadIdx.x == 0) partials[(size_t)k * gridDim.x + blockIdx.x] = s;
+        const double v = block_sum(t[k]);
+        if (threadIdx.x == 0) out[4 * i + k] = sqrt(v);
     }
 }
 
-// Largest alpha <= 1 with no density or pressure falling by more than the
-// fraction frac (linearised: dW = M dU); block minima, then one fold.
-__global__ void __launch_bounds__(kB) k_alpha(const adjk::AdjArgs a, const St* __restrict__ du, double frac,
-                                             double* __restrict__ partials) {
+// Per instance: D *= cfl[i] (D formed at CFL 1), and a zero right-hand side
+// for instances that take no step.
+__global__ void __launch_bounds__(kB) k_inst_prepare(double* __restrict__ D, St* __restrict__ R,
+                                                    const int* __restrict__ off, const double* __restrict__ cfl,
+                                                    const int* __restrict__ mask) {
+    const int i = blockIdx.x;
+    const double k = cfl[i];
+    const bool on = mask[i] != 0;
+    for (int c = off[i] + threadIdx.x; c < off[i + 1]; c += kB) {
+        D[c] *= k;
+        if (!on) st_state(R, c, st_make(0.0, 0.0, 0.0, 0.0));
+    }
+}
+
+// Per instance: the largest alpha <= 1 with no density or pressure of its
+// cells falling by more than the fraction frac (linearised).
+__global__ void __launch_bounds__(kB) k_inst_alpha(const adjk::AdjArgs a, const St* __restrict__ du,
+                                                  const int* __restrict__ off, double frac,
+                                                  double* __restrict__ alpha) {
+    const int i = blockIdx.x;
     double amin = 1.0;
-    for (int c = blockIdx.x * kB + threadIdx.x; c < a.n_cells; c += gridDim.x * kB) {
+    for (int c = off[i] + threadIdx.x; c < off[i + 1]; c += kB) {
         const St w = ld_state(a.W, c);
         double M[16];
         prim_jac(w, a.gamma, M);
@@ -324,34 +407,33 @@ __global__ void __launch_bounds__(kB) k_alpha(const adjk::AdjArgs a, const St* _
     if (threadIdx.x == 0) {
         double v = red[0];
         for (int w = 1; w < kB / 32; ++w) v = fmin(v, red[w]);
-        partials[blockIdx.x] = v;
+        alpha[i] = v;
     }
 }
 
-__global__ void __launch_bounds__(kB) k_min_fold(const double* __restrict__ partials, int nblk, double* __restrict__ out) {
-    double v = DBL_MAX;
-    for (int b = threadIdx.x; b < nblk; b += kB) v = fmin(v, partials[b]);
-    v = warp_min(v);
-    __shared__ double red[kB / 32];
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = red[0];
-        for (int w = 1; w < kB / 32; ++w) m = fmin(m, red[w]);
-        out[0] = m;
+// Per instance: U += alpha[i] dU where mask[i]; U = Ubak where revert[i].
+__global__ void __launch_bounds__(kB) k_inst_update(St* __restrict__ U, const St* __restrict__ du,
+                                                   const St* __restrict__ Ubak, const int* __restrict__ off,
+                                                   const double* __restrict__ alpha, const int* __restrict__ mask,
+                                                   const int* __restrict__ revert) {
+    const int i = blockIdx.x;
+    const bool step = mask && mask[i], back = revert && revert[i];
+    if (!step && !back) return;
+    const double al = step ? alpha[i] : 0.0;
+    for (int c = off[i] + threadIdx.x; c < off[i + 1]; c += kB) {
+        if (back) st_state(U, c, ld_state(Ubak, c));
+        else st_state(U, c, ld_state(U, c) + al * ld_state(du, c));
     }
-}
-
-// U += alpha dU
-__global__ void k_update(St* __restrict__ U, const St* __restrict__ du, double alpha, int n) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    st_state(U, c, ld_state(U, c) + alpha * ld_state(du, c));
 }
 
 }  // namespace nk
 
 namespace {
+
+// Relative GMRES residual of a Newton step's linear solve: at or below
+// kRelGrow the CFL number may grow; above kRelFail it is halved.
+constexpr double kRelGrow = 0.7;
+constexpr double kRelFail = 0.9;
 
 struct NewtonWork {
     int N = 0, m = 0;
@@ -359,7 +441,7 @@ struct NewtonWork {
     std::vector<void*> owned;
     double *V = nullptr, *Dinv = nullptr, *part = nullptr, *h = nullptr, *scal = nullptr;
     St *R = nullptr, *z = nullptr, *z2 = nullptr, *Mz = nullptr, *Jx = nullptr, *w = nullptr, *du = nullptr,
-       *Ubak = nullptr, *tmp = nullptr;
+       *Ubak = nullptr, *tmp = nullptr, *zx = nullptr;
     int kind = 1;                   // preconditioner: 0 block Jacobi, 1 multicolour symmetric Gauss-Seidel
     int* colour_cells = nullptr;    // cells grouped by colour
     std::vector<int> colour_off;    // [n_colours + 1]
@@ -443,6 +525,23 @@ void precondition(fv_adjoint_s* A, NewtonWork& W, const St* r, St* z, int sweeps
     }
 }
 
+// z = P^-T r from z = 0: `sweeps` symmetric Gauss-Seidel sweeps of the
+// transposed matrix over the colours.
+void precondition_t(fv_adjoint_s* A, NewtonWork& W, const St* r, St* z, int sweeps, cudaStream_t s) {
+    FV_CUDA(cudaMemsetAsync(z, 0, sizeof(St) * (size_t)W.N, s));
+    const int nc = (int)W.colour_off.size() - 1;
+    for (int sw = 0; sw < sweeps; ++sw)
+        for (int pass = 0; pass < 2; ++pass)
+            for (int q = 0; q < nc; ++q) {
+                const int k = pass == 0 ? q : nc - 1 - q;
+                const int n = W.colour_off[k + 1] - W.colour_off[k];
+                if (n == 0) continue;
+                nk::k_gs_colour_t<<<nk::blocks(n), nk::kB, 0, s>>>(A->a, W.Dinv, r, z, W.colour_cells + W.colour_off[k],
+                                                                   n);
+            }
+    check_launch();
+}
+
 // out[0..nv) = <V_i, w> (device), folded deterministically
 void mdot(NewtonWork& W, const double* V, int nv, const double* w, double* out, bool accumulate, cudaStream_t s) {
     const int grid = (int)std::min<size_t>(nk::kGrid, (W.n + nk::kB - 1) / nk::kB);
@@ -462,85 +561,114 @@ double norm2(NewtonWork& W, const double* x, double* dev_out, cudaStream_t s) {
     return v;
 }
 
-void residual_norms(fv_adjoint_s* A, NewtonWork& W, double out[4], cudaStream_t s) {
-    const int grid = std::min(nk::kGrid, nk::blocks(W.N));
-    nk::k_norm4<<<grid, nk::kB, 0, s>>>(W.R, W.N, W.part);
-    nk::k_mfold<<<4, nk::kB, 0, s>>>(W.part, grid, W.scal, 0, 1);
-    check_launch();
-    FV_CUDA(cudaMemcpyAsync(out, W.scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    FV_CUDA(cudaStreamSynchronize(s));
-}
-
-// Right-preconditioned GMRES(m) from x = 0 on (V/dt - J) x = b; returns the
-// matvec count and the final relative residual estimate.
-int gmres(fv_adjoint_s* A, NewtonWork& W, const St* b, St* x, int m, double rtol, int sweeps, double* rel,
-          cudaStream_t s) {
+// Right-preconditioned restarted GMRES on A x = b from the x given (zero
+// when x0_zero), at most max_mv applications of A, until the residual is
+// below rtol times |b|.  op(z, w): w = A z; pc(v, z): z = P^-1 v.  Returns
+// the matvec count; *rel the last relative residual estimate.
+template <class Op, class Pc>
+int gmres_gen(NewtonWork& W, const St* b, St* x, bool x0_zero, int m, int max_mv, double rtol, double* rel,
+              cudaStream_t s, Op op, Pc pc) {
     const size_t n = W.n;
     const int vb = (int)((n + nk::kB - 1) / nk::kB);
     auto V = [&](int i) { return W.V + (size_t)i * n; };
-    FV_CUDA(cudaMemcpyAsync(V(0), b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    const double beta = norm2(W, V(0), W.scal, s);
+    double* wv = reinterpret_cast<double*>(W.w);
+    FV_CUDA(cudaMemcpyAsync(W.tmp, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    const double bnorm = norm2(W, reinterpret_cast<const double*>(W.tmp), W.scal, s);
     *rel = 1.0;
-    if (!(beta > 0.0) || !std::isfinite(beta)) {
+    if (x0_zero) FV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    if (!(bnorm > 0.0) || !std::isfinite(bnorm)) {
         FV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
         return 0;
     }
-    nk::k_scale_inv<<<vb, nk::kB, 0, s>>>(V(0), V(0), W.scal, n);
-    check_launch();
     std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0), y(m), hc(m + 2);
-    g[0] = beta;
-    int k = 0;
-    double* wv = reinterpret_cast<double*>(W.w);
-    for (int j = 0; j < m; ++j) {
-        precondition(A, W, reinterpret_cast<const St*>(V(j)), W.z, sweeps, s);
-        adjh::jvp_dev(A, W.z, W.Jx);
-        nk::k_ptc<<<nk::blocks(W.N), nk::kB, 0, s>>>(A->a.D, W.z, W.Jx, W.w, W.N);
-        check_launch();
-        // classical Gram-Schmidt, twice
-        mdot(W, W.V, j + 1, wv, W.h, false, s);
-        nk::k_mupdate<<<vb, nk::kB, 0, s>>>(wv, W.V, W.h, j + 1, n);
-        mdot(W, W.V, j + 1, wv, W.h + m + 2, false, s);
-        nk::k_mupdate<<<vb, nk::kB, 0, s>>>(wv, W.V, W.h + m + 2, j + 1, n);
-        check_launch();
-        std::vector<double> h1(j + 1), h2(j + 1);
-        FV_CUDA(cudaMemcpyAsync(h1.data(), W.h, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
-        FV_CUDA(cudaMemcpyAsync(h2.data(), W.h + m + 2, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
-        const double hn = norm2(W, wv, W.scal, s);
-        for (int i = 0; i <= j; ++i) hc[i] = h1[i] + h2[i];
-        hc[j + 1] = hn;
-        for (int i = 0; i <= j + 1; ++i)
-            if (!std::isfinite(hc[i])) fvgb::raise(FV_ERR_NONFINITE, "Newton-Krylov: non-finite Krylov vector");
-        if (hn > 0.0) {
-            nk::k_scale_inv<<<vb, nk::kB, 0, s>>>(V(j + 1), wv, W.scal, n);
+    int mv = 0;
+    bool first = true;
+    while (mv < max_mv) {
+        // r = b - A x (x = 0 on the first cycle from zero)
+        if (first && x0_zero) {
+            FV_CUDA(cudaMemcpyAsync(V(0), b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        } else {
+            op(x, W.Jx);
+            ++mv;
+            nk::k_sub_state<<<nk::blocks(W.N), nk::kB, 0, s>>>(reinterpret_cast<St*>(V(0)), b, W.Jx, W.N);
             check_launch();
         }
-        for (int i = 0; i < j; ++i) {
-            const double t = cs[i] * hc[i] + sn[i] * hc[i + 1];
-            hc[i + 1] = -sn[i] * hc[i] + cs[i] * hc[i + 1];
-            hc[i] = t;
+        first = false;
+        const double beta = norm2(W, V(0), W.scal, s);
+        if (!std::isfinite(beta)) fvgb::raise(FV_ERR_NONFINITE, "GMRES: non-finite residual");
+        *rel = beta / bnorm;
+        if (*rel <= rtol || mv >= max_mv) break;
+        nk::k_scale_inv<<<vb, nk::kB, 0, s>>>(V(0), V(0), W.scal, n);
+        check_launch();
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int k = 0;
+        for (int j = 0; j < m && mv < max_mv; ++j) {
+            pc(reinterpret_cast<const St*>(V(j)), W.z);
+            op(W.z, W.w);
+            ++mv;
+            // classical Gram-Schmidt, twice
+            mdot(W, W.V, j + 1, wv, W.h, false, s);
+            nk::k_mupdate<<<vb, nk::kB, 0, s>>>(wv, W.V, W.h, j + 1, n);
+            mdot(W, W.V, j + 1, wv, W.h + m + 2, false, s);
+            nk::k_mupdate<<<vb, nk::kB, 0, s>>>(wv, W.V, W.h + m + 2, j + 1, n);
+            check_launch();
+            std::vector<double> h1(j + 1), h2(j + 1);
+            FV_CUDA(cudaMemcpyAsync(h1.data(), W.h, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
+            FV_CUDA(cudaMemcpyAsync(h2.data(), W.h + m + 2, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
+            const double hn = norm2(W, wv, W.scal, s);
+            for (int i = 0; i <= j; ++i) hc[i] = h1[i] + h2[i];
+            hc[j + 1] = hn;
+            for (int i = 0; i <= j + 1; ++i)
+                if (!std::isfinite(hc[i])) fvgb::raise(FV_ERR_NONFINITE, "GMRES: non-finite Krylov vector");
+            if (hn > 0.0) {
+                nk::k_scale_inv<<<vb, nk::kB, 0, s>>>(V(j + 1), wv, W.scal, n);
+                check_launch();
+            }
+            for (int i = 0; i < j; ++i) {
+                const double t = cs[i] * hc[i] + sn[i] * hc[i + 1];
+                hc[i + 1] = -sn[i] * hc[i] + cs[i] * hc[i + 1];
+                hc[i] = t;
+            }
+            const double den = std::hypot(hc[j], hc[j + 1]);
+            cs[j] = den > 0.0 ? hc[j] / den : 1.0;
+            sn[j] = den > 0.0 ? hc[j + 1] / den : 0.0;
+            hc[j] = den;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hc[i];
+            k = j + 1;
+            *rel = std::fabs(g[j + 1]) / bnorm;
+            if (*rel <= rtol || !(hn > 0.0)) break;
         }
-        const double den = std::hypot(hc[j], hc[j + 1]);
-        cs[j] = den > 0.0 ? hc[j] / den : 1.0;
-        sn[j] = den > 0.0 ? hc[j + 1] / den : 0.0;
-        hc[j] = den;
-        g[j + 1] = -sn[j] * g[j];
-        g[j] = cs[j] * g[j];
-        for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hc[i];
-        k = j + 1;
-        *rel = std::fabs(g[j + 1]) / beta;
-        if (*rel <= rtol || !(hn > 0.0)) break;
+        for (int i = k - 1; i >= 0; --i) {
+            double t = g[i];
+            for (int l = i + 1; l < k; ++l) t -= H[(size_t)i * m + l] * y[l];
+            y[i] = t / H[(size_t)i * m + i];
+        }
+        // x += P^-1 (V y)
+        FV_CUDA(cudaMemcpyAsync(W.h, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+        nk::k_combine<<<vb, nk::kB, 0, s>>>(reinterpret_cast<double*>(W.tmp), W.V, W.h, k, n);
+        check_launch();
+        pc(W.tmp, W.zx);
+        nk::k_axpy_state<<<nk::blocks(W.N), nk::kB, 0, s>>>(x, W.zx, W.N);
+        check_launch();
+        FV_CUDA(cudaStreamSynchronize(s));
+        if (*rel <= rtol) break;
     }
-    for (int i = k - 1; i >= 0; --i) {
-        double t = g[i];
-        for (int l = i + 1; l < k; ++l) t -= H[(size_t)i * m + l] * y[l];
-        y[i] = t / H[(size_t)i * m + i];
-    }
-    FV_CUDA(cudaMemcpyAsync(W.h, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
-    nk::k_combine<<<vb, nk::kB, 0, s>>>(reinterpret_cast<double*>(W.tmp), W.V, W.h, k, n);
-    check_launch();
-    precondition(A, W, W.tmp, x, sweeps, s);
-    FV_CUDA(cudaStreamSynchronize(s));
-    return k;
+    return mv;
+}
+
+// One GMRES(m) cycle from x = 0 on the Newton system (V/dt - J) x = b.
+int gmres(fv_adjoint_s* A, NewtonWork& W, const St* b, St* x, int m, double rtol, int sweeps, double* rel,
+          cudaStream_t s) {
+    auto op = [&](const St* z, St* w) {
+        adjh::jvp_dev(A, z, W.Jx);
+        nk::k_ptc<<<nk::blocks(W.N), nk::kB, 0, s>>>(A->a.D, z, W.Jx, w, W.N);
+        check_launch();
+    };
+    auto pc = [&](const St* v, St* z) { precondition(A, W, v, z, sweeps, s); };
+    return gmres_gen(W, b, x, true, m, m, rtol, rel, s, op, pc);
 }
 
 }  // namespace
@@ -562,7 +690,8 @@ void fv_newton_default(fv_newton_t* o) {
     o->max_rel_change = 0.2;
 }
 
-int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history, int32_t* iterations) {
+int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history, int32_t* iterations,
+                     int32_t* instance_steps) {
     return fvgb::guarded([&] {
         if (!solver || !opt) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
         const fv_newton_t o = *opt;
@@ -571,12 +700,8 @@ int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history
             o.precond_sweeps < 1 || o.precond_kind < 0 || o.precond_kind > 1 || !(o.max_rel_change > 0.0))
             fvgb::raise(FV_ERR_BAD_ARG, "fv_steady_newton: bad options");
         fvgb::Solver& s = solver->s;
-        if (s.batch) fvgb::raise(FV_ERR_UNSUPPORTED, "fv_steady_newton: single (not batched) Euler solvers");
         fv_adjoint_t Ah = nullptr;
-        {
-            const int rc = fv_adjoint_create(solver, o.limiter_mode, &Ah);
-            if (rc != FV_OK) fvgb::raise(rc, std::string("fv_steady_newton: ") + fvgb::last_error());
-        }
+        adjh::create(solver, o.limiter_mode, true, &Ah);
         std::unique_ptr<fv_adjoint_s> A(Ah);
         cudaStream_t st = s.stream;
         NewtonWork W;
@@ -597,76 +722,211 @@ int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history
         W.du = W.alloc<St>(s.N);
         W.Ubak = W.alloc<St>(s.N);
         W.tmp = W.alloc<St>(s.N);
-        const int agrid = std::min(nk::kGrid, nk::blocks(s.N));
+        W.zx = W.alloc<St>(s.N);
         W.kind = o.precond_kind;
         if (W.kind == 1) colour_cells(s, W, st);
+        // instances: contiguous cell ranges (a single solver is one)
+        const std::vector<int> off = s.batch ? std::vector<int>(s.group_off.begin(), s.group_off.end())
+                                             : std::vector<int>{0, s.N};
+        const int ni = (int)off.size() - 1;
+        int* d_off = W.alloc<int>(ni + 1);
+        fvgb::h2d_sync(d_off, off.data(), sizeof(int) * (ni + 1), st);
+        double* d_nrm = W.alloc<double>(4 * (size_t)ni);
+        double* d_cfl = W.alloc<double>(ni);
+        double* d_alpha = W.alloc<double>(ni);
+        int* d_mask = W.alloc<int>(ni);
+        int* d_revert = W.alloc<int>(ni);
+        std::vector<double> nr(4 * (size_t)ni), prev(ni, -1.0), cfl(ni, o.cfl0), last_cfl(ni, 0.0), alpha(ni, 0.0);
+        std::vector<int> stepped(ni, 0), rejects(ni, 0), mask(ni, 0), revert(ni, 0), conv_at(ni, -1);
         FV_CUDA(cudaStreamSynchronize(st));
-        double prev = -1.0, cfl = o.cfl0;
-        int it = 0, rejects = 0;
-        double last_alpha = 0.0, last_rel = 0.0, last_cfl = 0.0;
+        int it = 0;
+        double last_rel = 0.0;
         int last_mv = 0;
-        bool retry = false;  // the state was just restored: keep the reduced CFL number
         for (;;) {
             FV_CUDA(cudaMemcpyAsync(A->U, s.U, sizeof(St) * (size_t)s.N, cudaMemcpyDeviceToDevice, st));
             adjh::linearise(A.get());
             adjh::residual_dev(A.get(), W.R);
-            double nr[4];
-            residual_norms(A.get(), W, nr, st);
-            if (it == 0 && (!std::isfinite(nr[0]) || !std::isfinite(nr[3])))
-                fvgb::raise(FV_ERR_NONFINITE, "fv_steady_newton: non-finite residual at the start");
-            if (prev > 0.0 && !retry) {
-                const double ratio = nr[0] / prev;
-                if (!(ratio <= 10.0) || !std::isfinite(nr[3])) {
-                    if (rejects < 10) {
-                        // undo the step, retry at a quarter of the pseudo time step
-                        FV_CUDA(cudaMemcpyAsync(s.U, W.Ubak, sizeof(St) * (size_t)s.N, cudaMemcpyDeviceToDevice, st));
-                        cfl = std::max(o.cfl0 * 1e-3, 0.25 * last_cfl);
-                        ++rejects;
-                        retry = true;
-                        continue;
-                    }
-                } else if (ratio < 1.0) {
-                    cfl = std::min(o.cfl_max, last_cfl * o.cfl_growth);
-                } else if (ratio < 2.0) {
-                    cfl = last_cfl;
-                } else {
-                    cfl = std::max(o.cfl0 * 1e-3, 0.5 * last_cfl);
+            nk::k_inst_norm4<<<ni, nk::kB, 0, st>>>(W.R, d_off, d_nrm);
+            check_launch();
+            FV_CUDA(cudaMemcpyAsync(nr.data(), d_nrm, sizeof(double) * nr.size(), cudaMemcpyDeviceToHost, st));
+            FV_CUDA(cudaStreamSynchronize(st));
+            // per instance: accept the last step (adapt its CFL number) or undo it
+            bool any_revert = false;
+            for (int i = 0; i < ni; ++i) {
+                revert[i] = 0;
+                const double r = nr[4 * i], e = nr[4 * i + 3];
+                if (it == 0 && (!std::isfinite(r) || !std::isfinite(e)))
+                    fvgb::raise(FV_ERR_NONFINITE, "fv_steady_newton: non-finite residual at the start");
+                if (!stepped[i]) {
+                    if (prev[i] < 0.0) prev[i] = r;
+                    continue;
                 }
+                stepped[i] = 0;
+                const double ratio = r / prev[i];
+                if ((!(ratio <= 10.0) || !std::isfinite(e)) && rejects[i] < 10) {
+                    revert[i] = 1;
+                    any_revert = true;
+                    cfl[i] = std::max(o.cfl0 * 1e-3, 0.25 * last_cfl[i]);
+                    ++rejects[i];
+                    continue;
+                }
+                rejects[i] = 0;
+                // The CFL number grows only after a step that lowered the
+                // residual, was taken in full and came from a linear solve
+                // that reduced its residual at least to kRelGrow; a linear
+                // solve that made no headway (above kRelFail) halves it, as
+                // a large rise does.  Without the linear test the CFL number
+                // keeps growing on tiny decreases while GMRES no longer
+                // solves the system at all, and the iteration stalls there.
+                const bool lin_ok = last_rel <= kRelGrow, lin_fail = last_rel > kRelFail;
+                if (ratio < 1.0 && lin_ok && alpha[i] >= 1.0) cfl[i] = std::min(o.cfl_max, last_cfl[i] * o.cfl_growth);
+                else if (ratio < 2.0 && !lin_fail) cfl[i] = last_cfl[i];
+                else cfl[i] = std::max(o.cfl0 * 1e-3, 0.5 * last_cfl[i]);
+                prev[i] = r;
             }
-            if (!retry) rejects = 0;
-            retry = false;
+            if (any_revert) {
+                // undo those instances' steps and evaluate again
+                FV_CUDA(cudaMemcpyAsync(d_revert, revert.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, st));
+                nk::k_inst_update<<<ni, nk::kB, 0, st>>>(s.U, W.du, W.Ubak, d_off, d_alpha, nullptr, d_revert);
+                check_launch();
+                continue;
+            }
+            // history: norms over all instances, largest CFL, smallest step length
+            int active = 0;
+            for (int i = 0; i < ni; ++i) {
+                mask[i] = prev[i] >= o.tol ? 1 : 0;
+                if (!mask[i] && conv_at[i] < 0) conv_at[i] = it;
+                active += mask[i];
+            }
             if (history) {
                 double* row = history + 8 * (size_t)it;
-                for (int q = 0; q < 4; ++q) row[q] = nr[q];
-                row[4] = last_cfl;
+                for (int q = 0; q < 4; ++q) {
+                    double t = 0.0;
+                    for (int i = 0; i < ni; ++i) t += nr[4 * i + q] * nr[4 * i + q];
+                    row[q] = std::sqrt(t);
+                }
+                double cmax = 0.0, amin = it ? 1.0 : 0.0;
+                for (int i = 0; i < ni; ++i) {
+                    cmax = std::max(cmax, it ? last_cfl[i] : 0.0);
+                    if (it) amin = std::min(amin, alpha[i]);
+                }
+                row[4] = cmax;
                 row[5] = last_mv;
                 row[6] = last_rel;
-                row[7] = last_alpha;
+                row[7] = amin;
             }
-            prev = nr[0];
-            if (nr[0] < o.tol || it >= o.max_newton) break;
-            adjh::lin_dt(A.get(), cfl);
+            if (active == 0 || it >= o.max_newton) break;
+            // the step: (V/dt - J) dU = R per instance at its own CFL number
+            FV_CUDA(cudaMemcpyAsync(d_cfl, cfl.data(), sizeof(double) * ni, cudaMemcpyHostToDevice, st));
+            FV_CUDA(cudaMemcpyAsync(d_mask, mask.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, st));
+            adjh::lin_dt(A.get(), 1.0);
+            nk::k_inst_prepare<<<ni, nk::kB, 0, st>>>(A->a.D, W.R, d_off, d_cfl, d_mask);
             nk::k_pc_diag<<<nk::blocks(s.N), nk::kB, 0, st>>>(A->a, W.Dinv);
             check_launch();
             double rel = 0.0;
             const int mv = gmres(A.get(), W, W.R, W.du, o.krylov_dim, o.krylov_rtol, o.precond_sweeps, &rel, st);
-            nk::k_alpha<<<agrid, nk::kB, 0, st>>>(A->a, W.du, o.max_rel_change, W.part);
-            nk::k_min_fold<<<1, nk::kB, 0, st>>>(W.part, agrid, W.scal);
+            nk::k_inst_alpha<<<ni, nk::kB, 0, st>>>(A->a, W.du, d_off, o.max_rel_change, d_alpha);
             check_launch();
-            double alpha = 0.0;
-            FV_CUDA(cudaMemcpyAsync(&alpha, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st));
-            FV_CUDA(cudaStreamSynchronize(st));
+            FV_CUDA(cudaMemcpyAsync(alpha.data(), d_alpha, sizeof(double) * ni, cudaMemcpyDeviceToHost, st));
             FV_CUDA(cudaMemcpyAsync(W.Ubak, s.U, sizeof(St) * (size_t)s.N, cudaMemcpyDeviceToDevice, st));
-            nk::k_update<<<nk::blocks(s.N), nk::kB, 0, st>>>(s.U, W.du, alpha, s.N);
+            nk::k_inst_update<<<ni, nk::kB, 0, st>>>(s.U, W.du, W.Ubak, d_off, d_alpha, d_mask, nullptr);
             check_launch();
-            last_alpha = alpha;
+            FV_CUDA(cudaStreamSynchronize(st));
+            for (int i = 0; i < ni; ++i) {
+                stepped[i] = mask[i];
+                if (mask[i]) last_cfl[i] = cfl[i];
+            }
             last_rel = rel;
             last_mv = mv;
-            last_cfl = cfl;
             ++it;
         }
         if (iterations) *iterations = it;
+        if (instance_steps)
+            for (int i = 0; i < ni; ++i) instance_steps[i] = conv_at[i];
         s.refresh_primitives();
+        FV_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int fv_adjoint_solve_krylov(fv_adjoint_t A, const double* dJdU, double cfl, int32_t restart, int32_t max_matvec,
+                            double rtol, int32_t precond_sweeps, double* lambda, double* fsbar, double* history,
+                            int32_t* matvecs, double residual[4]) {
+    return fvgb::guarded([&] {
+        if (!A || !dJdU || !(cfl > 0.0) || restart < 1 || restart > 200 || max_matvec < 1 || !(rtol > 0.0) ||
+            precond_sweeps < 1)
+            fvgb::raise(FV_ERR_BAD_ARG, "fv_adjoint_solve_krylov: bad argument");
+        if (!A->linearised) fvgb::raise(FV_ERR_BAD_ARG, "call fv_residual_forward first");
+        fvgb::Solver& s = A->solver->s;
+        cudaStream_t st = s.stream;
+        NewtonWork W;
+        W.N = s.N;
+        W.n = 4 * (size_t)s.N;
+        W.m = restart;
+        W.V = W.alloc<double>((size_t)(restart + 1) * W.n);
+        W.Dinv = W.alloc<double>(16 * (size_t)s.N);
+        W.part = W.alloc<double>((size_t)nk::kGrid * std::max(restart + 2, 4));
+        W.h = W.alloc<double>(2 * (size_t)(restart + 2));
+        W.scal = W.alloc<double>(8);
+        W.R = W.alloc<St>(s.N);
+        W.z = W.alloc<St>(s.N);
+        W.z2 = W.alloc<St>(s.N);
+        W.Mz = W.alloc<St>(s.N);
+        W.Jx = W.alloc<St>(s.N);
+        W.w = W.alloc<St>(s.N);
+        W.du = W.alloc<St>(s.N);
+        W.tmp = W.alloc<St>(s.N);
+        W.zx = W.alloc<St>(s.N);
+        colour_cells(s, W, st);
+        // the preconditioner's pseudo time step; the primal's is restored after
+        const double cfl_primal = A->a.cfl;
+        adjh::lin_dt(A, cfl);
+        nk::k_pc_diag<<<nk::blocks(s.N), nk::kB, 0, st>>>(A->a, W.Dinv);
+        check_launch();
+        // -(dR/dU)^T lam = -dJ/dU
+        adjh::upload(A, dJdU, W.du);
+        nk::k_neg<<<nk::blocks(s.N), nk::kB, 0, st>>>(W.R, W.du, s.N);
+        check_launch();
+        auto op = [&](const St* z, St* w) {
+            adjh::vjp_dev(A, z, W.Jx);
+            nk::k_neg<<<nk::blocks(W.N), nk::kB, 0, st>>>(w, W.Jx, W.N);
+            check_launch();
+        };
+        auto pc = [&](const St* v, St* z) { precondition_t(A, W, v, z, precond_sweeps, st); };
+        double rel = 1.0;
+        // history: relative residual estimate after every restart cycle
+        std::vector<double> hh;
+        int mv = 0;
+        FV_CUDA(cudaMemsetAsync(A->lam, 0, sizeof(St) * (size_t)s.N, st));
+        while (mv < max_matvec) {
+            const int k = gmres_gen(W, W.R, A->lam, false, restart, std::min(max_matvec - mv, restart + 1), rtol, &rel,
+                                    st, op, pc);
+            mv += k;
+            hh.push_back(rel);
+            if (rel <= rtol || k == 0) break;
+        }
+        adjh::lin_dt(A, cfl_primal);
+        // residual of (dR/dU)^T lam - dJ/dU, per component
+        adjh::vjp_dev(A, A->lam, W.Jx);
+        nk::k_sub_state<<<nk::blocks(s.N), nk::kB, 0, st>>>(W.z, W.Jx, W.du, s.N);
+        int* d_off = W.alloc<int>(2);
+        const int off[2] = {0, s.N};
+        fvgb::h2d_sync(d_off, off, sizeof(off), st);
+        nk::k_inst_norm4<<<1, nk::kB, 0, st>>>(W.z, d_off, W.scal);
+        check_launch();
+        double r4[4];
+        FV_CUDA(cudaMemcpyAsync(r4, W.scal, sizeof(r4), cudaMemcpyDeviceToHost, st));
+        FV_CUDA(cudaStreamSynchronize(st));
+        if (residual)
+            for (int q = 0; q < 4; ++q) residual[q] = r4[q];
+        if (matvecs) *matvecs = mv;
+        if (history)
+            for (size_t i = 0; i < hh.size(); ++i) history[i] = hh[i];
+        A->solved = true;
+        if (lambda) adjh::download(A, A->lam, lambda);
+        if (fsbar) {
+            adjh::vjp_dev(A, A->lam, W.Jx);
+            adjh::fsbar(A, fsbar);
+        }
         FV_CUDA(cudaStreamSynchronize(st));
     });
 }

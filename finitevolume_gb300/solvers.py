@@ -337,7 +337,9 @@ class EulerFVMSolver:
             setattr(o, k, type(getattr(o, k))(v))
         hist = np.zeros((int(max_newton) + 1, 8))
         it = C.c_int32()
-        capi.check(capi.lib().fv_steady_newton(self._h, C.byref(o), capi.dptr(hist), C.byref(it)))
+        steps = np.zeros(max(1, getattr(self, "n_instances", 1)), np.int32)
+        capi.check(capi.lib().fv_steady_newton(self._h, C.byref(o), capi.dptr(hist), C.byref(it), capi.i32ptr(steps)))
+        self.last_newton_instance_steps = steps
         return hist[:it.value + 1], it.value
 
     def set_persistent(self, on: bool = True) -> None:
@@ -500,13 +502,21 @@ class DiscreteAdjoint:
                                                    capi.dptr(Ub), capi.dptr(fb)))
         return Ub, fb[:self.n_patches]
 
+    # preconditioner of method "krylov": pseudo-time CFL number and sweeps
+    krylov_cfl = 1e4
+    krylov_sweeps = 2
+
     def solve(self, dJdU, max_iter: int = 20000, tol: float = 1e-12, method: str = "rk", restart: int = 40):
         """Solve (dR/dU)^T lambda = dJdU.  method "rk": SSP-RK3 pseudo-time
         iteration until every residual-norm component is below tol (history
         [iterations, 4] of those norms); "gmres": GMRES(restart) on the
         fixed point of that iteration until its residual falls by the
         factor tol, max_iter matvecs (history [matvecs] of the relative
-        GMRES residual).  Returns lambda, fsbar, history, iterations; the
+        GMRES residual); "krylov": GMRES(restart) on (dR/dU)^T itself,
+        preconditioned by Gauss-Seidel sweeps of the transposed first-order
+        Jacobian (``krylov_cfl``, ``krylov_sweeps``), until its residual
+        falls by the factor tol, max_iter matvecs (history: relative
+        residual per restart cycle).  Returns lambda, fsbar, history, iterations; the
         final residual norms are kept in ``last_residual`` for "gmres"."""
         lam = np.zeros((self.n, 4))
         fb = np.zeros((_MAX_PATCHES, 4))
@@ -520,8 +530,18 @@ class DiscreteAdjoint:
                                                          C.byref(it), capi.dptr(res)))
             self.last_residual = res
             return lam, fb[:self.n_patches], hist[:it.value], it.value
+        if method == "krylov":
+            hist = np.zeros(max(max_iter // max(restart, 1) + 2, 1))
+            res = np.zeros(4)
+            capi.check(capi.lib().fv_adjoint_solve_krylov(self._h, capi.dptr(g), float(self.krylov_cfl), int(restart),
+                                                          int(max_iter), float(tol), int(self.krylov_sweeps),
+                                                          capi.dptr(lam), capi.dptr(fb), capi.dptr(hist),
+                                                          C.byref(it), capi.dptr(res)))
+            self.last_residual = res
+            n_cycles = int(np.count_nonzero(hist))
+            return lam, fb[:self.n_patches], hist[:n_cycles], it.value
         if method != "rk":
-            raise ValueError("method: 'rk' or 'gmres'")
+            raise ValueError("method: 'rk', 'gmres' or 'krylov'")
         hist = np.zeros((max(max_iter, 1), 4))
         capi.check(capi.lib().fv_adjoint_solve(self._h, capi.dptr(g), int(max_iter), float(tol), capi.dptr(lam),
                                                capi.dptr(fb), capi.dptr(hist), C.byref(it)))
@@ -707,6 +727,23 @@ class BatchSolver:
 
     def set_tolerance(self, tol: float) -> None:
         capi.check(capi.lib().fv_batch_set_tolerance(self._h, float(tol)))
+
+    @property
+    def n_instances(self) -> int:
+        return self.n
+
+    # Newton-Krylov over the whole batch (one block-diagonal system, every
+    # instance with its own CFL number and stopping test) and limiter
+    # freezing for every instance: the single-solver methods apply as is.
+    newton = EulerFVMSolver.newton
+    freeze_limiter = EulerFVMSolver.freeze_limiter
+
+    def limiter_values(self, instance: int) -> np.ndarray:
+        """The frozen limiter values [n_cells of the instance, 4]."""
+        out = np.zeros((self.mesh.n_cells, 4))
+        capi.check(capi.lib().fv_solver_limiter_values(self._h, capi.dptr(out), None))
+        o = self.mesh.offsets
+        return out[o[instance]:o[instance + 1]]
 
     def multigrid(self, levels: int = 4, smooth: int = 1, relax: float = 0.7) -> None:
         """Agglomeration multigrid for every instance (agglomerates never

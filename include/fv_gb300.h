@@ -378,6 +378,19 @@ int fv_adjoint_solve(fv_adjoint_t a, const double* dJdU, int32_t max_iter, doubl
  * Other outputs as fv_adjoint_solve; each may be NULL. */
 int fv_adjoint_solve_gmres(fv_adjoint_t a, const double* dJdU, int32_t restart, int32_t max_matvec, double rtol,
                            double* lambda, double* fsbar, double* history, int32_t* matvecs, double residual[4]);
+/* The same adjoint system by restarted GMRES(restart) on (dR/dU)^T directly,
+ * right-preconditioned by symmetric block Gauss-Seidel sweeps (over a cell
+ * colouring) of the transposed first-order Jacobian plus V/dt at the given
+ * CFL number (a large one, e.g. 1e4, for a converged state): for converged
+ * transonic states, where the pseudo-time iteration is slow.  Stops when the
+ * GMRES residual is below rtol |dJdU| or after max_matvec products;
+ * history [restart cycles] the relative residual after each cycle (at most
+ * max_matvec / restart + 1 entries); residual[4] the norms of
+ * (dR/dU)^T lam - dJdU.  Other outputs as fv_adjoint_solve; each may be
+ * NULL. */
+int fv_adjoint_solve_krylov(fv_adjoint_t a, const double* dJdU, double cfl, int32_t restart, int32_t max_matvec,
+                            double rtol, int32_t precond_sweeps, double* lambda, double* fsbar, double* history,
+                            int32_t* matvecs, double residual[4]);
 /* Shape gradient dJ/dX [2 n_nodes] (x, y per node, the mesh's node
  * numbering) of the objective the last fv_adjoint_solve was solved for:
  * dJ/dX|explicit - lambda^T dR/dX through face normals, lengths and
@@ -401,10 +414,15 @@ int fv_residual_shape_vjp(fv_adjoint_t a, fv_mesh_t mesh, const double* Rbar, do
  * Jacobi), then U += alpha dU with alpha <= 1 bounding the relative change
  * of every cell's density and pressure.  The CFL number of V/dt starts at
  * cfl0, grows by cfl_growth after each step that lowers the density
- * residual (up to cfl_max), holds after a rise below 2x, halves after a
- * larger one; a step that raises it more than 10x is undone and retried at
+ * residual, was taken in full (alpha = 1) and whose GMRES solve reached a
+ * relative residual of 0.7 or less (up to cfl_max); it holds after a rise
+ * below 2x and halves after a larger one or after a GMRES solve that ended
+ * above 0.9; a step that raises it more than 10x is undone and retried at
  * a quarter of its CFL number.  FP64 Euler solvers with the Rusanov or HLLC
- * flux (least-squares gradients at second order); not batched.
+ * flux (least-squares gradients at second order), single or batched: a
+ * batch is solved as one block-diagonal system in which every instance has
+ * its own residual norms, CFL number, step length and undo decision and
+ * stops once its own density residual is below tol.
  * --------------------------------------------------------------------- */
 typedef struct {
     int32_t limiter_mode;   /* FV_ADJ_FROZEN_LIMITER or FV_ADJ_FULL_LIMITER: the limiter's
@@ -425,10 +443,14 @@ typedef struct {
 void fv_newton_default(fv_newton_t* opt);
 /* Runs from the solver's current state and leaves the result there.
  * history (may be NULL) receives one row of 8 per evaluated state
- * [iterations + 1 rows]: the four residual norms, then the CFL number, the
- * GMRES iterations, its relative residual and the step length alpha of the
- * step that produced it (zeros in row 0). */
-int fv_steady_newton(fv_solver_t s, const fv_newton_t* opt, double* history, int32_t* iterations);
+ * [iterations + 1 rows]: the four residual norms (over all instances), then
+ * the largest CFL number, the GMRES iterations, its relative residual and
+ * the smallest step length alpha of the step that produced it (zeros in
+ * row 0).  instance_steps (may be NULL; one entry per batch instance, or
+ * one) receives the Newton step at which each instance converged, -1 where
+ * it did not. */
+int fv_steady_newton(fv_solver_t s, const fv_newton_t* opt, double* history, int32_t* iterations,
+                     int32_t* instance_steps);
 
 /* Wall-force coefficient J (objective 0 drag, 1 lift, 2 moment; pressure
  * part with the owner-cell pressure, ref as fv_wall_forces) at the
