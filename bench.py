@@ -560,12 +560,16 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, freeze_
     return out
 
 
-def rans_sa_rate(steps: int = 20, warm: int = 3):
+def rans_sa_rate(steps: int = 20, warm: int = 3, cpu: bool = True):
     """RANS with the Spalart-Allmaras model on the ~2M-cell NACA4412 hybrid
     mesh (40 wall-clustered quad layers, y+ ~ 1 at Re_c 6e6, growth 1.15,
     seeded random triangles to 30 chords): M 0.15, AoA 4 deg, Re_c 6e6,
     Pr 0.72, Pr_t 0.9, freestream nu-tilde = 3 nu, HLLC with Green-Gauss
-    viscous gradients, the reference's forward-Euler global-dt scheme."""
+    viscous gradients, the reference's forward-Euler global-dt scheme.
+    With ``cpu``: the oracle's restatement of RANSTurbulenceSASolver runs
+    the same warm + steps iterations from the same start on all host
+    threads (the CPU baseline, timed over the steps after the warm-up) and
+    its field and nu-tilde are compared with the GPU's (parity)."""
     import torch
     from finitevolume_gb300 import meshgen, solvers as S
     M, aoa, Re = 0.15, 4.0, 6e6
@@ -584,10 +588,35 @@ def rans_sa_rate(steps: int = 20, warm: int = 3):
     torch.cuda.synchronize()
     ms, launches = s.step_timed(steps)
     t = float(np.sum(ms))
-    return {"workload": "naca4412 hybrid, 40 quad layers + random triangles, M 0.15, AoA 4, Re 6e6, SA-noft2",
-            "cells": mesh.n_cells, "faces": mesh.n_faces, "value": round(mesh.n_cells * steps / (t / 1e3) / 1e6, 3),
-            "unit": "Mcell-iters/s", "ms_per_step": round(t / steps, 4), "steps": steps,
-            "nut_residual": s.nut_residual()}
+    out = {"workload": "naca4412 hybrid, 40 quad layers + random triangles, M 0.15, AoA 4, Re 6e6, SA-noft2",
+           "cells": mesh.n_cells, "faces": mesh.n_faces, "value": round(mesh.n_cells * steps / (t / 1e3) / 1e6, 3),
+           "unit": "Mcell-iters/s", "ms_per_step": round(t / steps, 4), "steps": steps,
+           "nut_residual": s.nut_residual()}
+    if cpu:
+        from oracle import port
+        poly = mesh.poly
+        om = port.OracleMesh(poly)
+        st = tuple(S.from_primitive(rho, u, v, p, GAMMA))
+        bcs = [{"type": "noslip"}, {"type": "farfield", "state": st, "nut": 3.0 * mu / rho}]
+        o = port.OracleRANS(om, bcs, GAMMA, R, mu, 0.72, 0.9, 0.5, {"rho": rho, "u": u, "v": v, "p": p},
+                            3.0 * mu / rho, flux=1, gradient=1)
+        o.run(warm)
+        t0 = time.perf_counter()
+        o.run(steps)
+        tc = time.perf_counter() - t0
+        f_cpu, nut_cpu, _ = o.get()
+        del o, om
+        out["cpu_baseline"] = {"value": round(mesh.n_cells * steps / tc / 1e6, 3), "unit": "Mcell-iters/s",
+                               "cores": port.num_threads(), "kind": "port",
+                               "sample": f"{steps} RANSTurbulenceSASolver steps (after {warm} warm-up) of the "
+                                         f"oracle restatement on the full mesh, OpenMP over {port.num_threads()} "
+                                         f"threads ({tc:.1f} s)"}
+        fg, ng = s.field(), s.nut_field()
+        out["parity"] = {"against": "oracle port (CPU FP64 RANSTurbulenceSASolver restatement), same start state",
+                         "iterations": warm + steps, "tolerance": 1e-10,
+                         "max_rel_field_err": float(np.max(np.abs(fg - f_cpu)) / np.max(np.abs(f_cpu))),
+                         "max_rel_nut_err": float(np.max(np.abs(ng - nut_cpu)) / np.max(np.abs(nut_cpu)))}
+    return out
 
 
 def sod_layout(nx: int = 1000, ny: int = 500, steps: int = 50):
@@ -713,7 +742,7 @@ def profile_target(target: str, steps: int) -> dict:
         _, g = S.force_gradient(s, S.Objective.Drag, np.array([1.0, fs[1], fs[2], fs[3], 1.0, 0.25, 0.0]))
         adj.solve(g, steps, 0.0)
     elif target == "rans":
-        rans_sa_rate(steps=steps, warm=1)
+        rans_sa_rate(steps=steps, warm=1, cpu=False)
     else:
         poly = load_mesh()
         s, _ = make_solver(poly)

@@ -22,6 +22,8 @@
 //   diffusion step   src/UnstructuredFVMSolver.cpp:44-129
 //   gradients        src/GradientReconstruction.cpp:45-200
 //   wall forces      src/WallTraction.cpp:163-217 (pressure part)
+//   RANS-SA step     src/RANSTurbulenceSASolver.cpp:118-336, 415-431,
+//                    src/SpalartAllmaras.cpp, src/WallDistance.cpp:11-44
 // Extensions (no reference code; this file is their CPU FP64 definition):
 //   local time stepping, characteristic farfield, MUSCL reconstruction of
 //   primitive variables with Barth-Jespersen / Venkatakrishnan limiting,
@@ -700,6 +702,364 @@ struct Diffusion {
     }
 };
 
+// ------------------------------------------------------ RANS-SA step ---
+// RANSTurbulenceSASolver (src/RANSTurbulenceSASolver.cpp:118-282, compute_dt
+// :296-336, ghost_state :415-431, boundary fields :70-110), its gradients
+// (src/GradientReconstruction.cpp:45-200: GradientCalculator, face_gradient,
+// corrected_face_gradient_vector, face_normal_distance), the SA-noft2
+// source terms (src/SpalartAllmaras.cpp, constants include/SpalartAllmaras.h:
+// 13-23) and the wall distance (src/WallDistance.cpp:11-44), in the
+// reference's evaluation order.  Patch kinds: BC_NOSLIP, BC_FARFIELD,
+// BC_OUTFLOW (NSBoundaryType); NoSlipWall patches carry wall_u, wall_v and,
+// when isothermal, wall_T.
+struct G2 { double x = 0.0, y = 0.0; };
+struct FaceGrad { double dn; G2 gf; };
+
+struct SAConst {
+    double cb1 = 0.1355, cb2 = 0.622, sigma = 2.0 / 3.0, kappa = 0.41, cw2 = 0.3, cw3 = 2.0, cv1 = 7.1,
+           cv2 = 0.7, cv3 = 0.9;
+};
+inline double sa_cw1(const SAConst& c) { return c.cb1 / (c.kappa * c.kappa) + (1.0 + c.cb2) / c.sigma; }
+inline double sa_fv1(double nut, double nu, const SAConst& c) {
+    if (nut <= 0.0) return 0.0;
+    double chi = nut / nu;
+    double chi3 = chi * chi * chi;
+    return chi3 / (chi3 + c.cv1 * c.cv1 * c.cv1);
+}
+inline double sa_nut(double nut, double nu, const SAConst& c) { return nut * sa_fv1(nut, nu, c); }
+// production - destruction + cross-diffusion (SpalartAllmaras.cpp).
+inline double sa_source(double nut, double nu, double omega, double d, const G2& gn, const SAConst& c) {
+    double chi = (nut > 0.0) ? nut / nu : 0.0;
+    double fv1 = sa_fv1(nut, nu, c);
+    double fv2 = 1.0 - chi / (1.0 + chi * fv1);
+    double d2 = d * d;
+    double s_bar = (nut / (c.kappa * c.kappa * d2)) * fv2;
+    double s_tilde;
+    if (s_bar >= -c.cv2 * omega) s_tilde = omega + s_bar;
+    else s_tilde = omega + omega * (c.cv2 * c.cv2 * omega + c.cv3 * s_bar) / ((c.cv3 - 2.0 * c.cv2) * omega - s_bar);
+    double production = c.cb1 * s_tilde * nut;
+    double destruction = 0.0;
+    if (nut > 0.0) {
+        double s_safe = std::max(s_tilde, 1e-10);
+        double r = std::min(nut / (s_safe * c.kappa * c.kappa * d2), 10.0);
+        double g = r + c.cw2 * (std::pow(r, 6.0) - r);
+        double fw = g * std::pow((1.0 + std::pow(c.cw3, 6.0)) / (std::pow(g, 6.0) + std::pow(c.cw3, 6.0)), 1.0 / 6.0);
+        double nd = nut / d;
+        destruction = sa_cw1(c) * fw * nd * nd;
+    }
+    double cross = (c.cb2 / c.sigma) * (gn.x * gn.x + gn.y * gn.y);
+    return production - destruction + cross;
+}
+
+struct RansBC {
+    int type = BC_NOSLIP;
+    State state;
+    double wall_u = 0.0, wall_v = 0.0, wall_T = 0.0, nut = 0.0;
+    int isothermal = 0;
+};
+
+struct Rans {
+    Mesh mesh;
+    std::vector<State> U;
+    std::vector<double> nut, walld, lsq;
+    std::vector<RansBC> bcs;
+    double gamma = 1.4, R = 287.0, mu = 0.0, Pr = 0.72, Prt = 0.9, cfl = 0.5, tol = 1e-6;
+    int flux = 0, gradient = 0, maxit = 20;
+    SAConst sa;
+    double last[5] = {0, 0, 0, 0, 0};
+
+    // GradientCalculator ctor (least squares over face neighbours, boundary
+    // midpoints standing in for the missing neighbour).
+    void setup() {
+        lsq.assign(3 * mesh.cells.size(), 0.0);
+        if (gradient == 0)
+            for (size_t c = 0; c < mesh.cells.size(); ++c) {
+                const Cell& cell = mesh.cells[c];
+                double m00 = 0.0, m01 = 0.0, m11 = 0.0;
+                for (int fi : cell.faces) {
+                    const Face& f = mesh.faces[fi];
+                    double px, py;
+                    if (f.cell_right == -1) { px = f.x_mid; py = f.y_mid; }
+                    else {
+                        int nb = (f.cell_left == (int)c) ? f.cell_right : f.cell_left;
+                        px = mesh.cells[nb].x_centroid; py = mesh.cells[nb].y_centroid;
+                    }
+                    double dx = px - cell.x_centroid, dy = py - cell.y_centroid;
+                    double w = 1.0 / (dx * dx + dy * dy);
+                    m00 += w * dx * dx; m01 += w * dx * dy; m11 += w * dy * dy;
+                }
+                double det = m00 * m11 - m01 * m01;
+                lsq[3 * c] = m11 / det; lsq[3 * c + 1] = -m01 / det; lsq[3 * c + 2] = m00 / det;
+            }
+        // compute_wall_distance over the no-slip boundary faces
+        std::vector<int> wf;
+        for (size_t i = 0; i < mesh.faces.size(); ++i)
+            if (mesh.faces[i].cell_right == -1 && bcs[mesh.faces[i].patch_id].type == BC_NOSLIP) wf.push_back((int)i);
+        walld.assign(mesh.cells.size(), std::numeric_limits<double>::infinity());
+        if (wf.empty()) return;
+#pragma omp parallel for
+        for (long c = 0; c < (long)mesh.cells.size(); ++c) {
+            const Cell& cell = mesh.cells[c];
+            double m = std::numeric_limits<double>::infinity();
+            for (int fi : wf) {
+                const Face& f = mesh.faces[fi];
+                const Node& a = mesh.nodes[f.node1];
+                const Node& b = mesh.nodes[f.node2];
+                double dx = b.x - a.x, dy = b.y - a.y;
+                double ls = dx * dx + dy * dy;
+                double t = (ls > 0.0) ? ((cell.x_centroid - a.x) * dx + (cell.y_centroid - a.y) * dy) / ls : 0.0;
+                t = std::clamp(t, 0.0, 1.0);
+                double ex = cell.x_centroid - (a.x + t * dx), ey = cell.y_centroid - (a.y + t * dy);
+                m = std::min(m, ex * ex + ey * ey);
+            }
+            walld[c] = std::sqrt(m);
+        }
+    }
+
+    // GradientCalculator::compute for one scalar with boundary-face values.
+    void grad(const std::vector<double>& phi, const std::vector<double>& bphi, std::vector<G2>& g) const {
+        g.assign(mesh.cells.size(), G2{});
+        if (gradient == 1) {
+#pragma omp parallel for
+            for (long c = 0; c < (long)mesh.cells.size(); ++c) {
+                const Cell& cell = mesh.cells[c];
+                double sx = 0.0, sy = 0.0;
+                for (int fi : cell.faces) {
+                    const Face& f = mesh.faces[fi];
+                    double pf;
+                    if (f.cell_right == -1) pf = bphi[fi];
+                    else {
+                        int o = (f.cell_left == (int)c) ? f.cell_right : f.cell_left;
+                        double dc = std::hypot(cell.x_centroid - f.x_mid, cell.y_centroid - f.y_mid);
+                        double dn = std::hypot(mesh.cells[o].x_centroid - f.x_mid, mesh.cells[o].y_centroid - f.y_mid);
+                        double wc = dn / (dc + dn);
+                        pf = wc * phi[c] + (1.0 - wc) * phi[o];
+                    }
+                    double nx = f.cell_left == (int)c ? f.nx : -f.nx, ny = f.cell_left == (int)c ? f.ny : -f.ny;
+                    sx += pf * nx * f.area;
+                    sy += pf * ny * f.area;
+                }
+                g[c].x = sx / cell.volume;
+                g[c].y = sy / cell.volume;
+            }
+            return;
+        }
+#pragma omp parallel for
+        for (long c = 0; c < (long)mesh.cells.size(); ++c) {
+            const Cell& cell = mesh.cells[c];
+            double bx = 0.0, by = 0.0;
+            for (int fi : cell.faces) {
+                const Face& f = mesh.faces[fi];
+                double px, py, pn;
+                if (f.cell_right == -1) { px = f.x_mid; py = f.y_mid; pn = bphi[fi]; }
+                else {
+                    int nb = (f.cell_left == (int)c) ? f.cell_right : f.cell_left;
+                    px = mesh.cells[nb].x_centroid; py = mesh.cells[nb].y_centroid; pn = phi[nb];
+                }
+                double dx = px - cell.x_centroid, dy = py - cell.y_centroid;
+                double w = 1.0 / (dx * dx + dy * dy);
+                double d = pn - phi[c];
+                bx += w * dx * d;
+                by += w * dy * d;
+            }
+            g[c].x = lsq[3 * c] * bx + lsq[3 * c + 1] * by;
+            g[c].y = lsq[3 * c + 1] * bx + lsq[3 * c + 2] * by;
+        }
+    }
+
+    // face_normal_geometry: distance, cos theta and unit direction from the
+    // owner's centroid to the neighbour's centroid (boundary: the midpoint).
+    void face_geom(const Face& f, double& dist, double& cth, double& hx, double& hy) const {
+        const Cell& L = mesh.cells[f.cell_left];
+        bool b = f.cell_right == -1;
+        double xr = b ? f.x_mid : mesh.cells[f.cell_right].x_centroid;
+        double yr = b ? f.y_mid : mesh.cells[f.cell_right].y_centroid;
+        double dx = xr - L.x_centroid, dy = yr - L.y_centroid;
+        dist = std::hypot(dx, dy);
+        hx = dx / dist; hy = dy / dist;
+        cth = f.nx * hx + f.ny * hy;
+    }
+    FaceGrad face_gradient(const Face& f, double pL, double pR, const G2& gL, const G2& gR, double pb) const {
+        const Cell& L = mesh.cells[f.cell_left];
+        bool b = f.cell_right == -1;
+        double xr = b ? f.x_mid : mesh.cells[f.cell_right].x_centroid;
+        double yr = b ? f.y_mid : mesh.cells[f.cell_right].y_centroid;
+        double pRv = b ? pb : pR;
+        double dist, cth, hx, hy;
+        face_geom(f, dist, cth, hx, hy);
+        double direct = (pRv - pL) / (dist * cth);
+        double kx = f.nx - hx / cth, ky = f.ny - hy / cth;
+        G2 gf;
+        if (b) gf = gL;
+        else {
+            double dL = std::hypot(L.x_centroid - f.x_mid, L.y_centroid - f.y_mid);
+            double dR = std::hypot(xr - f.x_mid, yr - f.y_mid);
+            double wL = dR / (dL + dR);
+            gf.x = wL * gL.x + (1.0 - wL) * gR.x;
+            gf.y = wL * gL.y + (1.0 - wL) * gR.y;
+        }
+        return {direct + gf.x * kx + gf.y * ky, gf};
+    }
+    static G2 corrected(const FaceGrad& fg, double nx, double ny) {
+        double avg = fg.gf.x * nx + fg.gf.y * ny;
+        double d = fg.dn - avg;
+        return {fg.gf.x + d * nx, fg.gf.y + d * ny};
+    }
+    double temperature(const State& s) const { return pressure(s, gamma) / (s.rho * R); }
+
+    State ghost_ns(const Face& f, const State& UL) const {
+        const RansBC& bc = bcs[f.patch_id];
+        if (bc.type == BC_FARFIELD) return bc.state;
+        if (bc.type == BC_OUTFLOW) return UL;
+        double uL = UL.rho_u / UL.rho, vL = UL.rho_v / UL.rho;
+        double pL = pressure(UL, gamma);
+        return from_primitive(UL.rho, 2.0 * bc.wall_u - uL, 2.0 * bc.wall_v - vL, pL, gamma);
+    }
+    State numflux(const State& L, const State& Rs, double nx, double ny) const {
+        if (flux == 1) return hllc(L, Rs, nx, ny, gamma);
+        if (flux == 2) return exact(L, Rs, nx, ny, gamma, tol, maxit);
+        return rusanov(L, Rs, nx, ny, gamma);
+    }
+
+    double compute_dt() const {
+        double dt = std::numeric_limits<double>::max();
+#pragma omp parallel for reduction(min : dt)
+        for (long i = 0; i < (long)mesh.faces.size(); ++i) {
+            const Face& f = mesh.faces[i];
+            const State& UL = U[f.cell_left];
+            double uL = UL.rho_u / UL.rho, vL = UL.rho_v / UL.rho;
+            double VnL = uL * f.nx + vL * f.ny;
+            double Smax = std::fabs(VnL) + sound_speed(UL, gamma);
+            double rmin = UL.rho;
+            double ntmax = sa_nut(nut[f.cell_left], mu / UL.rho, sa);
+            if (f.cell_right != -1) {
+                const State& UR = U[f.cell_right];
+                double uR = UR.rho_u / UR.rho, vR = UR.rho_v / UR.rho;
+                double VnR = uR * f.nx + vR * f.ny;
+                Smax = std::max(Smax, std::fabs(VnR) + sound_speed(UR, gamma));
+                rmin = std::min(rmin, UR.rho);
+                ntmax = std::max(ntmax, sa_nut(nut[f.cell_right], mu / UR.rho, sa));
+            }
+            double dist, cth, hx, hy;
+            face_geom(f, dist, cth, hx, hy);
+            double length = dist * cth;
+            double nl = (mu > 0.0) ? mu / rmin : 0.0;
+            double ne = nl + ntmax;
+            double St = Smax + 2.0 * ne / length;
+            dt = std::min(dt, cfl * length / St);
+        }
+        return dt;
+    }
+
+    void step() {
+        double dt = compute_dt();
+        const size_t N = mesh.cells.size(), F = mesh.faces.size();
+        std::vector<double> u(N), v(N), T(N), nl(N), nt(N);
+        for (size_t c = 0; c < N; ++c) {
+            u[c] = U[c].rho_u / U[c].rho;
+            v[c] = U[c].rho_v / U[c].rho;
+            T[c] = temperature(U[c]);
+            nl[c] = mu / U[c].rho;
+            nt[c] = sa_nut(nut[c], nl[c], sa);
+        }
+        std::vector<double> bu(F, 0.0), bv(F, 0.0), bT(F, 0.0), bn(F, 0.0);
+        for (size_t i = 0; i < F; ++i) {
+            const Face& f = mesh.faces[i];
+            if (f.cell_right != -1) continue;
+            int cl = f.cell_left;
+            const RansBC& bc = bcs[f.patch_id];
+            if (bc.type == BC_NOSLIP) {
+                bu[i] = bc.wall_u; bv[i] = bc.wall_v; bT[i] = bc.isothermal ? bc.wall_T : T[cl];
+                bn[i] = 0.0;
+            } else {
+                bu[i] = u[cl]; bv[i] = v[cl]; bT[i] = T[cl];
+                bn[i] = bc.type == BC_FARFIELD ? bc.nut : nut[cl];
+            }
+        }
+        std::vector<G2> gu, gv, gT, gn;
+        grad(u, bu, gu);
+        grad(v, bv, gv);
+        grad(T, bT, gT);
+        grad(nut, bn, gn);
+        std::vector<double> src(N);
+#pragma omp parallel for
+        for (long c = 0; c < (long)N; ++c) {
+            double omega = std::fabs(gv[c].x - gu[c].y);
+            src[c] = sa_source(nut[c], nl[c], omega, walld[c], gn[c], sa);
+        }
+        double cp = gamma * R / (gamma - 1.0);
+        std::vector<State> ff(F);
+        std::vector<double> nf(F);
+#pragma omp parallel for
+        for (long i = 0; i < (long)F; ++i) {
+            const Face& f = mesh.faces[i];
+            int cl = f.cell_left, cr = f.cell_right;
+            bool b = cr == -1;
+            const State& UL = U[cl];
+            State UR = b ? ghost_ns(f, UL) : U[cr];
+            State inv = numflux(UL, UR, f.nx, f.ny);
+            double uRg = UR.rho_u / UR.rho, vRg = UR.rho_v / UR.rho;
+            double Vn = 0.5 * ((u[cl] + uRg) * f.nx + (v[cl] + vRg) * f.ny);
+            double nR = b ? bn[i] : nut[cr];
+            double nup = (Vn >= 0.0) ? nut[cl] : nR;
+            double nadv = Vn * nup * f.area;
+            State vis;
+            double ndiff = 0.0;
+            bool visc = !b || bcs[f.patch_id].type == BC_NOSLIP;
+            if (visc) {
+                double pu = b ? bu[i] : u[cr], pv = b ? bv[i] : v[cr], pT = b ? bT[i] : T[cr];
+                G2 gru = b ? G2{} : gu[cr], grv = b ? G2{} : gv[cr], grT = b ? G2{} : gT[cr];
+                FaceGrad fu = face_gradient(f, u[cl], pu, gu[cl], gru, bu[i]);
+                FaceGrad fv = face_gradient(f, v[cl], pv, gv[cl], grv, bv[i]);
+                FaceGrad fT = face_gradient(f, T[cl], pT, gT[cl], grT, bT[i]);
+                G2 a = corrected(fu, f.nx, f.ny), bb = corrected(fv, f.nx, f.ny), cT = corrected(fT, f.nx, f.ny);
+                double nlR = b ? nl[cl] : nl[cr];
+                double ntR = b ? sa_nut(bn[i], nlR, sa) : nt[cr];
+                double rR = b ? U[cl].rho : U[cr].rho;
+                double tdv = 0.5 * (U[cl].rho * nt[cl] + rR * ntR);
+                double mue = mu + tdv;
+                double ke = cp * mu / Pr + cp * tdv / Prt;
+                double uf = b ? bu[i] : 0.5 * (u[cl] + u[cr]);
+                double vf = b ? bv[i] : 0.5 * (v[cl] + v[cr]);
+                double dv = a.x + bb.y;
+                double txx = mue * (2.0 * a.x - (2.0 / 3.0) * dv);
+                double tyy = mue * (2.0 * bb.y - (2.0 / 3.0) * dv);
+                double txy = mue * (a.y + bb.x);
+                double qx = -ke * cT.x, qy = -ke * cT.y;
+                if (b && !bcs[f.patch_id].isothermal) { qx = 0.0; qy = 0.0; }
+                vis.rho_u = txx * f.nx + txy * f.ny;
+                vis.rho_v = txy * f.nx + tyy * f.ny;
+                vis.E = (uf * txx + vf * txy - qx) * f.nx + (uf * txy + vf * tyy - qy) * f.ny;
+                double nlf = 0.5 * (nl[cl] + nlR);
+                double ntf = 0.5 * (nt[cl] + ntR);
+                G2 grn = b ? G2{} : gn[cr];
+                FaceGrad fn = face_gradient(f, nut[cl], nR, gn[cl], grn, bn[i]);
+                double dif = (nlf + ntf) / sa.sigma;
+                ndiff = -dif * fn.dn * f.area;
+            }
+            ff[i] = f.area * (inv - vis);
+            nf[i] = nadv + ndiff;
+        }
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0;
+#pragma omp parallel for reduction(+ : s0, s1, s2, s3, s4)
+        for (long c = 0; c < (long)N; ++c) {
+            State r;
+            double rn = 0.0;
+            for (int fi : mesh.cells[c].faces) {
+                const Face& f = mesh.faces[fi];
+                if ((long)f.cell_left == c) { r = r - ff[fi]; rn -= nf[fi]; }
+                else { r += ff[fi]; rn += nf[fi]; }
+            }
+            rn += mesh.cells[c].volume * src[c];
+            s0 += r.rho * r.rho; s1 += r.rho_u * r.rho_u; s2 += r.rho_v * r.rho_v; s3 += r.E * r.E; s4 += rn * rn;
+            U[c] += (dt / mesh.cells[c].volume) * r;
+            nut[c] += (dt / mesh.cells[c].volume) * rn;
+        }
+        last[0] = std::sqrt(s0); last[1] = std::sqrt(s1); last[2] = std::sqrt(s2); last[3] = std::sqrt(s3);
+        last[4] = std::sqrt(s4);
+    }
+};
+
 }  // namespace orc
 
 // =========================================================== C API ======
@@ -836,6 +1196,56 @@ void orc_diff_run(void* dp, int n, double* hist) {
 void orc_diff_field(void* dp, double* out) {
     auto* d = static_cast<orc::Diffusion*>(dp);
     std::memcpy(out, d->phi.data(), d->phi.size() * sizeof(double));
+}
+
+// RANS-SA (RANSTurbulenceSASolver): per patch bc_type (BC_NOSLIP,
+// BC_FARFIELD, BC_OUTFLOW), bc_state [4] (farfield, conserved), bc_wall [4]
+// (wall_u, wall_v, wall_T, farfield nu-tilde), bc_iso (isothermal wall);
+// ic[14] as orc_euler_create; iopt[3]: flux, gradient (0 LSQ, 1 GG), maxit;
+// dopt[8]: gamma, R, mu, Pr, Pr_t, cfl, exact tol, initial nu-tilde.
+void* orc_rans_create(void* mp, const int* bc_type, const double* bc_state, const double* bc_wall, const int* bc_iso,
+                      const double* ic, const int* iopt, const double* dopt) {
+    auto* m = static_cast<orc::Mesh*>(mp);
+    auto* r = new orc::Rans;
+    r->mesh = *m;
+    r->gamma = dopt[0]; r->R = dopt[1]; r->mu = dopt[2]; r->Pr = dopt[3]; r->Prt = dopt[4]; r->cfl = dopt[5];
+    r->tol = dopt[6];
+    r->flux = iopt[0]; r->gradient = iopt[1]; r->maxit = iopt[2];
+    r->bcs.resize(m->n_patches);
+    for (int p = 0; p < m->n_patches; ++p) {
+        orc::RansBC& b = r->bcs[p];
+        b.type = bc_type[p];
+        b.state = {bc_state[4 * p], bc_state[4 * p + 1], bc_state[4 * p + 2], bc_state[4 * p + 3]};
+        b.wall_u = bc_wall[4 * p]; b.wall_v = bc_wall[4 * p + 1]; b.wall_T = bc_wall[4 * p + 2];
+        b.nut = bc_wall[4 * p + 3];
+        b.isothermal = bc_iso[p];
+    }
+    size_t N = m->cells.size();
+    r->U.resize(N);
+    r->nut.assign(N, dopt[7]);
+    for (size_t i = 0; i < N; ++i) {
+        if (ic[0] == 0.0) r->U[i] = orc::from_primitive(ic[1], ic[2], ic[3], ic[4], r->gamma);
+        else if (m->cells[i].x_centroid < ic[13]) r->U[i] = orc::from_primitive(ic[5], ic[6], ic[7], ic[8], r->gamma);
+        else r->U[i] = orc::from_primitive(ic[9], ic[10], ic[11], ic[12], r->gamma);
+    }
+    r->setup();
+    return r;
+}
+void orc_rans_free(void* r) { delete static_cast<orc::Rans*>(r); }
+// n steps; hist [5 n] (four mean-flow residual norms and nu-tilde's), may be NULL
+void orc_rans_run(void* rp, int n, double* hist) {
+    auto* r = static_cast<orc::Rans*>(rp);
+    for (int s = 0; s < n; ++s) {
+        r->step();
+        if (hist) std::memcpy(hist + 5 * (size_t)s, r->last, sizeof(r->last));
+    }
+}
+// field [4 N] conserved, nut [N], walld [N]; each may be NULL
+void orc_rans_get(void* rp, double* field, double* nut, double* walld) {
+    auto* r = static_cast<orc::Rans*>(rp);
+    if (field) std::memcpy(field, r->U.data(), r->U.size() * sizeof(orc::State));
+    if (nut) std::memcpy(nut, r->nut.data(), r->nut.size() * sizeof(double));
+    if (walld) std::memcpy(walld, r->walld.data(), r->walld.size() * sizeof(double));
 }
 
 int orc_num_threads(void) {

@@ -49,6 +49,11 @@ def lib():
         L.orc_diff_free.argtypes = [C.c_void_p]
         L.orc_diff_run.argtypes = [C.c_void_p, C.c_int, _D]
         L.orc_diff_field.argtypes = [C.c_void_p, _D]
+        L.orc_rans_create.restype = C.c_void_p
+        L.orc_rans_create.argtypes = [C.c_void_p, _I, _D, _D, _I, _D, _I, _D]
+        L.orc_rans_free.argtypes = [C.c_void_p]
+        L.orc_rans_run.argtypes = [C.c_void_p, C.c_int, _D]
+        L.orc_rans_get.argtypes = [C.c_void_p, _D, _D, _D]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -171,6 +176,49 @@ class OracleDiffusion:
     def __del__(self):
         if getattr(self, "h", None):
             lib().orc_diff_free(self.h)
+            self.h = None
+
+
+class OracleRANS:
+    """CPU RANS-SA solver (RANSTurbulenceSASolver).  ``bcs``: per patch a dict
+    with ``type`` ("noslip", "farfield", "outflow"), and as the kind needs
+    ``state`` (conserved farfield state), ``nut`` (farfield nu-tilde),
+    ``wall_u``, ``wall_v``, ``wall_T`` (isothermal when given).  ``ic`` as
+    :class:`OracleEuler`; ``flux`` 0 Rusanov / 1 HLLC / 2 exact, ``gradient``
+    0 least squares / 1 Green-Gauss."""
+
+    KINDS = {"noslip": 4, "farfield": 1, "outflow": 2}
+
+    def __init__(self, mesh: OracleMesh, bcs, gamma, R, mu, Pr, Prt, cfl, ic, nut0, flux=0, gradient=0, tol=1e-6,
+                 maxit=20):
+        icv = [0.0, ic["rho"], ic["u"], ic["v"], ic["p"]] + [0.0] * 9
+        bt = np.array([self.KINDS[b["type"]] for b in bcs], dtype=np.intc)
+        bs = np.array([list(b.get("state", (0.0, 0.0, 0.0, 0.0))) for b in bcs], dtype=np.float64).reshape(-1)
+        bw = np.array([[b.get("wall_u", 0.0), b.get("wall_v", 0.0), b.get("wall_T", 0.0), b.get("nut", 0.0)]
+                       for b in bcs], dtype=np.float64).reshape(-1)
+        iso = np.array([1 if "wall_T" in b else 0 for b in bcs], dtype=np.intc)
+        iopt = np.array([flux, gradient, maxit], dtype=np.intc)
+        dopt = np.array([gamma, R, mu, Pr, Prt, cfl, tol, nut0], dtype=np.float64)
+        self.mesh = mesh
+        self.n_cells = mesh.n_cells
+        self.h = lib().orc_rans_create(mesh.h, bt.ctypes.data_as(_I), _d(bs), _d(bw), iso.ctypes.data_as(_I),
+                                       _d(np.array(icv)), iopt.ctypes.data_as(_I), _d(dopt))
+
+    def run(self, n: int) -> np.ndarray:
+        """n steps; history [n, 5] (rho, rho_u, rho_v, E and nu-tilde residual norms)."""
+        hist = np.zeros((n, 5))
+        lib().orc_rans_run(self.h, n, hist.ctypes.data_as(_D))
+        return hist
+
+    def get(self):
+        """(conserved field [N, 4], nu-tilde [N], wall distance [N])."""
+        f, nt, wd = np.zeros((self.n_cells, 4)), np.zeros(self.n_cells), np.zeros(self.n_cells)
+        lib().orc_rans_get(self.h, f.ctypes.data_as(_D), nt.ctypes.data_as(_D), wd.ctypes.data_as(_D))
+        return f, nt, wd
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_rans_free(self.h)
             self.h = None
 
 
