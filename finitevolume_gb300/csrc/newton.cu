@@ -270,6 +270,13 @@ __global__ void k_axpy_state(St* __restrict__ x, const St* __restrict__ y, int n
     st_state(x, c, ld_state(x, c) + ld_state(y, c));
 }
 
+// out = a + b
+__global__ void k_add_state(St* __restrict__ out, const St* __restrict__ a, const St* __restrict__ b, int n) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    st_state(out, c, ld_state(a, c) + ld_state(b, c));
+}
+
 // out = a - b
 __global__ void k_sub_state(St* __restrict__ out, const St* __restrict__ a, const St* __restrict__ b, int n) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -434,6 +441,9 @@ namespace {
 // kRelGrow the CFL number may grow; above kRelFail it is halved.
 constexpr double kRelGrow = 0.7;
 constexpr double kRelFail = 0.9;
+// Relative residual target of the inner GMRES cycle of an adjoint
+// pseudo-transient iteration.
+constexpr double kInnerRtol = 1e-2;
 
 struct NewtonWork {
     int N = 0, m = 0;
@@ -886,23 +896,42 @@ int fv_adjoint_solve_krylov(fv_adjoint_t A, const double* dJdU, double cfl, int3
         adjh::upload(A, dJdU, W.du);
         nk::k_neg<<<nk::blocks(s.N), nk::kB, 0, st>>>(W.R, W.du, s.N);
         check_launch();
+        // With A = -dR/dU the adjoint system is A^T lam = b, b = -dJ/dU.
+        // Pseudo-transient outer iterations: (V/dt + A)^T delta = b - A^T lam
+        // by one GMRES(restart) cycle, lam += delta; the shifted operator is
+        // the transpose of the primal Newton system, so the iteration
+        // contracts like the primal's steps at the same CFL number.
         auto op = [&](const St* z, St* w) {
             adjh::vjp_dev(A, z, W.Jx);
-            nk::k_neg<<<nk::blocks(W.N), nk::kB, 0, st>>>(w, W.Jx, W.N);
+            nk::k_ptc<<<nk::blocks(W.N), nk::kB, 0, st>>>(A->a.D, z, W.Jx, w, W.N);
             check_launch();
         };
         auto pc = [&](const St* v, St* z) { precondition_t(A, W, v, z, precond_sweeps, st); };
+        St* r = W.z2;
+        St* delta = W.Mz;
+        const double bnorm = norm2(W, reinterpret_cast<const double*>(W.R), W.scal, st);
         double rel = 1.0;
-        // history: relative residual estimate after every restart cycle
+        // history: relative residual |b - A^T lam| / |b| before every outer iteration
         std::vector<double> hh;
         int mv = 0;
         FV_CUDA(cudaMemsetAsync(A->lam, 0, sizeof(St) * (size_t)s.N, st));
-        while (mv < max_matvec) {
-            const int k = gmres_gen(W, W.R, A->lam, false, restart, std::min(max_matvec - mv, restart + 1), rtol, &rel,
+        while (bnorm > 0.0) {
+            // r = b - A^T lam = b + (dR/dU)^T lam
+            adjh::vjp_dev(A, A->lam, W.Jx);
+            nk::k_add_state<<<nk::blocks(s.N), nk::kB, 0, st>>>(r, W.R, W.Jx, s.N);
+            check_launch();
+            ++mv;
+            rel = norm2(W, reinterpret_cast<const double*>(r), W.scal, st) / bnorm;
+            if (!std::isfinite(rel)) fvgb::raise(FV_ERR_NONFINITE, "fv_adjoint_solve_krylov: non-finite residual");
+            hh.push_back(rel);
+            if (rel <= rtol || mv >= max_matvec) break;
+            double rin = 1.0;
+            const int k = gmres_gen(W, r, delta, true, restart, std::min(restart, max_matvec - mv), kInnerRtol, &rin,
                                     st, op, pc);
             mv += k;
-            hh.push_back(rel);
-            if (rel <= rtol || k == 0) break;
+            nk::k_axpy_state<<<nk::blocks(s.N), nk::kB, 0, st>>>(A->lam, delta, s.N);
+            check_launch();
+            if (k == 0) break;
         }
         adjh::lin_dt(A, cfl_primal);
         // residual of (dR/dU)^T lam - dJ/dU, per component

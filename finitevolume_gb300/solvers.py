@@ -502,9 +502,9 @@ class DiscreteAdjoint:
                                                    capi.dptr(Ub), capi.dptr(fb)))
         return Ub, fb[:self.n_patches]
 
-    # preconditioner of method "krylov": pseudo-time CFL number and sweeps
-    krylov_cfl = 1e4
-    krylov_sweeps = 2
+    # method "krylov": pseudo-time CFL number and preconditioner sweeps
+    krylov_cfl = 1e3
+    krylov_sweeps = 3
 
     def solve(self, dJdU, max_iter: int = 20000, tol: float = 1e-12, method: str = "rk", restart: int = 40):
         """Solve (dR/dU)^T lambda = dJdU.  method "rk": SSP-RK3 pseudo-time
@@ -512,11 +512,12 @@ class DiscreteAdjoint:
         [iterations, 4] of those norms); "gmres": GMRES(restart) on the
         fixed point of that iteration until its residual falls by the
         factor tol, max_iter matvecs (history [matvecs] of the relative
-        GMRES residual); "krylov": GMRES(restart) on (dR/dU)^T itself,
-        preconditioned by Gauss-Seidel sweeps of the transposed first-order
-        Jacobian (``krylov_cfl``, ``krylov_sweeps``), until its residual
-        falls by the factor tol, max_iter matvecs (history: relative
-        residual per restart cycle).  Returns lambda, fsbar, history, iterations; the
+        GMRES residual); "krylov": pseudo-transient outer iterations on
+        the transposed Newton system at CFL ``krylov_cfl``, each one
+        GMRES(restart) cycle preconditioned by ``krylov_sweeps`` Gauss-Seidel
+        sweeps of the transposed first-order Jacobian, until the adjoint
+        residual falls by the factor tol, max_iter matvecs (history:
+        relative residual per outer iteration).  Returns lambda, fsbar, history, iterations; the
         final residual norms are kept in ``last_residual`` for "gmres"."""
         lam = np.zeros((self.n, 4))
         fb = np.zeros((_MAX_PATCHES, 4))
@@ -531,7 +532,7 @@ class DiscreteAdjoint:
             self.last_residual = res
             return lam, fb[:self.n_patches], hist[:it.value], it.value
         if method == "krylov":
-            hist = np.zeros(max(max_iter // max(restart, 1) + 2, 1))
+            hist = np.zeros(max(max_iter // 2 + 2, 1))
             res = np.zeros(4)
             capi.check(capi.lib().fv_adjoint_solve_krylov(self._h, capi.dptr(g), float(self.krylov_cfl), int(restart),
                                                           int(max_iter), float(tol), int(self.krylov_sweeps),

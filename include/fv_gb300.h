@@ -378,16 +378,19 @@ int fv_adjoint_solve(fv_adjoint_t a, const double* dJdU, int32_t max_iter, doubl
  * Other outputs as fv_adjoint_solve; each may be NULL. */
 int fv_adjoint_solve_gmres(fv_adjoint_t a, const double* dJdU, int32_t restart, int32_t max_matvec, double rtol,
                            double* lambda, double* fsbar, double* history, int32_t* matvecs, double residual[4]);
-/* The same adjoint system by restarted GMRES(restart) on (dR/dU)^T directly,
- * right-preconditioned by symmetric block Gauss-Seidel sweeps (over a cell
- * colouring) of the transposed first-order Jacobian plus V/dt at the given
- * CFL number (a large one, e.g. 1e4, for a converged state): for converged
- * transonic states, where the pseudo-time iteration is slow.  Stops when the
- * GMRES residual is below rtol |dJdU| or after max_matvec products;
- * history [restart cycles] the relative residual after each cycle (at most
- * max_matvec / restart + 1 entries); residual[4] the norms of
- * (dR/dU)^T lam - dJdU.  Other outputs as fv_adjoint_solve; each may be
- * NULL. */
+/* The same adjoint system by pseudo-transient iterations with the Newton
+ * solver's linear algebra, for converged transonic states where the explicit
+ * pseudo-time iteration is slow: with A = -dR/dU, each outer iteration
+ * solves (V/dt + A)^T delta = -dJdU - A^T lambda by one GMRES(restart) cycle
+ * (to a relative residual of 1e-2), right-preconditioned by symmetric block
+ * Gauss-Seidel sweeps (over a cell colouring) of the transposed first-order
+ * Jacobian plus V/dt, V/dt at the given CFL number (the one the primal
+ * Newton iteration reached), and adds delta to lambda.  Stops when
+ * |(dR/dU)^T lambda - dJdU| is below rtol |dJdU| or after max_matvec
+ * products; history [outer iterations] that relative residual before each
+ * outer iteration (at most max_matvec / 2 + 1 entries);
+ * residual[4] the norms of (dR/dU)^T lambda - dJdU.  Other outputs as
+ * fv_adjoint_solve; each may be NULL. */
 int fv_adjoint_solve_krylov(fv_adjoint_t a, const double* dJdU, double cfl, int32_t restart, int32_t max_matvec,
                             double rtol, int32_t precond_sweeps, double* lambda, double* fsbar, double* history,
                             int32_t* matvecs, double residual[4]);
