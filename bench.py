@@ -375,6 +375,112 @@ def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 
     return out
 
 
+def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_newton: int = 200,
+                           n_seq: int = 24, seed: int = 1, cd_tol: float = 1e-5, fp32_max_iter: int = 4000,
+                           fp32_chunk: int = 250) -> dict:
+    """Converged steady solves per second of the 256-instance family, every
+    solve to its own L2 density residual below ``tol``.
+
+    The steady solver: ``warm`` SSP-RK3 iterations, the limiter frozen at
+    the state they reach, then Newton-Krylov on the frozen-limiter residual
+    (the explicit iteration alone limit-cycles on the transonic half).
+    - FP64 batched: all instances in one batch, one block-diagonal Newton
+      solve with per-instance CFL numbers and early exit.
+    - FP64 sequential (the plain GPU path): the same procedure, one plain
+      solver per instance, for a seeded sample of ``n_seq`` instances, each
+      timed in full to convergence; solves/s over that sample.
+    - FP32-flux batched (mixed precision; FP32 flux and gradients, FP64
+      accumulation, update and norms): the same warm-up and frozen limiter,
+      then explicit SSP-RK3 with agglomeration multigrid; an instance counts
+      as converged once |CD - CD_fp64| <= ``cd_tol`` against its converged
+      FP64 drag at two consecutive checkpoints (every ``fp32_chunk``
+      iterations) and is then frozen; at most ``fp32_max_iter`` iterations.
+    All wall times are host-side around the solver calls, ending in a
+    device synchronisation.
+    """
+    import torch
+    from finitevolume_gb300 import capi
+    n = len(meshes)
+    refs = [(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0) for fs in fss]
+    out = {"instances": n, "tol_l2_density": tol, "warm_rk3_iterations": warm,
+           "cells_total": int(sum(m.n_cells for m in meshes))}
+    # FP64 batched
+    b = _batch_solver(meshes, fss, False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run(warm)
+    b.freeze_limiter(True)
+    _, it = b.newton(max_newton=max_newton, tol=tol)
+    torch.cuda.synchronize()
+    tb = time.perf_counter() - t0
+    steps = b.last_newton_instance_steps.copy()
+    conv = steps >= 0
+    cd64 = np.array([b.wall_forces(i, *refs[i])["cd_total"] for i in range(n)])
+    del b
+    out["f64_batched"] = {"solves_per_s": round(int(conv.sum()) / tb, 4), "seconds": round(tb, 2),
+                          "converged": int(conv.sum()), "newton_steps": int(it),
+                          "instance_newton_steps_median": float(np.median(steps[conv])) if conv.any() else None}
+    # FP64 sequential, seeded sample, each solve timed in full
+    rng = np.random.default_rng(seed)
+    sample = np.sort(rng.choice(n, size=min(n_seq, n), replace=False))
+    ts, nconv, dcd = 0.0, 0, []
+    for i in sample:
+        s = _plain_solver(meshes[i], fss[i], False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ok = False
+        try:
+            s.run(warm)
+            s.freeze_limiter(True)
+            s.newton(max_newton=max_newton, tol=tol)
+            ok = bool(s.last_newton_instance_steps[0] >= 0)
+        except capi.FVError:
+            pass
+        torch.cuda.synchronize()
+        ts += time.perf_counter() - t0
+        if ok:
+            nconv += 1
+            if conv[i]:
+                dcd.append(abs(s.wall_forces(*refs[i])["cd_total"] - cd64[i]))
+        del s
+    out["f64_sequential"] = {"solves_per_s": round(nconv / ts, 4), "seconds": round(ts, 2), "converged": nconv,
+                             "sample": [int(i) for i in sample],
+                             "max_abs_dCD_vs_batched": float(max(dcd)) if dcd else None}
+    out["f64_batched"]["speedup_vs_sequential"] = round(out["f64_batched"]["solves_per_s"] /
+                                                        max(out["f64_sequential"]["solves_per_s"], 1e-30), 2)
+    # FP32-flux batched, drag criterion against the converged FP64 drag
+    b = _batch_solver(meshes, fss, True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run(warm)
+    b.freeze_limiter(True)
+    b.multigrid()
+    hits = np.zeros(n, np.int64)
+    conv32 = np.zeros(n, bool)
+    done = warm
+    while done < fp32_max_iter:
+        b.run(fp32_chunk)
+        done += fp32_chunk
+        for i in np.nonzero(conv & ~conv32)[0]:
+            cd = b.wall_forces(int(i), *refs[i])["cd_total"]
+            hits[i] = hits[i] + 1 if abs(cd - cd64[i]) <= cd_tol else 0
+            if hits[i] >= 2:
+                conv32[i] = True
+                b.set_active(int(i), False)
+        if conv32[conv].all():
+            break
+    torch.cuda.synchronize()
+    t32 = time.perf_counter() - t0
+    del b
+    out["fp32_flux_batched"] = {"solves_per_s": round(int(conv32.sum()) / t32, 4), "seconds": round(t32, 2),
+                                "converged": int(conv32.sum()), "iterations": int(done),
+                                "criterion": f"|CD - CD_fp64| <= {cd_tol} at two consecutive checkpoints",
+                                "solver": "explicit SSP-RK3 + 4-level agglomeration multigrid, frozen limiter"}
+    out["fp32_flux_batched"]["speedup_vs_f64_sequential"] = round(
+        out["fp32_flux_batched"]["solves_per_s"] / max(out["f64_sequential"]["solves_per_s"], 1e-30), 2)
+    return out
+
+
 def adjoint_cost(iters: int = 200, warm: int = 300):
     """Discrete adjoint against the primal on the 500k-cell NACA0012 O-grid
     (1024 x 488), M 0.75, AoA 2 deg, 2nd-order HLLC + LSQ/Venkatakrishnan,
@@ -415,7 +521,30 @@ def adjoint_cost(iters: int = 200, warm: int = 300):
                     "cost_vs_primal_per_iter": round(ta / tp, 3),
                     "cost_vs_primal_1000_iters": round((tl + 1000 * ta) / (1000 * tp), 3)}
         del adj
-    del s
+    # Converged: the primal to 1e-11 (SSP-RK3 warm-up from this state on,
+    # limiter frozen, Newton-Krylov), then the frozen-limiter drag adjoint
+    # to a relative residual of 1e-10 by pseudo-transient iterations on the
+    # transposed Newton system; wall times from the start of the primal.
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s2 = _plain_solver(mesh, fs, False)
+    s2.run(warm)
+    s2.freeze_limiter()
+    hp, kp = s2.newton(max_newton=400, tol=1e-11)
+    torch.cuda.synchronize()
+    tprim = time.perf_counter() - t0
+    adj = S.DiscreteAdjoint(s2, full_limiter=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gd = adj.freestream_gradient(S.Objective.Drag, M, aoa, [1], max_iter=40000, tol=1e-10, method="krylov")
+    torch.cuda.synchronize()
+    tadj = time.perf_counter() - t0
+    out["converged"] = {"primal_seconds": round(tprim, 2), "primal_residual": float(hp[-1, 0]),
+                        "primal_newton_steps": int(kp), "primal_warm_rk3_iterations": warm,
+                        "adjoint_seconds": round(tadj, 2), "adjoint_matvecs": gd["iterations"],
+                        "adjoint_residual": gd["adjoint_residual"], "dCD_dM": gd["dJ_dM"],
+                        "adjoint_vs_converged_primal": round(tadj / tprim, 3)}
+    del adj, s2, s
     return out
 
 
@@ -431,20 +560,27 @@ def _converge(s, tol: float, max_iter: int, chunk: int = 250):
     return done, last
 
 
-def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, freeze_after: int = 3000,
-                  max_cycles: int = 30000, adj_iters: int = 60000, adj_tol: float = 1e-13):
+def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, warm: int = 300, max_newton: int = 600,
+                  fd_tol: float = 1e-13, fd_max_newton: int = 200, sweeps: int = 8, adj_cfl: float = 3e3,
+                  adj_tol: float = 1e-10, adj_max_matvec: int = 40000):
     """Gradients of the 500k-cell NACA0012 O-grid case (1024 x 488, M 0.75,
-    AoA 2 deg, 2nd-order HLLC + LSQ/Venkatakrishnan K=5, SSP-RK3, local dt,
-    CFL 1.2) from the discrete adjoint against central differences of
-    converged primal solves: dCD/dM, dCD/dAoA, and dCL/dX along ``n_dirs``
-    seeded wall-normal displacement fields smoothed over 20 wall nodes,
-    step h.  The primal limit-cycles through the limiter's switching (its
-    residual stalls near 1e-3 even with multigrid), so the limiter is
-    frozen after ``freeze_after`` multigrid cycles and the frozen-limiter
-    scheme is converged to ``tol``; the differences are taken with the
-    limiter frozen at those values, so the frozen-limiter adjoint is the
-    exact linearisation and the full-limiter one differs by the limiter's
-    sensitivity."""
+    AoA 2 deg, 2nd-order HLLC + LSQ/Venkatakrishnan K=5, local dt) from the
+    discrete adjoint against central differences of converged primal
+    solves: dCD/dM, dCD/dAoA, and dCL/dX along ``n_dirs`` seeded
+    wall-normal displacement fields smoothed over 20 wall nodes, step h.
+
+    Primal: ``warm`` SSP-RK3 iterations, the limiter frozen there (the
+    live limiter limit-cycles near 1e-3 on this transonic case), then
+    Newton-Krylov on the frozen-limiter residual to ``tol``.  The
+    differences are converged the same way from the base state, to
+    ``fd_tol``, with the limiter frozen at the same values, so the
+    frozen-limiter adjoint is the exact linearisation of what they
+    difference; the full-limiter adjoint differs by the limiter's own
+    sensitivity.  Adjoint solves: pseudo-transient iterations on the
+    transposed Newton system at CFL ``adj_cfl`` to a relative residual of
+    ``adj_tol``.  Reported: relative errors, and the adjoint wall time
+    (drag + lift adjoints and the shape gradient) as a multiple of the
+    converged primal solve's."""
     import torch
     from finitevolume_gb300 import capi, meshgen, solvers as S
     M, aoa = 0.75, 2.0
@@ -463,18 +599,18 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, freeze_
     mesh = S.Mesh(poly, reorder="morton")
     fs = fs_of(M, aoa)
     out = {"workload": "naca0012 O-grid 1024x488, M 0.75, AoA 2, 2nd-order HLLC, LSQ + Venkatakrishnan K=5, "
-                       "SSP-RK3, local dt, CFL 1.2, 4-level multigrid",
+                       "local dt; primal: SSP-RK3 warm-up, limiter frozen, Newton-Krylov",
            "cells": mesh.n_cells, "tol_l2_density": tol, "h_shape": h, "directions": n_dirs}
     s = _plain_solver(mesh, fs, False)
-    s.multigrid()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    c1, r1 = _converge(s, tol, freeze_after)
+    s.run(warm)
     s.freeze_limiter()
-    c2, r2 = _converge(s, tol, max_cycles)
+    hp, kp = s.newton(max_newton=max_newton, tol=tol, precond_sweeps=sweeps)
+    torch.cuda.synchronize()
     tprimal = time.perf_counter() - t0
     psi = s.limiter_values()
-    out["primal"] = {"cycles_before_freeze": c1, "residual_at_freeze": r1, "cycles_frozen": c2, "residual": r2,
+    out["primal"] = {"warm_iterations": warm, "newton_steps": kp, "residual": float(hp[-1, 0]),
                      "seconds": round(tprimal, 2), "cells_limited": int((psi < 1.0).any(axis=1).sum())}
     log({"primal": out["primal"]})
     U0 = s.field()
@@ -485,12 +621,14 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, freeze_
     for full in (False, True):
         key = "full_limiter" if full else "frozen_limiter"
         adj = S.DiscreteAdjoint(s, full_limiter=full)
+        adj.krylov_cfl, adj.krylov_sweeps = adj_cfl, sweeps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         try:
-            gd = adj.freestream_gradient(S.Objective.Drag, M, aoa, [1], max_iter=adj_iters, tol=adj_tol)
+            gd = adj.freestream_gradient(S.Objective.Drag, M, aoa, [1], max_iter=adj_max_matvec, tol=adj_tol,
+                                         method="krylov")
             _, g = S.force_gradient(s, S.Objective.Lift, ref_of(M, aoa))
-            _, _, hist, it = adj.solve(g, adj_iters, adj_tol)
+            _, _, hist, it = adj.solve(g, adj_max_matvec, adj_tol, method="krylov")
             gl = adj.shape_gradient(S.Objective.Lift, ref_of(M, aoa))
         except capi.FVError as e:
             out[key] = {"error": str(e)}
@@ -500,9 +638,9 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, freeze_
         torch.cuda.synchronize()
         ta = time.perf_counter() - t0
         out[key] = {
-            "dCD_dM": gd["dJ_dM"], "dCD_dAoA_deg": gd["dJ_dAoA_deg"], "drag_iterations": gd["iterations"],
-            "drag_adjoint_residual": gd["adjoint_residual"], "lift_iterations": it,
-            "lift_adjoint_residual": hist[-1].tolist() if len(hist) else None,
+            "dCD_dM": gd["dJ_dM"], "dCD_dAoA_deg": gd["dJ_dAoA_deg"], "drag_matvecs": gd["iterations"],
+            "drag_adjoint_residual": gd["adjoint_residual"], "lift_matvecs": it,
+            "lift_adjoint_rel_residual": float(hist[-1]) if len(hist) else None,
             "dCL_dX_dirs": [float(np.sum(gl * d)) for d in dirs], "seconds": round(ta, 2),
             "seconds_vs_primal": round(ta / tprimal, 3)}
         log({key: out[key]})
@@ -510,7 +648,8 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, freeze_
 
     def frozen_solve(sp):
         sp.set_field(U0)
-        return _converge(sp, tol, max_cycles)
+        hh, k = sp.newton(max_newton=fd_max_newton, tol=fd_tol, precond_sweeps=sweeps)
+        return k, float(hh[-1, 0])
 
     # central differences, limiter frozen at psi: freestream
     hM, ha = 1e-6, 1e-5
@@ -518,33 +657,32 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, freeze_
     for key, (m, al) in {"M+": (M + hM, aoa), "M-": (M - hM, aoa), "a+": (M, aoa + ha), "a-": (M, aoa - ha)}.items():
         sp = _plain_solver(mesh, fs_of(m, al), False)
         sp.set_limiter_values(psi)
-        sp.multigrid()
         c, r = frozen_solve(sp)
         fd[key] = (sp.wall_forces(*ref_of(m, al))["cd_total"], c, r)
         del sp
     out["fd_freestream"] = {"dCD_dM": (fd["M+"][0] - fd["M-"][0]) / (2 * hM),
                             "dCD_dAoA_deg": (fd["a+"][0] - fd["a-"][0]) / (2 * ha),
                             "h_M": hM, "h_aoa_deg": ha,
-                            "cycles": [fd[k][1] for k in fd], "residuals": [fd[k][2] for k in fd]}
+                            "newton_steps": [fd[k][1] for k in fd], "residuals": [fd[k][2] for k in fd]}
     log({"fd_freestream": out["fd_freestream"]})
     # shape (one solver, geometry moved on the device)
     sp = _plain_solver(mesh, fs, False)
     sp.set_limiter_values(psi)
-    sp.multigrid()
     X = poly.nodes.copy()
-    fd_cl, cycles, resids = [], [], []
+    fd_cl, steps, resids = [], [], []
     for d in dirs:
         v = {}
         for sgn in (1, -1):
             sp.update_nodes(X + sgn * h * d)
             c, r = frozen_solve(sp)
-            cycles.append(c)
+            steps.append(c)
             resids.append(r)
             v[sgn] = sp.wall_forces(*ref_of(M, aoa))["cl"]
         fd_cl.append((v[1] - v[-1]) / (2 * h))
     sp.update_nodes(X)
-    out["fd_shape"] = {"dCL_dX_dirs": fd_cl, "cycles_median": float(np.median(cycles)),
+    out["fd_shape"] = {"dCL_dX_dirs": fd_cl, "newton_steps_median": float(np.median(steps)),
                        "residual_max": float(np.max(resids))}
+    log({"fd_shape": out["fd_shape"]})
     fdv = np.array(fd_cl)
     for key in ("frozen_limiter", "full_limiter"):
         o = out[key]
@@ -1032,6 +1170,7 @@ def main():
                 "speedup_vs_sequential": round(rb / rs, 3), "iterations": it,
                 "cells_total": int(sum(m.n_cells for m in bm)),
                 "workload": "256 NACA 4-digit O-grids, 4k-64k cells log-uniform, M 0.3-0.85, AoA -4..8"}
+        variants["batched_converged"] = batch_converged_newton(bm, bfs)
         del bm
         variants["adjoint_500k"] = adjoint_cost()
         variants["rans_sa_2M"] = rans_sa_rate()

@@ -695,7 +695,7 @@ void fv_newton_default(fv_newton_t* o) {
     o->cfl_growth = 1.5;
     o->krylov_dim = 80;
     o->krylov_rtol = 1e-2;
-    o->precond_sweeps = 3;
+    o->precond_sweeps = 8;
     o->precond_kind = 1;
     o->max_rel_change = 0.2;
 }

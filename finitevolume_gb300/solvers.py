@@ -503,8 +503,8 @@ class DiscreteAdjoint:
         return Ub, fb[:self.n_patches]
 
     # method "krylov": pseudo-time CFL number and preconditioner sweeps
-    krylov_cfl = 1e3
-    krylov_sweeps = 3
+    krylov_cfl = 3e3
+    krylov_sweeps = 8
 
     def solve(self, dJdU, max_iter: int = 20000, tol: float = 1e-12, method: str = "rk", restart: int = 40):
         """Solve (dR/dU)^T lambda = dJdU.  method "rk": SSP-RK3 pseudo-time
