@@ -1071,6 +1071,7 @@ void linearise(fv_adjoint_s* A) {
         o.lim_gu = A->Gu;
         o.lim_psi = A->psi;
         o.active = nullptr;
+        o.d2 = nullptr;  // limited gradients into G (the linearisation reads them)
         fvgb::o2::launch_prim_f64(o, s.stream);
         check_launch();
         fvgb::o2::launch_part_f64(o, s.cfg, 0, 0, s.stream);

@@ -224,15 +224,21 @@ __device__ __forceinline__ V4<T> hllc_p(const V4<T>& L, const V4<T>& R, T nx, T 
     if (SR <= T(0)) return phys_flux_p(R, R.p * igm1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v), VnR, nx, ny);
     const T dL = SL - VnL, dR = SR - VnR;
     T mL = L.r * dL, mR = R.r * dR;
-    // A reciprocal plus a multiply issues fewer FP64 instructions than a
-    // general division on this part.
-    T Ss = (R.p - L.p + mL * VnL - mR * VnR) * (T(1) / (mL - mR));
-    bool left = Ss >= T(0);
+    // S* = num / den with den = m_L - m_R < 0 (S_L < Vn_L and S_R > Vn_R),
+    // so the side is known before any division: S* >= 0 <=> num <= 0.  Both
+    // S* and q = 1 / (S_K - S*) = den / (S_K den - num) then come from one
+    // reciprocal of den (S_K den - num), which issues fewer FP64-pipe
+    // instructions on this part than two.
+    const T num = R.p - L.p + mL * VnL - mR * VnR, den = mL - mR;
+    bool left = num <= T(0);
     T SK = left ? SL : SR, VnK = left ? VnL : VnR;
     T mK = left ? mL : mR, dK = left ? dL : dR;
     V4<T> K = left ? L : R;
     const T EK = K.p * igm1 + T(0.5) * K.r * (K.u * K.u + K.v * K.v);
-    T q = T(1) / (SK - Ss);
+    const T t = SK * den - num;
+    const T rr = T(1) / (den * t);
+    const T Ss = num * (t * rr);
+    T q = den * (den * rr);
     T fac = mK * q;
     T VtK = -K.u * ny + K.v * nx;
     T mn = fac * Ss, mt = fac * VtK;
@@ -438,9 +444,26 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
                 for (int k = 0; k < 4; ++k) a.lim_psi[4 * c + k] = 1.0;
         }
     }
+    // FP64 with a limiter: k_face reconstructs from the per-entry
+    // increments and the per-cell limiter values (O2Args::d2); the limited
+    // gradients are not stored.
+    bool dpath = false;
+    if constexpr (sizeof(T) == 8) dpath = LIM != 0 && a.d2 != nullptr;
     if (LIM != 0 && a.psi_mode == 2) {
         // frozen limiter: the values captured earlier (psi = 1 scales exactly)
         const T* pb = static_cast<const T*>(a.psi_buf) + 4 * (size_t)c;
+        if constexpr (sizeof(T) == 8) {
+            if (dpath) {
+                for (int e = e0; e < e1; ++e) {
+                    T rx, ry;
+                    ld_pair<T>(a.erf, e, rx, ry);
+                    st_state(a.d2, e, st_make(gx[0] * rx + gy[0] * ry, gx[1] * rx + gy[1] * ry,
+                                              gx[2] * rx + gy[2] * ry, gx[3] * rx + gy[3] * ry));
+                }
+                st_state(a.psi4, c, st_make(pb[0], pb[1], pb[2], pb[3]));
+                return;
+            }
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const T psi = pb[k];
@@ -466,14 +489,20 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
         for (int e = e0; e < e1; ++e) {
             T rx, ry;
             ld_pair<T>(a.erf, e, rx, ry);
+            T d2v[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const I b = OK::bits(gx[k] * rx + gy[k] * ry);
+                d2v[k] = gx[k] * rx + gy[k] * ry;
+                const I b = OK::bits(d2v[k]);
                 pmax[k] = pmax[k] < b ? b : pmax[k];
                 const I bn = b ^ sign;
                 nmax[k] = nmax[k] < bn ? bn : nmax[k];
             }
+            if constexpr (sizeof(T) == 8) {
+                if (dpath) st_state(a.d2, e, st_make(d2v[0], d2v[1], d2v[2], d2v[3]));
+            }
         }
+        T psiv[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             T nmin = T(1), dmn = T(1);
@@ -520,9 +549,16 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock, sizeof(T) == 4 ? 2 : 1) k_gra
                 if (a.lim_psi) a.lim_psi[4 * c + k] = psi;
             }
             if (a.psi_mode == 1) static_cast<T*>(a.psi_buf)[4 * (size_t)c + k] = psi;
-            if (lim) {
+            psiv[k] = psi;
+            if (lim && !dpath) {
                 gx[k] *= psi;
                 gy[k] *= psi;
+            }
+        }
+        if constexpr (sizeof(T) == 8) {
+            if (dpath) {
+                st_state(a.psi4, c, st_make(psiv[0], psiv[1], psiv[2], psiv[3]));
+                return;
             }
         }
     }
@@ -540,6 +576,14 @@ __device__ __forceinline__ V4<T> recon(const V4<T>& w, const G8<T>& g, T rx, T r
     // Positivity fallback; "x > 0" tested on the integer pipe (sign bit clear
     // and not +0).
     if (OKey<T>::bits(o.r) <= 0 || OKey<T>::bits(o.p) <= 0) return w;
+    return o;
+}
+
+// w + psi * inc (the limited increment to the face, one multiply-add per
+// variable), with recon's positivity fallback.
+__device__ __forceinline__ V4<double> recon_inc(const V4<double>& w, const St& psi, const St& inc) {
+    const V4<double> o = {psi.r * inc.r + w.r, psi.ru * inc.ru + w.u, psi.rv * inc.rv + w.v, psi.E * inc.E + w.p};
+    if (OKey<double>::bits(o.r) <= 0 || OKey<double>::bits(o.p) <= 0) return w;
     return o;
 }
 
@@ -574,7 +618,15 @@ __global__ void __launch_bounds__(fvgb::kMaxBlock) k_face(const O2Args a) {
         face_geom<T>(a, f, nx, ny, ar, len);
         V4<T> wl = WS::ld(W, L), wr;
         const V4<T> wlc = wl;
-        if (ORDER == 2) {
+        bool dpath = false;
+        if constexpr (sizeof(T) == 8) dpath = ORDER == 2 && a.d2 != nullptr;
+        if (dpath) {
+            if constexpr (sizeof(T) == 8) {
+                const int2 ee = __ldg(a.fe + f);
+                wl = recon_inc(wl, ld_state(a.psi4, L), ld_state(a.d2, ee.x));
+                if (R >= 0) wr = recon_inc(WS::ld(W, R), ld_state(a.psi4, R), ld_state(a.d2, ee.y));
+            }
+        } else if (ORDER == 2) {
             T rxl, ryl, rxr, ryr;
             ld_quad<T>(a.frf, f, rxl, ryl, rxr, ryr);
             const G8<T> gl = GStore<T>::ld(static_cast<const typename GStore<T>::type*>(a.G), L);

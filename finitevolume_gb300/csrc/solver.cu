@@ -232,6 +232,18 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
         frf = up(h2.d_frf);
         eps2 = cfg.fp32 ? static_cast<const void*>(dupload(e32, owned)) : static_cast<const void*>(dupload(e64, owned));
         if (cfg.fp32) fgeom32 = reinterpret_cast<const float4*>(dupload(to_float(hm.d_fgeom), owned));
+        if (!cfg.fp32 && cfg.order == 2 && cfg.limiter != 0) {
+            const size_t E = h2.d_cf.size();
+            std::vector<int2> fev(F, make_int2(-1, -1));
+            for (size_t e = 0; e < E; ++e) {
+                const int ent = h2.d_cf[e];
+                if (ent & 1) fev[ent >> 1].x = (int)e;
+                else fev[ent >> 1].y = (int)e;
+            }
+            d2 = dalloc<St>(E, owned);
+            psi4 = dalloc<St>(N, owned);
+            fe = dupload(fev, owned);
+        }
     }
 
     if (batch) {
@@ -456,6 +468,9 @@ O2Args Solver::o2_args() const {
     a.lim_psi = nullptr;
     a.psi_buf = psi_buf;
     a.psi_mode = psi_mode;
+    a.d2 = d2;
+    a.psi4 = psi4;
+    a.fe = fe;
     a.forcing = forcing;
     a.resid = nullptr;
     return a;

@@ -104,6 +104,9 @@ struct Solver {
     const float4* fgeom32 = nullptr;
     const St* forcing = nullptr;    // multigrid coarse levels: FAS forcing term
     void* psi_buf = nullptr;        // frozen limiter values [4N], flux precision
+    St* d2 = nullptr;               // FP64 live limiter: per-entry increments [E] (O2Args::d2)
+    St* psi4 = nullptr;             //   and per-cell limiter values [N]
+    int2* fe = nullptr;             //   owner / neighbour entry per face [F]
     int psi_mode = 0;               // 0 evaluated, 2 frozen (see O2Args)
 
     // Persistent first-order path (order 1, forward Euler, FP64 Euler): one

@@ -125,6 +125,16 @@ struct O2Args {
     // instead of evaluating the limiter; 0 neither.
     void* psi_buf;
     int psi_mode;
+    // FP64 live-limiter reconstruction (null otherwise): per cell-face
+    // entry the unlimited increment g . (x_f - x_c) of the four primitives,
+    // per cell the four limiter values, and per face the entries of its
+    // owner and neighbour (-1 on a boundary face).  With psi_mode != 2
+    // k_grad writes the first two instead of the limited gradients, and
+    // k_face reconstructs W + psi * increment: the increments k_grad forms
+    // for the limiter anyway are not formed a second time.
+    St* d2;
+    St* psi4;
+    const int2* fe;
     // Multigrid (null otherwise): a forcing term added to every cell's
     // residual (coarse levels of the full-approximation scheme), and the
     // output of the residual-only pass.
