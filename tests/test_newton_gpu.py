@@ -13,6 +13,8 @@ Newton path is that it drives the same discrete residual to zero:
   block-diagonal system converges per instance, and every instance's field
   equals its standalone Newton solve (1e-8 relative: both are converged to
   1e-12 along different paths, not bit for bit);
+- the Krylov adjoint at a Newton-converged transonic state matches central
+  differences of Newton solves (1e-5 relative);
 - the options are validated before any device work.
 """
 import numpy as np
@@ -97,3 +99,35 @@ def test_newton_rejects_bad_options(gpu):
         with pytest.raises(capi.FVError):
             s.newton(max_newton=5, **kw)
     assert np.array_equal(s.field(), u0)
+
+
+def test_krylov_adjoint_matches_differences_of_newton_solves(gpu):
+    """The pseudo-transient Krylov adjoint (fv_adjoint_solve_krylov) at a
+    Newton-converged transonic state (frozen limiter): dCD/dM and dCD/dAoA
+    against central differences of Newton solves converged to 1e-13 from the
+    base state with the limiter frozen at the same values."""
+    poly = meshgen.naca_ogrid(64, 32)
+    M, aoa = 0.75, 2.0
+    s, fs = _solver(poly, M, aoa)
+    s.run(300)
+    s.freeze_limiter(True)
+    h, _ = s.newton(max_newton=200, tol=1e-12)
+    assert h[-1, 0] < 1e-12
+    U0, psi = s.field().copy(), s.limiter_values()
+    adj = S.DiscreteAdjoint(s, full_limiter=False)
+    gd = adj.freestream_gradient(S.Objective.Drag, M, aoa, [1], max_iter=20000, tol=1e-11, method="krylov")
+    assert max(gd["adjoint_residual"]) < 1e-9
+
+    def cd_at(m, al):
+        sp, f = _solver(poly, m, al)
+        sp.set_limiter_values(psi)
+        sp.set_field(U0)
+        hh, _ = sp.newton(max_newton=200, tol=1e-13)
+        assert hh[-1, 0] < 1e-13
+        return sp.wall_forces(*f, 1.0, 0.25, 0.0)["cd_total"]
+
+    hM, ha = 1e-6, 1e-5
+    fd_m = (cd_at(M + hM, aoa) - cd_at(M - hM, aoa)) / (2 * hM)
+    fd_a = (cd_at(M, aoa + ha) - cd_at(M, aoa - ha)) / (2 * ha)
+    assert abs(gd["dJ_dM"] - fd_m) <= 1e-5 * abs(fd_m), (gd["dJ_dM"], fd_m)
+    assert abs(gd["dJ_dAoA_deg"] - fd_a) <= 1e-5 * abs(fd_a), (gd["dJ_dAoA_deg"], fd_a)
