@@ -258,3 +258,35 @@ def test_gmres_adjoint_matches_pseudo_time_solution(gpu):
     # (small components to 1e-7 of the largest)
     assert np.allclose(fb_gm, fb_rk, rtol=1e-7, atol=1e-7 * np.abs(fb_rk).max())
 
+
+
+def test_frozen_residual_shape_cotangent_matches_central_differences(gpu):
+    """With the limiter frozen in the solver (active limiter, transonic
+    flow), the frozen-limiter map (dR/dX)^T Rbar against central
+    differences of the frozen-limiter residual under node displacements
+    (the map the shape-gradient checks of frozen solves rely on)."""
+    poly = meshgen.naca_ogrid(96, 48, r_far=10.0)
+    mesh = S.Mesh(poly)
+    s = _solver(mesh, _fs(0.75, 2.0), 2, S.NumericalFluxScheme.HLLC, S.Limiter.Venkatakrishnan)
+    s.run(400)
+    s.freeze_limiter()
+    assert (s.limiter_values() < 1.0).any()
+    U = s.field()
+    X = poly.nodes.copy()
+    x, y = X[:, 0], X[:, 1]
+    rng = np.random.default_rng(3)
+    Rb = rng.standard_normal(U.shape)
+    adj = S.DiscreteAdjoint(s, full_limiter=False)
+    for d in (0.1 * np.stack([np.sin(0.7 * x + 0.3 * y), np.cos(0.5 * x - 0.9 * y)], 1),
+              _wall_normal_directions(poly, 1, seed=4)[0]):
+        h = 1e-7
+        s.update_nodes(X + h * d)
+        Rp = adj.forward(U)
+        s.update_nodes(X - h * d)
+        Rm = adj.forward(U)
+        s.update_nodes(X)
+        adj.forward(U)
+        fd = float(np.sum(Rb * (Rp - Rm))) / (2 * h)
+        scale = float(np.sum(np.abs(Rb * (Rp - Rm)))) / (2 * h)
+        e = abs(float(np.sum(adj.shape_vjp(Rb) * d)) - fd) / scale
+        assert e < 1e-6, (e, fd, scale)
