@@ -1170,7 +1170,6 @@ def main():
                 "speedup_vs_sequential": round(rb / rs, 3), "iterations": it,
                 "cells_total": int(sum(m.n_cells for m in bm)),
                 "workload": "256 NACA 4-digit O-grids, 4k-64k cells log-uniform, M 0.3-0.85, AoA -4..8"}
-        variants["batched_converged"] = batch_converged_newton(bm, bfs)
         del bm
         variants["adjoint_500k"] = adjoint_cost()
         variants["rans_sa_2M"] = rans_sa_rate()
