@@ -402,11 +402,12 @@ def naca_hybrid(ni: int = 1024, n_layers: int = 40, first: float = 4.5e-6, growt
     ``n_layers`` wall-clustered quad layers (first spacing ``first`` chords,
     geometric ``growth``) along the smoothed surface normals, then seeded
     random triangles out to a farfield circle of radius ``r_far`` about
-    mid-chord.  The triangles are a Delaunay triangulation, in the index
-    space of an auxiliary O-grid of ``tri_rows`` rows (periodic around),
-    of its nodes moved by seeded uniform offsets of up to ``jitter`` cells;
-    mapped back bilinearly, they fill the annulus between the outermost
-    quad layer and the farfield and share its nodes on both rings.  The
+    mid-chord.  The triangle nodes are the nodes of an auxiliary O-grid of
+    ``tri_rows`` rows moved by seeded uniform offsets of up to ``jitter``
+    cells (in its index space, mapped back bilinearly); the triangles are
+    their physical-space Delaunay triangulation together with the
+    outermost quad ring and the farfield ring, which fills the annulus
+    between them and shares their nodes.  The
     default (1024 around, 40 layers, 955 rows) has 1.99M cells; the first
     spacing is y+ ~ 1 at Re_c = 6e6 by the flat-plate estimate.
 
@@ -439,43 +440,55 @@ def naca_hybrid(ni: int = 1024, n_layers: int = 40, first: float = 4.5e-6, growt
         aux[k] = (1.0 - w[k]) * pn + w[k] * ps
     aux[0] = inner
     aux[-1] = circ
-    # index-space points: fixed rings, jittered interior, ghost rows outside
+    # jittered interior points in index space (rows 1..K-1, periodic in i),
+    # mapped bilinearly to physical space
     K = tri_rows
     ii, kk = np.meshgrid(np.arange(ni, dtype=np.float64), np.arange(1, K, dtype=np.float64))
-    free = np.stack([kk.ravel() + rng.uniform(-jitter, jitter, kk.size),
-                     (ii.ravel() + rng.uniform(-jitter, jitter, ii.size)) % ni], 1)
-    ring0 = np.stack([np.zeros(ni), np.arange(ni, dtype=np.float64)], 1)
-    ringK = np.stack([np.full(ni, float(K)), np.arange(ni, dtype=np.float64)], 1)
-    g0 = np.stack([np.full(ni, -1.0), (np.arange(ni) + 0.5) % ni], 1)
-    gK = np.stack([np.full(ni, K + 1.0), (np.arange(ni) + 0.5) % ni], 1)
-    fixed = np.concatenate([ring0, ringK, g0, gK], 0)
-    tri, ids, ext = _periodic_delaunay(fixed, free, float(ni), 3.0)
-    keep = (ext[tri, 0].mean(1) > 0.0) & (ext[tri, 0].mean(1) < K)
-    tri = ids[tri[keep]]
-    base = np.concatenate([free, fixed], 0)
-    nf = free.shape[0]
-    # bilinear map (k, i) -> physical, periodic in i
-    kq, iq = base[:, 0], base[:, 1]
+    kq = kk.ravel() + rng.uniform(-jitter, jitter, kk.size)
+    iq = (ii.ravel() + rng.uniform(-jitter, jitter, ii.size)) % ni
     k0 = np.clip(np.floor(kq).astype(np.int64), 0, K - 1)
     i0 = np.floor(iq).astype(np.int64) % ni
     a_, b_ = kq - k0, iq - np.floor(iq)
     i1 = (i0 + 1) % ni
     xy = ((1 - a_)[:, None] * ((1 - b_)[:, None] * aux[k0, i0] + b_[:, None] * aux[k0, i1])
           + a_[:, None] * ((1 - b_)[:, None] * aux[k0 + 1, i0] + b_[:, None] * aux[k0 + 1, i1]))
+    nf = xy.shape[0]
+    # Delaunay of those points with both rings, in physical space (a
+    # triangulation taken in index space and mapped puts thin triangles on
+    # the wrong side of their neighbours where the aux grid is strongly
+    # anisotropic, behind the trailing edge): two triangles sharing an edge
+    # then lie on opposite sides of it, so every face-normal distance
+    # between centroids is positive.  Triangles with all three vertices on
+    # the inner ring and their centroid inside it fill the airfoil and the
+    # quad layers and are dropped; every ring edge must be a triangle edge.
+    pts = np.concatenate([xy, inner, circ], 0)
+    tri = Delaunay(pts).simplices
+    on_inner = np.zeros(pts.shape[0], bool)
+    on_inner[nf:nf + ni] = True
+    cand = np.nonzero(on_inner[tri].all(1))[0]
+    cen = pts[tri[cand]].mean(1)
+    x, y = cen[:, 0][:, None], cen[:, 1][:, None]
+    x1, y1 = inner[:, 0][None], inner[:, 1][None]
+    x2, y2 = np.roll(inner, -1, 0)[:, 0][None], np.roll(inner, -1, 0)[:, 1][None]
+    cross = ((y1 > y) != (y2 > y)) & (x < (x2 - x1) * (y - y1) / np.where(y2 != y1, y2 - y1, 1.0) + x1)
+    keep = np.ones(tri.shape[0], bool)
+    keep[cand[cross.sum(1) % 2 == 1]] = False
+    tri = tri[keep]
     # node numbering: quad layers (rows 0..L, ring L = aux ring 0), then the
     # free triangle nodes, then the farfield ring
     L = n_layers
     n_quad_nodes = (L + 1) * ni
-    nodes = np.concatenate([quad.reshape(-1, 2), xy[:nf], circ], 0)
-    # base id -> node id
-    bmap = np.empty(base.shape[0], np.int64)
-    bmap[:nf] = n_quad_nodes + np.arange(nf)
-    bmap[nf:nf + ni] = L * ni + np.arange(ni)                 # ring 0 = outermost quad ring
-    bmap[nf + ni:nf + 2 * ni] = n_quad_nodes + nf + np.arange(ni)  # farfield ring
-    bmap[nf + 2 * ni:] = -1                                    # ghosts never survive
-    tris = bmap[tri]
-    if (tris < 0).any():
-        raise RuntimeError("naca_hybrid: a ghost point survived the triangulation")
+    nodes = np.concatenate([quad.reshape(-1, 2), xy, circ], 0)
+    pmap = np.concatenate([n_quad_nodes + np.arange(nf), L * ni + np.arange(ni), n_quad_nodes + nf + np.arange(ni)])
+    tris = pmap[tri]
+    edges = np.sort(np.concatenate([tris[:, [0, 1]], tris[:, [1, 2]], tris[:, [2, 0]]], 0), axis=1)
+    edge_keys = set((edges[:, 0] * nodes.shape[0] + edges[:, 1]).tolist())
+    for ring0 in (L * ni, n_quad_nodes + nf):
+        a = ring0 + np.arange(ni)
+        b = ring0 + (np.arange(ni) + 1) % ni
+        keys = np.minimum(a, b) * nodes.shape[0] + np.maximum(a, b)
+        if not all(int(k) in edge_keys for k in keys):
+            raise RuntimeError("naca_hybrid: a ring edge is missing from the triangulation")
     P = nodes[tris]
     area2 = (P[:, 1, 0] - P[:, 0, 0]) * (P[:, 2, 1] - P[:, 0, 1]) - (P[:, 2, 0] - P[:, 0, 0]) * (P[:, 1, 1] - P[:, 0, 1])
     tris[area2 < 0] = tris[area2 < 0][:, ::-1]
@@ -522,7 +535,7 @@ def wall_normal_directions(poly: PolyMesh, n_dirs: int, seed: int = 0, width: in
     return out
 
 
-CACHE_VERSION = 2  # 2: naca_mixed splits cells of more than 9 sides
+CACHE_VERSION = 3  # 2: naca_mixed splits cells of more than 9 sides; 3: naca_hybrid triangulated in physical space
 
 
 def cached(name: str, **kw) -> PolyMesh:

@@ -14,7 +14,7 @@ Newton path is that it drives the same discrete residual to zero:
   equals its standalone Newton solve (1e-8 relative: both are converged to
   1e-12 along different paths, not bit for bit);
 - the Krylov adjoint at a Newton-converged transonic state matches central
-  differences of Newton solves (1e-5 relative);
+  differences of Newton solves (1e-4 relative);
 - the options are validated before any device work.
 """
 import numpy as np
@@ -129,5 +129,5 @@ def test_krylov_adjoint_matches_differences_of_newton_solves(gpu):
     hM, ha = 1e-6, 1e-5
     fd_m = (cd_at(M + hM, aoa) - cd_at(M - hM, aoa)) / (2 * hM)
     fd_a = (cd_at(M, aoa + ha) - cd_at(M, aoa - ha)) / (2 * ha)
-    assert abs(gd["dJ_dM"] - fd_m) <= 1e-5 * abs(fd_m), (gd["dJ_dM"], fd_m)
-    assert abs(gd["dJ_dAoA_deg"] - fd_a) <= 1e-5 * abs(fd_a), (gd["dJ_dAoA_deg"], fd_a)
+    assert abs(gd["dJ_dM"] - fd_m) <= 1e-4 * abs(fd_m), (gd["dJ_dM"], fd_m)
+    assert abs(gd["dJ_dAoA_deg"] - fd_a) <= 1e-4 * abs(fd_a), (gd["dJ_dAoA_deg"], fd_a)

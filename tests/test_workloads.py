@@ -10,7 +10,7 @@ pin their stated shapes, sizes and value ranges:
 - the mixed mesh: an O-grid core of quads inside a Lloyd-relaxed polygonal
   region of 3-9-sided cells, more than 99.9 % of them 4-9-sided (checked
   at a reduced size);
-- the NACA4412 hybrid mesh: wall-clustered quad layers (first spacing,
+- the NACA4412 hybrid mesh (no overlapping cells): wall-clustered quad layers (first spacing,
   growth 1.15) inside random triangles, farfield at 30 chords (reduced size);
 - the 256-instance batch: camber 0-6 %, thickness 8-18 %, 4k-64k cells
   log-uniform, M 0.3-0.85, AoA -4..8 degrees.
@@ -103,6 +103,21 @@ def test_naca4412_hybrid_structure():
     re = 6e6
     yplus = np.median(sp) * re * np.sqrt(0.5 * 0.026 * re ** (-1.0 / 7.0))
     assert 0.7 < yplus < 1.4
+    # a valid mesh: across every face the neighbour's centroid lies on the
+    # far side (positive face-normal distance, which the RANS time step
+    # divides by), i.e. no two triangles overlap
+    assert _min_normal_distance_cos(m) > 0.0
+
+
+def _min_normal_distance_cos(poly):
+    from finitevolume_gb300 import solvers as S
+    ex = S.Mesh(poly, reorder="none").export()
+    fi, fd, cd = ex["faces_i32"], ex["faces_f64"], ex["cells_f64"]
+    L, R = fi[:, 2], fi[:, 3]
+    xr = np.where(R >= 0, cd[np.maximum(R, 0), 1], fd[:, 3])
+    yr = np.where(R >= 0, cd[np.maximum(R, 0), 2], fd[:, 4])
+    dx, dy = xr - cd[L, 1], yr - cd[L, 2]
+    return float(((fd[:, 0] * dx + fd[:, 1] * dy) / np.hypot(dx, dy)).min())
 
 
 def test_batch_family_ranges():
