@@ -391,11 +391,13 @@ def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_
       solver per instance, for a seeded sample of ``n_seq`` instances, each
       timed in full to convergence; solves/s over that sample.
     - FP32-flux batched (mixed precision; FP32 flux and gradients, FP64
-      accumulation, update and norms): the same warm-up and frozen limiter,
-      then explicit SSP-RK3 with agglomeration multigrid; an instance counts
+      accumulation, update and norms): the same warm-up, then explicit
+      SSP-RK3 with agglomeration multigrid; an instance counts
       as converged once |CD - CD_fp64| <= ``cd_tol`` against its converged
       FP64 drag at two consecutive checkpoints (every ``fp32_chunk``
       iterations) and is then frozen; at most ``fp32_max_iter`` iterations.
+      Its limiter is frozen at the FP64 batch's values, so both precisions
+      solve the same discrete scheme.
     All wall times are host-side around the solver calls, ending in a
     device synchronisation.
     """
@@ -417,6 +419,7 @@ def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_
     steps = b.last_newton_instance_steps.copy()
     conv = steps >= 0
     cd64 = np.array([b.wall_forces(i, *refs[i])["cd_total"] for i in range(n)])
+    psi64 = np.concatenate([b.limiter_values(i) for i in range(n)], 0)
     del b
     out["f64_batched"] = {"solves_per_s": round(int(conv.sum()) / tb, 4), "seconds": round(tb, 2),
                           "converged": int(conv.sum()), "newton_steps": int(it),
@@ -454,7 +457,7 @@ def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b.run(warm)
-    b.freeze_limiter(True)
+    b.set_limiter_values(psi64)  # the same frozen-limiter scheme as the FP64 solves
     b.multigrid()
     hits = np.zeros(n, np.int64)
     conv32 = np.zeros(n, bool)

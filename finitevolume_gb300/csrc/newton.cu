@@ -418,6 +418,17 @@ __global__ void __launch_bounds__(kB) k_inst_alpha(const adjk::AdjArgs a, const 
     }
 }
 
+// Per instance: x *= s[i] (inverse: x /= s[i]).
+__global__ void __launch_bounds__(kB) k_inst_scale(St* __restrict__ x, const int* __restrict__ off,
+                                                  const double* __restrict__ s, int inverse) {
+    const int i = blockIdx.x;
+    const double k = s[i];
+    for (int c = off[i] + threadIdx.x; c < off[i + 1]; c += kB) {
+        const St v = ld_state(x, c);
+        st_state(x, c, inverse ? st_make(v.r / k, v.ru / k, v.rv / k, v.E / k) : k * v);
+    }
+}
+
 // Per instance: U += alpha[i] dU where mask[i]; U = Ubak where revert[i].
 __global__ void __launch_bounds__(kB) k_inst_update(St* __restrict__ U, const St* __restrict__ du,
                                                    const St* __restrict__ Ubak, const int* __restrict__ off,
@@ -746,6 +757,8 @@ int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history
         double* d_alpha = W.alloc<double>(ni);
         int* d_mask = W.alloc<int>(ni);
         int* d_revert = W.alloc<int>(ni);
+        double* d_scale = W.alloc<double>(ni);
+        std::vector<double> scale(ni, 1.0);
         std::vector<double> nr(4 * (size_t)ni), prev(ni, -1.0), cfl(ni, o.cfl0), last_cfl(ni, 0.0), alpha(ni, 0.0);
         std::vector<int> stepped(ni, 0), rejects(ni, 0), mask(ni, 0), revert(ni, 0), conv_at(ni, -1);
         FV_CUDA(cudaStreamSynchronize(st));
@@ -833,8 +846,29 @@ int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history
             nk::k_inst_prepare<<<ni, nk::kB, 0, st>>>(A->a.D, W.R, d_off, d_cfl, d_mask);
             nk::k_pc_diag<<<nk::blocks(s.N), nk::kB, 0, st>>>(A->a, W.Dinv);
             check_launch();
+            // The system is block diagonal over the instances, so scaling an
+            // instance's right-hand side scales only its own solution.  Each
+            // is scaled to unit norm before GMRES (and its solution back
+            // after): the minimisation then weighs every instance's
+            // equations alike instead of being dominated by the instances
+            // with the largest residuals.  One instance: a no-op up to
+            // rounding.
+            for (int i = 0; i < ni; ++i) {
+                const double r2 = nr[4 * i] * nr[4 * i] + nr[4 * i + 1] * nr[4 * i + 1] +
+                                  nr[4 * i + 2] * nr[4 * i + 2] + nr[4 * i + 3] * nr[4 * i + 3];
+                scale[i] = (mask[i] && r2 > 0.0 && std::isfinite(r2)) ? 1.0 / std::sqrt(r2) : 1.0;
+            }
+            if (ni > 1) {
+                FV_CUDA(cudaMemcpyAsync(d_scale, scale.data(), sizeof(double) * ni, cudaMemcpyHostToDevice, st));
+                nk::k_inst_scale<<<ni, nk::kB, 0, st>>>(W.R, d_off, d_scale, 0);
+                check_launch();
+            }
             double rel = 0.0;
             const int mv = gmres(A.get(), W, W.R, W.du, o.krylov_dim, o.krylov_rtol, o.precond_sweeps, &rel, st);
+            if (ni > 1) {
+                nk::k_inst_scale<<<ni, nk::kB, 0, st>>>(W.du, d_off, d_scale, 1);
+                check_launch();
+            }
             nk::k_inst_alpha<<<ni, nk::kB, 0, st>>>(A->a, W.du, d_off, o.max_rel_change, d_alpha);
             check_launch();
             FV_CUDA(cudaMemcpyAsync(alpha.data(), d_alpha, sizeof(double) * ni, cudaMemcpyDeviceToHost, st));

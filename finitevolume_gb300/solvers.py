@@ -739,6 +739,12 @@ class BatchSolver:
     newton = EulerFVMSolver.newton
     freeze_limiter = EulerFVMSolver.freeze_limiter
 
+    def set_limiter_values(self, psi) -> None:
+        """Freeze every instance's limiter at the given values [total cells,
+        4] (the instances' cells one after another)."""
+        capi.check(capi.lib().fv_solver_limiter_values(self._h, None,
+                                                       capi.dptr(np.ascontiguousarray(psi, dtype=np.float64))))
+
     def limiter_values(self, instance: int) -> np.ndarray:
         """The frozen limiter values [n_cells of the instance, 4]."""
         out = np.zeros((self.mesh.n_cells, 4))

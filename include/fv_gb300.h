@@ -425,7 +425,9 @@ int fv_residual_shape_vjp(fv_adjoint_t a, fv_mesh_t mesh, const double* Rbar, do
  * flux (least-squares gradients at second order), single or batched: a
  * batch is solved as one block-diagonal system in which every instance has
  * its own residual norms, CFL number, step length and undo decision and
- * stops once its own density residual is below tol.
+ * stops once its own density residual is below tol; each instance's
+ * right-hand side is scaled to unit norm for the GMRES solve, so that every
+ * instance's equations weigh alike.
  * --------------------------------------------------------------------- */
 typedef struct {
     int32_t limiter_mode;   /* FV_ADJ_FROZEN_LIMITER or FV_ADJ_FULL_LIMITER: the limiter's
