@@ -11,6 +11,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "../../include/fv_gb300.h"
@@ -265,6 +266,16 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
     if (viscous) {
         HostGradGeom hg;
         build_grad_geom(hm, hg);
+        // The viscous time step divides by the face-normal distance between
+        // the two centroids (face_normal_distance, src/GradientReconstruction
+        // .cpp:186-190); it is positive on any mesh whose cells do not
+        // overlap.  The reference takes the minimum over faces unguarded,
+        // so one non-positive distance makes its dt non-positive; it is
+        // refused here instead of being silently skipped by the device min.
+        for (int i = 0; i < F; ++i)
+            if (!(hg.fgrad[8 * (size_t)i + 5] > 0.0))
+                raise(FV_ERR_BAD_MESH, "face " + std::to_string(hm.fperm[i]) +
+                                           ": neighbouring centroids on one side (overlapping cells)");
         NSArgs& a = ns;
         a.g.n_cells = N;
         a.g.n_faces = F;

@@ -70,3 +70,21 @@ def test_ns_vs_reference(gpu, name, flux, grad, strict):
             "cd_total", "cl", "cm"]
     for i, k in enumerate(keys):
         assert abs(f[k] - total[i + 1]) <= 1e-10 * max(1.0, abs(total[i + 1])), k
+
+
+def test_overlapping_cells_are_refused(gpu):
+    """Two triangles on the same side of their shared edge (both valid
+    polygons, positive areas) put the neighbour's centroid behind the face:
+    the face-normal distance the viscous time step divides by is negative,
+    so the viscous solver refuses the mesh instead of stepping with it."""
+    from finitevolume_gb300 import capi
+    from finitevolume_gb300.fvmesh import from_cells
+    nodes = np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.9, 0.2]])
+    cells = [[0, 1, 2], [0, 3, 2]]
+    bedges = np.array([[0, 1], [1, 2], [0, 3], [3, 2]])
+    poly = from_cells(nodes, cells, bedges, np.zeros(4, np.int32), ["wall"])
+    bcs = [S.NSBoundaryCondition(S.NSBoundaryType.NoSlipWall)]
+    ic = S.EulerInitialCondition(S.EulerICMode.Freestream, rho=1.0, u=0.0, v=0.0, p=1.0 / GAMMA)
+    with pytest.raises(capi.FVError):
+        S.NavierStokesFVMSolver(S.Mesh(poly), bcs, GAMMA, 287.0, 1e-3, 0.72, 0.5, ic,
+                                S.NumericalFluxScheme.Rusanov, S.GradientScheme.GreenGauss)
