@@ -377,7 +377,7 @@ def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 
 
 def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_newton: int = 80,
                            n_seq: int = 12, seed: int = 1, cd_tol: float = 1e-5, fp32_max_iter: int = 3000,
-                           fp32_chunk: int = 250) -> dict:
+                           fp32_chunk: int = 250, round_steps: int = 20) -> dict:
     """Converged steady solves per second of a batch of the steady family,
     every solve to its own L2 density residual below ``tol`` within
     ``max_newton`` Newton steps (the same cap for every path).
@@ -386,7 +386,9 @@ def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_
     the state they reach, then Newton-Krylov on the frozen-limiter residual
     (the explicit iteration alone limit-cycles on the transonic half).
     - FP64 batched: all instances in one batch, one block-diagonal Newton
-      solve with per-instance CFL numbers and early exit.
+      solve with per-instance CFL numbers and early exit, in rounds of
+      ``round_steps`` Newton steps after which the unconverged instances
+      are repacked into a smaller batch.
     - FP64 sequential (the plain GPU path): the same procedure, one plain
       solver per instance, for a seeded sample of ``n_seq`` instances, each
       timed in full to convergence; solves/s over that sample.
@@ -407,22 +409,52 @@ def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_
     refs = [(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0) for fs in fss]
     out = {"instances": n, "tol_l2_density": tol, "warm_rk3_iterations": warm,
            "cells_total": int(sum(m.n_cells for m in meshes))}
-    # FP64 batched
+    # FP64 batched, in rounds: after each round the instances still
+    # unconverged are repacked into a smaller batch (their states and frozen
+    # limiter values carried over), so the shared Newton steps stop paying
+    # for instances that are done.
     b = _batch_solver(meshes, fss, False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b.run(warm)
     b.freeze_limiter(True)
-    _, it = b.newton(max_newton=max_newton, tol=tol)
+    psi64 = np.concatenate([b.limiter_values(i) for i in range(n)], 0)
+    off = np.cumsum([0] + [m.n_cells for m in meshes])
+    steps = np.full(n, -1, np.int64)
+    cd64 = np.full(n, np.nan)
+    live = np.arange(n)
+    done_steps, rounds = 0, []
+    while live.size and done_steps < max_newton:
+        k = min(round_steps, max_newton - done_steps)
+        # later rounds restart the CFL ramp higher (the controller halves it
+        # again where that is too much)
+        _, it = b.newton(max_newton=k, tol=tol, **({} if not rounds else {"cfl0": 200.0}))
+        st = b.last_newton_instance_steps.copy()
+        fld = b.field_all()
+        loff = np.cumsum([0] + [meshes[i].n_cells for i in live])
+        for j, i in enumerate(live):
+            if st[j] >= 0:
+                steps[i] = done_steps + st[j]
+                cd64[i] = b.wall_forces(j, *refs[i])["cd_total"]
+        rounds.append({"instances": int(live.size), "newton_steps": int(it), "converged": int((st >= 0).sum())})
+        done_steps += k
+        keep = st < 0
+        if not keep.any() or done_steps >= max_newton:
+            break
+        nxt = live[keep]
+        U = np.concatenate([fld[loff[j]:loff[j + 1]] for j in np.nonzero(keep)[0]], 0)
+        P = np.concatenate([psi64[off[i]:off[i + 1]] for i in nxt], 0)
+        del b
+        b = _batch_solver([meshes[i] for i in nxt], [fss[i] for i in nxt], False)
+        b.set_field(U)
+        b.set_limiter_values(P)
+        live = nxt
+    del b
     torch.cuda.synchronize()
     tb = time.perf_counter() - t0
-    steps = b.last_newton_instance_steps.copy()
     conv = steps >= 0
-    cd64 = np.array([b.wall_forces(i, *refs[i])["cd_total"] for i in range(n)])
-    psi64 = np.concatenate([b.limiter_values(i) for i in range(n)], 0)
-    del b
     out["f64_batched"] = {"solves_per_s": round(int(conv.sum()) / tb, 4), "seconds": round(tb, 2),
-                          "converged": int(conv.sum()), "newton_steps": int(it),
+                          "converged": int(conv.sum()), "rounds": rounds,
                           "instance_newton_steps_median": float(np.median(steps[conv])) if conv.any() else None}
     # FP64 sequential, seeded sample, each solve timed in full
     rng = np.random.default_rng(seed)
@@ -564,14 +596,16 @@ def _converge(s, tol: float, max_iter: int, chunk: int = 250):
     return done, last
 
 
-def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, warm: int = 300, max_newton: int = 600,
+def adjoint_check(n_dirs: int = 16, h: float = 1e-6, h_small: float = 1e-8, tol: float = 1e-11, warm: int = 300,
+                  max_newton: int = 600,
                   fd_tol: float = 1e-13, fd_max_newton: int = 200, sweeps: int = 8, adj_cfl: float = 3e3,
                   adj_tol: float = 1e-10, adj_max_matvec: int = 40000):
     """Gradients of the 500k-cell NACA0012 O-grid case (1024 x 488, M 0.75,
     AoA 2 deg, 2nd-order HLLC + LSQ/Venkatakrishnan K=5, local dt) from the
     discrete adjoint against central differences of converged primal
     solves: dCD/dM, dCD/dAoA, and dCL/dX along ``n_dirs`` seeded
-    wall-normal displacement fields smoothed over 20 wall nodes, step h.
+    wall-normal displacement fields smoothed over 20 wall nodes, at the
+    configured step h and at ``h_small``.
 
     Primal: ``warm`` SSP-RK3 iterations, the limiter frozen there (the
     live limiter limit-cycles near 1e-3 on this transonic case), then
@@ -671,33 +705,40 @@ def adjoint_check(n_dirs: int = 16, h: float = 1e-6, tol: float = 1e-11, warm: i
                             "h_M": hM, "h_aoa_deg": ha,
                             "newton_steps": [fd[k][1] for k in fd], "residuals": [fd[k][2] for k in fd]}
     log({"fd_freestream": out["fd_freestream"]})
-    # shape (one solver, geometry moved on the device)
+    # shape (one solver, geometry moved on the device), at the configured
+    # step h and at h_small: the differenced solves cross the kinks of the
+    # discrete scheme (wave-branch switches at sonic faces), so the central
+    # difference approaches the derivative only as h shrinks
     sp = _plain_solver(mesh, fs, False)
     sp.set_limiter_values(psi)
     X = poly.nodes.copy()
-    fd_cl, steps, resids = [], [], []
-    for d in dirs:
-        v = {}
-        for sgn in (1, -1):
-            sp.update_nodes(X + sgn * h * d)
-            c, r = frozen_solve(sp)
-            steps.append(c)
-            resids.append(r)
-            v[sgn] = sp.wall_forces(*ref_of(M, aoa))["cl"]
-        fd_cl.append((v[1] - v[-1]) / (2 * h))
+    fd_by_h = {}
+    for hh in (h, h_small):
+        fd_cl, steps, resids = [], [], []
+        for d in dirs:
+            v = {}
+            for sgn in (1, -1):
+                sp.update_nodes(X + sgn * hh * d)
+                c, r = frozen_solve(sp)
+                steps.append(c)
+                resids.append(r)
+                v[sgn] = sp.wall_forces(*ref_of(M, aoa))["cl"]
+            fd_cl.append((v[1] - v[-1]) / (2 * hh))
+        fd_by_h[hh] = fd_cl
+        out[f"fd_shape_h{hh:g}"] = {"h": hh, "dCL_dX_dirs": fd_cl, "newton_steps_median": float(np.median(steps)),
+                                    "residual_max": float(np.max(resids))}
+        log({f"fd_shape_h{hh:g}": out[f"fd_shape_h{hh:g}"]})
     sp.update_nodes(X)
-    out["fd_shape"] = {"dCL_dX_dirs": fd_cl, "newton_steps_median": float(np.median(steps)),
-                       "residual_max": float(np.max(resids))}
-    log({"fd_shape": out["fd_shape"]})
-    fdv = np.array(fd_cl)
     for key in ("frozen_limiter", "full_limiter"):
         o = out[key]
         if "error" in o:
             continue
         ad = np.array(o["dCL_dX_dirs"])
-        rel = np.abs(ad - fdv) / np.maximum(np.abs(fdv), 1e-3)
-        o["shape_rel_err_max"] = float(rel.max())
-        o["shape_rel_err_median"] = float(np.median(rel))
+        for hh, fd_cl in fd_by_h.items():
+            fdv = np.array(fd_cl)
+            rel = np.abs(ad - fdv) / np.maximum(np.abs(fdv), 1e-3)
+            o[f"shape_rel_err_max_h{hh:g}"] = float(rel.max())
+            o[f"shape_rel_err_median_h{hh:g}"] = float(np.median(rel))
         o["dCD_dM_rel_err"] = abs(o["dCD_dM"] - out["fd_freestream"]["dCD_dM"]) / abs(out["fd_freestream"]["dCD_dM"])
         o["dCD_dAoA_rel_err"] = (abs(o["dCD_dAoA_deg"] - out["fd_freestream"]["dCD_dAoA_deg"]) /
                                  abs(out["fd_freestream"]["dCD_dAoA_deg"]))

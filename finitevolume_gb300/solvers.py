@@ -739,6 +739,14 @@ class BatchSolver:
     newton = EulerFVMSolver.newton
     freeze_limiter = EulerFVMSolver.freeze_limiter
 
+    def set_field(self, new_U) -> None:
+        """Every instance's state [total cells, 4] (the instances' cells one
+        after another); the instances' step counters restart."""
+        u = np.ascontiguousarray(new_U, dtype=np.float64)
+        if u.shape != (self.mesh.n_cells, 4):
+            raise ValueError(f"set_field expects shape {(self.mesh.n_cells, 4)}, got {u.shape}")
+        capi.check(capi.lib().fv_set_field(self._h, capi.dptr(u)))
+
     def set_limiter_values(self, psi) -> None:
         """Freeze every instance's limiter at the given values [total cells,
         4] (the instances' cells one after another)."""
@@ -783,10 +791,14 @@ class BatchSolver:
         return act.astype(bool), it, nr
 
     def field(self, instance: int) -> np.ndarray:
+        o = self.mesh.offsets
+        return self.field_all()[o[instance]:o[instance + 1]]
+
+    def field_all(self) -> np.ndarray:
+        """Every instance's state [total cells, 4], instances one after another."""
         out = np.zeros((self.mesh.n_cells, 4))
         capi.check(capi.lib().fv_get_field(self._h, capi.dptr(out)))
-        o = self.mesh.offsets
-        return out[o[instance]:o[instance + 1]]
+        return out
 
     def wall_forces(self, instance: int, rho_ref, u_ref, v_ref, p_ref, length_ref=1.0, moment_x=0.25,
                     moment_y=0.0) -> dict:
