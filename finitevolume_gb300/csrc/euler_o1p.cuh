@@ -259,7 +259,10 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_o1_persistent(const O1Args
         // face phase
         const double cfl = a.ctl->cfl;
         double cand = DBL_MAX;
-        for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += nb * blockDim.x) {
+        // each block takes an equal contiguous range of faces, so that every
+        // SM (the grid is a multiple of the SM count) gets the same share
+        const int f0 = (int)((long long)F * blockIdx.x / nb), f1 = (int)((long long)F * (blockIdx.x + 1) / nb);
+        for (int f = f0 + threadIdx.x; f < f1; f += blockDim.x) {
             const int L = a.m.fl[f], R = a.m.fr[f];
             const double4_32a geo = a.m.fgeom[f];
             const St UL = ld_state_cg(a.U, L);

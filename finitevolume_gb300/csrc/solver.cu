@@ -175,14 +175,17 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
 
     if (!general && !viscous) {
         // Persistent first-order path: co-resident grid sized to the larger
-        // of the face tiles and the 256-cell tiles, capped at what fits.
+        // of the face tiles and the 256-cell tiles, rounded up to a whole
+        // number of blocks per SM (the face phase splits the faces evenly
+        // over the blocks), capped at what fits.
         int dev = 0, coop = 0, sms = 0;
         FV_CUDA(cudaGetDevice(&dev));
         FV_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
         FV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const int per_sm = opt.strict ? strict::o1p_max_blocks_per_sm(opt.flux, opt.dt_mode == FV_DT_LOCAL)
                                       : fast::o1p_max_blocks_per_sm(opt.flux, opt.dt_mode == FV_DT_LOCAL);
-        const int want = std::max((F + kCellBlock - 1) / kCellBlock, (N + kCellBlock - 1) / kCellBlock);
+        int want = std::max((F + kCellBlock - 1) / kCellBlock, (N + kCellBlock - 1) / kCellBlock);
+        if (sms > 0 && want > sms) want = (want + sms - 1) / sms * sms;
         p_grid = std::min(want, per_sm * sms);
         persistent_ok = coop != 0 && p_grid > 0;
         if (persistent_ok) {
