@@ -24,7 +24,10 @@
 //     step, and per face the coupling to the neighbour's block.  It is
 //     nu symmetric block Gauss-Seidel sweeps over a colouring of the cells
 //     (no two neighbours share a colour, so each colour is one kernel that
-//     updates its cells in place), or nu block-Jacobi sweeps;
+//     updates its cells in place), by default on FP32 copies of the blocks
+//     formed once per step (the sweeps only approximate the inverse; the
+//     residual, the Jacobian-vector products and the Krylov vectors stay
+//     FP64), or in FP64, or nu block-Jacobi sweeps;
 //   - U += alpha dU, alpha <= 1 the largest step that changes no cell's
 //     density or pressure by more than a set fraction (linear estimate).
 // A step whose residual comes out more than ten times larger than the one
@@ -255,6 +258,98 @@ __global__ void k_gs_colour_t(const adjk::AdjArgs a, const double* __restrict__ 
     st_state(z, c, st_make(o[0], o[1], o[2], o[3]));
 }
 
+// ---- FP32 preconditioner (kind 2) -------------------------------------
+// The Gauss-Seidel sweeps only have to approximate the inverse of the
+// first-order PTC matrix, so they run on FP32 copies of its blocks: per
+// cell-face entry e of cell c (neighbour nb across face f) the coupling
+// block B_e = sg J M_nb of the forward sweep (16 floats), per cell Dinv.
+// The sweeps then cost one 4x4 float block-vector product per neighbour,
+// on the FP32 pipe, instead of forming M_nb and two FP64 products per
+// neighbour and sweep; their input and output stay FP64 vectors.
+
+// Per cell: the FP32 coupling blocks of its entries and its Dinv.
+__global__ void k_pc_blocks(const adjk::AdjArgs a, const double* __restrict__ Dinv, float* __restrict__ B,
+                            float* __restrict__ Dinvf) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.n_cells) return;
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int ent = a.cf[e];
+        const int f = ent >> 1;
+        const int L = a.fl[f], R = a.fr[f];
+        float* o = B + 16 * (size_t)e;
+        if (R < 0) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) o[i] = 0.0f;
+            continue;
+        }
+        const bool own = ent & 1;
+        const int nb = own ? R : L;
+        const double* J = own ? a.JR + 16 * (size_t)f : a.JL + 16 * (size_t)f;
+        const double sg = own ? -1.0 : 1.0;
+        double M[16];
+        prim_jac(ld_state(a.W, nb), a.gamma, M);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                double t = 0.0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) t += J[4 * i + j] * M[4 * j + k];
+                o[4 * i + k] = (float)(sg * t);
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) Dinvf[16 * (size_t)c + i] = (float)Dinv[16 * (size_t)c + i];
+}
+
+// One colour of a Gauss-Seidel sweep on the FP32 blocks, in place on the
+// float iterate zf: t = r_c + sum_e B_e zf_nb, zf_c = Dinv_c t (TRANS: the
+// transposed matrix, t = r_c + sum_e B_twin(e)^T zf_nb, zf_c = Dinv_c^T t).
+template <bool TRANS>
+__global__ void k_gs_colour_f(const adjk::AdjArgs a, const float* __restrict__ B, const int* __restrict__ twin,
+                              const float* __restrict__ Dinvf, const St* __restrict__ r, float4* __restrict__ zf,
+                              const int* __restrict__ cells, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cells[i];
+    const St rc = ld_state(r, c);
+    float t[4] = {(float)rc.r, (float)rc.ru, (float)rc.rv, (float)rc.E};
+    for (int e = a.cf_off[c]; e < a.cf_off[c + 1]; ++e) {
+        const int ent = a.cf[e];
+        const int f = ent >> 1;
+        const int L = a.fl[f], R = a.fr[f];
+        if (R < 0) continue;
+        const int nb = (ent & 1) ? R : L;
+        const float4 z = zf[nb];
+        const float x[4] = {z.x, z.y, z.z, z.w};
+        if (TRANS) {
+            const float* Bt = B + 16 * (size_t)twin[e];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) t[k] += Bt[k] * x[0] + Bt[4 + k] * x[1] + Bt[8 + k] * x[2] + Bt[12 + k] * x[3];
+        } else {
+            const float* Be = B + 16 * (size_t)e;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                t[k] += Be[4 * k] * x[0] + Be[4 * k + 1] * x[1] + Be[4 * k + 2] * x[2] + Be[4 * k + 3] * x[3];
+        }
+    }
+    const float* X = Dinvf + 16 * (size_t)c;
+    float o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        o[k] = TRANS ? X[k] * t[0] + X[4 + k] * t[1] + X[8 + k] * t[2] + X[12 + k] * t[3]
+                     : X[4 * k] * t[0] + X[4 * k + 1] * t[1] + X[4 * k + 2] * t[2] + X[4 * k + 3] * t[3];
+    zf[c] = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// z = widened zf
+__global__ void k_widen(St* __restrict__ z, const float4* __restrict__ zf, int n) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const float4 v = zf[c];
+    st_state(z, c, st_make(v.x, v.y, v.z, v.w));
+}
+
 // out = -x
 __global__ void k_neg(St* __restrict__ out, const St* __restrict__ x, int n) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -463,7 +558,12 @@ struct NewtonWork {
     double *V = nullptr, *Dinv = nullptr, *part = nullptr, *h = nullptr, *scal = nullptr;
     St *R = nullptr, *z = nullptr, *z2 = nullptr, *Mz = nullptr, *Jx = nullptr, *w = nullptr, *du = nullptr,
        *Ubak = nullptr, *tmp = nullptr, *zx = nullptr;
-    int kind = 1;                   // preconditioner: 0 block Jacobi, 1 multicolour symmetric Gauss-Seidel
+    int kind = 2;                   // preconditioner: 0 block Jacobi, 1 multicolour symmetric Gauss-Seidel
+                                    // (FP64), 2 the same on FP32 blocks
+    float* Bf = nullptr;            // kind 2: coupling blocks [16 E], Dinv [16 N], iterate [N]
+    float* Dinvf = nullptr;
+    float4* zf = nullptr;
+    int* twin = nullptr;            // kind 2, transposed sweeps: the other entry of each entry's face
     int* colour_cells = nullptr;    // cells grouped by colour
     std::vector<int> colour_off;    // [n_colours + 1]
     ~NewtonWork() {
@@ -519,7 +619,62 @@ void colour_cells(const fvgb::Solver& s, NewtonWork& W, cudaStream_t st) {
 
 // z = P^-1 r from z = 0: `sweeps` symmetric Gauss-Seidel sweeps (forward
 // then backward over the colours), or `sweeps` block-Jacobi sweeps.
+// Kind 2: `sweeps` symmetric Gauss-Seidel sweeps on the FP32 blocks (TRANS:
+// of the transposed matrix), from zero, widened into z.
+template <bool TRANS>
+void precondition_f32(fv_adjoint_s* A, NewtonWork& W, const St* r, St* z, int sweeps, cudaStream_t s) {
+    FV_CUDA(cudaMemsetAsync(W.zf, 0, sizeof(float4) * (size_t)W.N, s));
+    const int nc = (int)W.colour_off.size() - 1;
+    for (int sw = 0; sw < sweeps; ++sw)
+        for (int pass = 0; pass < 2; ++pass)
+            for (int q = 0; q < nc; ++q) {
+                const int k = pass == 0 ? q : nc - 1 - q;
+                const int n = W.colour_off[k + 1] - W.colour_off[k];
+                if (n == 0) continue;
+                nk::k_gs_colour_f<TRANS><<<nk::blocks(n), nk::kB, 0, s>>>(A->a, W.Bf, W.twin, W.Dinvf, r, W.zf,
+                                                                          W.colour_cells + W.colour_off[k], n);
+            }
+    nk::k_widen<<<nk::blocks(W.N), nk::kB, 0, s>>>(z, W.zf, W.N);
+    check_launch();
+}
+
+// The FP32 blocks of kind 2 (after k_pc_diag has formed Dinv).
+void pc_blocks(fv_adjoint_s* A, NewtonWork& W, cudaStream_t s) {
+    nk::k_pc_blocks<<<nk::blocks(W.N), nk::kB, 0, s>>>(A->a, W.Dinv, W.Bf, W.Dinvf);
+    check_launch();
+}
+
+// Storage of kind 2 (and, with transposed sweeps, the entry twins).
+void alloc_f32_pc(const fvgb::Solver& s, NewtonWork& W, bool twins, cudaStream_t st) {
+    const int N = s.N, F = s.F;
+    std::vector<int> off(N + 1);
+    FV_CUDA(cudaMemcpyAsync(off.data(), s.dm.cf_off, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, st));
+    FV_CUDA(cudaStreamSynchronize(st));
+    const size_t E = (size_t)off[N];
+    W.Bf = W.alloc<float>(16 * E);
+    W.Dinvf = W.alloc<float>(16 * (size_t)N);
+    W.zf = W.alloc<float4>(N);
+    if (!twins) return;
+    std::vector<int> cf(E), tw(E, -1), first(F, -1);
+    FV_CUDA(cudaMemcpyAsync(cf.data(), s.dm.cf, sizeof(int) * E, cudaMemcpyDeviceToHost, st));
+    FV_CUDA(cudaStreamSynchronize(st));
+    for (size_t e = 0; e < E; ++e) {
+        const int f = cf[e] >> 1;
+        if (first[f] < 0) first[f] = (int)e;
+        else {
+            tw[e] = first[f];
+            tw[first[f]] = (int)e;
+        }
+    }
+    W.twin = W.alloc<int>(E);
+    fvgb::h2d_sync(W.twin, tw.data(), sizeof(int) * E, st);
+}
+
 void precondition(fv_adjoint_s* A, NewtonWork& W, const St* r, St* z, int sweeps, cudaStream_t s) {
+    if (W.kind == 2) {
+        precondition_f32<false>(A, W, r, z, sweeps, s);
+        return;
+    }
     if (W.kind == 1) {
         FV_CUDA(cudaMemsetAsync(z, 0, sizeof(St) * (size_t)W.N, s));
         const int nc = (int)W.colour_off.size() - 1;
@@ -549,6 +704,10 @@ void precondition(fv_adjoint_s* A, NewtonWork& W, const St* r, St* z, int sweeps
 // z = P^-T r from z = 0: `sweeps` symmetric Gauss-Seidel sweeps of the
 // transposed matrix over the colours.
 void precondition_t(fv_adjoint_s* A, NewtonWork& W, const St* r, St* z, int sweeps, cudaStream_t s) {
+    if (W.kind == 2) {
+        precondition_f32<true>(A, W, r, z, sweeps, s);
+        return;
+    }
     FV_CUDA(cudaMemsetAsync(z, 0, sizeof(St) * (size_t)W.N, s));
     const int nc = (int)W.colour_off.size() - 1;
     for (int sw = 0; sw < sweeps; ++sw)
@@ -707,7 +866,7 @@ void fv_newton_default(fv_newton_t* o) {
     o->krylov_dim = 80;
     o->krylov_rtol = 1e-2;
     o->precond_sweeps = 8;
-    o->precond_kind = 1;
+    o->precond_kind = 2;
     o->max_rel_change = 0.2;
 }
 
@@ -718,7 +877,7 @@ int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history
         const fv_newton_t o = *opt;
         if (o.max_newton < 0 || !(o.tol >= 0.0) || !(o.cfl0 > 0.0) || !(o.cfl_max >= o.cfl0) ||
             !(o.cfl_growth >= 1.0) || o.krylov_dim < 1 || o.krylov_dim > 200 || !(o.krylov_rtol > 0.0) ||
-            o.precond_sweeps < 1 || o.precond_kind < 0 || o.precond_kind > 1 || !(o.max_rel_change > 0.0))
+            o.precond_sweeps < 1 || o.precond_kind < 0 || o.precond_kind > 2 || !(o.max_rel_change > 0.0))
             fvgb::raise(FV_ERR_BAD_ARG, "fv_steady_newton: bad options");
         fvgb::Solver& s = solver->s;
         fv_adjoint_t Ah = nullptr;
@@ -745,7 +904,8 @@ int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history
         W.tmp = W.alloc<St>(s.N);
         W.zx = W.alloc<St>(s.N);
         W.kind = o.precond_kind;
-        if (W.kind == 1) colour_cells(s, W, st);
+        if (W.kind >= 1) colour_cells(s, W, st);
+        if (W.kind == 2) alloc_f32_pc(s, W, false, st);
         // instances: contiguous cell ranges (a single solver is one)
         const std::vector<int> off = s.batch ? std::vector<int>(s.group_off.begin(), s.group_off.end())
                                              : std::vector<int>{0, s.N};
@@ -846,6 +1006,7 @@ int fv_steady_newton(fv_solver_t solver, const fv_newton_t* opt, double* history
             nk::k_inst_prepare<<<ni, nk::kB, 0, st>>>(A->a.D, W.R, d_off, d_cfl, d_mask);
             nk::k_pc_diag<<<nk::blocks(s.N), nk::kB, 0, st>>>(A->a, W.Dinv);
             check_launch();
+            if (W.kind == 2) pc_blocks(A.get(), W, st);
             // The system is block diagonal over the instances, so scaling an
             // instance's right-hand side scales only its own solution.  Each
             // is scaled to unit norm before GMRES (and its solution back
@@ -921,11 +1082,14 @@ int fv_adjoint_solve_krylov(fv_adjoint_t A, const double* dJdU, double cfl, int3
         W.tmp = W.alloc<St>(s.N);
         W.zx = W.alloc<St>(s.N);
         colour_cells(s, W, st);
+        W.kind = 2;
+        alloc_f32_pc(s, W, true, st);
         // the preconditioner's pseudo time step; the primal's is restored after
         const double cfl_primal = A->a.cfl;
         adjh::lin_dt(A, cfl);
         nk::k_pc_diag<<<nk::blocks(s.N), nk::kB, 0, st>>>(A->a, W.Dinv);
         check_launch();
+        pc_blocks(A, W, st);
         // -(dR/dU)^T lam = -dJ/dU
         adjh::upload(A, dJdU, W.du);
         nk::k_neg<<<nk::blocks(s.N), nk::kB, 0, st>>>(W.R, W.du, s.N);

@@ -324,8 +324,9 @@ class EulerFVMSolver:
         continuation, exact Jacobian-vector products, block-Jacobi
         preconditioned GMRES).  ``limiter_mode`` 0 frozen / 1 full limiter
         Jacobian; other keywords: cfl0, cfl_max, cfl_growth, krylov_dim,
-        krylov_rtol, precond_sweeps, precond_kind (1 multicolour symmetric
-        Gauss-Seidel, 0 block Jacobi), max_rel_change.  Returns (history
+        krylov_rtol, precond_sweeps, precond_kind (2 multicolour symmetric
+        Gauss-Seidel on FP32 blocks, 1 the same in FP64, 0 block Jacobi),
+        max_rel_change.  Returns (history
         [(steps + 1) x 8]: four residual norms, CFL, GMRES iterations, GMRES
         relative residual, step length; Newton steps taken)."""
         o = capi.NewtonOpts()

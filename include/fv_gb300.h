@@ -383,8 +383,8 @@ int fv_adjoint_solve_gmres(fv_adjoint_t a, const double* dJdU, int32_t restart, 
  * pseudo-time iteration is slow: with A = -dR/dU, each outer iteration
  * solves (V/dt + A)^T delta = -dJdU - A^T lambda by one GMRES(restart) cycle
  * (to a relative residual of 1e-2), right-preconditioned by symmetric block
- * Gauss-Seidel sweeps (over a cell colouring) of the transposed first-order
- * Jacobian plus V/dt, V/dt at the given CFL number (the one the primal
+ * Gauss-Seidel sweeps (over a cell colouring, on FP32 copies of the blocks)
+ * of the transposed first-order Jacobian plus V/dt, V/dt at the given CFL number (the one the primal
  * Newton iteration reached), and adds delta to lambda.  Stops when
  * |(dR/dU)^T lambda - dJdU| is below rtol |dJdU| or after max_matvec
  * products; history [outer iterations] that relative residual before each
@@ -413,8 +413,8 @@ int fv_residual_shape_vjp(fv_adjoint_t a, fv_mesh_t mesh, const double* Rbar, do
  * characteristic-farfield extensions) to zero by pseudo-transient
  * continuation: each step solves (V/dt - dR/dU) dU = R by GMRES with the
  * adjoint's exact Jacobian-vector products, preconditioned on the
- * first-order Jacobian (multicolour symmetric block Gauss-Seidel, or block
- * Jacobi), then U += alpha dU with alpha <= 1 bounding the relative change
+ * first-order Jacobian (multicolour symmetric block Gauss-Seidel on FP32 or
+ * FP64 blocks, or block Jacobi), then U += alpha dU with alpha <= 1 bounding the relative change
  * of every cell's density and pressure.  The CFL number of V/dt starts at
  * cfl0, grows by cfl_growth after each step that lowers the density
  * residual, was taken in full (alpha = 1) and whose GMRES solve reached a
@@ -439,7 +439,8 @@ typedef struct {
     int32_t krylov_dim;     /* GMRES(m), one cycle per Newton step (1..200)               */
     double krylov_rtol;     /* relative GMRES tolerance                                   */
     int32_t precond_sweeps; /* preconditioner sweeps                                      */
-    int32_t precond_kind;   /* 1 multicolour symmetric block Gauss-Seidel, 0 block Jacobi  */
+    int32_t precond_kind;   /* 2 multicolour symmetric block Gauss-Seidel on FP32 copies of
+                               the blocks (default), 1 the same in FP64, 0 block Jacobi   */
     double max_rel_change;  /* bound on the relative density / pressure change per step   */
 } fv_newton_t;
 /* Defaults: frozen-limiter Jacobian, 200 steps, tol 1e-11, CFL 10 growing

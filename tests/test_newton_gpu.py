@@ -94,7 +94,7 @@ def test_newton_rejects_bad_options(gpu):
     poly = meshgen.naca_ogrid(32, 16)
     s, _ = _solver(poly, 0.5, 2.0)
     u0 = s.field().copy()
-    for kw in ({"krylov_dim": 0}, {"krylov_dim": 201}, {"cfl0": -1.0}, {"cfl_growth": 0.5}, {"precond_kind": 2},
+    for kw in ({"krylov_dim": 0}, {"krylov_dim": 201}, {"cfl0": -1.0}, {"cfl_growth": 0.5}, {"precond_kind": 3},
                {"precond_sweeps": 0}, {"max_rel_change": 0.0}):
         with pytest.raises(capi.FVError):
             s.newton(max_newton=5, **kw)
