@@ -79,7 +79,9 @@ def test_overlapping_cells_are_refused(gpu):
     so the viscous solver refuses the mesh instead of stepping with it."""
     from finitevolume_gb300 import capi
     from finitevolume_gb300.fvmesh import from_cells
-    nodes = np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.9, 0.2]])
+    # the second triangle lies below the shared diagonal too, with its
+    # centroid further from it than the first one's
+    nodes = np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [1.5, -0.5]])
     cells = [[0, 1, 2], [0, 3, 2]]
     bedges = np.array([[0, 1], [1, 2], [0, 3], [3, 2]])
     poly = from_cells(nodes, cells, bedges, np.zeros(4, np.int32), ["wall"])
