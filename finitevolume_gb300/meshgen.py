@@ -452,6 +452,19 @@ def naca_hybrid(ni: int = 1024, n_layers: int = 40, first: float = 4.5e-6, growt
     i1 = (i0 + 1) % ni
     xy = ((1 - a_)[:, None] * ((1 - b_)[:, None] * aux[k0, i0] + b_[:, None] * aux[k0, i1])
           + a_[:, None] * ((1 - b_)[:, None] * aux[k0 + 1, i0] + b_[:, None] * aux[k0 + 1, i1]))
+    # Free points inside the diametral circle of a ring edge are dropped,
+    # so that every ring edge is a Gabriel edge and hence an edge of the
+    # Delaunay triangulation below.
+    from scipy.spatial import cKDTree
+    tree = cKDTree(xy)
+    drop = set()
+    for ring in (inner, circ):
+        a, b = ring, np.roll(ring, -1, axis=0)
+        mid, rad = 0.5 * (a + b), 0.5 * np.linalg.norm(b - a, axis=1)
+        for j, hits in enumerate(tree.query_ball_point(mid, rad * (1.0 + 1e-9))):
+            drop.update(hits)
+    if drop:
+        xy = np.delete(xy, np.fromiter(sorted(drop), np.int64), axis=0)
     nf = xy.shape[0]
     # Delaunay of those points with both rings, in physical space (a
     # triangulation taken in index space and mapped puts thin triangles on
@@ -535,7 +548,7 @@ def wall_normal_directions(poly: PolyMesh, n_dirs: int, seed: int = 0, width: in
     return out
 
 
-CACHE_VERSION = 3  # 2: naca_mixed splits cells of more than 9 sides; 3: naca_hybrid triangulated in physical space
+CACHE_VERSION = 4  # 2: naca_mixed splits cells of more than 9 sides; 3: naca_hybrid triangulated in physical space; 4: without ring-encroaching points
 
 
 def cached(name: str, **kw) -> PolyMesh:
