@@ -389,9 +389,12 @@ def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_
       solve with per-instance CFL numbers and early exit, in rounds of
       ``round_steps`` Newton steps after which the unconverged instances
       are repacked into a smaller batch.
-    - FP64 sequential (the plain GPU path): the same procedure, one plain
-      solver per instance, for a seeded sample of ``n_seq`` instances, each
-      timed in full to convergence; solves/s over that sample.
+    - sequential: the same procedure, one plain solver per instance, for a
+      seeded sample of ``n_seq`` instances, each timed in full to
+      convergence; solves/s over that sample.  Twice: with the Newton
+      preconditioner in FP64 (the plain FP64 GPU path) and with its blocks
+      in FP32 (mixed precision, the default; the residual, the
+      Jacobian-vector products and the solution stay FP64).
     - FP32-flux batched (mixed precision; FP32 flux and gradients, FP64
       accumulation, update and norms): the same warm-up, then explicit
       SSP-RK3 with agglomeration multigrid; an instance counts
@@ -454,36 +457,42 @@ def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_
     tb = time.perf_counter() - t0
     conv = steps >= 0
     out["f64_batched"] = {"solves_per_s": round(int(conv.sum()) / tb, 4), "seconds": round(tb, 2),
-                          "converged": int(conv.sum()), "rounds": rounds,
+                          "converged": int(conv.sum()), "rounds": rounds, "preconditioner": "FP32 blocks",
                           "instance_newton_steps_median": float(np.median(steps[conv])) if conv.any() else None}
-    # FP64 sequential, seeded sample, each solve timed in full
+    # plain solver per instance, seeded sample, each solve timed in full:
+    # all-FP64 (FP64 preconditioner, the plain FP64 GPU path) and mixed
+    # (FP32 preconditioner blocks, the default; the same FP64 residual,
+    # Jacobian-vector products and converged solution)
     rng = np.random.default_rng(seed)
     sample = np.sort(rng.choice(n, size=min(n_seq, n), replace=False))
-    ts, nconv, dcd = 0.0, 0, []
-    for i in sample:
-        s = _plain_solver(meshes[i], fss[i], False)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ok = False
-        try:
-            s.run(warm)
-            s.freeze_limiter(True)
-            s.newton(max_newton=max_newton, tol=tol)
-            ok = bool(s.last_newton_instance_steps[0] >= 0)
-        except capi.FVError:
-            pass
-        torch.cuda.synchronize()
-        ts += time.perf_counter() - t0
-        if ok:
-            nconv += 1
-            if conv[i]:
-                dcd.append(abs(s.wall_forces(*refs[i])["cd_total"] - cd64[i]))
-        del s
-    out["f64_sequential"] = {"solves_per_s": round(nconv / ts, 4), "seconds": round(ts, 2), "converged": nconv,
-                             "sample": [int(i) for i in sample],
-                             "max_abs_dCD_vs_batched": float(max(dcd)) if dcd else None}
-    out["f64_batched"]["speedup_vs_sequential"] = round(out["f64_batched"]["solves_per_s"] /
-                                                        max(out["f64_sequential"]["solves_per_s"], 1e-30), 2)
+    for tag, kind in (("f64_sequential", 1), ("mixed_sequential", 2)):
+        ts, nconv, dcd = 0.0, 0, []
+        for i in sample:
+            s = _plain_solver(meshes[i], fss[i], False)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ok = False
+            try:
+                s.run(warm)
+                s.freeze_limiter(True)
+                s.newton(max_newton=max_newton, tol=tol, precond_kind=kind)
+                ok = bool(s.last_newton_instance_steps[0] >= 0)
+            except capi.FVError:
+                pass
+            torch.cuda.synchronize()
+            ts += time.perf_counter() - t0
+            if ok:
+                nconv += 1
+                if conv[i]:
+                    dcd.append(abs(s.wall_forces(*refs[i])["cd_total"] - cd64[i]))
+            del s
+        out[tag] = {"solves_per_s": round(nconv / ts, 4), "seconds": round(ts, 2), "converged": nconv,
+                    "preconditioner": "FP64 blocks" if kind == 1 else "FP32 blocks",
+                    "sample": [int(i) for i in sample],
+                    "max_abs_dCD_vs_batched": float(max(dcd)) if dcd else None}
+    base = max(out["f64_sequential"]["solves_per_s"], 1e-30)
+    out["f64_batched"]["speedup_vs_f64_sequential"] = round(out["f64_batched"]["solves_per_s"] / base, 2)
+    out["mixed_sequential"]["speedup_vs_f64_sequential"] = round(out["mixed_sequential"]["solves_per_s"] / base, 2)
     # FP32-flux batched, drag criterion against the converged FP64 drag
     b = _batch_solver(meshes, fss, True)
     torch.cuda.synchronize()
@@ -512,8 +521,7 @@ def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_
                                 "converged": int(conv32.sum()), "iterations": int(done),
                                 "criterion": f"|CD - CD_fp64| <= {cd_tol} at two consecutive checkpoints",
                                 "solver": "explicit SSP-RK3 + 4-level agglomeration multigrid, frozen limiter"}
-    out["fp32_flux_batched"]["speedup_vs_f64_sequential"] = round(
-        out["fp32_flux_batched"]["solves_per_s"] / max(out["f64_sequential"]["solves_per_s"], 1e-30), 2)
+    out["fp32_flux_batched"]["speedup_vs_f64_sequential"] = round(out["fp32_flux_batched"]["solves_per_s"] / base, 2)
     return out
 
 
