@@ -265,116 +265,6 @@ def batch_throughput(meshes, fss, fp32: bool, iters: int):
     return cells * iters / tb / 1e6, cells * iters / ts / 1e6
 
 
-def _per_iter_seconds(mesh, fs, fp32: bool, mg: bool, iters: int = 40) -> float:
-    """Per-iteration wall time of one plain (unbatched) solve of a case."""
-    from finitevolume_gb300 import capi
-    s = _plain_solver(mesh, fs, fp32)
-    try:
-        if mg:
-            s.multigrid()
-        s.run(5)
-        t0 = time.perf_counter()
-        s.run(iters)
-        return (time.perf_counter() - t0) / iters
-    except capi.FVError:
-        return float("nan")
-    finally:
-        del s
-
-
-def _batch_to_tolerance(meshes, fss, fp32, tol, max_iter, mg, chunk=500):
-    b = _batch_solver(meshes, fss, fp32, tol)
-    if mg:
-        b.multigrid()
-    t0 = time.perf_counter()
-    done = 0
-    while done < max_iter:
-        b.run(chunk)
-        done += chunk
-        act, it, nr = b.status()
-        if not act.any():
-            break
-    t = time.perf_counter() - t0
-    return b, t, (~act) & (nr[:, 0] < tol), it.copy()
-
-
-def batch_converged(cases, meshes, fss, tol: float, max_iter: int, chunk: int = 500, cd_tol: float = 1e-5):
-    """Converged steady solves per second, batched vs plain sequential, with
-    and without agglomeration multigrid.
-
-    FP64: the batch runs with per-instance early exit at the density
-    tolerance (capped at ``max_iter``); instance i takes K_i iterations.
-    FP32-flux (with multigrid): an instance counts as converged at the first
-    of two consecutive checkpoints (every ``chunk`` iterations) with
-    |CD - CD_fp64| <= ``cd_tol`` against its converged FP64 (multigrid)
-    drag, and is then frozen; instances without a converged FP64 reference
-    run to the cap and count as not converged.
-    Sequential: each plain solve of the same case performs the same
-    arithmetic as its batch instance (the batch reproduces a standalone
-    solve to round-off), so it takes the same K_i iterations; its time is
-    K_i times the measured per-iteration time of that solve on its own.
-    """
-    n = len(meshes)
-    refs = [(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0) for fs in fss]
-    out = {"instances": n}
-    res = {}
-    for tag, mg in (("f64_plain", False), ("f64_multigrid", True)):
-        b, t, conv, k = _batch_to_tolerance(meshes, fss, False, tol, max_iter, mg, chunk)
-        cd = np.array([b.wall_forces(i, *refs[i])["cd_total"] for i in range(n)])
-        del b
-        res[tag] = (t, conv, k, cd)
-    # FP32-flux with multigrid, drag criterion against the FP64 multigrid drag
-    cd64 = res["f64_multigrid"][3]
-    conv64 = res["f64_multigrid"][1]
-    b = _batch_solver(meshes, fss, True, -1.0)
-    b.multigrid()
-    k32 = np.full(n, max_iter, np.int64)
-    hits = np.zeros(n, np.int64)
-    conv32 = np.zeros(n, bool)
-    t32 = 0.0
-    done = 0
-    while done < max_iter:
-        t0 = time.perf_counter()
-        b.run(chunk)
-        b.status()
-        t32 += time.perf_counter() - t0
-        done += chunk
-        for i in np.nonzero(conv64 & ~conv32)[0]:
-            cd = b.wall_forces(int(i), *refs[i])["cd_total"]
-            hits[i] = hits[i] + 1 if abs(cd - cd64[i]) <= cd_tol else 0
-            if hits[i] >= 2:
-                conv32[i] = True
-                k32[i] = done
-                b.set_active(int(i), False)
-        if conv32[conv64].all():
-            break
-    _, it32, _ = b.status()
-    k32 = np.where(conv32, k32, it32)
-    del b
-    # plain sequential solves: per-iteration time of each case
-    t_plain = np.array([_per_iter_seconds(m, fs, False, False) for m, fs in zip(meshes, fss)])
-    t_mg = np.array([_per_iter_seconds(m, fs, False, True) for m, fs in zip(meshes, fss)])
-    t_mg32 = np.array([_per_iter_seconds(m, fs, True, True) for m, fs in zip(meshes, fss)])
-    for tag, tseq in (("f64_plain", t_plain), ("f64_multigrid", t_mg)):
-        t, conv, k, _ = res[tag]
-        s_seq = float(np.nansum(k * tseq))
-        nconv = int(conv.sum())
-        out[tag] = {"batched_solves_per_s": round(nconv / t, 5), "batched_seconds": round(t, 2), "converged": nconv,
-                    "sequential_solves_per_s": round(nconv / s_seq, 5), "sequential_seconds": round(s_seq, 2),
-                    "iterations_median": int(np.median(k)),
-                    "iterations_converged_median": int(np.median(k[conv])) if nconv else None}
-    s32 = float(np.nansum(k32 * t_mg32))
-    n32 = int(conv32.sum())
-    out["fp32_flux_multigrid"] = {"batched_solves_per_s": round(n32 / t32, 5), "batched_seconds": round(t32, 2),
-                                  "converged": n32, "criterion": f"|CD - CD_fp64| <= {cd_tol} at two checkpoints",
-                                  "sequential_solves_per_s": round(n32 / s32, 5), "sequential_seconds": round(s32, 2),
-                                  "iterations_converged_median": int(np.median(k32[conv32])) if n32 else None}
-    out["sequential_method"] = ("K_i x measured per-iteration time of the solve of case i on its own "
-                                "(40 iterations after 5 warm-up), summed over all instances")
-    out["multigrid"] = "4 agglomerated levels, 1 smoothing iteration per level, correction relaxation 0.7"
-    return out
-
-
 def batch_converged_newton(meshes, fss, tol: float = 1e-8, warm: int = 200, max_newton: int = 80,
                            n_seq: int = 12, seed: int = 1, cd_tol: float = 1e-5, fp32_max_iter: int = 3000,
                            fp32_chunk: int = 250, round_steps: int = 20) -> dict:
@@ -590,18 +480,6 @@ def adjoint_cost(iters: int = 200, warm: int = 300):
                         "adjoint_vs_converged_primal": round(tadj / tprim, 3)}
     del adj, s2, s
     return out
-
-
-def _converge(s, tol: float, max_iter: int, chunk: int = 250):
-    """Run until the density residual norm falls below tol (or max_iter)."""
-    done, last = 0, float("nan")
-    while done < max_iter:
-        h = s.run(min(chunk, max_iter - done), history=True)
-        done += len(h)
-        last = float(h[-1, 0])
-        if not np.isfinite(last) or last < tol:
-            break
-    return done, last
 
 
 def adjoint_check(n_dirs: int = 16, h: float = 1e-6, h_small: float = 1e-8, tol: float = 1e-11, warm: int = 300,
@@ -946,18 +824,18 @@ def profile_target(target: str, steps: int) -> dict:
 
 
 def run_batched(args):
-    """--batched: converged solves/s of the 256-instance family, FP64 and
-    FP32-flux, batched vs plain sequential solves."""
+    """--batched: converged solves/s of the whole 256-instance family
+    (batch_converged_newton over every instance, a 24-instance sequential
+    sample, FP64 and mixed-precision preconditioners)."""
     import torch
     torch.cuda.init()
-    cases, meshes, fss = batch_workload(args.instances)
+    _, meshes, fss = batch_workload(args.instances)
     out = {"metric": "converged steady solves/s, 256-instance batched Euler (per-instance early exit)",
            "unit": "solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic (seeded NACA family)",
            "config": {"workload": "naca4_family_ogrid_batch", "instances": len(meshes),
                       "cells_total": int(sum(m.n_cells for m in meshes)), "tol_l2_density": args.tol,
-                      "max_iter": args.max_iter, "cfl": CFL},
-           "results": {}}
-    out["results"] = batch_converged(cases, meshes, fss, args.tol, args.max_iter)
+                      "max_newton": args.max_newton, "cfl": CFL}}
+    out["results"] = batch_converged_newton(meshes, fss, tol=args.tol, max_newton=args.max_newton, n_seq=24)
     print(json.dumps(out), flush=True)
 
 
@@ -1056,7 +934,7 @@ def main():
                     help="converged solves/s of the batched airfoil family instead of the headline")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--max-iter", type=int, default=20000)
+    ap.add_argument("--max-newton", type=int, default=120)
     args = ap.parse_args()
     if args.batched:
         run_batched(args)
