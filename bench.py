@@ -796,8 +796,9 @@ def config1_cpu_rate(steps: int = 3000, seconds: float = 3.0) -> dict:
 
 def profile_target(target: str, steps: int) -> dict:
     """Profiler targets beside the headline: the adjoint iteration on the
-    500k-cell O-grid, the RANS-SA step on the 2M-cell hybrid mesh, and a
-    multigrid V-cycle on the 1M-cell mixed mesh (direct launches)."""
+    500k-cell O-grid, the RANS-SA step on the 2M-cell hybrid mesh, config 1
+    (``steps`` calls of 100 persistent first-order steps on the 32k O-grid)
+    and a multigrid V-cycle on the 1M-cell mixed mesh (direct launches)."""
     import torch
     from finitevolume_gb300 import meshgen, solvers as S
     t0 = time.perf_counter()
@@ -814,6 +815,19 @@ def profile_target(target: str, steps: int) -> dict:
         adj.solve(g, steps, 0.0)
     elif target == "rans":
         rans_sa_rate(steps=steps, warm=1, cpu=False)
+    elif target == "config1":
+        # the 32k O-grid, first-order Rusanov, local dt: one persistent
+        # launch per fv_step of up to 256 steps
+        M, aoa = 0.5, 2.0
+        a = np.radians(aoa)
+        fs = (1.0, M * np.cos(a), M * np.sin(a), 1.0 / GAMMA)
+        mesh = S.Mesh(meshgen.naca_ogrid(256, 128), reorder="morton")
+        bcs = [S.EulerBoundaryCondition(S.EulerBoundaryType.Wall),
+               S.EulerBoundaryCondition(S.EulerBoundaryType.CharacteristicFarfield, S.from_primitive(*fs, GAMMA))]
+        ic = S.EulerInitialCondition(S.EulerICMode.Freestream, rho=fs[0], u=fs[1], v=fs[2], p=fs[3])
+        s = S.EulerFVMSolver(mesh, bcs, GAMMA, 0.5, ic, S.NumericalFluxScheme.Rusanov, local_dt=True)
+        for _ in range(steps):
+            s.run(100)
     else:
         poly = load_mesh()
         s, _ = make_solver(poly)
@@ -926,7 +940,7 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="profiler target: build the workload, run --steps iterations with direct launches, exit")
     ap.add_argument("--fp32", action="store_true", help="with --profile: the FP32-flux variant")
-    ap.add_argument("--profile-target", choices=["euler", "adjoint", "rans", "multigrid"], default="euler",
+    ap.add_argument("--profile-target", choices=["euler", "adjoint", "rans", "multigrid", "config1"], default="euler",
                     help="with --profile: which kernels to run (profiler target)")
     ap.add_argument("--adjoint-check", action="store_true",
                     help="adjoint gradients of the 500k-cell case against central differences of converged solves")
