@@ -725,8 +725,9 @@ def config1_rate(steps: int = 3000):
     Rusanov, forward Euler with local time stepping at CFL 0.5, slip wall
     and characteristic farfield, M 0.5, AoA 2 deg, 3,000 iterations; CL, CD
     and the final density residual.  Timed (wall clock around fv_step, after
-    an untimed run that builds the graphs) on the persistent kernel and on
-    the two-kernel path."""
+    an untimed run that builds the graphs) in three forms: the dataflow form
+    of the persistent kernel (the default with local dt), its grid-barrier
+    form and the two-kernel path."""
     import torch
     from finitevolume_gb300 import meshgen, solvers as S
     M, aoa = 0.5, 2.0
@@ -749,13 +750,18 @@ def config1_rate(steps: int = 3000):
         return s, h, time.perf_counter() - t0
 
     s, h, t = timed(True)
+    _, h3, t3 = timed("barrier")
     _, h2, t2 = timed(False)
     f = s.wall_forces(fs[0], fs[1], fs[2], fs[3], 1.0, 0.25, 0.0)
+    form = {0: "two-kernel", 1: "grid-barrier", 2: "dataflow"}
     out = {"workload": "naca0012 O-grid 256x128, 1st-order Rusanov, forward Euler, local dt, CFL 0.5, M 0.5, AoA 2",
            "cells": mesh.n_cells, "steps": steps, "seconds": round(t, 4),
            "value": round(mesh.n_cells * steps / t / 1e6, 3),
            "unit": "Mcell-iters/s (wall clock around fv_step, persistent kernel)",
+           "persistent_form": form[s.persistent()[0]],
            "persistent_grid_blocks": s.persistent()[1],
+           "grid_barrier_form": {"seconds": round(t3, 4), "value": round(mesh.n_cells * steps / t3 / 1e6, 3),
+                                 "history_equal": bool(np.array_equal(h, h3))},
            "two_kernel_path": {"seconds": round(t2, 4), "value": round(mesh.n_cells * steps / t2 / 1e6, 3)},
            "speedup_vs_two_kernel": round(t2 / t, 3),
            "history_equal_two_kernel_rtol": float(np.max(np.abs(h - h2) / np.abs(h2))),

@@ -46,6 +46,7 @@
 
 namespace FV_KNS {
 
+using fvgb::DfPlan;
 using fvgb::PersistCtl;
 
 struct Prim {
@@ -165,6 +166,65 @@ __device__ __forceinline__ double face_smax_p(const Prim& PL, const Prim& PR, bo
     return Smax;
 }
 
+// One face of the face phase: the flux times the face length into ff[f]
+// and, with local dt, lambda * length into dtf[f].  Returns the face's
+// global-dt candidate cfl * (CFL length) / max(|Vn| + c) (DBL_MAX with
+// local dt).
+template <int FLUX, bool LOCAL>
+__device__ __forceinline__ double face_phase_face(const O1Args& a, const double4_32a* P, int f, double g,
+                                                  double cfl) {
+    const int L = a.m.fl[f], R = a.m.fr[f];
+    const double4_32a geo = a.m.fgeom[f];
+    const St UL = ld_state_cg(a.U, L);
+    const Prim PL = ld_prim(P, L);
+    St UR;
+    Prim PR;
+    if (R >= 0) {
+        UR = ld_state_cg(a.U, R);
+        PR = ld_prim(P, R);
+    } else {
+        UR = ghost_state(a.bc, a.m.fpatch[f], UL, geo.x, geo.y, g);
+        PR = prim_of(UR, g);
+    }
+    const St Fl = num_flux_p<FLUX>(UL, PL, UR, PR, geo.x, geo.y, g, a.exact_tol, a.exact_max_iter);
+    st_state(a.ff, f, geo.z * Fl);
+    const double Smax = face_smax_p(PL, PR, R >= 0, geo.x, geo.y);
+    if (LOCAL) {
+        a.dtf[f] = Smax * geo.z;
+        return DBL_MAX;
+    }
+    return cfl * geo.w / Smax;
+}
+
+// One cell of the cell phase: the signed gather of its face fluxes,
+// U += dt/V R, the new primitives, and the squares of R for the norms.
+template <bool LOCAL>
+__device__ __forceinline__ void cell_phase_cell(const O1Args& a, double4_32a* P, int c, double g, double cfl,
+                                                double dt_g, double& s0, double& s1, double& s2, double& s3) {
+    double dt = dt_g;
+    St Rs = st_make(0.0, 0.0, 0.0, 0.0);
+    const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
+    double lam = 0.0;
+    for (int e = e0; e < e1; ++e) {
+        const int ent = a.m.cf[e];
+        const int f = ent >> 1;
+        Rs += flip_if(ld_state_cg(a.ff, f), ent);
+        if (LOCAL) lam += __ldcg(a.dtf + f);
+    }
+    double coef;  // dt / V
+#ifdef FV_STRICT_ORDER
+    if (LOCAL) dt = cfl * a.m.vol[c] / lam;
+    coef = dt / a.m.vol[c];
+#else
+    coef = LOCAL ? cfl * fvconv::rcp_nr3(lam) : dt / a.m.vol[c];
+#endif
+    s0 = Rs.r * Rs.r; s1 = Rs.ru * Rs.ru; s2 = Rs.rv * Rs.rv; s3 = Rs.E * Rs.E;
+    const St u = ld_state_cg(a.U, c);
+    const St un = u + coef * Rs;
+    st_state(a.U, c, un);
+    st_prim(P, c, prim_of(un, g));
+}
+
 // Grid barrier with a bounded wait.  Returns false (in every thread of the
 // block) once any block has given up; the caller then returns.
 __device__ __forceinline__ bool grid_barrier(PersistCtl* pc, unsigned int expected) {
@@ -262,26 +322,8 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_o1_persistent(const O1Args
         // each block takes an equal contiguous range of faces, so that every
         // SM (the grid is a multiple of the SM count) gets the same share
         const int f0 = (int)((long long)F * blockIdx.x / nb), f1 = (int)((long long)F * (blockIdx.x + 1) / nb);
-        for (int f = f0 + threadIdx.x; f < f1; f += blockDim.x) {
-            const int L = a.m.fl[f], R = a.m.fr[f];
-            const double4_32a geo = a.m.fgeom[f];
-            const St UL = ld_state_cg(a.U, L);
-            const Prim PL = ld_prim(P, L);
-            St UR;
-            Prim PR;
-            if (R >= 0) {
-                UR = ld_state_cg(a.U, R);
-                PR = ld_prim(P, R);
-            } else {
-                UR = ghost_state(a.bc, a.m.fpatch[f], UL, geo.x, geo.y, g);
-                PR = prim_of(UR, g);
-            }
-            const St Fl = num_flux_p<FLUX>(UL, PL, UR, PR, geo.x, geo.y, g, a.exact_tol, a.exact_max_iter);
-            st_state(a.ff, f, geo.z * Fl);
-            const double Smax = face_smax_p(PL, PR, R >= 0, geo.x, geo.y);
-            if (LOCAL) a.dtf[f] = Smax * geo.z;
-            else cand = fmin(cand, cfl * geo.w / Smax);
-        }
+        for (int f = f0 + threadIdx.x; f < f1; f += blockDim.x)
+            cand = fmin(cand, face_phase_face<FLUX, LOCAL>(a, P, f, g, cfl));
         if (!LOCAL) {
             __shared__ double smin[fvgb::kCellBlock / 32];
             cand = warp_min(cand);
@@ -300,30 +342,7 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_o1_persistent(const O1Args
         for (int tile = blockIdx.x; tile < n_tiles; tile += nb) {
             const int c = tile * fvgb::kCellBlock + threadIdx.x;
             double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-            if (c < N) {
-                double dt = dt_g;
-                St Rs = st_make(0.0, 0.0, 0.0, 0.0);
-                const int e0 = a.m.cf_off[c], e1 = a.m.cf_off[c + 1];
-                double lam = 0.0;
-                for (int e = e0; e < e1; ++e) {
-                    const int ent = a.m.cf[e];
-                    const int f = ent >> 1;
-                    Rs += flip_if(ld_state_cg(a.ff, f), ent);
-                    if (LOCAL) lam += __ldcg(a.dtf + f);
-                }
-                double coef;  // dt / V
-#ifdef FV_STRICT_ORDER
-                if (LOCAL) dt = cfl * a.m.vol[c] / lam;
-                coef = dt / a.m.vol[c];
-#else
-                coef = LOCAL ? cfl * fvconv::rcp_nr3(lam) : dt / a.m.vol[c];
-#endif
-                s0 = Rs.r * Rs.r; s1 = Rs.ru * Rs.ru; s2 = Rs.rv * Rs.rv; s3 = Rs.E * Rs.E;
-                const St u = ld_state_cg(a.U, c);
-                const St un = u + coef * Rs;
-                st_state(a.U, c, un);
-                st_prim(P, c, prim_of(un, g));
-            }
+            if (c < N) cell_phase_cell<LOCAL>(a, P, c, g, cfl, dt_g, s0, s1, s2, s3);
             // the tile's partial: finish_norms' block reduction
             __shared__ double red[fvgb::kCellBlock / 32][4];
             const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -340,6 +359,215 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_o1_persistent(const O1Args
         if (!grid_barrier(pc, expected)) return;
     }
     if (blockIdx.x == 0 && nsteps > 0) fold_step_norms(a.ctl, a.partials, n_tiles, a.hist, a.hist_cap);
+}
+
+// ---------------------------------------------------------------------------
+// Dataflow form (local dt only).  The local-dt step has no global
+// dependency inside a step, only the face -> cell -> face ones between
+// neighbouring cells, so the grid barriers of k_o1_persistent are replaced
+// by waits on the few blocks that share faces with this one (DfPlan).
+// Blocks then drift by up to a step against distant blocks instead of
+// meeting at every phase, and each block's wait costs one L2 round trip to
+// a neighbour's progress word instead of a 2 x grid-wide arrival.  One block
+// of kDfBlock threads per SM owns a contiguous range of whole cell warps
+// (a Morton-ordered mesh keeps that range compact, so a block has a handful
+// of neighbours).  The arithmetic per face and per cell is
+// face_phase_face / cell_phase_cell, and the norm partials are formed per
+// 32-cell warp and folded tile by tile in k_cell_o1's order, so fields and
+// residual histories are the same bits as the barrier form's.
+
+// Thread 0 waits until every block in deps[0..n) has published progress
+// >= target and, when ring_step >= 0, until ring slot `slot` has been
+// folded up to step ring_step; bounded by pc->limit cycles like the grid
+// barrier (a wait that runs out sets pc->err; every later wait then gives
+// up at once).  Returns false in every thread when the launch must end.
+__device__ __forceinline__ bool df_wait(PersistCtl* pc, const unsigned int* prog, const int* deps, int n,
+                                        unsigned int target, const int* folded, int slot, int ring_step) {
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        volatile int* verr = &pc->err;
+        const long long t0 = clock64();
+        const long long lim = pc->limit;
+        int good = 1;
+        for (int i = 0; i < n && good; ++i) {
+            const volatile unsigned int* p = prog + deps[i];
+            while (*p < target) {
+                if (*verr || clock64() - t0 > lim) {
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        if (good && ring_step >= 0) {
+            const volatile int* q = folded + slot;
+            while (*q < ring_step) {
+                if (*verr || clock64() - t0 > lim) {
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        if (!good) atomicExch(&pc->err, 1);
+        __threadfence();
+        ok = good && !*verr;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// All of this block's writes of the phase are done (block barrier), then
+// made visible (fence) before its progress word moves.
+__device__ __forceinline__ void df_publish(unsigned int* prog, unsigned int v) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicExch(prog + blockIdx.x, v);
+    }
+}
+
+// Fold of one step's per-warp partials in the order of fold_step_norms over
+// k_cell_o1's tile partials: a tile's partial is the sum of its 8 warp
+// sums in warp order (from 0.0; warps past the last cell add nothing, as
+// their zero sums add nothing there), the tiles are strided over the first
+// kCellBlock threads, then the transposed warp sums and the warps in order.
+__device__ __forceinline__ void df_fold(const O1Args& a, const DfPlan& d, int slot, int row) {
+    constexpr int nw = fvgb::kCellBlock / 32;
+    __shared__ double red[nw][4];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int n_tiles = (a.m.n_cells + fvgb::kCellBlock - 1) / fvgb::kCellBlock;
+    const double* wp = d.wpart + (size_t)slot * d.n_warps * 4;
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    if (tid < fvgb::kCellBlock) {
+        for (int tile = tid; tile < n_tiles; tile += fvgb::kCellBlock) {
+            double v[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int i = 0; i < nw; ++i) {
+                const int cw = tile * nw + i;
+                if (cw < d.n_warps) {
+                    const double2* p = reinterpret_cast<const double2*>(wp + 4 * (size_t)cw);
+                    const double2 x = __ldcg(p), y = __ldcg(p + 1);
+                    v[0] += x.x; v[1] += x.y; v[2] += y.x; v[3] += y.y;
+                }
+            }
+            t[0] += v[0]; t[1] += v[1]; t[2] += v[2]; t[3] += v[3];
+        }
+    }
+    const double ts = warp_sum4(t[0], t[1], t[2], t[3]);
+    if (w < nw && (lane & 7) == 0) red[w][lane >> 3] = ts;
+    __syncthreads();
+    if (tid == 0) {
+        int bad = 0;
+        for (int k = 0; k < 4; ++k) {
+            double v = 0.0;
+            for (int i = 0; i < nw; ++i) v += red[i][k];
+            const double n = sqrt(v);
+            if (!isfinite(n)) bad = 1;
+            a.hist[row * 4 + k] = n;
+            d.fnorm[slot * 4 + k] = n;
+        }
+        if (bad) a.ctl->nonfinite = 1;
+    }
+    __syncthreads();
+}
+
+template <int FLUX>
+__global__ void __launch_bounds__(fvgb::kDfBlock, 1) k_o1_dataflow(const O1Args a, double4_32a* __restrict__ P,
+                                                                  PersistCtl* __restrict__ pc, const DfPlan d,
+                                                                  int nsteps) {
+    constexpr int R = fvgb::kDfRing;
+    const double g = a.gamma;
+    const int b = blockIdx.x, nb = gridDim.x;
+    const unsigned int expected = (unsigned int)nb + (unsigned int)pc->phantom;
+    const int N = a.m.n_cells;
+    const int c0 = d.cell_off[b], c1 = d.cell_off[b + 1];
+    const int fa = d.face_off[b], fz = d.face_off[b + 1];
+    const int step0 = a.ctl->step;
+    const double cfl = a.ctl->cfl;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int nwarps = fvgb::kDfBlock / 32;
+
+    __shared__ int dep_f[fvgb::kDfMaxDeps], dep_c[fvgb::kDfMaxDeps];
+    __shared__ int folder;
+    const int nf = d.dep_face_off[b + 1] - d.dep_face_off[b];
+    const int nc = d.dep_cell_off[b + 1] - d.dep_cell_off[b];
+    if (threadIdx.x < nf) dep_f[threadIdx.x] = d.dep_face[d.dep_face_off[b] + threadIdx.x];
+    if (threadIdx.x < nc) dep_c[threadIdx.x] = d.dep_cell[d.dep_cell_off[b] + threadIdx.x];
+
+    // prologue: primitives of the own cells, progress words and ring reset
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) st_prim(P, c, prim_of(ld_state_cg(a.U, c), g));
+    if (threadIdx.x == 0) d.prog[b] = 0u;
+    if (b == 0 && threadIdx.x < R) {
+        d.arrive[threadIdx.x] = 0u;
+        d.folded[threadIdx.x] = (int)threadIdx.x - R;
+    }
+    if (!grid_barrier(pc, expected)) return;
+
+    for (int s = 0; s < nsteps; ++s) {
+        const int slot = s % R;
+        // face phase: the right cells' states of step s are final
+        if (s > 0 && !df_wait(pc, d.prog, dep_f, nf, 2u * s, d.folded, 0, -1)) return;
+        for (int j = fa + threadIdx.x; j < fz; j += blockDim.x)
+            face_phase_face<FLUX, true>(a, P, d.faces[j], g, cfl);
+        df_publish(d.prog, 2u * s + 1u);
+
+        // cell phase: every face of the own cells has its step-s flux, no
+        // block still reads the own cells' step-s states, and the ring slot
+        // is free
+        if (!df_wait(pc, d.prog, dep_c, nc, 2u * s + 1u, d.folded, slot, s - R)) return;
+        for (int cw = c0 / 32 + warp; cw * 32 < c1; cw += nwarps) {
+            const int c = cw * 32 + lane;
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            if (c < N) cell_phase_cell<true>(a, P, c, g, cfl, 0.0, s0, s1, s2, s3);
+            const double ws = warp_sum4(s0, s1, s2, s3);
+            if ((lane & 7) == 0) d.wpart[((size_t)slot * d.n_warps + cw) * 4 + (lane >> 3)] = ws;
+        }
+        df_publish(d.prog, 2u * s + 2u);
+        if (threadIdx.x == 0) {
+            const unsigned int before = atomicAdd(d.arrive + slot, 1u);
+            folder = before == (unsigned int)nb - 1u;
+            if (folder) {
+                atomicExch(d.arrive + slot, 0u);
+                __threadfence();
+            }
+        }
+        __syncthreads();
+        if (folder) {
+            df_fold(a, d, slot, (step0 + s) % a.hist_cap);
+            if (threadIdx.x == 0) {
+                __threadfence();
+                atomicExch(d.folded + slot, s);
+            }
+        }
+    }
+    if (!grid_barrier(pc, expected)) return;
+    if (b == 0 && threadIdx.x == 0 && nsteps > 0) {
+        const int slot = (nsteps - 1) % R;
+        for (int k = 0; k < 4; ++k) a.ctl->norms[k] = __ldcg(d.fnorm + slot * 4 + k);
+        a.ctl->step = step0 + nsteps;
+    }
+}
+
+template <int FLUX>
+static int o1df_blocks_per_sm() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_o1_dataflow<FLUX>, fvgb::kDfBlock, 0) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
+template <int FLUX>
+static cudaError_t launch_o1df(const O1Args& a, double4_32a* P, PersistCtl* pc, const DfPlan& d, int nsteps,
+                               int grid, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(fvgb::kDfBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_o1_dataflow<FLUX>, a, P, pc, d, nsteps);
 }
 
 template <int FLUX, bool LOCAL>
@@ -384,6 +612,21 @@ int o1p_max_blocks_per_sm(int flux, int local) {
         case 3: return ::FV_KNS::o1p_blocks_per_sm<1, true>();
         case 4: return ::FV_KNS::o1p_blocks_per_sm<2, false>();
         default: return ::FV_KNS::o1p_blocks_per_sm<2, true>();
+    }
+}
+int o1df_max_blocks_per_sm(int flux) {
+    switch (flux) {
+        case 0: return ::FV_KNS::o1df_blocks_per_sm<0>();
+        case 1: return ::FV_KNS::o1df_blocks_per_sm<1>();
+        default: return ::FV_KNS::o1df_blocks_per_sm<2>();
+    }
+}
+cudaError_t launch_o1_dataflow(const O1Args& a, double4_32a* P, PersistCtl* pc, const DfPlan& d, int nsteps,
+                               int grid, cudaStream_t s) {
+    switch (a.flux) {
+        case 0: return ::FV_KNS::launch_o1df<0>(a, P, pc, d, nsteps, grid, s);
+        case 1: return ::FV_KNS::launch_o1df<1>(a, P, pc, d, nsteps, grid, s);
+        default: return ::FV_KNS::launch_o1df<2>(a, P, pc, d, nsteps, grid, s);
     }
 }
 cudaError_t launch_o1_persistent(const O1Args& a, double4_32a* P, PersistCtl* pc, int nsteps, int grid,

@@ -196,6 +196,7 @@ void Solver::init(const HostMesh& hm, const fv_bc_t* bcs, int n_bcs, double g, d
             p0.limit = kDefaultWaitCycles;
             h2d_sync(pctl, &p0, sizeof(p0), stream);
             persistent = true;
+            if (opt.dt_mode == FV_DT_LOCAL) build_dataflow(hm, sms);
         }
     }
 
@@ -541,6 +542,72 @@ void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* ev
     }
 }
 
+void Solver::build_dataflow(const HostMesh& hm, int sms) {
+    // One block per SM (fewer on a mesh of fewer 32-cell warps), each
+    // owning an equal share of whole cell warps and the faces whose left
+    // cell it owns; the dependency lists are the blocks it shares faces
+    // with.  A mesh whose cell order leaves a block more neighbours than
+    // kDfMaxDeps keeps the barrier form.
+    const int per_sm = opt.strict ? strict::o1df_max_blocks_per_sm(opt.flux) : fast::o1df_max_blocks_per_sm(opt.flux);
+    if (per_sm < 1 || sms < 1) return;
+    const int Wn = (N + 31) / 32;
+    const int nb = std::min(sms, Wn);
+    std::vector<int> cell_off(nb + 1), owner(N);
+    for (int b = 0; b <= nb; ++b) cell_off[b] = (int)std::min<long long>(32LL * ((long long)Wn * b / nb), N);
+    for (int b = 0; b < nb; ++b)
+        for (int c = cell_off[b]; c < cell_off[b + 1]; ++c) owner[c] = b;
+    std::vector<int> face_off(nb + 1, 0), faces(F);
+    for (int f = 0; f < F; ++f) ++face_off[owner[hm.d_fl[f]] + 1];
+    for (int b = 0; b < nb; ++b) face_off[b + 1] += face_off[b];
+    {
+        std::vector<int> pos(face_off.begin(), face_off.end() - 1);
+        for (int f = 0; f < F; ++f) faces[pos[owner[hm.d_fl[f]]]++] = f;
+    }
+    std::vector<std::vector<int>> dface(nb), dcell(nb);
+    for (int f = 0; f < F; ++f) {
+        if (hm.d_fr[f] < 0) continue;
+        const int a = owner[hm.d_fl[f]], r = owner[hm.d_fr[f]];
+        if (a == r) continue;
+        dface[a].push_back(r);  // a's face phase reads r's cells
+        dcell[r].push_back(a);  // r's cell phase reads a's faces
+    }
+    std::vector<int> df, dfo(nb + 1, 0), dc, dco(nb + 1, 0);
+    for (int b = 0; b < nb; ++b) {
+        for (auto* v : {&dface[b], &dcell[b]}) {
+            std::sort(v->begin(), v->end());
+            v->erase(std::unique(v->begin(), v->end()), v->end());
+            if ((int)v->size() > kDfMaxDeps) return;
+        }
+        df.insert(df.end(), dface[b].begin(), dface[b].end());
+        dc.insert(dc.end(), dcell[b].begin(), dcell[b].end());
+        dfo[b + 1] = (int)df.size();
+        dco[b + 1] = (int)dc.size();
+    }
+    if (df.empty()) df.push_back(0);
+    if (dc.empty()) dc.push_back(0);
+    dfp.faces = dupload(faces, owned);
+    dfp.face_off = dupload(face_off, owned);
+    dfp.cell_off = dupload(cell_off, owned);
+    dfp.dep_face = dupload(df, owned);
+    dfp.dep_face_off = dupload(dfo, owned);
+    dfp.dep_cell = dupload(dc, owned);
+    dfp.dep_cell_off = dupload(dco, owned);
+    dfp.prog = dalloc<unsigned int>(nb, owned);
+    dfp.arrive = dalloc<unsigned int>(kDfRing, owned);
+    dfp.folded = dalloc<int>(kDfRing, owned);
+    dfp.fnorm = dalloc<double>(4 * kDfRing, owned);
+    dfp.wpart = dalloc<double>((size_t)4 * kDfRing * Wn, owned);
+    dfp.n_warps = Wn;
+    FV_CUDA(cudaMemsetAsync(dfp.arrive, 0, kDfRing * sizeof(unsigned int), stream));
+    df_grid = nb;
+    dataflow_ok = true;
+}
+
+int Solver::persistent_form() const {
+    if (!persistent) return 0;
+    return dataflow_ok && !barrier_form ? 2 : 1;
+}
+
 void Solver::launch_steps(int k, std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos) {
     if (!persistent) {
         for (int i = 0; i < k; ++i) launch_step(classes, events, ev_pos);
@@ -549,19 +616,27 @@ void Solver::launch_steps(int k, std::vector<int>* classes, std::vector<cudaEven
     // re-arm the barrier (arrival counter, error flag), then one launch
     FV_CUDA(cudaMemsetAsync(pctl, 0, 2 * sizeof(int), stream));
     const O1Args a = o1_args();
-    const cudaError_t rc = opt.strict ? strict::launch_o1_persistent(a, Pc, pctl, k, p_grid, stream)
-                                      : fast::launch_o1_persistent(a, Pc, pctl, k, p_grid, stream);
+    cudaError_t rc;
+    if (persistent_form() == 2)
+        rc = opt.strict ? strict::launch_o1_dataflow(a, Pc, pctl, dfp, k, df_grid, stream)
+                        : fast::launch_o1_dataflow(a, Pc, pctl, dfp, k, df_grid, stream);
+    else
+        rc = opt.strict ? strict::launch_o1_persistent(a, Pc, pctl, k, p_grid, stream)
+                        : fast::launch_o1_persistent(a, Pc, pctl, k, p_grid, stream);
     FV_CUDA(rc);
     if (classes) classes->push_back(1);
     if (events) FV_CUDA(cudaEventRecord((*events)[++*ev_pos], stream));
 }
 
-void Solver::set_persistent(bool on) {
+void Solver::set_persistent(int mode) {
+    if (mode < 0 || mode > 2) raise(FV_ERR_BAD_ARG, "persistent mode must be 0, 1 or 2");
+    const bool on = mode != 0;
     if (on && !persistent_ok)
         raise(FV_ERR_UNSUPPORTED, "the persistent kernel covers the first-order forward-Euler FP64 Euler path on a "
                                   "device with cooperative launch");
     FV_CUDA(cudaStreamSynchronize(stream));
     persistent = on;
+    barrier_form = mode == 2;
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
 }
@@ -580,7 +655,9 @@ void Solver::check_persistent() {
     FV_CUDA(cudaMemcpyAsync(&err, reinterpret_cast<const char*>(pctl) + offsetof(PersistCtl, err), sizeof(int),
                             cudaMemcpyDeviceToHost, stream));
     FV_CUDA(cudaStreamSynchronize(stream));
-    if (err) raise(FV_ERR_TIMEOUT, "a grid barrier of the persistent kernel gave up waiting (the state is unspecified)");
+    if (err)
+        raise(FV_ERR_TIMEOUT,
+              "a wait of the persistent kernel (grid barrier or neighbour progress) gave up (the state is unspecified)");
 }
 
 void Solver::step_timed(int n, double ms[3], int launches[3]) {
@@ -1145,15 +1222,16 @@ int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]) {
 int fv_solver_set_persistent(fv_solver_t s, int32_t on) {
     return guarded([&] {
         if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
-        s->s.set_persistent(on != 0);
+        s->s.set_persistent(on);
     });
 }
 
 int fv_solver_persistent(fv_solver_t s, int32_t* on, int32_t* grid) {
     return guarded([&] {
         if (!s) fvgb::raise(FV_ERR_BAD_ARG, "null solver");
-        if (on) *on = s->s.persistent ? 1 : 0;
-        if (grid) *grid = s->s.p_grid;
+        const int form = s->s.persistent_form();
+        if (on) *on = form;
+        if (grid) *grid = form == 2 ? s->s.df_grid : s->s.p_grid;
     });
 }
 

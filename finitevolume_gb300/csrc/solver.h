@@ -116,6 +116,12 @@ struct Solver {
     int p_grid = 0;                 // co-resident blocks of the launch
     PersistCtl* pctl = nullptr;
     double4_32a* Pc = nullptr;      // per-cell primitives u, v, p, c
+    // Its dataflow form (local dt): neighbour waits instead of grid
+    // barriers, one block per SM (DfPlan).  Used unless barrier_form.
+    bool dataflow_ok = false;
+    bool barrier_form = false;
+    int df_grid = 0;
+    DfPlan dfp{};
     static constexpr int kPersistChunk = 256;
     static constexpr long long kDefaultWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
@@ -135,7 +141,12 @@ struct Solver {
     void launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos);
     // k steps: one persistent launch, or k x launch_step
     void launch_steps(int k, std::vector<int>* classes, std::vector<cudaEvent_t>* events, size_t* ev_pos);
-    void set_persistent(bool on);
+    // 0 two-kernel path, 1 persistent (dataflow form where planned), 2
+    // persistent barrier form
+    void set_persistent(int mode);
+    // 0 two-kernel path, 1 barrier form, 2 dataflow form
+    int persistent_form() const;
+    void build_dataflow(const HostMesh& hm, int sms);
     void set_wait_limit(long long cycles, int phantom);
     // FV_ERR_TIMEOUT if a persistent launch gave up at a grid barrier
     void check_persistent();

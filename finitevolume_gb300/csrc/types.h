@@ -64,6 +64,37 @@ struct PersistCtl {
     unsigned long long dt_slot[2];
 };
 
+// Plan of the dataflow form of the persistent first-order kernel (local
+// dt): block b owns the cells [cell_off[b], cell_off[b+1]) (whole 32-cell
+// warps) and the faces whose left cell it owns (faces[face_off[b] ..
+// face_off[b+1])).  Instead of grid barriers, each phase waits only for the
+// blocks it shares faces with: the face phase of step s for the cell phase
+// of step s-1 of dep_face's blocks (the owners of its faces' right cells),
+// the cell phase for the face phase of step s of dep_cell's blocks (the
+// owners of the other faces of its cells).  prog[b] is 2s+1 once block b
+// has finished the face phase of step s and 2s+2 once it has finished the
+// cell phase.  Each warp of cells leaves its residual partial in a ring of
+// kDfRing step slots; the last block to finish a step's cell phase folds
+// that step's norms and marks the slot free (folded[slot] = step).
+struct DfPlan {
+    const int* faces;         // [F] face ids grouped by owning block
+    const int* face_off;      // [nb+1]
+    const int* cell_off;      // [nb+1]
+    const int* dep_face;      // blocks the face phase waits for
+    const int* dep_face_off;  // [nb+1]
+    const int* dep_cell;      // blocks the cell phase waits for
+    const int* dep_cell_off;  // [nb+1]
+    unsigned int* prog;       // [nb]
+    unsigned int* arrive;     // [kDfRing] cell-phase arrivals per slot
+    int* folded;              // [kDfRing] last step folded from each slot
+    double* fnorm;            // [kDfRing * 4] norms of the step folded there
+    double* wpart;            // [kDfRing * n_warps * 4] per-warp partials
+    int n_warps;              // cell warps, ceil(N / 32)
+};
+constexpr int kDfBlock = 512;   // threads per block (one block per SM)
+constexpr int kDfRing = 8;      // norm-partial slots
+constexpr int kDfMaxDeps = 32;  // dependency list bound per block and phase
+
 struct O1Args {
     DevMesh m;
     St* U;
@@ -190,6 +221,18 @@ namespace strict {
 int o1p_max_blocks_per_sm(int flux, int local);
 cudaError_t launch_o1_persistent(const O1Args& a, double4_32a* P, PersistCtl* pc, int nsteps, int grid,
                                  cudaStream_t s);
+}  // namespace strict
+// Its dataflow form for local dt (grid = the plan's block count, kDfBlock
+// threads per block, at most one block per SM).
+namespace fast {
+int o1df_max_blocks_per_sm(int flux);
+cudaError_t launch_o1_dataflow(const O1Args& a, double4_32a* P, PersistCtl* pc, const DfPlan& d, int nsteps,
+                               int grid, cudaStream_t s);
+}  // namespace fast
+namespace strict {
+int o1df_max_blocks_per_sm(int flux);
+cudaError_t launch_o1_dataflow(const O1Args& a, double4_32a* P, PersistCtl* pc, const DfPlan& d, int nsteps,
+                               int grid, cudaStream_t s);
 }  // namespace strict
 
 }  // namespace fvgb

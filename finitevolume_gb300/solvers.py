@@ -343,17 +343,20 @@ class EulerFVMSolver:
         self.last_newton_instance_steps = steps
         return hist[:it.value + 1], it.value
 
-    def set_persistent(self, on: bool = True) -> None:
+    def set_persistent(self, on=True) -> None:
         """First-order forward-Euler FP64 path: one persistent cooperative
-        launch per chunk of steps (on, the default where supported) or two
-        kernels per step (off)."""
-        capi.check(capi.lib().fv_solver_set_persistent(self._h, 1 if on else 0))
+        launch per chunk of steps (on, the default where supported; with
+        local dt in its dataflow form), two kernels per step (off), or
+        ``"barrier"`` for the grid-barrier form of the persistent kernel."""
+        mode = 2 if on == "barrier" else (1 if on else 0)
+        capi.check(capi.lib().fv_solver_set_persistent(self._h, mode))
 
     def persistent(self):
-        """(in use, grid size in blocks) of the persistent kernel."""
+        """(form in use, grid size in blocks) of the persistent kernel: form
+        0 two-kernel path, 1 grid-barrier form, 2 dataflow form."""
         on, grid = C.c_int32(), C.c_int32()
         capi.check(capi.lib().fv_solver_persistent(self._h, C.byref(on), C.byref(grid)))
-        return bool(on.value), int(grid.value)
+        return int(on.value), int(grid.value)
 
     def set_wait_limit(self, cycles: int, phantom_arrivals: int = 0) -> None:
         """Bound (SM clock cycles) on each grid-barrier wait of the persistent

@@ -225,10 +225,14 @@ int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]);
  * steps, meeting the flux -> update and global-dt dependencies at grid
  * barriers instead of kernel boundaries; same results as the two-kernel
  * path (bit for bit in strict mode).  On by default where the device
- * supports cooperative launch; on = 0 selects the two-kernel path.
- * fv_solver_persistent reports whether it is in use and its grid size
- * (either pointer may be NULL).  No reference counterpart (the reference's
- * loops are OpenMP). */
+ * supports cooperative launch; on = 0 selects the two-kernel path.  With
+ * local time stepping the kernel runs in a dataflow form: one block per SM
+ * owns a range of cells, and each phase waits only for the blocks it shares
+ * faces with instead of for the whole grid (same results again); on = 2
+ * keeps the grid-barrier form.  fv_solver_persistent reports the form in
+ * use (0 two-kernel path, 1 grid-barrier form, 2 dataflow form) and its
+ * grid size (either pointer may be NULL).  No reference counterpart (the
+ * reference's loops are OpenMP). */
 int fv_solver_set_persistent(fv_solver_t s, int32_t on);
 int fv_solver_persistent(fv_solver_t s, int32_t* on, int32_t* grid);
 /* Bound on every grid-barrier wait of the persistent kernel, in SM clock

@@ -1,15 +1,20 @@
 """The persistent first-order kernel (one cooperative launch per chunk of
-steps, grid barriers between the face and cell phases) against the
-two-kernel path, and its bounded barrier waits.
+steps, grid barriers between the face and cell phases, or with local dt
+neighbour-progress waits: the dataflow form) against the two-kernel path,
+and its bounded waits.
 
 - Same fields and residual histories bit for bit as the two-kernel path in
   strict mode (Rusanov and HLLC, global dt with the fixed farfield, local dt
   with the characteristic farfield), and within 1e-10 in the default build
   (which forms 1/rho and the local-dt factor with fewer FP64 instructions).
+- The dataflow form (the default with local dt) gives the same fields and
+  histories as the grid-barrier form, bit for bit in strict mode, on meshes
+  from 64 blocks of one cell warp each to blocks of several hundred cells
+  and faces (the loops over a block's cells and faces).
 - A barrier that waits for an arrival that never comes gives up after its
   cycle limit: fv_step returns FV_ERR_TIMEOUT, nothing hangs, the state is
   untouched (the first barrier precedes every update) and the solver steps
-  normally once the limit is restored.
+  normally once the limit is restored; in both forms.
 
 Reference: src/EulerFVMSolver.cpp:58-162 (step, compute_dt).
 """
@@ -39,7 +44,7 @@ def test_persistent_matches_two_kernel_path(gpu, flux, local, strict):
     a = gpu_solver(poly, bcs, ic, flux, cfl=0.5, local_dt=local, strict=strict)
     b = gpu_solver(poly, bcs, ic, flux, cfl=0.5, local_dt=local, strict=strict)
     on, grid = a.persistent()
-    assert on and grid > 0
+    assert on == (2 if local else 1) and grid > 0
     b.set_persistent(False)
     assert not b.persistent()[0]
     ha = a.run(300, history=True)
@@ -57,10 +62,33 @@ def test_persistent_matches_two_kernel_path(gpu, flux, local, strict):
     assert np.array_equal(c.field(), a.field())
 
 
-def test_barrier_wait_runs_out_and_reports_timeout(gpu):
+@pytest.mark.parametrize("flux", ["rusanov", "hllc"])
+@pytest.mark.parametrize("strict", [True, False])
+@pytest.mark.parametrize("size", [(64, 32), (128, 64), (512, 256)])
+def test_dataflow_form_matches_barrier_form(gpu, flux, strict, size):
+    poly = meshgen.naca_ogrid(*size)
+    bcs, ic = _case(True)
+    a = gpu_solver(poly, bcs, ic, flux, cfl=0.5, local_dt=True, strict=strict)
+    b = gpu_solver(poly, bcs, ic, flux, cfl=0.5, local_dt=True, strict=strict)
+    b.set_persistent("barrier")
+    assert a.persistent()[0] == 2 and b.persistent()[0] == 1
+    n = 300 if size[0] < 512 else 60
+    ha = a.run(n, history=True)
+    hb = b.run(n, history=True)
+    if strict:
+        assert np.array_equal(a.field(), b.field())
+        assert np.array_equal(ha, hb)
+    else:
+        assert rel_err(a.field(), b.field()) <= 1e-13
+        np.testing.assert_allclose(ha, hb, rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("local", [False, True])
+def test_barrier_wait_runs_out_and_reports_timeout(gpu, local):
     poly = meshgen.naca_ogrid(64, 32)
-    bcs, ic = _case(False)
-    s = gpu_solver(poly, bcs, ic, "rusanov", cfl=0.5)
+    bcs, ic = _case(local)
+    s = gpu_solver(poly, bcs, ic, "rusanov", cfl=0.5, local_dt=local)
+    assert s.persistent()[0] == (2 if local else 1)
     s.run(5)
     before = s.field()
     # every barrier now waits for one more block than the grid has
@@ -72,6 +100,6 @@ def test_barrier_wait_runs_out_and_reports_timeout(gpu):
     # restored: steps again, same as a solver that never timed out
     s.set_wait_limit(2_000_000_000, phantom_arrivals=0)
     s.run(3)
-    ref = gpu_solver(poly, bcs, ic, "rusanov", cfl=0.5)
+    ref = gpu_solver(poly, bcs, ic, "rusanov", cfl=0.5, local_dt=local)
     ref.run(8)
     assert np.array_equal(s.field(), ref.field())
