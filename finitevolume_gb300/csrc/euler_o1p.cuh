@@ -166,6 +166,75 @@ __device__ __forceinline__ double face_smax_p(const Prim& PL, const Prim& PR, bo
     return Smax;
 }
 
+#ifndef FV_STRICT_ORDER
+// The characteristic farfield (physics.cuh, char_farfield) from the
+// interior primitives P instead of the conserved state, returning the
+// ghost's primitives too: its sound speed is |cb| (p_b = rho_b cb^2 / g),
+// and the boundary density rho_s (cb^2 / (g s))^(1/(g-1)) with the upwind
+// side's entropy s = p_s / rho_s^g is rho_s |cb / c_s|^(2/(g-1)), taken by
+// pow_near1.  This is the longest dependent chain of the face phase and a
+// few blocks own all the farfield faces, so no division, square root or
+// library power depends on the interior state here.
+__device__ __forceinline__ void char_farfield_p(const St& UL, const Prim& PL, const double* sinf, double nx,
+                                                double ny, double g, St& UR, Prim& PR) {
+    const double rf = sinf[0], irf = fvconv::rcp_nr3(rf), uf = sinf[1] * irf, vf = sinf[2] * irf;
+    const double pf = (g - 1.0) * (sinf[3] - 0.5 * rf * (uf * uf + vf * vf));
+    const double cf = sqrt(g * pf * irf);
+    const double vni = PL.u * nx + PL.v * ny, vnf = uf * nx + vf * ny;
+    const double ici = fvconv::rcp_nr3(PL.c), icf = fvconv::rcp_nr3(cf);  // off the chain
+    if (vnf <= -cf) {  // supersonic inflow
+        UR = st_make(sinf[0], sinf[1], sinf[2], sinf[3]);
+        PR.u = uf; PR.v = vf; PR.p = pf; PR.c = cf;
+        return;
+    }
+    if (vni >= PL.c) {  // supersonic outflow
+        UR = UL;
+        PR = PL;
+        return;
+    }
+    const double k = 2.0 / (g - 1.0);
+    const double Rp = vni + k * PL.c, Rm = vnf - k * cf;
+    const double vnb = 0.5 * (Rp + Rm);
+    const double cb = 0.25 * (g - 1.0) * (Rp - Rm);
+    const bool out = vnb > 0.0;
+    const double rs = out ? UL.r : rf, ics = out ? ici : icf;
+    const double ut = out ? PL.u - vni * nx : uf - vnf * nx;
+    const double vt = out ? PL.v - vni * ny : vf - vnf * ny;
+    const double rb = rs * fvconv::pow_near1(fabs(cb) * ics, k);
+    const double ub = ut + vnb * nx, vb = vt + vnb * ny;
+    const double pb = rb * cb * cb * (1.0 / g);
+    UR = st_make(rb, rb * ub, rb * vb, pb * (1.0 / (g - 1.0)) + 0.5 * rb * (ub * ub + vb * vb));
+    PR.u = ub; PR.v = vb; PR.p = pb; PR.c = fabs(cb);
+}
+
+// Ghost state and its primitives from the interior state and primitives:
+// the characteristic farfield above; the slip wall as the mirror image
+// (density, pressure, sound speed and speed, hence E, unchanged, the
+// normal velocity reversed); outflow the interior itself; the fixed
+// farfield and the no-slip wall through ghost_state.  Same states as
+// ghost_state + prim_of up to rounding, with short dependent chains.
+__device__ __forceinline__ void ghost_p(const BCTable& bc, int patch, const St& UL, const Prim& PL, double nx,
+                                        double ny, double g, St& UR, Prim& PR) {
+    const int t = bc.type[patch];
+    if (t == BC_CHAR) {
+        char_farfield_p(UL, PL, bc.st[patch], nx, ny, g, UR, PR);
+    } else if (t == BC_WALL) {
+        const double Vn = PL.u * nx + PL.v * ny;
+        PR.u = PL.u - 2.0 * Vn * nx;
+        PR.v = PL.v - 2.0 * Vn * ny;
+        PR.p = PL.p;
+        PR.c = PL.c;
+        UR = st_make(UL.r, UL.r * PR.u, UL.r * PR.v, UL.E);
+    } else if (t == BC_OUTFLOW) {
+        UR = UL;
+        PR = PL;
+    } else {
+        UR = ghost_state(bc, patch, UL, nx, ny, g);
+        PR = prim_of(UR, g);
+    }
+}
+#endif
+
 // One face of the face phase: the flux times the face length into ff[f]
 // and, with local dt, lambda * length into dtf[f].  Returns the face's
 // global-dt candidate cfl * (CFL length) / max(|Vn| + c) (DBL_MAX with
@@ -183,8 +252,12 @@ __device__ __forceinline__ double face_phase_face(const O1Args& a, const double4
         UR = ld_state_cg(a.U, R);
         PR = ld_prim(P, R);
     } else {
+#ifndef FV_STRICT_ORDER
+        ghost_p(a.bc, a.m.fpatch[f], UL, PL, geo.x, geo.y, g, UR, PR);
+#else
         UR = ghost_state(a.bc, a.m.fpatch[f], UL, geo.x, geo.y, g);
         PR = prim_of(UR, g);
+#endif
     }
     const St Fl = num_flux_p<FLUX>(UL, PL, UR, PR, geo.x, geo.y, g, a.exact_tol, a.exact_max_iter);
     st_state(a.ff, f, geo.z * Fl);
@@ -366,90 +439,108 @@ __global__ void __launch_bounds__(fvgb::kCellBlock) k_o1_persistent(const O1Args
 // dependency inside a step, only the face -> cell -> face ones between
 // neighbouring cells, so the grid barriers of k_o1_persistent are replaced
 // by waits on the few blocks that share faces with this one (DfPlan).
-// Blocks then drift by up to a step against distant blocks instead of
-// meeting at every phase, and each block's wait costs one L2 round trip to
-// a neighbour's progress word instead of a 2 x grid-wide arrival.  One block
-// of kDfBlock threads per SM owns a contiguous range of whole cell warps
-// (a Morton-ordered mesh keeps that range compact, so a block has a handful
-// of neighbours).  The arithmetic per face and per cell is
+// Blocks then drift against distant blocks instead of meeting at every
+// phase, and a wait costs one L2 round trip to a neighbour's progress word.
+// One block of kDfBlock threads per SM owns a contiguous range of whole
+// cell warps (a Morton-ordered mesh keeps that range compact, so a block
+// has a handful of neighbours).  The arithmetic per face and per cell is
 // face_phase_face / cell_phase_cell, and the norm partials are formed per
-// 32-cell warp and folded tile by tile in k_cell_o1's order, so fields and
-// residual histories are the same bits as the barrier form's.
+// 32-cell warp and folded, after the last step, tile by tile in
+// k_cell_o1's order: fields and residual histories are the same bits as
+// the barrier form's.
+//
+// Progress words are published with st.release.gpu after a block barrier
+// (the block's writes of the phase, gathered by bar.sync, are ordered
+// before it) and polled with relaxed loads followed by one
+// fence.acq_rel.gpu and a block barrier (the PTX release/acquire pattern;
+// every data load of the next phase is an L2 load, ld.global.cg).
+
+__device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 
 // Thread 0 waits until every block in deps[0..n) has published progress
-// >= target and, when ring_step >= 0, until ring slot `slot` has been
-// folded up to step ring_step; bounded by pc->limit cycles like the grid
-// barrier (a wait that runs out sets pc->err; every later wait then gives
-// up at once).  Returns false in every thread when the launch must end.
+// >= target, bounded by pc->limit cycles like the grid barrier (a wait that
+// runs out, or sees pc->err set by another block, sets pc->err and ends
+// the launch).  Returns false in every thread when the launch must end.
 __device__ __forceinline__ bool df_wait(PersistCtl* pc, const unsigned int* prog, const int* deps, int n,
-                                        unsigned int target, const int* folded, int slot, int ring_step) {
+                                        unsigned int target) {
     __shared__ int ok;
     if (threadIdx.x == 0) {
-        volatile int* verr = &pc->err;
+        const volatile int* verr = &pc->err;
         const long long t0 = clock64();
         const long long lim = pc->limit;
         int good = 1;
         for (int i = 0; i < n && good; ++i) {
-            const volatile unsigned int* p = prog + deps[i];
-            while (*p < target) {
-                if (*verr || clock64() - t0 > lim) {
-                    good = 0;
-                    break;
-                }
-            }
-        }
-        if (good && ring_step >= 0) {
-            const volatile int* q = folded + slot;
-            while (*q < ring_step) {
-                if (*verr || clock64() - t0 > lim) {
+            const unsigned int* p = prog + (size_t)deps[i] * fvgb::kDfProgStride;
+            for (unsigned int it = 0; ld_relaxed_gpu(p) < target; ++it) {
+                if ((it & 31u) == 31u && (*verr || clock64() - t0 > lim)) {
                     good = 0;
                     break;
                 }
             }
         }
         if (!good) atomicExch(&pc->err, 1);
-        __threadfence();
-        ok = good && !*verr;
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        ok = good;
     }
     __syncthreads();
     return ok != 0;
 }
 
 // All of this block's writes of the phase are done (block barrier), then
-// made visible (fence) before its progress word moves.
+// its progress word moves with release semantics.
 __device__ __forceinline__ void df_publish(unsigned int* prog, unsigned int v) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        atomicExch(prog + blockIdx.x, v);
+        unsigned int* p = prog + (size_t)blockIdx.x * fvgb::kDfProgStride;
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
     }
 }
 
-// Fold of one step's per-warp partials in the order of fold_step_norms over
-// k_cell_o1's tile partials: a tile's partial is the sum of its 8 warp
-// sums in warp order (from 0.0; warps past the last cell add nothing, as
-// their zero sums add nothing there), the tiles are strided over the first
+// Fold of step s's per-warp partials in the order of fold_step_norms over
+// k_cell_o1's tile partials: a tile's partial is the sum of its 8 warp sums
+// in warp order (from 0.0; warps past the last cell add nothing, as their
+// zero sums add nothing there), the tiles are strided over the first
 // kCellBlock threads, then the transposed warp sums and the warps in order.
-__device__ __forceinline__ void df_fold(const O1Args& a, const DfPlan& d, int slot, int row) {
+// The warp partials are staged in shared memory kDfBlock at a time (64
+// tiles), so that the loads are one round of independent L2 reads.
+__device__ __forceinline__ void df_fold(const O1Args& a, const DfPlan& d, int s, int row, bool last) {
     constexpr int nw = fvgb::kCellBlock / 32;
+    constexpr int CH = fvgb::kDfBlock;
+    __shared__ double2 wsm[CH][2];
     __shared__ double red[nw][4];
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int W = d.n_warps;
     const int n_tiles = (a.m.n_cells + fvgb::kCellBlock - 1) / fvgb::kCellBlock;
-    const double* wp = d.wpart + (size_t)slot * d.n_warps * 4;
+    const double* wp = d.wpart + (size_t)s * W * 4;
     double t[4] = {0.0, 0.0, 0.0, 0.0};
-    if (tid < fvgb::kCellBlock) {
-        for (int tile = tid; tile < n_tiles; tile += fvgb::kCellBlock) {
-            double v[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int i = 0; i < nw; ++i) {
-                const int cw = tile * nw + i;
-                if (cw < d.n_warps) {
-                    const double2* p = reinterpret_cast<const double2*>(wp + 4 * (size_t)cw);
-                    const double2 x = __ldcg(p), y = __ldcg(p + 1);
-                    v[0] += x.x; v[1] += x.y; v[2] += y.x; v[3] += y.y;
-                }
-            }
-            t[0] += v[0]; t[1] += v[1]; t[2] += v[2]; t[3] += v[3];
+    for (int base = 0; base < W; base += CH) {
+        if (base + tid < W) {
+            const double2* p = reinterpret_cast<const double2*>(wp + 4 * (size_t)(base + tid));
+            wsm[tid][0] = __ldcg(p);
+            wsm[tid][1] = __ldcg(p + 1);
         }
+        __syncthreads();
+        if (tid < fvgb::kCellBlock) {
+            // this thread's tile among the chunk's CH / nw tiles, if any
+            const int t0 = base / nw;
+            const int tile = t0 + (((tid - t0) % fvgb::kCellBlock) + fvgb::kCellBlock) % fvgb::kCellBlock;
+            if (tile < t0 + CH / nw && tile < n_tiles) {
+                double v[4] = {0.0, 0.0, 0.0, 0.0};
+                for (int i = 0; i < nw; ++i) {
+                    const int cw = tile * nw + i;
+                    if (cw < W) {
+                        const double2 x = wsm[cw - base][0], y = wsm[cw - base][1];
+                        v[0] += x.x; v[1] += x.y; v[2] += y.x; v[3] += y.y;
+                    }
+                }
+                t[0] += v[0]; t[1] += v[1]; t[2] += v[2]; t[3] += v[3];
+            }
+        }
+        __syncthreads();
     }
     const double ts = warp_sum4(t[0], t[1], t[2], t[3]);
     if (w < nw && (lane & 7) == 0) red[w][lane >> 3] = ts;
@@ -462,7 +553,7 @@ __device__ __forceinline__ void df_fold(const O1Args& a, const DfPlan& d, int sl
             const double n = sqrt(v);
             if (!isfinite(n)) bad = 1;
             a.hist[row * 4 + k] = n;
-            d.fnorm[slot * 4 + k] = n;
+            if (last) a.ctl->norms[k] = n;
         }
         if (bad) a.ctl->nonfinite = 1;
     }
@@ -473,7 +564,6 @@ template <int FLUX>
 __global__ void __launch_bounds__(fvgb::kDfBlock, 1) k_o1_dataflow(const O1Args a, double4_32a* __restrict__ P,
                                                                   PersistCtl* __restrict__ pc, const DfPlan d,
                                                                   int nsteps) {
-    constexpr int R = fvgb::kDfRing;
     const double g = a.gamma;
     const int b = blockIdx.x, nb = gridDim.x;
     const unsigned int expected = (unsigned int)nb + (unsigned int)pc->phantom;
@@ -486,64 +576,40 @@ __global__ void __launch_bounds__(fvgb::kDfBlock, 1) k_o1_dataflow(const O1Args 
     constexpr int nwarps = fvgb::kDfBlock / 32;
 
     __shared__ int dep_f[fvgb::kDfMaxDeps], dep_c[fvgb::kDfMaxDeps];
-    __shared__ int folder;
     const int nf = d.dep_face_off[b + 1] - d.dep_face_off[b];
     const int nc = d.dep_cell_off[b + 1] - d.dep_cell_off[b];
     if (threadIdx.x < nf) dep_f[threadIdx.x] = d.dep_face[d.dep_face_off[b] + threadIdx.x];
     if (threadIdx.x < nc) dep_c[threadIdx.x] = d.dep_cell[d.dep_cell_off[b] + threadIdx.x];
 
-    // prologue: primitives of the own cells, progress words and ring reset
+    // prologue: primitives of the own cells, progress word reset
     for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) st_prim(P, c, prim_of(ld_state_cg(a.U, c), g));
-    if (threadIdx.x == 0) d.prog[b] = 0u;
-    if (b == 0 && threadIdx.x < R) {
-        d.arrive[threadIdx.x] = 0u;
-        d.folded[threadIdx.x] = (int)threadIdx.x - R;
-    }
+    if (threadIdx.x == 0) d.prog[(size_t)b * fvgb::kDfProgStride] = 0u;
     if (!grid_barrier(pc, expected)) return;
 
     for (int s = 0; s < nsteps; ++s) {
-        const int slot = s % R;
         // face phase: the right cells' states of step s are final
-        if (s > 0 && !df_wait(pc, d.prog, dep_f, nf, 2u * s, d.folded, 0, -1)) return;
+        if (s > 0 && !df_wait(pc, d.prog, dep_f, nf, 2u * s)) return;
         for (int j = fa + threadIdx.x; j < fz; j += blockDim.x)
             face_phase_face<FLUX, true>(a, P, d.faces[j], g, cfl);
         df_publish(d.prog, 2u * s + 1u);
 
-        // cell phase: every face of the own cells has its step-s flux, no
-        // block still reads the own cells' step-s states, and the ring slot
-        // is free
-        if (!df_wait(pc, d.prog, dep_c, nc, 2u * s + 1u, d.folded, slot, s - R)) return;
+        // cell phase: every face of the own cells has its step-s flux and
+        // no block still reads the own cells' step-s states
+        if (!df_wait(pc, d.prog, dep_c, nc, 2u * s + 1u)) return;
+        double* wp = d.wpart + (size_t)s * d.n_warps * 4;
         for (int cw = c0 / 32 + warp; cw * 32 < c1; cw += nwarps) {
             const int c = cw * 32 + lane;
             double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
             if (c < N) cell_phase_cell<true>(a, P, c, g, cfl, 0.0, s0, s1, s2, s3);
             const double ws = warp_sum4(s0, s1, s2, s3);
-            if ((lane & 7) == 0) d.wpart[((size_t)slot * d.n_warps + cw) * 4 + (lane >> 3)] = ws;
+            if ((lane & 7) == 0) wp[(size_t)cw * 4 + (lane >> 3)] = ws;
         }
         df_publish(d.prog, 2u * s + 2u);
-        if (threadIdx.x == 0) {
-            const unsigned int before = atomicAdd(d.arrive + slot, 1u);
-            folder = before == (unsigned int)nb - 1u;
-            if (folder) {
-                atomicExch(d.arrive + slot, 0u);
-                __threadfence();
-            }
-        }
-        __syncthreads();
-        if (folder) {
-            df_fold(a, d, slot, (step0 + s) % a.hist_cap);
-            if (threadIdx.x == 0) {
-                __threadfence();
-                atomicExch(d.folded + slot, s);
-            }
-        }
     }
     if (!grid_barrier(pc, expected)) return;
-    if (b == 0 && threadIdx.x == 0 && nsteps > 0) {
-        const int slot = (nsteps - 1) % R;
-        for (int k = 0; k < 4; ++k) a.ctl->norms[k] = __ldcg(d.fnorm + slot * 4 + k);
-        a.ctl->step = step0 + nsteps;
-    }
+    // the launch's norms, steps strided over the blocks
+    for (int s = b; s < nsteps; s += nb) df_fold(a, d, s, (step0 + s) % a.hist_cap, s == nsteps - 1);
+    if (b == 0 && threadIdx.x == 0) a.ctl->step = step0 + nsteps;
 }
 
 template <int FLUX>

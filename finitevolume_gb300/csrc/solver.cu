@@ -556,12 +556,17 @@ void Solver::build_dataflow(const HostMesh& hm, int sms) {
     for (int b = 0; b <= nb; ++b) cell_off[b] = (int)std::min<long long>(32LL * ((long long)Wn * b / nb), N);
     for (int b = 0; b < nb; ++b)
         for (int c = cell_off[b]; c < cell_off[b + 1]; ++c) owner[c] = b;
+    // A block's boundary faces come first: their ghost states are the
+    // longest dependent chains of the face phase, and the lowest warps of a
+    // block get issue priority.
     std::vector<int> face_off(nb + 1, 0), faces(F);
     for (int f = 0; f < F; ++f) ++face_off[owner[hm.d_fl[f]] + 1];
     for (int b = 0; b < nb; ++b) face_off[b + 1] += face_off[b];
     {
         std::vector<int> pos(face_off.begin(), face_off.end() - 1);
-        for (int f = 0; f < F; ++f) faces[pos[owner[hm.d_fl[f]]]++] = f;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int f = 0; f < F; ++f)
+                if ((hm.d_fr[f] < 0) == (pass == 0)) faces[pos[owner[hm.d_fl[f]]]++] = f;
     }
     std::vector<std::vector<int>> dface(nb), dcell(nb);
     for (int f = 0; f < F; ++f) {
@@ -592,13 +597,13 @@ void Solver::build_dataflow(const HostMesh& hm, int sms) {
     dfp.dep_face_off = dupload(dfo, owned);
     dfp.dep_cell = dupload(dc, owned);
     dfp.dep_cell_off = dupload(dco, owned);
-    dfp.prog = dalloc<unsigned int>(nb, owned);
-    dfp.arrive = dalloc<unsigned int>(kDfRing, owned);
-    dfp.folded = dalloc<int>(kDfRing, owned);
-    dfp.fnorm = dalloc<double>(4 * kDfRing, owned);
-    dfp.wpart = dalloc<double>((size_t)4 * kDfRing * Wn, owned);
+    // the per-warp partials of every step of a launch: up to kPersistChunk
+    // steps, fewer on a large mesh (kDfPartialBytes)
+    const size_t per_step = (size_t)Wn * 4 * sizeof(double);
+    dfp.max_steps = (int)std::max<size_t>(8, std::min<size_t>(kPersistChunk, kDfPartialBytes / per_step));
+    dfp.prog = dalloc<unsigned int>((size_t)nb * kDfProgStride, owned);
+    dfp.wpart = dalloc<double>((size_t)dfp.max_steps * Wn * 4, owned);
     dfp.n_warps = Wn;
-    FV_CUDA(cudaMemsetAsync(dfp.arrive, 0, kDfRing * sizeof(unsigned int), stream));
     df_grid = nb;
     dataflow_ok = true;
 }
@@ -613,17 +618,25 @@ void Solver::launch_steps(int k, std::vector<int>* classes, std::vector<cudaEven
         for (int i = 0; i < k; ++i) launch_step(classes, events, ev_pos);
         return;
     }
-    // re-arm the barrier (arrival counter, error flag), then one launch
-    FV_CUDA(cudaMemsetAsync(pctl, 0, 2 * sizeof(int), stream));
+    // One launch per chunk (the dataflow form keeps every step's norm
+    // partials of a launch), each re-arming the barrier's arrival counter.
+    // The error flag is cleared once per fv_step (reset_wait_error), so
+    // that a wait that ran out in an early launch is still reported.
     const O1Args a = o1_args();
-    cudaError_t rc;
-    if (persistent_form() == 2)
-        rc = opt.strict ? strict::launch_o1_dataflow(a, Pc, pctl, dfp, k, df_grid, stream)
-                        : fast::launch_o1_dataflow(a, Pc, pctl, dfp, k, df_grid, stream);
-    else
-        rc = opt.strict ? strict::launch_o1_persistent(a, Pc, pctl, k, p_grid, stream)
-                        : fast::launch_o1_persistent(a, Pc, pctl, k, p_grid, stream);
-    FV_CUDA(rc);
+    const bool df = persistent_form() == 2;
+    for (int done = 0; done < k;) {
+        const int n = df ? std::min(k - done, dfp.max_steps) : k;
+        FV_CUDA(cudaMemsetAsync(pctl, 0, sizeof(int), stream));
+        cudaError_t rc;
+        if (df)
+            rc = opt.strict ? strict::launch_o1_dataflow(a, Pc, pctl, dfp, n, df_grid, stream)
+                            : fast::launch_o1_dataflow(a, Pc, pctl, dfp, n, df_grid, stream);
+        else
+            rc = opt.strict ? strict::launch_o1_persistent(a, Pc, pctl, n, p_grid, stream)
+                            : fast::launch_o1_persistent(a, Pc, pctl, n, p_grid, stream);
+        FV_CUDA(rc);
+        done += n;
+    }
     if (classes) classes->push_back(1);
     if (events) FV_CUDA(cudaEventRecord((*events)[++*ev_pos], stream));
 }
@@ -647,6 +660,11 @@ void Solver::set_wait_limit(long long cycles, int phantom) {
     FV_CUDA(cudaStreamSynchronize(stream));
     h2d_sync(reinterpret_cast<char*>(pctl) + offsetof(PersistCtl, phantom), &phantom, sizeof(int), stream);
     h2d_sync(reinterpret_cast<char*>(pctl) + offsetof(PersistCtl, limit), &cycles, sizeof(long long), stream);
+}
+
+void Solver::reset_wait_error() {
+    if (persistent_ok)
+        FV_CUDA(cudaMemsetAsync(reinterpret_cast<char*>(pctl) + offsetof(PersistCtl, err), 0, sizeof(int), stream));
 }
 
 void Solver::check_persistent() {
@@ -673,6 +691,7 @@ void Solver::step_timed(int n, double ms[3], int launches[3]) {
     std::vector<int> classes;
     classes.reserve(need);
     size_t pos = 0;
+    if (persistent) reset_wait_error();
     FV_CUDA(cudaEventRecord(events[0], stream));
     launch_steps(n, &classes, &events, &pos);
     FV_CUDA(cudaGetLastError());
@@ -715,6 +734,7 @@ void Solver::step_async(int n) {
         steps_taken += n;
         return;
     }
+    if (persistent) reset_wait_error();
     const int chunk = persistent ? kPersistChunk : kGraphChunk;
     int q = n / chunk, r = n % chunk;
     if (q) {

@@ -148,8 +148,10 @@ struct Solver {
     int persistent_form() const;
     void build_dataflow(const HostMesh& hm, int sms);
     void set_wait_limit(long long cycles, int phantom);
-    // FV_ERR_TIMEOUT if a persistent launch gave up at a grid barrier
+    // FV_ERR_TIMEOUT if a persistent launch gave up at a wait since the
+    // last reset_wait_error (called at the start of every step call)
     void check_persistent();
+    void reset_wait_error();
     void step_timed(int n, double ms[3], int launches[3]);
     cudaGraphExec_t graph_for(int k);
     void step_async(int n);

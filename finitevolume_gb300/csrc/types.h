@@ -71,11 +71,12 @@ struct PersistCtl {
 // blocks it shares faces with: the face phase of step s for the cell phase
 // of step s-1 of dep_face's blocks (the owners of its faces' right cells),
 // the cell phase for the face phase of step s of dep_cell's blocks (the
-// owners of the other faces of its cells).  prog[b] is 2s+1 once block b
-// has finished the face phase of step s and 2s+2 once it has finished the
-// cell phase.  Each warp of cells leaves its residual partial in a ring of
-// kDfRing step slots; the last block to finish a step's cell phase folds
-// that step's norms and marks the slot free (folded[slot] = step).
+// owners of the other faces of its cells).  prog[b * kDfProgStride] is
+// 2s+1 once block b has finished the face phase of step s and 2s+2 once it
+// has finished the cell phase (one 128-byte line per block, so that the
+// polls of one block's word do not hit the others').  Each warp of cells
+// leaves the residual partial of every step of the launch in wpart; the
+// norms are folded after the last step.
 struct DfPlan {
     const int* faces;         // [F] face ids grouped by owning block
     const int* face_off;      // [nb+1]
@@ -84,16 +85,15 @@ struct DfPlan {
     const int* dep_face_off;  // [nb+1]
     const int* dep_cell;      // blocks the cell phase waits for
     const int* dep_cell_off;  // [nb+1]
-    unsigned int* prog;       // [nb]
-    unsigned int* arrive;     // [kDfRing] cell-phase arrivals per slot
-    int* folded;              // [kDfRing] last step folded from each slot
-    double* fnorm;            // [kDfRing * 4] norms of the step folded there
-    double* wpart;            // [kDfRing * n_warps * 4] per-warp partials
+    unsigned int* prog;       // [nb * kDfProgStride]
+    double* wpart;            // [max_steps * n_warps * 4] per-warp partials
     int n_warps;              // cell warps, ceil(N / 32)
+    int max_steps;            // steps per launch (wpart capacity)
 };
-constexpr int kDfBlock = 512;   // threads per block (one block per SM)
-constexpr int kDfRing = 8;      // norm-partial slots
-constexpr int kDfMaxDeps = 32;  // dependency list bound per block and phase
+constexpr int kDfBlock = 512;          // threads per block (one block per SM)
+constexpr int kDfProgStride = 32;      // progress words per block (128 bytes)
+constexpr int kDfMaxDeps = 32;         // dependency list bound per block and phase
+constexpr size_t kDfPartialBytes = 64u << 20;  // wpart budget (bounds steps per launch)
 
 struct O1Args {
     DevMesh m;

@@ -1,0 +1,54 @@
+// Checks fvconv::pow_near1 (fpconv.cuh) against the library pow on
+// pseudo-random bases in [0.75, 1.25] (the series range [7/8, 9/8] and
+// both sides of it) and exponents 2/(g-1) of the gases the solvers take
+// (g in [1.1, 1.67]) plus a few others.  Inside the series range the result
+// must be within 8 ulps of pow; outside it (where pow_near1 calls pow) it
+// must be pow's result exactly.  Prints "pow_checked N pow_series S
+// pow_max_ulp U pow_bad B" (S: series results that differ from pow).
+#include <cstdio>
+#include <cstdint>
+
+#include "fpconv.cuh"
+
+__device__ unsigned long long g_count[3];  // series inputs, bad, max ulp
+
+__device__ __forceinline__ uint64_t mix(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+__global__ void check_pow(uint64_t count, uint64_t seed) {
+    const double ks[8] = {5.0, 2.0 / (1.4 - 1.0), 2.0 / (1.67 - 1.0), 2.0 / (1.1 - 1.0), 2.5, 1.0, 0.5, 7.0};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = mix(i * 0x9e3779b97f4a7c15ull + seed);
+        const double x = 0.75 + 0.5 * (double)(b >> 11) * (1.0 / 9007199254740992.0);
+        const double k = ks[i & 7u];
+        const double mine = fvconv::pow_near1(x, k), ref = pow(x, k);
+        const long long d = __double_as_longlong(mine) - __double_as_longlong(ref);
+        const unsigned long long ad = (unsigned long long)(d < 0 ? -d : d);
+        const bool series = fabs(x - 1.0) <= 0.125 && mine != ref;
+        bool bad = ad > 8;
+        if (fabs(x - 1.0) > 0.125) bad = d != 0;
+        if (series) atomicAdd(&g_count[0], 1ull);
+        atomicMax(&g_count[2], ad);
+        if (bad) atomicAdd(&g_count[1], 1ull);
+    }
+}
+
+int main() {
+    unsigned long long zero[3] = {0, 0, 0};
+    cudaMemcpyToSymbol(g_count, zero, sizeof(zero));
+    const uint64_t n = 1ull << 26;
+    check_pow<<<152 * 8, 256>>>(n, 12345);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        printf("cuda_error %s\n", cudaGetErrorString(e));
+        return 2;
+    }
+    unsigned long long c[3];
+    cudaMemcpyFromSymbol(c, g_count, sizeof(c));
+    printf("pow_checked %llu pow_series %llu pow_max_ulp %llu pow_bad %llu\n", (unsigned long long)n, c[0], c[2], c[1]);
+    return 0;
+}
