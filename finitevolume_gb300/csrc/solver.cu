@@ -552,8 +552,23 @@ void Solver::build_dataflow(const HostMesh& hm, int sms) {
     if (per_sm < 1 || sms < 1) return;
     const int Wn = (N + 31) / 32;
     const int nb = std::min(sms, Wn);
+    // Cell warps split into equal shares of weight: a warp with a cell on a
+    // characteristic farfield face weighs 1.7, the others 1.  That face's
+    // ghost state is the longest dependent chain of the face phase, so the
+    // few blocks that hold those faces get fewer cells.
+    std::vector<double> wsum(Wn + 1, 0.0);
+    {
+        std::vector<char> far(Wn, 0);
+        for (int f = 0; f < F; ++f)
+            if (hm.d_fr[f] < 0 && bc.type[hm.d_fpatch[f]] == FV_BC_CHAR_FARFIELD) far[hm.d_fl[f] / 32] = 1;
+        for (int w = 0; w < Wn; ++w) wsum[w + 1] = wsum[w] + (far[w] ? 1.7 : 1.0);
+    }
     std::vector<int> cell_off(nb + 1), owner(N);
-    for (int b = 0; b <= nb; ++b) cell_off[b] = (int)std::min<long long>(32LL * ((long long)Wn * b / nb), N);
+    for (int b = 0; b <= nb; ++b) {
+        const int w = b == nb ? Wn
+                              : (int)(std::lower_bound(wsum.begin(), wsum.end(), wsum[Wn] * b / nb) - wsum.begin());
+        cell_off[b] = (int)std::min<long long>(32LL * std::min(w, Wn), N);
+    }
     for (int b = 0; b < nb; ++b)
         for (int c = cell_off[b]; c < cell_off[b + 1]; ++c) owner[c] = b;
     // A block's boundary faces come first: their ghost states are the
