@@ -86,6 +86,7 @@ SIGNATURES = {
     "fv_mesh_counts": (C.c_int, [_P, _I64]),
     "fv_mesh_export": (C.c_int, [_P, _I32, _D, _D, _I32, _I32]),
     "fv_mesh_permutation": (C.c_int, [_P, _I32]),
+    "fv_mesh_dataflow_plan": (C.c_int, [_P, _I32, C.c_int32, _I32, _I32, _I32, _I32, _I32, _I32, _I32, _I32, _I32]),
     "fv_mesh_agglomerate": (C.c_int, [_P, _I32, _I32, _D, _I32, _D]),
     "fv_mesh_destroy": (C.c_int, [_P]),
     "fv_options_default": (None, [C.POINTER(Options)]),

@@ -542,14 +542,14 @@ void Solver::launch_step(std::vector<int>* classes, std::vector<cudaEvent_t>* ev
     }
 }
 
-void Solver::build_dataflow(const HostMesh& hm, int sms) {
+bool dataflow_plan(const HostMesh& hm, const int* patch_type, int sms, DataflowPlan& p) {
     // One block per SM (fewer on a mesh of fewer 32-cell warps), each
-    // owning an equal share of whole cell warps and the faces whose left
-    // cell it owns; the dependency lists are the blocks it shares faces
-    // with.  A mesh whose cell order leaves a block more neighbours than
-    // kDfMaxDeps keeps the barrier form.
-    const int per_sm = opt.strict ? strict::o1df_max_blocks_per_sm(opt.flux) : fast::o1df_max_blocks_per_sm(opt.flux);
-    if (per_sm < 1 || sms < 1) return;
+    // owning a share of whole cell warps and the faces whose left cell it
+    // owns; the dependency lists are the blocks it shares faces with.  A
+    // mesh whose cell order leaves a block more neighbours than kDfMaxDeps
+    // has no plan (the barrier form runs).
+    const int N = hm.n_cells, F = hm.n_faces;
+    if (sms < 1 || N < 1) return false;
     const int Wn = (N + 31) / 32;
     const int nb = std::min(sms, Wn);
     // Cell warps split into equal shares of weight: a warp with a cell on a
@@ -560,28 +560,31 @@ void Solver::build_dataflow(const HostMesh& hm, int sms) {
     {
         std::vector<char> far(Wn, 0);
         for (int f = 0; f < F; ++f)
-            if (hm.d_fr[f] < 0 && bc.type[hm.d_fpatch[f]] == FV_BC_CHAR_FARFIELD) far[hm.d_fl[f] / 32] = 1;
+            if (hm.d_fr[f] < 0 && patch_type[hm.d_fpatch[f]] == FV_BC_CHAR_FARFIELD) far[hm.d_fl[f] / 32] = 1;
         for (int w = 0; w < Wn; ++w) wsum[w + 1] = wsum[w] + (far[w] ? 1.7 : 1.0);
     }
-    std::vector<int> cell_off(nb + 1), owner(N);
+    p.nb = nb;
+    p.cell_off.assign(nb + 1, 0);
+    std::vector<int> owner(N);
     for (int b = 0; b <= nb; ++b) {
         const int w = b == nb ? Wn
                               : (int)(std::lower_bound(wsum.begin(), wsum.end(), wsum[Wn] * b / nb) - wsum.begin());
-        cell_off[b] = (int)std::min<long long>(32LL * std::min(w, Wn), N);
+        p.cell_off[b] = (int)std::min<long long>(32LL * std::min(w, Wn), N);
     }
     for (int b = 0; b < nb; ++b)
-        for (int c = cell_off[b]; c < cell_off[b + 1]; ++c) owner[c] = b;
+        for (int c = p.cell_off[b]; c < p.cell_off[b + 1]; ++c) owner[c] = b;
     // A block's boundary faces come first: their ghost states are the
     // longest dependent chains of the face phase, and the lowest warps of a
     // block get issue priority.
-    std::vector<int> face_off(nb + 1, 0), faces(F);
-    for (int f = 0; f < F; ++f) ++face_off[owner[hm.d_fl[f]] + 1];
-    for (int b = 0; b < nb; ++b) face_off[b + 1] += face_off[b];
+    p.face_off.assign(nb + 1, 0);
+    p.faces.assign(F, 0);
+    for (int f = 0; f < F; ++f) ++p.face_off[owner[hm.d_fl[f]] + 1];
+    for (int b = 0; b < nb; ++b) p.face_off[b + 1] += p.face_off[b];
     {
-        std::vector<int> pos(face_off.begin(), face_off.end() - 1);
+        std::vector<int> pos(p.face_off.begin(), p.face_off.end() - 1);
         for (int pass = 0; pass < 2; ++pass)
             for (int f = 0; f < F; ++f)
-                if ((hm.d_fr[f] < 0) == (pass == 0)) faces[pos[owner[hm.d_fl[f]]]++] = f;
+                if ((hm.d_fr[f] < 0) == (pass == 0)) p.faces[pos[owner[hm.d_fl[f]]]++] = f;
     }
     std::vector<std::vector<int>> dface(nb), dcell(nb);
     for (int f = 0; f < F; ++f) {
@@ -591,27 +594,41 @@ void Solver::build_dataflow(const HostMesh& hm, int sms) {
         dface[a].push_back(r);  // a's face phase reads r's cells
         dcell[r].push_back(a);  // r's cell phase reads a's faces
     }
-    std::vector<int> df, dfo(nb + 1, 0), dc, dco(nb + 1, 0);
+    p.dep_face.clear();
+    p.dep_cell.clear();
+    p.dep_face_off.assign(nb + 1, 0);
+    p.dep_cell_off.assign(nb + 1, 0);
+    bool ok = true;
     for (int b = 0; b < nb; ++b) {
         for (auto* v : {&dface[b], &dcell[b]}) {
             std::sort(v->begin(), v->end());
             v->erase(std::unique(v->begin(), v->end()), v->end());
-            if ((int)v->size() > kDfMaxDeps) return;
+            if ((int)v->size() > kDfMaxDeps) ok = false;
         }
-        df.insert(df.end(), dface[b].begin(), dface[b].end());
-        dc.insert(dc.end(), dcell[b].begin(), dcell[b].end());
-        dfo[b + 1] = (int)df.size();
-        dco[b + 1] = (int)dc.size();
+        p.dep_face.insert(p.dep_face.end(), dface[b].begin(), dface[b].end());
+        p.dep_cell.insert(p.dep_cell.end(), dcell[b].begin(), dcell[b].end());
+        p.dep_face_off[b + 1] = (int)p.dep_face.size();
+        p.dep_cell_off[b + 1] = (int)p.dep_cell.size();
     }
+    return ok;
+}
+
+void Solver::build_dataflow(const HostMesh& hm, int sms) {
+    const int per_sm = opt.strict ? strict::o1df_max_blocks_per_sm(opt.flux) : fast::o1df_max_blocks_per_sm(opt.flux);
+    if (per_sm < 1) return;
+    DataflowPlan p;
+    if (!dataflow_plan(hm, bc.type, sms, p)) return;
+    const int nb = p.nb, Wn = (N + 31) / 32;
+    std::vector<int> df = p.dep_face, dc = p.dep_cell;
     if (df.empty()) df.push_back(0);
     if (dc.empty()) dc.push_back(0);
-    dfp.faces = dupload(faces, owned);
-    dfp.face_off = dupload(face_off, owned);
-    dfp.cell_off = dupload(cell_off, owned);
+    dfp.faces = dupload(p.faces, owned);
+    dfp.face_off = dupload(p.face_off, owned);
+    dfp.cell_off = dupload(p.cell_off, owned);
     dfp.dep_face = dupload(df, owned);
-    dfp.dep_face_off = dupload(dfo, owned);
+    dfp.dep_face_off = dupload(p.dep_face_off, owned);
     dfp.dep_cell = dupload(dc, owned);
-    dfp.dep_cell_off = dupload(dco, owned);
+    dfp.dep_cell_off = dupload(p.dep_cell_off, owned);
     // the per-warp partials of every step of a launch: up to kPersistChunk
     // steps, fewer on a large mesh (kDfPartialBytes)
     const size_t per_step = (size_t)Wn * 4 * sizeof(double);
@@ -1098,6 +1115,40 @@ int fv_mesh_permutation(fv_mesh_t mesh, int32_t* perm) {
     return guarded([&] {
         if (!mesh || !perm) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
         std::copy(mesh->h.perm.begin(), mesh->h.perm.end(), perm);
+    });
+}
+
+int fv_mesh_dataflow_plan(fv_mesh_t mesh, const int32_t* patch_types, int32_t blocks, int32_t counts[4],
+                          int32_t* cell_off, int32_t* face_off, int32_t* faces, int32_t* dep_face_off,
+                          int32_t* dep_face, int32_t* dep_cell_off, int32_t* dep_cell, int32_t* face_cells) {
+    return guarded([&] {
+        if (!mesh || !patch_types || !counts) fvgb::raise(FV_ERR_BAD_ARG, "null argument");
+        if (blocks < 1) fvgb::raise(FV_ERR_BAD_ARG, "blocks must be >= 1");
+        const fvgb::HostMesh& h = mesh->h;
+        for (int p = 0; p < h.n_patches; ++p)
+            if (patch_types[p] < FV_BC_WALL || patch_types[p] > FV_BC_NOSLIP)
+                fvgb::raise(FV_ERR_BAD_ARG, "unknown boundary type");
+        fvgb::DataflowPlan p;
+        const bool ok = fvgb::dataflow_plan(h, patch_types, blocks, p);
+        counts[0] = p.nb;
+        counts[1] = (int32_t)p.dep_face.size();
+        counts[2] = (int32_t)p.dep_cell.size();
+        counts[3] = ok ? 1 : 0;
+        auto put = [](const std::vector<int>& v, int32_t* out) {
+            if (out) std::copy(v.begin(), v.end(), out);
+        };
+        put(p.cell_off, cell_off);
+        put(p.face_off, face_off);
+        put(p.faces, faces);
+        put(p.dep_face_off, dep_face_off);
+        put(p.dep_face, dep_face);
+        put(p.dep_cell_off, dep_cell_off);
+        put(p.dep_cell, dep_cell);
+        if (face_cells)
+            for (int f = 0; f < h.n_faces; ++f) {
+                face_cells[2 * (size_t)f] = h.d_fl[f];
+                face_cells[2 * (size_t)f + 1] = h.d_fr[f];
+            }
     });
 }
 

@@ -39,6 +39,19 @@ struct MGLevel {
     St* Rc = nullptr;          // coarse residual at the restricted state
 };
 
+// The dataflow form's partition of a mesh in device order (DfPlan's host
+// side): nb blocks, the cells [cell_off[b], cell_off[b+1]) and the faces
+// faces[face_off[b] .. face_off[b+1]) of block b, and the blocks its face
+// and cell phases wait for.
+struct DataflowPlan {
+    int nb = 0;
+    std::vector<int> cell_off, face_off, faces, dep_face_off, dep_face, dep_cell_off, dep_cell;
+};
+// Builds the plan over min(sms, cell warps) blocks; patch_type[p] is the
+// FV_BC_* of patch p.  False when a block would wait for more than
+// kDfMaxDeps blocks in one phase (the plan is still filled in).
+bool dataflow_plan(const HostMesh& hm, const int* patch_type, int sms, DataflowPlan& p);
+
 struct Solver {
     static constexpr int kGraphChunk = 32;
 

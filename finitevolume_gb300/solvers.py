@@ -139,6 +139,37 @@ class Mesh:
                                              capi.i32ptr(off), capi.i32ptr(cf)))
         return {"faces_i32": fi, "faces_f64": fd, "cells_f64": cd, "cell_face_off": off, "cell_faces": cf}
 
+    def dataflow_plan(self, patch_types, blocks: int = 152) -> dict:
+        """The partition of the persistent first-order kernel's dataflow form
+        over ``blocks`` blocks (one per SM; host side, for inspection):
+        device-numbered ``cell_off``, ``face_off``, ``faces``, the dependency
+        lists ``dep_face``/``dep_cell`` with their offsets, ``face_cells``
+        (left, right of each face), ``nb`` and ``used`` (False when a block
+        would wait for more than 32 blocks in a phase)."""
+        pt = np.ascontiguousarray(patch_types, dtype=np.int32)
+        if pt.shape[0] < self.n_patches:
+            raise ValueError("one boundary type per patch")
+        cnt = np.zeros(4, np.int32)
+        null = C.POINTER(C.c_int32)()
+        L = capi.lib()
+        capi.check(L.fv_mesh_dataflow_plan(self._h, capi.i32ptr(pt), int(blocks), capi.i32ptr(cnt), null, null, null,
+                                           null, null, null, null, null))
+        nb, nd1, nd2 = int(cnt[0]), int(cnt[1]), int(cnt[2])
+        out = {"cell_off": np.zeros(nb + 1, np.int32), "face_off": np.zeros(nb + 1, np.int32),
+               "faces": np.zeros(self.n_faces, np.int32), "dep_face_off": np.zeros(nb + 1, np.int32),
+               "dep_face": np.zeros(max(nd1, 1), np.int32), "dep_cell_off": np.zeros(nb + 1, np.int32),
+               "dep_cell": np.zeros(max(nd2, 1), np.int32), "face_cells": np.zeros((self.n_faces, 2), np.int32)}
+        capi.check(L.fv_mesh_dataflow_plan(self._h, capi.i32ptr(pt), int(blocks), capi.i32ptr(cnt),
+                                           *(capi.i32ptr(out[k]) for k in ("cell_off", "face_off", "faces",
+                                                                            "dep_face_off", "dep_face",
+                                                                            "dep_cell_off", "dep_cell",
+                                                                            "face_cells"))))
+        out["dep_face"] = out["dep_face"][:nd1]
+        out["dep_cell"] = out["dep_cell"][:nd2]
+        out["nb"] = nb
+        out["used"] = bool(cnt[3])
+        return out
+
     def permutation(self) -> np.ndarray:
         p = np.zeros(self.n_cells, np.int32)
         capi.check(capi.lib().fv_mesh_permutation(self._h, capi.i32ptr(p)))

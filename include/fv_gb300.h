@@ -100,6 +100,23 @@ int fv_mesh_export(fv_mesh_t mesh, int32_t* face_i32, double* face_f64, double* 
                    int32_t* cell_face_off, int32_t* cell_faces);
 /* Device-order permutation: perm[new] = reference cell index. */
 int fv_mesh_permutation(fv_mesh_t mesh, int32_t* perm);
+/* The partition the persistent first-order kernel's dataflow form makes of
+ * this mesh over `blocks` blocks (one per SM on the device; host only;
+ * inspection and test helper; no reference counterpart).  patch_types
+ * [n_patches] are the FV_BC_* of the solver's patches (warps with a cell on
+ * a characteristic farfield face weigh more).  counts[4] receives the block
+ * count nb (min(blocks, ceil(N/32))), the lengths of dep_face and dep_cell,
+ * and 1 if the plan is used (no block waits for more than 32 blocks in a
+ * phase) else 0.  In device numbering: block b owns the cells
+ * [cell_off[b], cell_off[b+1]) and the faces faces[face_off[b] ..
+ * face_off[b+1]) (boundary faces first); its face phase waits for the
+ * blocks dep_face[dep_face_off[b] .. dep_face_off[b+1]), its cell phase for
+ * dep_cell[...]; face_cells[2F] the left and right cell (-1: boundary) of
+ * each face.  Array sizes: nb+1 for the offsets, F for faces, 2F for
+ * face_cells; any array may be NULL (call with NULL arrays to size). */
+int fv_mesh_dataflow_plan(fv_mesh_t mesh, const int32_t* patch_types, int32_t blocks, int32_t counts[4],
+                          int32_t* cell_off, int32_t* face_off, int32_t* faces, int32_t* dep_face_off,
+                          int32_t* dep_face, int32_t* dep_cell_off, int32_t* dep_cell, int32_t* face_cells);
 /* The first coarse level that fv_solver_multigrid builds from this mesh
  * (host only; inspection and test helper; no reference counterpart).
  * counts[2] receives the coarse cell and face counts; any other pointer may
