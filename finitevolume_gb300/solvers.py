@@ -390,9 +390,10 @@ class EulerFVMSolver:
         return int(on.value), int(grid.value)
 
     def set_wait_limit(self, cycles: int, phantom_arrivals: int = 0) -> None:
-        """Bound (SM clock cycles) on each grid-barrier wait of the persistent
-        kernel; phantom_arrivals > 0 makes every barrier wait for arrivals
-        that never come (checks the FV_ERR_TIMEOUT path)."""
+        """Bound (SM clock cycles) on each wait of the persistent kernel
+        (grid barrier or neighbour progress); phantom_arrivals > 0 makes
+        every grid barrier wait for arrivals that never come (checks the
+        FV_ERR_TIMEOUT path)."""
         capi.check(capi.lib().fv_solver_set_wait_limit(self._h, int(cycles), int(phantom_arrivals)))
 
     def freeze_limiter(self, on: bool = True) -> None:

@@ -252,12 +252,14 @@ int fv_solver_set_launch(fv_solver_t s, const int32_t blocks[3]);
  * reference's loops are OpenMP). */
 int fv_solver_set_persistent(fv_solver_t s, int32_t on);
 int fv_solver_persistent(fv_solver_t s, int32_t* on, int32_t* grid);
-/* Bound on every grid-barrier wait of the persistent kernel, in SM clock
- * cycles (default 2e9, about one second).  A wait that runs out makes the
- * launch end early and fv_step / fv_step_timed return FV_ERR_TIMEOUT (the
- * state is then unspecified).  phantom_arrivals > 0 makes every barrier wait
- * for that many arrivals that never come: a check of the timeout path that
- * faults and hangs nothing; set it back to 0 afterwards. */
+/* Bound on every wait of the persistent kernel (grid barrier, or a
+ * neighbour's progress word in the dataflow form), in SM clock cycles
+ * (default 2e9, about one second).  A wait that runs out makes the launch
+ * end early and fv_step / fv_step_timed return FV_ERR_TIMEOUT (the state is
+ * then unspecified).  phantom_arrivals > 0 makes every grid barrier (both
+ * forms begin with one) wait for that many arrivals that never come: a
+ * check of the timeout path that faults and hangs nothing; set it back to
+ * 0 afterwards. */
 int fv_solver_set_wait_limit(fv_solver_t s, int64_t cycles, int32_t phantom_arrivals);
 /* Limiter freezing (second order with a limiter; a no-op otherwise): on=1
  * evaluates the limiter once at the current state and reuses those values
