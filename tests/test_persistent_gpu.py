@@ -83,6 +83,27 @@ def test_dataflow_form_matches_barrier_form(gpu, flux, strict, size):
         np.testing.assert_allclose(ha, hb, rtol=1e-13, atol=0)
 
 
+@pytest.mark.parametrize("strict", [True, False])
+def test_exact_riemann_flux_in_both_forms(gpu, strict):
+    # the exact Riemann flux (its Newton iteration and powers inside the
+    # face phase): dataflow form, grid-barrier form and two-kernel path
+    poly = meshgen.naca_ogrid(64, 32)
+    bcs, ic = _case(True)
+    runs = []
+    for mode in (True, "barrier", False):
+        s = gpu_solver(poly, bcs, ic, "exact", cfl=0.5, local_dt=True, strict=strict)
+        s.set_persistent(mode)
+        h = s.run(200, history=True)
+        runs.append((s.field(), h))
+    if strict:
+        assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+        assert np.array_equal(runs[0][0], runs[2][0]) and np.array_equal(runs[0][1], runs[2][1])
+    else:
+        assert rel_err(runs[0][0], runs[1][0]) <= 1e-13
+        assert rel_err(runs[0][0], runs[2][0]) <= 1e-10
+        np.testing.assert_allclose(runs[0][1], runs[2][1], rtol=1e-10, atol=0)
+
+
 @pytest.mark.parametrize("local", [False, True])
 def test_barrier_wait_runs_out_and_reports_timeout(gpu, local):
     poly = meshgen.naca_ogrid(64, 32)
