@@ -5,8 +5,9 @@
 // faces of the CFL step (compute_dt, :133-162) before the first update.  The
 // two-kernel path (euler_o1.cuh) makes those dependencies kernel boundaries,
 // which on a 32k-cell mesh costs more than the arithmetic.  Here one launch
-// of co-resident blocks (a cooperative launch) runs K steps and
-// meets each dependency at a grid barrier:
+// of co-resident blocks (a cooperative launch) runs K steps.  Its
+// grid-barrier form (k_o1_persistent) meets each dependency at a grid
+// barrier:
 //
 //   prologue   per-cell primitives P = (u, v, p, c) of the current state
 //   per step   face phase: fluxes (and the CFL candidate or lambda*A),
@@ -27,15 +28,21 @@
 // DFMA) and products with it instead of three divisions per cell, the
 // normal velocity of the Rusanov flux from P instead of a division per face
 // side, and the local-dt update factor dt/V = cfl / sum lambda A by one
-// reciprocal; it agrees with the reference within 1e-10.  In both builds the
+// reciprocal, and the ghost states from P with short dependent chains
+// (ghost_p); it agrees with the reference within 1e-10.  In both builds the
 // norm partials are formed over the same 256-cell tiles and folded in the
 // same order as k_cell_o1's, so the residual history is bit-identical to
 // the two-kernel path too.
 //
-// The grid barrier is a counter plus a generation word.  Every wait is
-// bounded (PersistCtl::limit, in SM clock cycles): a block that gives up
-// sets PersistCtl::err and leaves, so the others give up at their next
-// barrier too and the launch always ends; the host reports FV_ERR_TIMEOUT.
+// With local dt a step has no global dependency, and the dataflow form
+// (k_o1_dataflow, further down) replaces the grid barriers by waits on the
+// few blocks that share faces with each block.
+//
+// The grid barrier is a counter plus a generation word.  Every wait (grid
+// barrier or neighbour progress) is bounded (PersistCtl::limit, in SM clock
+// cycles): a block that gives up sets PersistCtl::err and leaves, so the
+// others give up at their next wait too and the launch always ends; the
+// host reports FV_ERR_TIMEOUT.
 //
 // Included by kernels_fast.cu and kernels_strict.cu with FV_KNS defined,
 // after euler_o1.cuh.
