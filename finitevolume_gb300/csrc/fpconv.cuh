@@ -100,20 +100,43 @@ __device__ __forceinline__ double rcp_nr3(double x) {
 
 // x^k for x near 1 with a short chain of dependent FP64 operations (for
 // boundary states on a critical path; the library pow is a much longer
-// chain).  For x in [7/8, 9/8] and |k ln x| <= 3/4:
-//   ln x = 2 atanh z,  z = (x - 1) / (x + 1),  |z| <= 1/15, with
-//   atanh z = z (1 + z^2/3 + z^4/5 + ... + z^14/15) (the first omitted term
-//   is below 2^-58 of the sum), then e^y, y = k ln x, as (e^(y/8))^8 with
-//   e^t (|t| <= 3/32) by its Taylor series to degree 10 (remainder below
-//   2^-62), kept as e^t - 1 through the squarings.  x - 1 is exact there;
-//   the rounding of y (a few ulps, times |y| <= 3/4) dominates, and the
-//   result is within 8 ulps of x^k (5 measured against the library pow on
-//   2^26 bases).  Outside that range the library pow.
+// chain).  ln x = 2 atanh z with z = (x - 1) / (x + 1) (x - 1 is exact for
+// x in [1/2, 2]), then e^y with y = k ln x:
+//   |x - 1| <= 1/64 (|z| <= 1/127): atanh z = z (1 + z^2/3 + ... + z^8/9)
+//     (the first omitted term is below 2^-70 of the sum) and, for
+//     |y| <= 1/12, e^y = (e^(y/2))^2 with e^t - 1 = t (1 + t/2 + ... +
+//     t^7/8!) (|t| <= 1/24, remainder below 2^-64), both polynomials by
+//     Estrin's scheme (half the dependent depth of Horner's);
+//   |x - 1| <= 1/8 (|z| <= 1/15): the atanh series to z^14/15 (below 2^-58)
+//     and, for |y| <= 3/4, e^y = (e^(y/8))^8 with e^t - 1 to degree 10
+//     (|t| <= 3/32, below 2^-62), by Horner;
+//   otherwise the library pow.
+// e^t - 1 is carried through the squarings ((1 + u)^2 - 1 = u (u + 2)) so
+// that the small part keeps its relative accuracy until the final 1 + u.
+// The rounding of y (a few ulps, times |y|) dominates: the result is within
+// 8 ulps of x^k (5 measured against the library pow on 2^26 bases).
 __device__ __forceinline__ double pow_near1(double x, double k) {
     const double xm = x - 1.0;
-    if (!(fabs(xm) <= 0.125)) return pow(x, k);
+    const double axm = fabs(xm);
+    if (!(axm <= 0.125)) return pow(x, k);
     const double z = xm * rcp_nr3(x + 1.0);
     const double z2 = z * z;
+    if (axm <= 1.0 / 64.0) {
+        const double z4 = z2 * z2;
+        const double inner = fma(z4, 1.0 / 9.0, fma(z2, 1.0 / 7.0, 1.0 / 5.0));
+        const double q = fma(z4, inner, fma(z2, 1.0 / 3.0, 1.0));
+        const double y = (2.0 * k) * (z * q);
+        if (fabs(y) <= 1.0 / 12.0) {
+            const double t = 0.5 * y;
+            const double t2 = t * t, t4 = t2 * t2;
+            const double p01 = fma(t, 0.5, 1.0), p23 = fma(t, 1.0 / 24.0, 1.0 / 6.0);
+            const double p45 = fma(t, 1.0 / 720.0, 1.0 / 120.0), p67 = fma(t, 1.0 / 40320.0, 1.0 / 5040.0);
+            const double lo = fma(t2, p23, p01), hi = fma(t2, p67, p45);
+            double u = t * fma(t4, hi, lo);
+            u = fma(u, u, u + u);
+            return 1.0 + u;
+        }
+    }
     double q = 1.0 / 15.0;
     q = fma(q, z2, 1.0 / 13.0);
     q = fma(q, z2, 1.0 / 11.0);
@@ -124,8 +147,6 @@ __device__ __forceinline__ double pow_near1(double x, double k) {
     q = fma(q, z2, 1.0);
     const double y = (2.0 * k) * (z * q);
     if (!(fabs(y) <= 0.75)) return pow(x, k);
-    // u = e^t - 1 and (1 + u)^2 - 1 = u (u + 2), so that the small part
-    // keeps its relative accuracy until the final 1 + u
     const double t = 0.125 * y;
     double u = 1.0 / 3628800.0;  // 1/10!
     u = fma(u, t, 1.0 / 362880.0);

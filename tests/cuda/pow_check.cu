@@ -1,6 +1,7 @@
 // Checks fvconv::pow_near1 (fpconv.cuh) against the library pow on
-// pseudo-random bases in [0.75, 1.25] (the series range [7/8, 9/8] and
-// both sides of it) and exponents 2/(g-1) of the gases the solvers take
+// pseudo-random bases, half within 1/64 of 1 (its short path) and half in
+// [0.75, 1.25] (its other series range [7/8, 9/8] and both sides of it),
+// and exponents 2/(g-1) of the gases the solvers take
 // (g in [1.1, 1.67]) plus a few others.  Inside the series range the result
 // must be within 8 ulps of pow; outside it (where pow_near1 calls pow) it
 // must be pow's result exactly.  Prints "pow_checked N pow_series S
@@ -23,7 +24,9 @@ __global__ void check_pow(uint64_t count, uint64_t seed) {
     const double ks[8] = {5.0, 2.0 / (1.4 - 1.0), 2.0 / (1.67 - 1.0), 2.0 / (1.1 - 1.0), 2.5, 1.0, 0.5, 7.0};
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t b = mix(i * 0x9e3779b97f4a7c15ull + seed);
-        const double x = 0.75 + 0.5 * (double)(b >> 11) * (1.0 / 9007199254740992.0);
+        const double r01 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
+        // half the bases within 1/64 of 1 (the Estrin path), half in [3/4, 5/4]
+        const double x = (i & 8u) ? 1.0 + (r01 - 0.5) * (1.0 / 32.0) : 0.75 + 0.5 * r01;
         const double k = ks[i & 7u];
         const double mine = fvconv::pow_near1(x, k), ref = pow(x, k);
         const long long d = __double_as_longlong(mine) - __double_as_longlong(ref);
